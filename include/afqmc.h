@@ -1,0 +1,213 @@
+/*
+ * afqmc.h -- C ABI of the GB300-native phaseless AFQMC walker step.
+ *
+ * One handle = one system (Hamiltonian + left trial) and one batch of walkers
+ * resident on one GPU.  Every entry point returns an int status
+ * (AFQMC_OK = 0); afqmc_last_error() gives the message.  Nothing calls exit().
+ * A handle is used by one host thread at a time; its work runs in order on the
+ * handle's own CUDA stream, and every call returns after that work finished
+ * unless its comment says otherwise.
+ *
+ * Interfaces replaced (reference paths are relative to the reference checkout):
+ *   Hamiltonian ctor + floattenCholesky + rotateCholesky
+ *       DQMC/Hamiltonian.cpp:9-42, :179-219, :52-133   -> afqmc_create
+ *   RHF / UHF left trial (Wavefunction plug-in)
+ *       DQMC/Wavefunction.h:7-20, DQMC/RHF.cpp:9-17, DQMC/UHF.cpp -> afqmc_trial
+ *   DQMCWalker::prepProp (mean-field shifts, exp(-dt/2 h1'))
+ *       DQMC/DQMCWalker.cpp:32-103, :106-187            -> afqmc_create
+ *   DQMCWalker::setDet / getDet (serial layout)
+ *       DQMC/DQMCWalker.cpp:251-290                      -> afqmc_set_walkers / afqmc_get_walkers
+ *   DQMCWalker::forceBias -> RHF/UHF::forceBias
+ *       DQMC/DQMCWalker.cpp:569-576, DQMC/RHF.cpp:42-61  -> afqmc_force_bias
+ *   the per-walker loop of propagatePhaseless + weight update and cap
+ *       DQMC/MixedEstimator.cpp:461-468, DQMC/DQMCWalker.cpp:441-554 -> afqmc_step
+ *   population-control shift
+ *       DQMC/MixedEstimator.cpp:472-475                  -> afqmc_step (device eshift)
+ *   DQMCWalker::orthogonalize
+ *       DQMC/DQMCWalker.cpp:295-326                      -> afqmc_orthonormalize
+ *   DQMCWalker::hamAndOverlap -> RHF/UHF::hamAndOverlap
+ *       DQMC/DQMCWalker.cpp:592-601, DQMC/RHF.cpp:70-131 -> afqmc_local_energy
+ *   Hamiltonian::setNcholEne
+ *       DQMC/Hamiltonian.cpp:45-48                       -> afqmc_set_nchol_ene
+ */
+#ifndef AFQMC_GB300_H
+#define AFQMC_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define AFQMC_OK 0
+#define AFQMC_ERR_ARG 1          /* bad argument or size */
+#define AFQMC_ERR_CUDA 2         /* a CUDA runtime call failed */
+#define AFQMC_ERR_NAN 3          /* non-finite local energy */
+#define AFQMC_ERR_TIMEOUT 4      /* a bounded device wait gave up */
+#define AFQMC_ERR_UNSUPPORTED 5  /* combination not implemented */
+#define AFQMC_ERR_STATE 6        /* call made in the wrong state */
+
+/* integral type: DQMC/Hamiltonian.cpp:20-31 ("r" restricted, "u" unrestricted) */
+#define AFQMC_INT_R 0
+#define AFQMC_INT_U 1
+
+/* left-trial kind */
+#define AFQMC_TRIAL_RHF 0
+#define AFQMC_TRIAL_UHF 1
+
+/* arithmetic of the step */
+#define AFQMC_PREC_FP64 0   /* everything in FP64 (the FP64 oracle's algorithm) */
+#define AFQMC_PREC_MIXED 1  /* tensor-core Cholesky contractions, FP32 propagator, FP64 QR/LU/weights */
+#define AFQMC_PREC_REF32 2  /* FP64 except the reference's own FP32 parts: FP32 VHS from the
+                               FP32 packed Cholesky copy with complex<float> fields, and
+                               mean-field shifts from that FP32 copy (DQMCWalker.cpp:72-84, :406-421) */
+
+typedef struct afqmc_ham {
+  int norb, nalpha, nbeta, nchol;
+  int int_type;        /* AFQMC_INT_R or AFQMC_INT_U */
+  double ecore;
+  /* nsp = 1 (INT_R) or 2 (INT_U: up then down) */
+  const double* h1;    /* [nsp][norb][norb] row-major */
+  const double* h1mod; /* [nsp][norb][norb] row-major, h1 - 1/2 sum_g L_g L_g */
+  const double* chol;  /* [nsp][nchol][norb][norb]; chol[g][i][j] = reference chol[g](i, j) */
+} afqmc_ham;
+
+typedef struct afqmc_trial {
+  int kind;            /* AFQMC_TRIAL_RHF or AFQMC_TRIAL_UHF */
+  const double* phi_a; /* [norb][nalpha] row-major real orbitals */
+  const double* phi_b; /* [norb][nbeta]  (UHF only; RHF uses the first nbeta columns of phi_a) */
+} afqmc_trial;
+
+typedef struct afqmc_opts {
+  int nwalk;           /* walkers in this handle */
+  int rhf_walker;      /* 1: one spin det per walker (DQMCWalker(true, ...)); 0: two */
+  int precision;       /* AFQMC_PREC_* */
+  int device;          /* CUDA device ordinal */
+  double dt;
+  const double* ref_a; /* mean-field reference det [norb][nalpha] (rhf.txt / uhf.txt block);
+                          NULL: the trial's orbitals */
+  const double* ref_b; /* [norb][nbeta]; NULL with ref_a set: first nbeta columns of ref_a */
+  const double* green; /* optional [2][norb][norb] mean-field Green's function (the reference's
+                          spinRDM.0.0.txt override, DQMCWalker.cpp:39-58); NULL: from ref */
+  double weight_cap;   /* <= 0: max(100, nwalk / 10) as MixedEstimator.cpp:452-454 */
+  double pop_target;   /* walkers of the whole population (nwalk x ranks); <= 0: nwalk */
+  uint64_t seed;       /* device Philox seed for fields when no host fields are given */
+} afqmc_opts;
+
+typedef struct afqmc_handle afqmc_handle;
+
+/* Message of the last failure of h (or of the last failed afqmc_create if h is NULL). */
+const char* afqmc_last_error(const afqmc_handle* h);
+
+int afqmc_create(const afqmc_ham* ham, const afqmc_trial* trial, const afqmc_opts* opts,
+                 afqmc_handle** out);
+int afqmc_destroy(afqmc_handle* h);
+
+/* Sizes: serial det length N*(nalpha+nbeta) per walker, as DQMCWalker::getDet. */
+int afqmc_sizes(const afqmc_handle* h, int* norb, int* nalpha, int* nbeta, int* nchol, int* nwalk);
+
+/* Walker state through host buffers (complex = interleaved re, im doubles).
+ * dets:     [nwalk][N*(nalpha+nbeta)] in the reference's serial layout
+ *           (row-major alpha block, then row-major beta block; DQMCWalker.cpp:272-290).
+ *           For the restricted walker only the alpha block is read; both are written.
+ * overlaps: [nwalk] complex; NULL on set: computed as <Psi_T|phi>.
+ * weights:  [nwalk]; NULL on set: 1.  */
+int afqmc_set_walkers(afqmc_handle* h, const double* dets, const double* overlaps,
+                      const double* weights);
+int afqmc_get_walkers(afqmc_handle* h, double* dets, double* overlaps, double* weights);
+
+/* Force bias of every walker: fb [nwalk][nchol] complex. */
+int afqmc_force_bias(afqmc_handle* h, double* fb);
+
+/* One phaseless step of every live walker (weight > 1e-8), then the weight cap.
+ * xi:     [nwalk][nchol] standard normals in host memory (rows of dead walkers
+ *         ignored), or NULL to draw them on the device (Philox, key = seed).
+ * eshift: if non-NULL, the energy shift for this step; if NULL, the device value
+ *         left by the previous step's population control,
+ *         eshift = e_estimate - 0.1 ln(sum_w / pop_target) / dt.
+ * Asynchronous: returns once the work is queued on the handle's stream. */
+int afqmc_step(afqmc_handle* h, const double* xi, const double* eshift);
+
+/* Set the energy estimate used by the device population control, and optionally
+ * the current eshift (NULL leaves it). */
+int afqmc_set_energy_estimate(afqmc_handle* h, double e_estimate, const double* eshift);
+
+/* Sum of weights after the last step, and the eshift the next step will use. */
+int afqmc_population(afqmc_handle* h, double* sum_w, double* eshift_next, long* n_capped);
+
+/* Householder QR of every walker det (all walkers, as the reference), psi <- Q,
+ * overlap /= prod diag(R) (squared for the restricted walker). */
+int afqmc_orthonormalize(afqmc_handle* h);
+
+/* Number of Cholesky vectors used by the local energy (Hamiltonian::setNcholEne). */
+int afqmc_set_nchol_ene(afqmc_handle* h, int nchol_ene);
+
+/* Local energy E_L = <Psi_T|H|phi>/<Psi_T|phi> of every walker: eloc [nwalk] complex. */
+int afqmc_local_energy(afqmc_handle* h, double* eloc);
+
+/* Mean-field data from set-up: mf [nchol] complex, prop_constant (complex),
+ * expm [nsp][N][N] complex row-major = exp(-dt/2 h1'_s).  Any pointer may be NULL. */
+int afqmc_prop_info(afqmc_handle* h, double* mf, double* prop_constant, double* expm);
+
+/* Milliseconds of device time of the named stage over all steps since the last
+ * reset ("fb", "fields", "vhs", "prop", "overlap", "weights", "ortho", "energy"),
+ * when timing was enabled with afqmc_enable_timing(h, 1). */
+int afqmc_enable_timing(afqmc_handle* h, int on);
+int afqmc_stage_time(afqmc_handle* h, const char* stage, double* ms);
+
+/* Kernels launched by this handle since creation (device work items). */
+int afqmc_launch_count(const afqmc_handle* h, long* count);
+
+/* Device-time stopwatch on the handle's stream (CUDA events): start, then stop
+ * returns the milliseconds between the two points of the stream. */
+int afqmc_timer_start(afqmc_handle* h);
+int afqmc_timer_stop(afqmc_handle* h, double* ms);
+
+/* Synchronise the handle's stream. */
+int afqmc_sync(afqmc_handle* h);
+
+/* ---- host driver: calcMixedEstimatorLongProp (DQMC/MixedEstimator.cpp:309-660) ---- */
+typedef struct afqmc_run_opts {
+  int nprocs;        /* emulated MPI ranks; the handle holds nprocs x nwalk walkers, rank r
+                        owning walkers [r nwalk, (r + 1) nwalk) */
+  int nsteps;        /* steps per block (sampling.nsteps) */
+  int nsweeps;       /* blocks (sampling.stochasticIter) */
+  int ortho_steps;   /* sampling.orthoSteps */
+  int burn_iter;     /* sampling.burnIter */
+  unsigned seed;     /* sampling.seed; rank r draws from std::mt19937(seed + r) */
+  int field_source;  /* 0: the reference's order (host mt19937, one normal_distribution per
+                        walker, dead walkers draw nothing); 1: device Philox stream */
+  int comb;          /* 1: comb reconfiguration after every measurement (as the reference) */
+  double cholesky_threshold;  /* sampling.choleskyThreshold (energy Cholesky truncation) */
+  long max_steps;    /* > 0: stop after this many steps */
+} afqmc_run_opts;
+
+typedef struct afqmc_run_stats {
+  int nchol_ene;            /* Cholesky vectors used for the energy */
+  double delta;             /* energy correction of the truncation */
+  double e_ref;             /* energy of the reference determinant */
+  long n_large_deviations;  /* capped weights + clamped local energies */
+} afqmc_run_stats;
+
+/* Run the phaseless AFQMC loop from the walkers currently in h (set them with
+ * afqmc_set_walkers first, e.g. to the right trial's determinant).  Writes the
+ * samples.dat columns: total_weights[nsweeps], total_energies[nsweeps]. */
+int afqmc_run(afqmc_handle* h, const afqmc_run_opts* opts, double* total_weights, double* total_energies,
+              afqmc_run_stats* stats);
+
+/* The reference's field order for one emulated rank: std::mt19937(seed) and nwalk
+ * std::normal_distribution<double>(0, 1) objects (DQMC/DQMCWalker.h:18). */
+typedef struct afqmc_refrng afqmc_refrng;
+afqmc_refrng* afqmc_refrng_create(unsigned seed, int nwalk);
+void afqmc_refrng_destroy(afqmc_refrng* r);
+/* out[w][g] for walkers with weights[w] > 1e-8, in walker order; zeros for the others. */
+int afqmc_refrng_draw_step(afqmc_refrng* r, const double* weights, int nfields, double* out);
+/* std::uniform_real_distribution<double>(0, 1) draw (the comb's zeta). */
+double afqmc_refrng_uniform(afqmc_refrng* r);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* AFQMC_GB300_H */

@@ -1,0 +1,759 @@
+// C ABI of the phaseless AFQMC walker step: set-up (the reference's
+// Hamiltonian / trial / prepProp work, done once on the host in FP64), device
+// memory, and the per-step launch sequence.
+#include <cuda_runtime.h>
+#include <math.h>
+#include <string.h>
+
+#include <algorithm>
+#include <complex>
+#include <string>
+#include <vector>
+
+#include "afqmc_internal.h"
+
+using afqmc::Channel;
+using afqmc::cplx;
+using afqmc::PropChunk;
+
+namespace {
+
+thread_local std::string g_create_err;
+
+#define CK(call)                                                              \
+  do {                                                                        \
+    cudaError_t e_ = (call);                                                  \
+    if (e_ != cudaSuccess) {                                                  \
+      h->err = std::string(#call) + ": " + cudaGetErrorString(e_);            \
+      return AFQMC_ERR_CUDA;                                                  \
+    }                                                                         \
+  } while (0)
+
+int fail(afqmc_handle* h, int code, const std::string& msg) {
+  if (h) h->err = msg;
+  else g_create_err = msg;
+  return code;
+}
+
+int after_launch(afqmc_handle* h, const char* what) {
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    h->err = std::string(what) + ": " + cudaGetErrorString(e);
+    return AFQMC_ERR_CUDA;
+  }
+  return AFQMC_OK;
+}
+
+// exp(A) of a complex N x N matrix (row-major): scaling and squaring with a
+// Taylor polynomial truncated once the terms fall below 1e-17 of the sum
+// (the reference uses Eigen's Pade form, DQMCWalker.cpp:102; both approximate
+// the same function to FP64 rounding for the small ||dt h1'|| of a step).
+std::vector<cplx> expm(const std::vector<cplx>& A, int n) {
+  double norm = 0.0;
+  for (int j = 0; j < n; ++j) {
+    double c = 0.0;
+    for (int i = 0; i < n; ++i) c += std::abs(A[(size_t)i * n + j]);
+    norm = std::max(norm, c);
+  }
+  int s = 0;
+  while (norm / std::ldexp(1.0, s) > 0.25) ++s;
+  const double sc = std::ldexp(1.0, -s);
+  std::vector<cplx> X(A.size()), term((size_t)n * n), sum((size_t)n * n), tmp((size_t)n * n);
+  for (size_t e = 0; e < A.size(); ++e) X[e] = A[e] * sc;
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < n; ++j) sum[(size_t)i * n + j] = term[(size_t)i * n + j] = (i == j) ? 1.0 : 0.0;
+  auto matmul = [n](const std::vector<cplx>& a, const std::vector<cplx>& b, std::vector<cplx>& c) {
+    std::fill(c.begin(), c.end(), cplx(0.0));
+    for (int i = 0; i < n; ++i)
+      for (int k = 0; k < n; ++k) {
+        const cplx aik = a[(size_t)i * n + k];
+        if (aik == cplx(0.0)) continue;
+        for (int j = 0; j < n; ++j) c[(size_t)i * n + j] += aik * b[(size_t)k * n + j];
+      }
+  };
+  for (int k = 1; k <= 30; ++k) {
+    matmul(X, term, tmp);
+    double tn = 0.0, sn = 0.0;
+    for (size_t e = 0; e < tmp.size(); ++e) {
+      term[e] = tmp[e] / (double)k;
+      sum[e] += term[e];
+      tn = std::max(tn, std::abs(term[e]));
+      sn = std::max(sn, std::abs(sum[e]));
+    }
+    if (tn <= 1e-17 * sn) break;
+  }
+  for (int q = 0; q < s; ++q) {
+    matmul(sum, sum, tmp);
+    sum.swap(tmp);
+  }
+  return sum;
+}
+
+// inverse of a small real matrix (Gauss-Jordan, partial pivoting)
+bool inverse_real(std::vector<double>& a, int n) {
+  std::vector<double> inv((size_t)n * n, 0.0);
+  for (int i = 0; i < n; ++i) inv[(size_t)i * n + i] = 1.0;
+  for (int k = 0; k < n; ++k) {
+    int p = k;
+    for (int i = k + 1; i < n; ++i)
+      if (std::fabs(a[(size_t)i * n + k]) > std::fabs(a[(size_t)p * n + k])) p = i;
+    if (a[(size_t)p * n + k] == 0.0) return false;
+    for (int j = 0; j < n; ++j) {
+      std::swap(a[(size_t)k * n + j], a[(size_t)p * n + j]);
+      std::swap(inv[(size_t)k * n + j], inv[(size_t)p * n + j]);
+    }
+    const double d = 1.0 / a[(size_t)k * n + k];
+    for (int j = 0; j < n; ++j) { a[(size_t)k * n + j] *= d; inv[(size_t)k * n + j] *= d; }
+    for (int i = 0; i < n; ++i) {
+      if (i == k) continue;
+      const double f = a[(size_t)i * n + k];
+      if (f == 0.0) continue;
+      for (int j = 0; j < n; ++j) {
+        a[(size_t)i * n + j] -= f * a[(size_t)k * n + j];
+        inv[(size_t)i * n + j] -= f * inv[(size_t)k * n + j];
+      }
+    }
+  }
+  a.swap(inv);
+  return true;
+}
+
+template <typename T>
+int dalloc(afqmc_handle* h, T** p, size_t count) {
+  cudaError_t e = cudaMalloc((void**)p, std::max<size_t>(count, 1) * sizeof(T));
+  if (e != cudaSuccess) {
+    h->err = std::string("cudaMalloc(") + std::to_string(count * sizeof(T)) + " bytes): " + cudaGetErrorString(e);
+    return AFQMC_ERR_CUDA;
+  }
+  return AFQMC_OK;
+}
+
+template <typename T>
+int upload(afqmc_handle* h, T* d, const std::vector<T>& v) {
+  CK(cudaMemcpyAsync(d, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  return AFQMC_OK;
+}
+
+__global__ void k_set_scalar(double* p, int idx, double v) { p[idx] = v; }
+__global__ void k_fill(double* p, size_t n, double v) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) p[i] = v;
+}
+
+void stage_begin(afqmc_handle* h, int st, cudaEvent_t* ev) {
+  if (!h->timing) return;
+  cudaEventCreate(ev);
+  cudaEventRecord(*ev, h->stream);
+  (void)st;
+}
+void stage_end(afqmc_handle* h, int st, cudaEvent_t ev0) {
+  if (!h->timing) return;
+  cudaEvent_t ev1;
+  cudaEventCreate(&ev1);
+  cudaEventRecord(ev1, h->stream);
+  h->ev[st].push_back({ev0, ev1});
+}
+
+void release(afqmc_handle* h) {
+  void* ptrs[] = {h->psi, h->phi, h->rot, h->h1phi, h->LT, h->LT32, h->tri, h->expm, h->mf, h->theta,
+                  h->det, h->ovlp, h->weights, h->fb, h->xi, h->x, h->x32, h->shift, h->fbterm, h->V,
+                  h->qwork, h->epart, h->eloc, h->scal, h->d_chunks};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  if (h->host_pinned) cudaFreeHost(h->host_pinned);
+  if (h->timer[0]) { cudaEventDestroy(h->timer[0]); cudaEventDestroy(h->timer[1]); }
+  for (int s = 0; s < afqmc::ST_N; ++s)
+    for (auto& e : h->ev[s]) { cudaEventDestroy(e.first); cudaEventDestroy(e.second); }
+  if (h->stream) cudaStreamDestroy(h->stream);
+}
+
+}  // namespace
+
+namespace afqmc {
+bool check_launch(afqmc_handle* h, const char* what) { return after_launch(h, what) == AFQMC_OK; }
+}  // namespace afqmc
+
+extern "C" {
+
+const char* afqmc_last_error(const afqmc_handle* h) {
+  return h ? h->err.c_str() : g_create_err.c_str();
+}
+
+int afqmc_create(const afqmc_ham* ham, const afqmc_trial* trial, const afqmc_opts* opts, afqmc_handle** out) {
+  if (!ham || !trial || !opts || !out) return fail(nullptr, AFQMC_ERR_ARG, "null argument");
+  *out = nullptr;
+  const int N = ham->norb, na = ham->nalpha, nb = ham->nbeta, G = ham->nchol;
+  if (N <= 0 || na <= 0 || nb < 0 || na > N || nb > N || G <= 0 || !ham->h1 || !ham->h1mod || !ham->chol)
+    return fail(nullptr, AFQMC_ERR_ARG, "bad Hamiltonian sizes or null arrays");
+  if (ham->int_type != AFQMC_INT_R && ham->int_type != AFQMC_INT_U)
+    return fail(nullptr, AFQMC_ERR_ARG, "int_type must be AFQMC_INT_R or AFQMC_INT_U");
+  if (trial->kind != AFQMC_TRIAL_RHF && trial->kind != AFQMC_TRIAL_UHF)
+    return fail(nullptr, AFQMC_ERR_ARG, "trial kind must be RHF or UHF");
+  if (!trial->phi_a || (trial->kind == AFQMC_TRIAL_UHF && nb > 0 && !trial->phi_b))
+    return fail(nullptr, AFQMC_ERR_ARG, "trial orbitals missing");
+  if (opts->nwalk <= 0 || !(opts->dt > 0.0)) return fail(nullptr, AFQMC_ERR_ARG, "nwalk and dt must be positive");
+  if (opts->precision != AFQMC_PREC_FP64 && opts->precision != AFQMC_PREC_REF32 &&
+      opts->precision != AFQMC_PREC_MIXED)
+    return fail(nullptr, AFQMC_ERR_ARG, "unknown precision");
+  if (trial->kind == AFQMC_TRIAL_RHF && na != nb)
+    return fail(nullptr, AFQMC_ERR_UNSUPPORTED, "RHF trial needs nalpha == nbeta (RHF.cpp:27-31)");
+  if (opts->rhf_walker && na != nb)
+    return fail(nullptr, AFQMC_ERR_ARG, "restricted walker needs nalpha == nbeta");
+  if (ham->int_type == AFQMC_INT_U && (opts->rhf_walker || trial->kind != AFQMC_TRIAL_UHF))
+    return fail(nullptr, AFQMC_ERR_UNSUPPORTED, "intType u runs the UHF walker with a UHF trial (UHF.cpp)");
+  if (std::max(na, nb) > 128) return fail(nullptr, AFQMC_ERR_UNSUPPORTED, "nocc > 128");
+  if (opts->precision == AFQMC_PREC_MIXED)
+    return fail(nullptr, AFQMC_ERR_UNSUPPORTED, "mixed precision is provided by afqmc_create_mixed");
+
+  afqmc_handle* h = new afqmc_handle();
+  h->N = N; h->na = na; h->nb = nb; h->G = G; h->T = N * (N + 1) / 2;
+  h->int_type = ham->int_type; h->nsp = ham->int_type == AFQMC_INT_U ? 2 : 1; h->nspV = h->nsp;
+  h->nwalk = opts->nwalk; h->rhf_walker = opts->rhf_walker ? 1 : 0; h->precision = opts->precision;
+  h->device = opts->device; h->dt = opts->dt; h->ecore = ham->ecore; h->seed = opts->seed;
+  h->pop_target = opts->pop_target > 0 ? opts->pop_target : (double)opts->nwalk;
+  h->weight_cap = opts->weight_cap > 0 ? opts->weight_cap : std::max(100.0, opts->nwalk / 10.0);
+  h->ncw = h->rhf_walker ? na : na + nb;
+  h->nchol_ene = G;
+
+  // channels (see afqmc_internal.h)
+  if (trial->kind == AFQMC_TRIAL_RHF && h->rhf_walker) {
+    h->nchan = 1; h->mult = 2;
+    h->chan[0] = Channel{0, na, 0, 0};
+  } else {
+    h->nchan = 2; h->mult = 1;
+    h->chan[0] = Channel{0, na, 0, 0};
+    h->chan[1] = Channel{h->rhf_walker ? 0 : na, nb, na, h->nsp == 2 ? 1 : 0};
+  }
+  h->nce = 0;
+  for (int c = 0; c < h->nchan; ++c) h->nce += h->chan[c].n;
+
+  int rc;
+  cudaError_t ce = cudaSetDevice(h->device);
+  if (ce != cudaSuccess) { std::string m = cudaGetErrorString(ce); delete h; return fail(nullptr, AFQMC_ERR_CUDA, "cudaSetDevice: " + m); }
+  ce = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+  if (ce != cudaSuccess) { std::string m = cudaGetErrorString(ce); delete h; return fail(nullptr, AFQMC_ERR_CUDA, "cudaStreamCreate: " + m); }
+
+  const int nsp = h->nsp, T = h->T;
+  const size_t NN = (size_t)N * N;
+  // --- packed lower triangle, FP64 and FP32 (Hamiltonian.cpp:179-219) ---
+  std::vector<int2> tri(T);
+  for (int i = 0, t = 0; i < N; ++i)
+    for (int j = 0; j <= i; ++j, ++t) tri[t] = make_int2(i, j);
+  std::vector<double> LT((size_t)nsp * T * G);
+  std::vector<float> LT32((size_t)nsp * T * G);
+  for (int s = 0; s < nsp; ++s)
+    for (int g = 0; g < G; ++g) {
+      const double* L = ham->chol + ((size_t)s * G + g) * NN;
+      for (int t = 0; t < T; ++t) {
+        const double v = L[(size_t)tri[t].x * N + tri[t].y];
+        LT[((size_t)s * T + t) * G + g] = v;
+        LT32[((size_t)s * T + t) * G + g] = (float)v;
+      }
+    }
+  // symmetric Cholesky from the packed triangle, in the precision of the mean field
+  auto lsym = [&](int s, int g, int i, int j) -> double {
+    const int a = std::max(i, j), b = std::min(i, j);
+    const size_t t = (size_t)a * (a + 1) / 2 + b;
+    return h->precision == AFQMC_PREC_REF32 ? (double)LT32[((size_t)s * T + t) * G + g]
+                                            : LT[((size_t)s * T + t) * G + g];
+  };
+
+  // --- channel orbitals, half-rotated Cholesky (Hamiltonian.cpp:52-133), h1 Phi ---
+  std::vector<double> phi((size_t)h->nce * N), rot((size_t)G * h->nce * N, 0.0), h1phi((size_t)h->nce * N, 0.0);
+  for (int c = 0; c < h->nchan; ++c) {
+    const Channel ch = h->chan[c];
+    const bool beta = (c == 1);
+    const double* src = (beta && trial->kind == AFQMC_TRIAL_UHF) ? trial->phi_b : trial->phi_a;
+    const int ld = (beta && trial->kind == AFQMC_TRIAL_UHF) ? nb : na;
+    for (int i = 0; i < ch.n; ++i)
+      for (int p = 0; p < N; ++p) phi[(size_t)(ch.col_off + i) * N + p] = src[(size_t)p * ld + i];
+    for (int g = 0; g < G; ++g) {
+      const double* L = ham->chol + ((size_t)ch.lspin * G + g) * NN;
+      double* r = rot.data() + (size_t)g * h->nce * N;
+      for (int q = 0; q < N; ++q)
+        for (int i = 0; i < ch.n; ++i) {
+          const double a = phi[(size_t)(ch.col_off + i) * N + q];
+          if (a == 0.0) continue;
+          double* ri = r + (size_t)(ch.col_off + i) * N;
+          const double* Lq = L + (size_t)q * N;
+          for (int p = 0; p < N; ++p) ri[p] += a * Lq[p];
+        }
+    }
+    const double* h1s = ham->h1 + (size_t)ch.lspin * NN;
+    for (int i = 0; i < ch.n; ++i)
+      for (int p = 0; p < N; ++p) {
+        double acc = 0.0;
+        for (int q = 0; q < N; ++q) acc += h1s[(size_t)p * N + q] * phi[(size_t)(ch.col_off + i) * N + q];
+        h1phi[(size_t)(ch.col_off + i) * N + p] = acc;
+      }
+  }
+
+  // mean-field reference determinant (rhf.txt / uhf.txt block, else the trial)
+  h->ref_serial.assign((size_t)N * (na + nb), 0.0);
+  for (int s = 0; s < 2; ++s) {
+    const int n = s == 0 ? na : nb;
+    const double* R;
+    int ld;
+    if (opts->ref_a) {
+      if (s == 1 && opts->ref_b) { R = opts->ref_b; ld = nb; }
+      else { R = opts->ref_a; ld = na; }
+    } else if (s == 1 && trial->kind == AFQMC_TRIAL_UHF) { R = trial->phi_b; ld = nb; }
+    else { R = trial->phi_a; ld = na; }
+    for (int p = 0; p < N; ++p)
+      for (int j = 0; j < n; ++j) h->ref_serial[(s == 0 ? 0 : (size_t)N * na) + (size_t)p * n + j] = R[(size_t)p * ld + j];
+  }
+
+  // --- prepProp (DQMCWalker.cpp:32-103 / :106-187) ---
+  std::vector<double> green((size_t)2 * NN, 0.0);
+  if (opts->green) {
+    std::copy(opts->green, opts->green + 2 * NN, green.begin());
+  } else {
+    for (int s = 0; s < 2; ++s) {
+      const int n = s == 0 ? na : nb;
+      if (n == 0) continue;
+      const double* R;
+      int ld;
+      if (opts->ref_a) {
+        if (s == 1 && opts->ref_b) { R = opts->ref_b; ld = nb; }
+        else { R = opts->ref_a; ld = na; }
+      } else if (s == 1 && trial->kind == AFQMC_TRIAL_UHF) { R = trial->phi_b; ld = nb; }
+      else { R = trial->phi_a; ld = na; }
+      std::vector<double> rtr((size_t)n * n, 0.0);
+      for (int i = 0; i < n; ++i)
+        for (int j = 0; j < n; ++j) {
+          double a = 0.0;
+          for (int p = 0; p < N; ++p) a += R[(size_t)p * ld + i] * R[(size_t)p * ld + j];
+          rtr[(size_t)i * n + j] = a;
+        }
+      if (!inverse_real(rtr, n)) { release(h); delete h; return fail(nullptr, AFQMC_ERR_ARG, "singular reference determinant"); }
+      std::vector<double> ri((size_t)N * n, 0.0);  // R (R^T R)^{-1}
+      for (int p = 0; p < N; ++p)
+        for (int j = 0; j < n; ++j) {
+          double a = 0.0;
+          for (int i = 0; i < n; ++i) a += R[(size_t)p * ld + i] * rtr[(size_t)i * n + j];
+          ri[(size_t)p * n + j] = a;
+        }
+      for (int p = 0; p < N; ++p)
+        for (int q = 0; q < N; ++q) {
+          double a = 0.0;
+          for (int j = 0; j < n; ++j) a += ri[(size_t)p * n + j] * R[(size_t)q * ld + j];
+          green[(size_t)s * NN + (size_t)p * N + q] = a;
+        }
+    }
+  }
+  h->mf_host.assign(G, cplx(0.0));
+  cplx constant = -ham->ecore;
+  for (int g = 0; g < G; ++g) {
+    double acc = 0.0;
+    for (int s = 0; s < 2; ++s) {
+      const int ls = nsp == 2 ? s : 0;
+      for (int p = 0; p < N; ++p)
+        for (int q = 0; q < N; ++q) acc += green[(size_t)s * NN + (size_t)p * N + q] * lsym(ls, g, p, q);
+    }
+    h->mf_host[g] = cplx(0.0, acc);
+    constant -= h->mf_host[g] * h->mf_host[g] / 2.0;
+  }
+  h->prop_constant = constant;
+  h->expm_host.assign((size_t)nsp * NN, cplx(0.0));
+  std::vector<cplx> expm_cm((size_t)nsp * NN);
+  for (int s = 0; s < nsp; ++s) {
+    std::vector<cplx> A(NN);
+    const double* hm = ham->h1mod + (size_t)s * NN;
+    for (int p = 0; p < N; ++p)
+      for (int q = 0; q < N; ++q) {
+        cplx v = hm[(size_t)p * N + q];
+        for (int g = 0; g < G; ++g) v -= h->mf_host[g] * cplx(0.0, lsym(s, g, p, q));
+        A[(size_t)p * N + q] = -h->dt * v / 2.0;
+      }
+    std::vector<cplx> E = expm(A, N);
+    for (int p = 0; p < N; ++p)
+      for (int q = 0; q < N; ++q) {
+        h->expm_host[(size_t)s * NN + (size_t)p * N + q] = E[(size_t)p * N + q];
+        expm_cm[(size_t)s * NN + (size_t)q * N + p] = E[(size_t)p * N + q];
+      }
+  }
+
+  // --- propagator column chunks ---
+  {
+    const int nblk = h->rhf_walker ? 1 : 2;
+    for (int b = 0; b < nblk; ++b) {
+      const int off = b == 0 ? 0 : na, n = b == 0 ? na : nb;
+      for (int c = 0; c < n; c += afqmc::PROP_CH) h->chunks.push_back(PropChunk{off + c, std::min(afqmc::PROP_CH, n - c), b});
+    }
+    h->nchunks = (int)h->chunks.size();
+  }
+  h->nechunk = std::max(1, std::min(G, (4 * 152 + h->nwalk - 1) / h->nwalk));
+
+  // --- device buffers ---
+  const size_t W = h->nwalk;
+#define ALLOC(ptr, n)                                   \
+  if ((rc = dalloc(h, &h->ptr, (n))) != AFQMC_OK) {     \
+    g_create_err = h->err;                              \
+    release(h);                                         \
+    delete h;                                           \
+    return rc;                                          \
+  }
+  ALLOC(psi, W * h->ncw * N);
+  ALLOC(phi, (size_t)h->nce * N);
+  ALLOC(rot, (size_t)G * h->nce * N);
+  ALLOC(h1phi, (size_t)h->nce * N);
+  ALLOC(LT, (size_t)nsp * T * G);
+  if (h->precision == AFQMC_PREC_REF32) { ALLOC(LT32, (size_t)nsp * T * G); ALLOC(x32, W * 2 * G); }
+  ALLOC(tri, (size_t)T);
+  ALLOC(expm, (size_t)nsp * NN);
+  ALLOC(mf, (size_t)G);
+  ALLOC(theta, W * 2 * h->nce * N);
+  ALLOC(det, W * 2);
+  ALLOC(ovlp, W);
+  ALLOC(weights, W);
+  ALLOC(fb, W * 2 * G);
+  ALLOC(xi, W * G);
+  ALLOC(x, W * 2 * G);
+  ALLOC(shift, W);
+  ALLOC(fbterm, W);
+  ALLOC(V, W * h->nspV * 2 * NN);
+  ALLOC(qwork, W * h->ncw * N);
+  ALLOC(epart, W * h->nechunk);
+  ALLOC(eloc, W);
+  ALLOC(scal, (size_t)afqmc::S_NSLOTS);
+  ALLOC(d_chunks, (size_t)h->nchunks);
+#undef ALLOC
+  ce = cudaMallocHost((void**)&h->host_pinned, W * G * sizeof(double));
+  if (ce != cudaSuccess) { g_create_err = cudaGetErrorString(ce); release(h); delete h; return AFQMC_ERR_CUDA; }
+  h->host_pinned_bytes = W * G * sizeof(double);
+
+  std::vector<double2> mf2(G), expm2((size_t)nsp * NN);
+  for (int g = 0; g < G; ++g) mf2[g] = make_double2(h->mf_host[g].real(), h->mf_host[g].imag());
+  for (size_t e = 0; e < expm2.size(); ++e) expm2[e] = make_double2(expm_cm[e].real(), expm_cm[e].imag());
+#define UP(ptr, vec)                                               \
+  if ((rc = upload(h, h->ptr, vec)) != AFQMC_OK) {                 \
+    g_create_err = h->err;                                         \
+    release(h);                                                    \
+    delete h;                                                      \
+    return rc;                                                     \
+  }
+  UP(phi, phi);
+  UP(rot, rot);
+  UP(h1phi, h1phi);
+  UP(LT, LT);
+  if (h->LT32) UP(LT32, LT32);
+  UP(tri, tri);
+  UP(expm, expm2);
+  UP(mf, mf2);
+  UP(d_chunks, h->chunks);
+  std::vector<double> sc(afqmc::S_NSLOTS, 0.0);
+  UP(scal, sc);
+  // walkers start at the trial determinant with unit weight
+  {
+    std::vector<double2> p0(W * h->ncw * N);
+    for (size_t w = 0; w < W; ++w)
+      for (int c = 0; c < h->ncw; ++c) {
+        const bool beta = c >= na;
+        const int i = beta ? c - na : c;
+        for (int p = 0; p < N; ++p) {
+          const double v = (beta && trial->kind == AFQMC_TRIAL_UHF) ? trial->phi_b[(size_t)p * nb + i]
+                                                                     : trial->phi_a[(size_t)p * na + i];
+          p0[(w * h->ncw + c) * N + p] = make_double2(v, 0.0);
+        }
+      }
+    UP(psi, p0);
+  }
+#undef UP
+  k_fill<<<64, 256, 0, h->stream>>>(h->weights, W, 1.0);
+  afqmc::launch_overlap_theta(h, false);
+  afqmc::launch_init_overlap(h);
+  ce = cudaStreamSynchronize(h->stream);
+  if (ce == cudaSuccess) ce = cudaGetLastError();
+  if (ce != cudaSuccess) { g_create_err = cudaGetErrorString(ce); release(h); delete h; return AFQMC_ERR_CUDA; }
+  *out = h;
+  return AFQMC_OK;
+}
+
+int afqmc_destroy(afqmc_handle* h) {
+  if (!h) return AFQMC_ERR_ARG;
+  cudaSetDevice(h->device);
+  cudaStreamSynchronize(h->stream);
+  release(h);
+  delete h;
+  return AFQMC_OK;
+}
+
+int afqmc_sizes(const afqmc_handle* h, int* norb, int* nalpha, int* nbeta, int* nchol, int* nwalk) {
+  if (!h) return AFQMC_ERR_ARG;
+  if (norb) *norb = h->N;
+  if (nalpha) *nalpha = h->na;
+  if (nbeta) *nbeta = h->nb;
+  if (nchol) *nchol = h->G;
+  if (nwalk) *nwalk = h->nwalk;
+  return AFQMC_OK;
+}
+
+int afqmc_set_walkers(afqmc_handle* h, const double* dets, const double* overlaps, const double* weights) {
+  if (!h || !dets) return fail(h, AFQMC_ERR_ARG, "null dets");
+  cudaSetDevice(h->device);
+  const int N = h->N, na = h->na, nb = h->nb;
+  const size_t W = h->nwalk, ser = (size_t)N * (na + nb);
+  std::vector<double2> p((size_t)W * h->ncw * N);
+  for (size_t w = 0; w < W; ++w) {
+    const double* s = dets + 2 * w * ser;
+    for (int i = 0; i < N; ++i)
+      for (int j = 0; j < na; ++j) {
+        const size_t e = (size_t)i * na + j;
+        p[(w * h->ncw + j) * N + i] = make_double2(s[2 * e], s[2 * e + 1]);
+      }
+    if (!h->rhf_walker)
+      for (int i = 0; i < N; ++i)
+        for (int j = 0; j < nb; ++j) {
+          const size_t e = (size_t)na * N + (size_t)i * nb + j;
+          p[(w * h->ncw + na + j) * N + i] = make_double2(s[2 * e], s[2 * e + 1]);
+        }
+  }
+  int rc = upload(h, h->psi, p);
+  if (rc) return rc;
+  if (weights) {
+    std::vector<double> wv(weights, weights + W);
+    if ((rc = upload(h, h->weights, wv))) return rc;
+  } else {
+    k_fill<<<64, 256, 0, h->stream>>>(h->weights, W, 1.0);
+    h->launches++;
+  }
+  afqmc::launch_overlap_theta(h, false);
+  if (overlaps) {
+    std::vector<double2> o(W);
+    for (size_t w = 0; w < W; ++w) o[w] = make_double2(overlaps[2 * w], overlaps[2 * w + 1]);
+    if ((rc = upload(h, h->ovlp, o))) return rc;
+  } else {
+    afqmc::launch_init_overlap(h);
+  }
+  if ((rc = after_launch(h, "set_walkers"))) return rc;
+  CK(cudaStreamSynchronize(h->stream));
+  return AFQMC_OK;
+}
+
+int afqmc_get_walkers(afqmc_handle* h, double* dets, double* overlaps, double* weights) {
+  if (!h) return AFQMC_ERR_ARG;
+  cudaSetDevice(h->device);
+  const int N = h->N, na = h->na, nb = h->nb;
+  const size_t W = h->nwalk, ser = (size_t)N * (na + nb);
+  CK(cudaStreamSynchronize(h->stream));
+  if (dets) {
+    std::vector<double2> p((size_t)W * h->ncw * N);
+    CK(cudaMemcpy(p.data(), h->psi, p.size() * sizeof(double2), cudaMemcpyDeviceToHost));
+    for (size_t w = 0; w < W; ++w) {
+      double* s = dets + 2 * w * ser;
+      for (int i = 0; i < N; ++i)
+        for (int j = 0; j < na; ++j) {
+          const size_t e = (size_t)i * na + j;
+          const double2 v = p[(w * h->ncw + j) * N + i];
+          s[2 * e] = v.x;
+          s[2 * e + 1] = v.y;
+        }
+      for (int i = 0; i < N; ++i)
+        for (int j = 0; j < nb; ++j) {
+          const size_t e = (size_t)na * N + (size_t)i * nb + j;
+          const int col = h->rhf_walker ? j : na + j;
+          const double2 v = p[(w * h->ncw + col) * N + i];
+          s[2 * e] = v.x;
+          s[2 * e + 1] = v.y;
+        }
+    }
+  }
+  if (overlaps) CK(cudaMemcpy(overlaps, h->ovlp, W * sizeof(double2), cudaMemcpyDeviceToHost));
+  if (weights) CK(cudaMemcpy(weights, h->weights, W * sizeof(double), cudaMemcpyDeviceToHost));
+  return AFQMC_OK;
+}
+
+int afqmc_force_bias(afqmc_handle* h, double* fb) {
+  if (!h || !fb) return fail(h, AFQMC_ERR_ARG, "null argument");
+  cudaSetDevice(h->device);
+  afqmc::launch_force_bias(h);
+  int rc = after_launch(h, "force_bias");
+  if (rc) return rc;
+  std::vector<double> buf((size_t)h->nwalk * 2 * h->G);
+  CK(cudaMemcpyAsync(buf.data(), h->fb, buf.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  for (int w = 0; w < h->nwalk; ++w)
+    for (int g = 0; g < h->G; ++g) {
+      fb[2 * ((size_t)w * h->G + g)] = buf[(size_t)(2 * w) * h->G + g];
+      fb[2 * ((size_t)w * h->G + g) + 1] = buf[(size_t)(2 * w + 1) * h->G + g];
+    }
+  return AFQMC_OK;
+}
+
+int afqmc_step(afqmc_handle* h, const double* xi, const double* eshift) {
+  if (!h) return AFQMC_ERR_ARG;
+  cudaSetDevice(h->device);
+  if (eshift) {
+    k_set_scalar<<<1, 1, 0, h->stream>>>(h->scal, afqmc::S_ESHIFT, *eshift);
+    h->launches++;
+  }
+  if (xi) {
+    // the previous step's copy out of the staging buffer must be done
+    CK(cudaStreamSynchronize(h->stream));
+    memcpy(h->host_pinned, xi, (size_t)h->nwalk * h->G * sizeof(double));
+    CK(cudaMemcpyAsync(h->xi, h->host_pinned, (size_t)h->nwalk * h->G * sizeof(double), cudaMemcpyHostToDevice,
+                       h->stream));
+  }
+  cudaEvent_t e0;
+  stage_begin(h, afqmc::ST_FB, &e0);
+  afqmc::launch_force_bias(h);
+  stage_end(h, afqmc::ST_FB, e0);
+  stage_begin(h, afqmc::ST_FIELDS, &e0);
+  afqmc::launch_fields(h, xi == nullptr);
+  stage_end(h, afqmc::ST_FIELDS, e0);
+  stage_begin(h, afqmc::ST_VHS, &e0);
+  afqmc::launch_vhs(h);
+  stage_end(h, afqmc::ST_VHS, e0);
+  stage_begin(h, afqmc::ST_PROP, &e0);
+  afqmc::launch_propagate(h);
+  stage_end(h, afqmc::ST_PROP, e0);
+  stage_begin(h, afqmc::ST_OVERLAP, &e0);
+  afqmc::launch_overlap_theta(h, true);
+  stage_end(h, afqmc::ST_OVERLAP, e0);
+  stage_begin(h, afqmc::ST_WEIGHTS, &e0);
+  afqmc::launch_weights(h);
+  stage_end(h, afqmc::ST_WEIGHTS, e0);
+  h->step_counter++;
+  return after_launch(h, "step");
+}
+
+int afqmc_set_energy_estimate(afqmc_handle* h, double e_estimate, const double* eshift) {
+  if (!h) return AFQMC_ERR_ARG;
+  cudaSetDevice(h->device);
+  k_set_scalar<<<1, 1, 0, h->stream>>>(h->scal, afqmc::S_EEST, e_estimate);
+  h->launches++;
+  if (eshift) {
+    k_set_scalar<<<1, 1, 0, h->stream>>>(h->scal, afqmc::S_ESHIFT, *eshift);
+    h->launches++;
+  }
+  return after_launch(h, "set_energy_estimate");
+}
+
+int afqmc_population(afqmc_handle* h, double* sum_w, double* eshift_next, long* n_capped) {
+  if (!h) return AFQMC_ERR_ARG;
+  cudaSetDevice(h->device);
+  double sc[afqmc::S_NSLOTS];
+  CK(cudaStreamSynchronize(h->stream));
+  CK(cudaMemcpy(sc, h->scal, sizeof(sc), cudaMemcpyDeviceToHost));
+  if (sum_w) *sum_w = sc[afqmc::S_SUMW];
+  if (eshift_next) *eshift_next = sc[afqmc::S_ESHIFT];
+  if (n_capped) *n_capped = (long)sc[afqmc::S_NCAP];
+  return AFQMC_OK;
+}
+
+int afqmc_orthonormalize(afqmc_handle* h) {
+  if (!h) return AFQMC_ERR_ARG;
+  cudaSetDevice(h->device);
+  if (h->ncw > 0 && std::max(h->na, h->nb) > afqmc::QR_MAXN) return fail(h, AFQMC_ERR_UNSUPPORTED, "nocc too large for QR");
+  cudaEvent_t e0;
+  stage_begin(h, afqmc::ST_ORTHO, &e0);
+  afqmc::launch_ortho(h);
+  afqmc::launch_overlap_theta(h, false);
+  stage_end(h, afqmc::ST_ORTHO, e0);
+  return after_launch(h, "orthonormalize");
+}
+
+int afqmc_set_nchol_ene(afqmc_handle* h, int nchol_ene) {
+  if (!h || nchol_ene < 0 || nchol_ene > h->G) return fail(h, AFQMC_ERR_ARG, "nchol_ene out of range");
+  h->nchol_ene = nchol_ene;
+  return AFQMC_OK;
+}
+
+int afqmc_local_energy(afqmc_handle* h, double* eloc) {
+  if (!h) return AFQMC_ERR_ARG;
+  cudaSetDevice(h->device);
+  const int nmax = std::max(h->chan[0].n, h->nchan > 1 ? h->chan[1].n : 0);
+  const size_t smem = ((size_t)h->nce * h->N + (size_t)h->nchan * nmax * nmax) * sizeof(double2);
+  if (smem > 220 * 1024) return fail(h, AFQMC_ERR_UNSUPPORTED, "FP64 local energy: theta does not fit in shared memory");
+  cudaEvent_t e0;
+  stage_begin(h, afqmc::ST_ENERGY, &e0);
+  afqmc::launch_local_energy(h);
+  stage_end(h, afqmc::ST_ENERGY, e0);
+  int rc = after_launch(h, "local_energy");
+  if (rc) return rc;
+  if (eloc) {
+    CK(cudaMemcpyAsync(eloc, h->eloc, (size_t)h->nwalk * sizeof(double2), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+  }
+  return AFQMC_OK;
+}
+
+int afqmc_prop_info(afqmc_handle* h, double* mf, double* prop_constant, double* expm_out) {
+  if (!h) return AFQMC_ERR_ARG;
+  if (mf)
+    for (int g = 0; g < h->G; ++g) { mf[2 * g] = h->mf_host[g].real(); mf[2 * g + 1] = h->mf_host[g].imag(); }
+  if (prop_constant) { prop_constant[0] = h->prop_constant.real(); prop_constant[1] = h->prop_constant.imag(); }
+  if (expm_out)
+    for (size_t e = 0; e < h->expm_host.size(); ++e) { expm_out[2 * e] = h->expm_host[e].real(); expm_out[2 * e + 1] = h->expm_host[e].imag(); }
+  return AFQMC_OK;
+}
+
+int afqmc_enable_timing(afqmc_handle* h, int on) {
+  if (!h) return AFQMC_ERR_ARG;
+  cudaSetDevice(h->device);
+  CK(cudaStreamSynchronize(h->stream));
+  for (int s = 0; s < afqmc::ST_N; ++s) {
+    for (auto& e : h->ev[s]) { cudaEventDestroy(e.first); cudaEventDestroy(e.second); }
+    h->ev[s].clear();
+    h->stage_ms[s] = 0.0;
+  }
+  h->timing = on != 0;
+  return AFQMC_OK;
+}
+
+int afqmc_stage_time(afqmc_handle* h, const char* stage, double* ms) {
+  static const char* names[afqmc::ST_N] = {"fb", "fields", "vhs", "prop", "overlap", "weights", "ortho", "energy"};
+  if (!h || !stage || !ms) return AFQMC_ERR_ARG;
+  int st = -1;
+  for (int s = 0; s < afqmc::ST_N; ++s)
+    if (strcmp(stage, names[s]) == 0) st = s;
+  if (st < 0) return fail(h, AFQMC_ERR_ARG, std::string("unknown stage ") + stage);
+  cudaSetDevice(h->device);
+  CK(cudaStreamSynchronize(h->stream));
+  double tot = 0.0;
+  for (auto& e : h->ev[st]) {
+    float t = 0.f;
+    CK(cudaEventElapsedTime(&t, e.first, e.second));
+    tot += t;
+  }
+  *ms = tot;
+  return AFQMC_OK;
+}
+
+int afqmc_launch_count(const afqmc_handle* h, long* count) {
+  if (!h || !count) return AFQMC_ERR_ARG;
+  *count = h->launches;
+  return AFQMC_OK;
+}
+
+int afqmc_timer_start(afqmc_handle* h) {
+  if (!h) return AFQMC_ERR_ARG;
+  cudaSetDevice(h->device);
+  if (!h->timer[0]) {
+    CK(cudaEventCreate(&h->timer[0]));
+    CK(cudaEventCreate(&h->timer[1]));
+  }
+  CK(cudaEventRecord(h->timer[0], h->stream));
+  return AFQMC_OK;
+}
+
+int afqmc_timer_stop(afqmc_handle* h, double* ms) {
+  if (!h || !ms || !h->timer[0]) return AFQMC_ERR_ARG;
+  cudaSetDevice(h->device);
+  CK(cudaEventRecord(h->timer[1], h->stream));
+  CK(cudaEventSynchronize(h->timer[1]));
+  float t = 0.f;
+  CK(cudaEventElapsedTime(&t, h->timer[0], h->timer[1]));
+  *ms = t;
+  return AFQMC_OK;
+}
+
+int afqmc_sync(afqmc_handle* h) {
+  if (!h) return AFQMC_ERR_ARG;
+  cudaSetDevice(h->device);
+  CK(cudaStreamSynchronize(h->stream));
+  CK(cudaGetLastError());
+  return AFQMC_OK;
+}
+
+}  // extern "C"

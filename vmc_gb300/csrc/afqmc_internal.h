@@ -1,0 +1,117 @@
+// Internal declarations shared by the C-ABI layer and the kernels.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <complex>
+#include <string>
+#include <vector>
+
+#include "../../include/afqmc.h"
+
+namespace afqmc {
+
+using cplx = std::complex<double>;
+
+// A trial "channel": one (walker det block, trial orbital block) pair of the
+// trial contractions.  RHF trial x restricted walker is one channel counted
+// twice (mult = 2, DQMC/RHF.cpp:34-39, :54-61, :104-131); all other pairings
+// have two channels with mult = 1.
+struct Channel {
+  int psi_off;  // first walker-det column of this channel
+  int n;        // occupied orbitals
+  int col_off;  // first column in the channel-ordered arrays (phi, rot, theta, h1phi)
+  int lspin;    // which Cholesky / h1 spin block it contracts with (0 unless int_type U)
+};
+
+// A column chunk of the walker det for the propagator: columns [c0, c0 + nc)
+// all in walker spin block `spin` (which selects V and exp(-dt/2 h1')).
+struct PropChunk {
+  int c0, nc, spin;
+};
+
+constexpr int PROP_CH = 8;   // walker-det columns per propagator CTA
+constexpr int QR_MAXN = 128; // largest nocc the QR kernel handles
+
+// Device scalars of the population control (slots of Handle::scal).
+enum { S_ESHIFT = 0, S_EEST = 1, S_SUMW = 2, S_NCAP = 3, S_NSLOTS = 8 };
+
+// Stage names for timing.
+enum Stage { ST_FB = 0, ST_FIELDS, ST_VHS, ST_PROP, ST_OVERLAP, ST_WEIGHTS, ST_ORTHO, ST_ENERGY, ST_N };
+
+}  // namespace afqmc
+
+struct afqmc_handle {
+  // sizes
+  int N = 0, na = 0, nb = 0, G = 0, T = 0, nsp = 1, int_type = 0;
+  int nwalk = 0, rhf_walker = 0, precision = 0, device = 0;
+  int ncw = 0;          // walker det columns (na, or na + nb)
+  int nchan = 0, mult = 1, nce = 0;
+  afqmc::Channel chan[2];
+  std::vector<afqmc::PropChunk> chunks;
+  int nspV = 1;         // distinct VHS matrices per walker (1 for INT_R, 2 for INT_U)
+  double dt = 0, ecore = 0, weight_cap = 0, pop_target = 0;
+  uint64_t seed = 0, step_counter = 0;
+  int nchol_ene = 0;
+  afqmc::cplx prop_constant;
+  std::vector<afqmc::cplx> mf_host;    // [G]
+  std::vector<afqmc::cplx> expm_host;  // [nsp][N][N] row-major
+  std::vector<double> ref_serial;      // mean-field reference det, serial layout N*(na+nb)
+  cudaStream_t stream = nullptr;
+  std::string err;
+  long launches = 0;
+  bool timing = false;
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev[afqmc::ST_N];
+  std::vector<cudaEvent_t> ev_pool;
+  double stage_ms[afqmc::ST_N] = {0};
+  cudaEvent_t timer[2] = {nullptr, nullptr};
+
+  // device buffers (FP64 form)
+  double2* psi = nullptr;     // [W][ncw][N]          walker dets, column-major per walker
+  double* phi = nullptr;      // [nce][N]             channel trial orbitals
+  double* rot = nullptr;      // [G][nce*N]           rot[g][(col)*N + p] = (Phi^T L_g)[i, p]
+  double* h1phi = nullptr;    // [nce][N]             (h1 Phi)[p, i]
+  double* LT = nullptr;       // [nsp][T][G]          packed lower-triangle Cholesky, FP64
+  float* LT32 = nullptr;      // [nsp][T][G]          FP32 copy (REF32)
+  int2* tri = nullptr;        // [T]                  packed index -> (i, j), j <= i
+  double2* expm = nullptr;    // [nsp][N][N]          column-major exp(-dt/2 h1'_s)
+  double2* mf = nullptr;      // [G]
+  double* theta = nullptr;    // [W][2][nce*N]        re / im planes
+  double2* det = nullptr;     // [W][2]               det(Phi_s^T psi_s) per channel
+  double2* ovlp = nullptr;    // [W]
+  double* weights = nullptr;  // [W]
+  double* fb = nullptr;       // [W][2][G]
+  double* xi = nullptr;       // [W][G]
+  double* x = nullptr;        // [W][2][G]
+  float* x32 = nullptr;       // [W][2][G]
+  double2* shift = nullptr;   // [W]
+  double2* fbterm = nullptr;  // [W]
+  double* V = nullptr;        // [W][nspV][2][N*N]    full VHS matrices, re / im planes
+  double2* qwork = nullptr;   // [W][ncw][N]          QR scratch (Q)
+  double2* epart = nullptr;   // [W][nechunk]         local-energy partial sums
+  double2* eloc = nullptr;    // [W]
+  double* scal = nullptr;     // [S_NSLOTS]
+  double* host_pinned = nullptr;  // pinned staging for xi
+  size_t host_pinned_bytes = 0;
+  int nechunk = 0;
+  afqmc::PropChunk* d_chunks = nullptr;
+  int nchunks = 0;
+};
+
+namespace afqmc {
+
+// ---- kernels (kernels_fp64.cu) ----
+void launch_overlap_theta(afqmc_handle* h, bool only_live);
+void launch_force_bias(afqmc_handle* h);
+void launch_fields(afqmc_handle* h, bool device_rng);
+void launch_vhs(afqmc_handle* h);
+void launch_propagate(afqmc_handle* h);
+void launch_weights(afqmc_handle* h);
+void launch_ortho(afqmc_handle* h);
+void launch_local_energy(afqmc_handle* h);
+void launch_init_overlap(afqmc_handle* h);
+
+// error helper used by kernels' launchers
+bool check_launch(afqmc_handle* h, const char* what);
+
+}  // namespace afqmc

@@ -1,0 +1,634 @@
+// FP64 kernels of the phaseless AFQMC step (and the FP64 parts shared with the
+// mixed-precision form: overlap / inverse / theta, field shifts, weights, QR).
+//
+// Reference algorithm: DQMC/DQMCWalker.cpp:441-554 (step), :295-326 (QR),
+// DQMC/RHF.cpp, DQMC/UHF.cpp (trial contractions), DQMC/MixedEstimator.cpp:461-475
+// (weights, cap, population control).
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+
+#include <algorithm>
+
+#include "afqmc_internal.h"
+#include "device_common.cuh"
+
+namespace afqmc {
+
+// ---------------------------------------------------------------------------
+// overlap, inverse and theta:  M_s = Phi_s^T psi_s, det(M_s), theta_s = psi_s M_s^{-1}
+// (RHF.cpp:27-61, UHF.cpp:31-65).  Gauss-Jordan with partial pivoting, pivot =
+// first row of largest |M_ik| as Eigen's PartialPivLU.  One CTA per (walker, channel).
+// ---------------------------------------------------------------------------
+__global__ void k_overlap_theta(const double2* __restrict__ psi, const double* __restrict__ phi,
+                                double* __restrict__ theta, double2* __restrict__ det,
+                                const double* __restrict__ weights, int N, int ncw, int nce,
+                                Channel c0, Channel c1, int only_live) {
+  const int w = blockIdx.x;
+  const Channel ch = blockIdx.y == 0 ? c0 : c1;
+  if (only_live && !(weights[w] > 1.0e-8)) return;
+  extern __shared__ double2 sm[];
+  const int n = ch.n, n2 = 2 * n;
+  double2* a = sm;           // [n][2n]
+  double2* fcol = sm + n * n2;  // [n]
+  __shared__ int s_piv;
+  const double2* ps = psi + (size_t)w * ncw * N + (size_t)ch.psi_off * N;
+  const double* ph = phi + (size_t)ch.col_off * N;
+  for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+    const int i = e / n, j = e % n;
+    double re = 0.0, im = 0.0;
+    for (int p = 0; p < N; ++p) {
+      const double f = ph[i * N + p];
+      const double2 v = ps[j * N + p];
+      re = fma(f, v.x, re);
+      im = fma(f, v.y, im);
+    }
+    a[i * n2 + j] = make_double2(re, im);
+    a[i * n2 + n + j] = make_double2(i == j ? 1.0 : 0.0, 0.0);
+  }
+  __syncthreads();
+  double2 detv = make_double2(1.0, 0.0);  // meaningful in thread 0
+  for (int k = 0; k < n; ++k) {
+    if (threadIdx.x < 32) {
+      double best = -1.0;
+      int bi = k;
+      for (int i = k + threadIdx.x; i < n; i += 32) {
+        const double v = cabs2(a[i * n2 + k]);
+        if (v > best) { best = v; bi = i; }
+      }
+      for (int off = 16; off > 0; off >>= 1) {
+        const double ob = __shfl_down_sync(0xffffffffu, best, off);
+        const int oi = __shfl_down_sync(0xffffffffu, bi, off);
+        if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+      }
+      if (threadIdx.x == 0) s_piv = bi;
+    }
+    __syncthreads();
+    const int pr = s_piv;
+    if (pr != k) {
+      for (int j = threadIdx.x; j < n2; j += blockDim.x) {
+        const double2 t = a[k * n2 + j];
+        a[k * n2 + j] = a[pr * n2 + j];
+        a[pr * n2 + j] = t;
+      }
+    }
+    __syncthreads();
+    const double2 pv = a[k * n2 + k];
+    if (threadIdx.x == 0) {
+      detv = cmul(detv, pv);
+      if (pr != k) detv = make_double2(-detv.x, -detv.y);
+    }
+    const double2 inv = crecip(pv);
+    for (int i = threadIdx.x; i < n; i += blockDim.x) fcol[i] = a[i * n2 + k];
+    __syncthreads();
+    for (int j = k + threadIdx.x; j < n2; j += blockDim.x) a[k * n2 + j] = cmul(a[k * n2 + j], inv);
+    __syncthreads();
+    for (int e = threadIdx.x; e < n * (n2 - k); e += blockDim.x) {
+      const int i = e / (n2 - k), j = k + e % (n2 - k);
+      if (i == k) continue;
+      a[i * n2 + j] = csub(a[i * n2 + j], cmul(fcol[i], a[k * n2 + j]));
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) det[2 * w + blockIdx.y] = detv;
+  // theta[p][j] = sum_i psi[p][i] Minv[i][j]
+  double* tre = theta + (size_t)(2 * w) * nce * N + (size_t)ch.col_off * N;
+  double* tim = tre + (size_t)nce * N;
+  for (int e = threadIdx.x; e < N * n; e += blockDim.x) {
+    const int j = e / N, p = e % N;
+    double re = 0.0, im = 0.0;
+    for (int i = 0; i < n; ++i) {
+      const double2 v = ps[i * N + p];
+      const double2 m = a[i * n2 + n + j];
+      re += v.x * m.x - v.y * m.y;
+      im += v.x * m.y + v.y * m.x;
+    }
+    tre[j * N + p] = re;
+    tim[j * N + p] = im;
+  }
+}
+
+void launch_overlap_theta(afqmc_handle* h, bool only_live) {
+  int nmax = std::max(h->chan[0].n, h->nchan > 1 ? h->chan[1].n : 0);
+  size_t smem = (size_t)nmax * 2 * nmax * sizeof(double2) + nmax * sizeof(double2);
+  static bool attr_set = false;
+  if (!attr_set) {
+    cudaFuncSetAttribute(k_overlap_theta, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    attr_set = true;
+  }
+  dim3 grid(h->nwalk, h->nchan);
+  k_overlap_theta<<<grid, 256, smem, h->stream>>>(h->psi, h->phi, h->theta, h->det, h->weights, h->N,
+                                                  h->ncw, h->nce, h->chan[0], h->chan[1],
+                                                  only_live ? 1 : 0);
+  h->launches++;
+}
+
+// overlap = prod_s det_s^mult (used after set_walkers)
+__global__ void k_init_overlap(const double2* __restrict__ det, double2* __restrict__ ovlp, int W,
+                               int nchan, int mult) {
+  const int w = blockIdx.x * blockDim.x + threadIdx.x;
+  if (w >= W) return;
+  double2 o = det[2 * w];
+  if (nchan > 1) o = cmul(o, det[2 * w + 1]);
+  if (mult == 2) o = cmul(o, o);
+  ovlp[w] = o;
+}
+
+void launch_init_overlap(afqmc_handle* h) {
+  k_init_overlap<<<(h->nwalk + 127) / 128, 128, 0, h->stream>>>(h->det, h->ovlp, h->nwalk, h->nchan,
+                                                               h->mult);
+  h->launches++;
+}
+
+// ---------------------------------------------------------------------------
+// generic SIMT GEMM  C[m][n] = sum_k A[m][k] B[n][k]  (both operands K-contiguous),
+// 64 x 64 x 16 tiles, 256 threads x (4 x 4) outputs, result passed to an epilogue.
+// ---------------------------------------------------------------------------
+template <typename T, class Epi>
+__global__ void __launch_bounds__(256) k_gemm_nt(int M, int Nn, int K, const T* __restrict__ A, int lda,
+                                                 const T* __restrict__ B, int ldb, Epi epi) {
+  constexpr int BM = 64, BN = 64, BK = 16;
+  __shared__ T As[BK][BM + 1];
+  __shared__ T Bs[BK][BN + 1];
+  const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
+  const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
+  T acc[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) acc[i][j] = T(0);
+  for (int k0 = 0; k0 < K; k0 += BK) {
+    for (int e = threadIdx.x; e < BM * BK; e += 256) {
+      const int mm = e / BK, kk = e % BK;
+      const int gm = m0 + mm, gk = k0 + kk;
+      As[kk][mm] = (gm < M && gk < K) ? A[(size_t)gm * lda + gk] : T(0);
+      const int gn = n0 + mm;
+      Bs[kk][mm] = (gn < Nn && gk < K) ? B[(size_t)gn * ldb + gk] : T(0);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < BK; ++kk) {
+      T a[4], b[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) a[i] = As[kk][ty + 16 * i];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) b[j] = Bs[kk][tx + 16 * j];
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] = fma_t(a[i], b[j], acc[i][j]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int m = m0 + ty + 16 * i, n = n0 + tx + 16 * j;
+      if (m < M && n < Nn) epi(m, n, acc[i][j]);
+    }
+}
+
+struct EpiScale {
+  double* C;
+  int ldc;
+  double alpha;
+  __device__ void operator()(int m, int n, double v) const { C[(size_t)m * ldc + n] = alpha * v; }
+};
+
+// VHS epilogue: GEMM row m = (walker, plane) with plane 0 = L.Re(x) (propr) and
+// plane 1 = L.Im(x) (propi), column = packed index t = (i, j).  Writes the full
+// symmetric V = sqrt(dt) (i propr - propi) (DQMCWalker.cpp:406-421, :461-462).
+template <typename T>
+struct EpiVHS {
+  double* V;
+  const int2* tri;
+  int N, nspV, s;
+  double sdt;
+  __device__ void operator()(int m, int n, T v) const {
+    const int w = m >> 1, plane = m & 1;
+    const int2 ij = tri[n];
+    const double dv = (double)v;
+    const double val = plane == 0 ? sdt * dv : -(sdt * dv);
+    double* Vb = V + ((size_t)(w * nspV + s) * 2 + (plane == 0 ? 1 : 0)) * N * N;
+    Vb[(size_t)ij.y * N + ij.x] = val;
+    Vb[(size_t)ij.x * N + ij.y] = val;
+  }
+};
+
+// force bias: fb[(w, plane)][g] = mult * sum_k theta[(w, plane)][k] rot[g][k]   (RHF.cpp:42-61)
+void launch_force_bias(afqmc_handle* h) {
+  const int M = 2 * h->nwalk, Nn = h->G, K = h->nce * h->N;
+  dim3 grid((Nn + 63) / 64, (M + 63) / 64);
+  EpiScale epi{h->fb, h->G, (double)h->mult};
+  k_gemm_nt<double, EpiScale><<<grid, 256, 0, h->stream>>>(M, Nn, K, h->theta, K, h->rot, K, epi);
+  h->launches++;
+}
+
+void launch_vhs(afqmc_handle* h) {
+  const int M = 2 * h->nwalk, Nn = h->T, K = h->G;
+  dim3 grid((Nn + 63) / 64, (M + 63) / 64);
+  const double sdt = sqrt(h->dt);
+  for (int s = 0; s < h->nspV; ++s) {
+    if (h->precision == AFQMC_PREC_REF32) {
+      EpiVHS<float> epi{h->V, h->tri, h->N, h->nspV, s, sdt};
+      k_gemm_nt<float, EpiVHS<float>><<<grid, 256, 0, h->stream>>>(M, Nn, K, h->x32, K,
+                                                                   h->LT32 + (size_t)s * h->T * h->G, K, epi);
+    } else {
+      EpiVHS<double> epi{h->V, h->tri, h->N, h->nspV, s, sdt};
+      k_gemm_nt<double, EpiVHS<double>><<<grid, 256, 0, h->stream>>>(M, Nn, K, h->x, K,
+                                                                     h->LT + (size_t)s * h->T * h->G, K, epi);
+    }
+    h->launches++;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// shifted fields (DQMCWalker.cpp:451-457):  s_g = -sqrt(dt)(i fb_g - mf_g),
+// x_g = xi_g - s_g, shift = sum_g x_g mf_g, fbTerm = sum_g (xi_g s_g - s_g^2 / 2).
+// One CTA per walker; xi from host memory or from the device Philox stream.
+// ---------------------------------------------------------------------------
+__global__ void k_fields(const double* __restrict__ fb, const double2* __restrict__ mf,
+                         const double* __restrict__ xi, double* __restrict__ x, float* __restrict__ x32,
+                         double2* __restrict__ shift, double2* __restrict__ fbterm,
+                         const double* __restrict__ weights, int G, double sdt, int use_rng,
+                         uint64_t seed, uint64_t step, int write32) {
+  const int w = blockIdx.x;
+  const bool live = weights[w] > 1.0e-8;
+  double shr = 0.0, shi = 0.0, ftr = 0.0, fti = 0.0;
+  const double* fbr = fb + (size_t)(2 * w) * G;
+  const double* fbi = fbr + G;
+  double* xr_out = x + (size_t)(2 * w) * G;
+  double* xi_out = xr_out + G;
+  for (int g = threadIdx.x; g < G; g += blockDim.x) {
+    const double xg = use_rng ? philox_normal(seed, step, (uint32_t)w, (uint32_t)g)
+                              : xi[(size_t)w * G + g];
+    const double2 m = mf[g];
+    const double fsr = -sdt * (-fbi[g] - m.x);
+    const double fsi = -sdt * (fbr[g] - m.y);
+    double xr = xg - fsr, xim = -fsi;
+    shr += xr * m.x - xim * m.y;
+    shi += xr * m.y + xim * m.x;
+    ftr += xg * fsr - 0.5 * (fsr * fsr - fsi * fsi);
+    fti += xg * fsi - 0.5 * (2.0 * fsr * fsi);
+    if (!live) { xr = 0.0; xim = 0.0; }
+    xr_out[g] = xr;
+    xi_out[g] = xim;
+    if (write32) {
+      x32[(size_t)(2 * w) * G + g] = (float)xr;
+      x32[(size_t)(2 * w + 1) * G + g] = (float)xim;
+    }
+  }
+  shr = block_sum(shr);
+  shi = block_sum(shi);
+  ftr = block_sum(ftr);
+  fti = block_sum(fti);
+  if (threadIdx.x == 0) {
+    shift[w] = make_double2(shr, shi);
+    fbterm[w] = make_double2(ftr, fti);
+  }
+}
+
+void launch_fields(afqmc_handle* h, bool device_rng) {
+  k_fields<<<h->nwalk, 256, 0, h->stream>>>(h->fb, h->mf, h->xi, h->x, h->x32, h->shift, h->fbterm,
+                                            h->weights, h->G, sqrt(h->dt), device_rng ? 1 : 0, h->seed,
+                                            h->step_counter, h->precision == AFQMC_PREC_REF32 ? 1 : 0);
+  h->launches++;
+}
+
+// ---------------------------------------------------------------------------
+// propagator (DQMCWalker.cpp:424-431, :482-491, :537-543):
+//   psi <- B (sum_{k=0}^{5} V^k / k!) B psi, the series by temp = V temp / k.
+// One CTA per (walker, column chunk); the Taylor recurrence is column-wise, so
+// a chunk keeps its columns in shared memory and streams B and V from L2.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void cmat_apply(const double* __restrict__ Mr, const double* __restrict__ Mi,
+                                           const double2* __restrict__ Mc, const double2* in,
+                                           double2* out, int N, int nc, double scale) {
+  // out[j][p] = scale * sum_q M(p, q) in[j][q]; M column-major (M(p,q) at q*N + p)
+  for (int p = threadIdx.x; p < N; p += blockDim.x) {
+    double2 acc[PROP_CH];
+#pragma unroll
+    for (int j = 0; j < PROP_CH; ++j) acc[j] = make_double2(0.0, 0.0);
+    for (int q = 0; q < N; ++q) {
+      double2 m;
+      if (Mc) m = Mc[(size_t)q * N + p];
+      else m = make_double2(Mr[(size_t)q * N + p], Mi[(size_t)q * N + p]);
+#pragma unroll
+      for (int j = 0; j < PROP_CH; ++j)
+        if (j < nc) acc[j] = cfma(m, in[j * N + q], acc[j]);
+    }
+#pragma unroll
+    for (int j = 0; j < PROP_CH; ++j)
+      if (j < nc) out[j * N + p] = make_double2(acc[j].x * scale, acc[j].y * scale);
+  }
+}
+
+__global__ void k_propagate(double2* __restrict__ psi, const double* __restrict__ V,
+                            const double2* __restrict__ expm, const double* __restrict__ weights,
+                            const PropChunk* __restrict__ chunks, int N, int ncw, int nspV, int nspB) {
+  const int w = blockIdx.x;
+  if (!(weights[w] > 1.0e-8)) return;
+  const PropChunk c = chunks[blockIdx.y];
+  extern __shared__ double2 sm[];
+  double2* cur = sm;
+  double2* nxt = sm + N * PROP_CH;
+  double2* acc = sm + 2 * N * PROP_CH;
+  const int nc = c.nc;
+  const double2* B = expm + (size_t)(nspB == 1 ? 0 : c.spin) * N * N;
+  const double* Vr = V + ((size_t)(w * nspV + (nspV == 1 ? 0 : c.spin)) * 2) * N * N;
+  const double* Vi = Vr + (size_t)N * N;
+  double2* ps = psi + (size_t)w * ncw * N + (size_t)c.c0 * N;
+  for (int e = threadIdx.x; e < N * nc; e += blockDim.x) cur[e] = ps[e];
+  __syncthreads();
+  cmat_apply(nullptr, nullptr, B, cur, nxt, N, nc, 1.0);
+  __syncthreads();
+  for (int e = threadIdx.x; e < N * nc; e += blockDim.x) acc[e] = nxt[e];
+  __syncthreads();
+  double2* t = cur; cur = nxt; nxt = t;
+  for (int k = 1; k <= 5; ++k) {
+    cmat_apply(Vr, Vi, nullptr, cur, nxt, N, nc, 1.0 / k);
+    __syncthreads();
+    for (int e = threadIdx.x; e < N * nc; e += blockDim.x) acc[e] = cadd(acc[e], nxt[e]);
+    __syncthreads();
+    t = cur; cur = nxt; nxt = t;
+  }
+  cmat_apply(nullptr, nullptr, B, acc, nxt, N, nc, 1.0);
+  __syncthreads();
+  for (int e = threadIdx.x; e < N * nc; e += blockDim.x) ps[e] = nxt[e];
+}
+
+
+// ---------------------------------------------------------------------------
+// weights (DQMCWalker.cpp:495-502, MixedEstimator.cpp:461-475): importance
+// function, phaseless projection, cap, sum of weights, next eshift.  One CTA.
+// ---------------------------------------------------------------------------
+__global__ void k_weights(double* __restrict__ weights, double2* __restrict__ ovlp,
+                          const double2* __restrict__ det, const double2* __restrict__ shift,
+                          const double2* __restrict__ fbterm, double* __restrict__ scal, int W, int nchan,
+                          int mult, double dt, double c0r, double c0i, double cap, double target) {
+  const double eshift = scal[S_ESHIFT];
+  const double sdt = sqrt(dt);
+  double sumw = 0.0;
+  double ncap = 0.0;
+  for (int w = threadIdx.x; w < W; w += blockDim.x) {
+    double wt = weights[w];
+    if (wt > 1.0e-8) {
+      double2 on = det[2 * w];
+      if (nchan > 1) on = cmul(on, det[2 * w + 1]);
+      if (mult == 2) on = cmul(on, on);
+      const double2 ratio = cdiv(on, ovlp[w]);
+      const double2 sh = shift[w], ft = fbterm[w];
+      const double2 ex = make_double2(-sdt * sh.x + ft.x + dt * (eshift + c0r), -sdt * sh.y + ft.y + dt * c0i);
+      const double2 imp = cmul(cexp_d(ex), ratio);
+      const double2 ph = cmul(cexp_d(make_double2(-sdt * sh.x, -sdt * sh.y)), ratio);
+      const double th = atan2(ph.y, ph.x);
+      double val = hypot(imp.x, imp.y) * cos(th);
+      if (val < 1.0e-3 || val > 100.0 || isnan(val)) val = 0.0;
+      wt *= val;
+      if (wt > cap) { wt = 0.0; ncap += 1.0; }
+      weights[w] = wt;
+      ovlp[w] = on;
+    }
+    sumw += wt;
+  }
+  sumw = block_sum(sumw);
+  ncap = block_sum(ncap);
+  if (threadIdx.x == 0) {
+    scal[S_SUMW] = sumw;
+    scal[S_NCAP] += ncap;
+    scal[S_ESHIFT] = scal[S_EEST] - 0.1 * log(sumw / target) / dt;
+  }
+}
+
+void launch_weights(afqmc_handle* h) {
+  const double cr = h->prop_constant.real(), ci = h->prop_constant.imag();
+  k_weights<<<1, 1024, 0, h->stream>>>(h->weights, h->ovlp, h->det, h->shift, h->fbterm, h->scal, h->nwalk,
+                                       h->nchan, h->mult, h->dt, cr, ci, h->weight_cap, h->pop_target);
+  h->launches++;
+}
+
+// ---------------------------------------------------------------------------
+// Householder QR with Eigen's conventions (DQMCWalker.cpp:295-326 calls
+// HouseholderQR; reflector of column k: beta = -sign(Re c0) ||x||,
+// tau = conj((beta - c0) / beta), v = [1, x_tail / (c0 - beta)], a tail of
+// squared norm <= DBL_MIN with Im(c0)^2 <= DBL_MIN gives tau = 0, beta = Re c0).
+// psi <- Q = prod_k (I - conj(tau_k) v_k v_k^H) I,  overlap /= prod beta_k.
+// One CTA per walker; columns are worked in place in global memory (L2).
+// ---------------------------------------------------------------------------
+__global__ void k_ortho(double2* __restrict__ psi, double2* __restrict__ qwork, double2* __restrict__ ovlp,
+                        int N, int ncw, int na, int nb, int rhf_walker) {
+  const int w = blockIdx.x;
+  __shared__ double2 s_tau[QR_MAXN];
+  __shared__ double s_beta[QR_MAXN];
+  __shared__ double2 s_scale;
+  __shared__ int s_zero;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  double2 fac = make_double2(1.0, 0.0);
+  const int nblk = rhf_walker ? 1 : 2;
+  for (int b = 0; b < nblk; ++b) {
+    const int off = b == 0 ? 0 : na, n = b == 0 ? na : nb;
+    double2* A = psi + (size_t)w * ncw * N + (size_t)off * N;
+    double2* Q = qwork + (size_t)w * ncw * N + (size_t)off * N;
+    for (int k = 0; k < n; ++k) {
+      double2* col = A + (size_t)k * N;
+      double t = 0.0;
+      for (int i = k + 1 + threadIdx.x; i < N; i += blockDim.x) t += cabs2(col[i]);
+      const double tail = block_sum(t);
+      if (threadIdx.x == 0) {
+        const double2 c0 = col[k];
+        const double tiny = 2.2250738585072014e-308;
+        if (tail <= tiny && c0.y * c0.y <= tiny) {
+          s_tau[k] = make_double2(0.0, 0.0);
+          s_beta[k] = c0.x;
+          s_zero = 1;
+        } else {
+          double beta = sqrt(cabs2(c0) + tail);
+          if (c0.x >= 0.0) beta = -beta;
+          s_beta[k] = beta;
+          s_scale = crecip(make_double2(c0.x - beta, c0.y));
+          const double2 tb = make_double2((beta - c0.x) / beta, -c0.y / beta);
+          s_tau[k] = make_double2(tb.x, -tb.y);
+          s_zero = 0;
+        }
+      }
+      __syncthreads();
+      const int zero = s_zero;
+      const double2 sc = s_scale;
+      for (int i = k + 1 + threadIdx.x; i < N; i += blockDim.x)
+        col[i] = zero ? make_double2(0.0, 0.0) : cmul(col[i], sc);
+      __syncthreads();
+      if (threadIdx.x == 0) col[k] = make_double2(s_beta[k], 0.0);
+      const double2 tau = s_tau[k];
+      if (!zero) {
+        for (int j = k + 1 + warp; j < n; j += nwarps) {
+          double2* cj = A + (size_t)j * N;
+          double2 d = make_double2(0.0, 0.0);
+          for (int i = k + 1 + lane; i < N; i += 32) d = cfma(cconj(col[i]), cj[i], d);
+          d = warp_sum2(d);
+          const double2 dot = cadd(cj[k], d);
+          const double2 td = cmul(tau, dot);
+          __syncwarp();
+          if (lane == 0) cj[k] = csub(cj[k], td);
+          for (int i = k + 1 + lane; i < N; i += 32) cj[i] = csub(cj[i], cmul(col[i], td));
+        }
+      }
+      __syncthreads();
+    }
+    // Q = H_0' ... H_{n-1}' I  with H_k' = I - conj(tau_k) v_k v_k^H
+    for (int e = threadIdx.x; e < N * n; e += blockDim.x) {
+      const int j = e / N, i = e % N;
+      Q[(size_t)j * N + i] = make_double2(i == j ? 1.0 : 0.0, 0.0);
+    }
+    __syncthreads();
+    for (int k = n - 1; k >= 0; --k) {
+      const double2 ct = cconj(s_tau[k]);
+      if (ct.x == 0.0 && ct.y == 0.0) continue;
+      const double2* v = A + (size_t)k * N;  // v[k] = 1 implicitly, v[i > k] stored
+      for (int j = k + warp; j < n; j += nwarps) {
+        double2* qj = Q + (size_t)j * N;
+        double2 d = make_double2(0.0, 0.0);
+        for (int i = k + 1 + lane; i < N; i += 32) d = cfma(cconj(v[i]), qj[i], d);
+        d = warp_sum2(d);
+        const double2 dot = cadd(qj[k], d);
+        const double2 td = cmul(ct, dot);
+        __syncwarp();
+        if (lane == 0) qj[k] = csub(qj[k], td);
+        for (int i = k + 1 + lane; i < N; i += 32) qj[i] = csub(qj[i], cmul(v[i], td));
+      }
+      __syncthreads();
+    }
+    for (int e = threadIdx.x; e < N * n; e += blockDim.x) A[e] = Q[e];
+    __syncthreads();
+    if (threadIdx.x == 0)
+      for (int k = 0; k < n; ++k) fac = cmul(fac, make_double2(s_beta[k], 0.0));
+  }
+  if (threadIdx.x == 0) {
+    if (rhf_walker) fac = cmul(fac, fac);
+    ovlp[w] = cdiv(ovlp[w], fac);
+  }
+}
+
+void launch_ortho(afqmc_handle* h) {
+  k_ortho<<<h->nwalk, 256, 0, h->stream>>>(h->psi, h->qwork, h->ovlp, h->N, h->ncw, h->na, h->nb,
+                                           h->rhf_walker);
+  h->launches++;
+}
+
+// ---------------------------------------------------------------------------
+// local energy (RHF.cpp:70-131, UHF.cpp:75-140):
+//   E = ecore + mult sum_s sum_{p,i} theta_s[p,i] (h1 Phi_s)[p,i]
+//       + 1/2 sum_{g < ncholEne} [(mult sum_s c_sg)^2 - mult sum_s sum_ij f_sg[i,j] f_sg[j,i]]
+// f_sg = rot_s[g] theta_s (n x n), c_sg = tr f_sg.  One CTA per (walker, g chunk).
+// ---------------------------------------------------------------------------
+__global__ void k_energy(const double* __restrict__ theta, const double* __restrict__ rot,
+                         double2* __restrict__ epart, int N, int nce, int Gene, int gper, int nechunk,
+                         Channel c0, Channel c1, int nchan, int mult) {
+  const int w = blockIdx.x;
+  const int gs = blockIdx.y * gper, ge = min(Gene, gs + gper);
+  extern __shared__ double2 sm[];
+  double2* th = sm;                                   // [nce*N]
+  double2* f = sm + (size_t)nce * N;                  // [nchan][nmax*nmax]
+  const int nmax = max(c0.n, nchan > 1 ? c1.n : 0);
+  const double* tre = theta + (size_t)(2 * w) * nce * N;
+  const double* tim = tre + (size_t)nce * N;
+  for (int e = threadIdx.x; e < nce * N; e += blockDim.x) th[e] = make_double2(tre[e], tim[e]);
+  __syncthreads();
+  double2 xacc = make_double2(0.0, 0.0);  // sum of f[i][j] f[j][i] over this thread's entries
+  double2 coul = make_double2(0.0, 0.0);  // thread 0: sum_g (mult sum_s c_sg)^2
+  for (int g = gs; g < ge; ++g) {
+    const double* rg = rot + (size_t)g * nce * N;
+    for (int s = 0; s < nchan; ++s) {
+      const Channel ch = s == 0 ? c0 : c1;
+      const int n = ch.n;
+      for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+        const int i = e / n, j = e % n;
+        const double* r = rg + (size_t)(ch.col_off + i) * N;
+        const double2* t = th + (size_t)(ch.col_off + j) * N;
+        double re = 0.0, im = 0.0;
+        for (int p = 0; p < N; ++p) {
+          re = fma(r[p], t[p].x, re);
+          im = fma(r[p], t[p].y, im);
+        }
+        f[s * nmax * nmax + i * n + j] = make_double2(re, im);
+      }
+    }
+    __syncthreads();
+    for (int s = 0; s < nchan; ++s) {
+      const int n = s == 0 ? c0.n : c1.n;
+      const double2* fs = f + s * nmax * nmax;
+      for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+        const int i = e / n, j = e % n;
+        xacc = cfma(fs[i * n + j], fs[j * n + i], xacc);
+      }
+    }
+    if (threadIdx.x == 0) {
+      double2 c = make_double2(0.0, 0.0);
+      for (int s = 0; s < nchan; ++s) {
+        const int n = s == 0 ? c0.n : c1.n;
+        for (int i = 0; i < n; ++i) c = cadd(c, f[s * nmax * nmax + i * n + i]);
+      }
+      c = make_double2(mult * c.x, mult * c.y);
+      coul = cfma(c, c, coul);
+    }
+    __syncthreads();
+  }
+  xacc.x = block_sum(xacc.x);
+  xacc.y = block_sum(xacc.y);
+  if (threadIdx.x == 0)
+    epart[(size_t)w * nechunk + blockIdx.y] =
+        make_double2(0.5 * (coul.x - mult * xacc.x), 0.5 * (coul.y - mult * xacc.y));
+}
+
+__global__ void k_energy_final(const double* __restrict__ theta, const double* __restrict__ h1phi,
+                               const double2* __restrict__ epart, double2* __restrict__ eloc, int N, int nce,
+                               int nechunk, int mult, double ecore) {
+  const int w = blockIdx.x;
+  const double* tre = theta + (size_t)(2 * w) * nce * N;
+  const double* tim = tre + (size_t)nce * N;
+  double re = 0.0, im = 0.0;
+  for (int k = threadIdx.x; k < nce * N; k += blockDim.x) {
+    re += tre[k] * h1phi[k];
+    im += tim[k] * h1phi[k];
+  }
+  re = block_sum(re);
+  im = block_sum(im);
+  if (threadIdx.x == 0) {
+    double2 e = make_double2(ecore + mult * re, mult * im);
+    for (int c = 0; c < nechunk; ++c) e = cadd(e, epart[(size_t)w * nechunk + c]);
+    eloc[w] = e;
+  }
+}
+
+void launch_local_energy(afqmc_handle* h) {
+  const int nmax = std::max(h->chan[0].n, h->nchan > 1 ? h->chan[1].n : 0);
+  const size_t smem = ((size_t)h->nce * h->N + (size_t)h->nchan * nmax * nmax) * sizeof(double2);
+  static bool attr_set = false;
+  if (!attr_set) {
+    cudaFuncSetAttribute(k_energy, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
+    attr_set = true;
+  }
+  const int gper = (h->nchol_ene + h->nechunk - 1) / h->nechunk;
+  dim3 grid(h->nwalk, h->nechunk);
+  k_energy<<<grid, 256, smem, h->stream>>>(h->theta, h->rot, h->epart, h->N, h->nce, h->nchol_ene, gper,
+                                           h->nechunk, h->chan[0], h->chan[1], h->nchan, h->mult);
+  k_energy_final<<<h->nwalk, 256, 0, h->stream>>>(h->theta, h->h1phi, h->epart, h->eloc, h->N, h->nce,
+                                                  h->nechunk, h->mult, h->ecore);
+  h->launches += 2;
+}
+
+void launch_propagate(afqmc_handle* h) {
+  const size_t smem = 3 * (size_t)h->N * PROP_CH * sizeof(double2);
+  static bool attr_set = false;
+  if (!attr_set) {
+    cudaFuncSetAttribute(k_propagate, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    attr_set = true;
+  }
+  const int threads = std::min(256, ((h->N + 31) / 32) * 32);
+  dim3 grid(h->nwalk, h->nchunks);
+  k_propagate<<<grid, threads, smem, h->stream>>>(h->psi, h->V, h->expm, h->weights, h->d_chunks, h->N, h->ncw,
+                                                  h->nspV, h->nsp);
+  h->launches++;
+}
+
+}  // namespace afqmc
