@@ -135,6 +135,18 @@ int upload(afqmc_handle* h, T* d, const std::vector<T>& v) {
   return AFQMC_OK;
 }
 
+// code left by a bounded device wait that gave up (kernels set it, never trap)
+int device_error(afqmc_handle* h) {
+  int e = 0;
+  CK(cudaMemcpy(&e, h->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+  if (e != 0) {
+    h->err = "a tensor-core pipeline wait timed out (stage code " + std::to_string(e) + ")";
+    cudaMemset(h->d_err, 0, sizeof(int));
+    return AFQMC_ERR_TIMEOUT;
+  }
+  return AFQMC_OK;
+}
+
 __global__ void k_set_scalar(double* p, int idx, double v) { p[idx] = v; }
 __global__ void k_fill(double* p, size_t n, double v) {
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) p[i] = v;
@@ -157,7 +169,8 @@ void stage_end(afqmc_handle* h, int st, cudaEvent_t ev0) {
 void release(afqmc_handle* h) {
   void* ptrs[] = {h->psi, h->phi, h->rot, h->h1phi, h->LT, h->LT32, h->tri, h->expm, h->mf, h->theta,
                   h->det, h->ovlp, h->weights, h->fb, h->xi, h->x, h->x32, h->shift, h->fbterm, h->V,
-                  h->qwork, h->epart, h->eloc, h->scal, h->d_chunks};
+                  h->qwork, h->epart, h->eloc, h->scal, h->d_chunks, h->d_err, h->rotA, h->LTA,
+                  h->thetaB, h->xB, h->fb32, h->V32, h->expm32, h->d_chunks32};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (h->host_pinned) cudaFreeHost(h->host_pinned);
@@ -202,8 +215,6 @@ int afqmc_create(const afqmc_ham* ham, const afqmc_trial* trial, const afqmc_opt
   if (ham->int_type == AFQMC_INT_U && (opts->rhf_walker || trial->kind != AFQMC_TRIAL_UHF))
     return fail(nullptr, AFQMC_ERR_UNSUPPORTED, "intType u runs the UHF walker with a UHF trial (UHF.cpp)");
   if (std::max(na, nb) > 128) return fail(nullptr, AFQMC_ERR_UNSUPPORTED, "nocc > 128");
-  if (opts->precision == AFQMC_PREC_MIXED)
-    return fail(nullptr, AFQMC_ERR_UNSUPPORTED, "mixed precision is provided by afqmc_create_mixed");
 
   afqmc_handle* h = new afqmc_handle();
   h->N = N; h->na = na; h->nb = nb; h->G = G; h->T = N * (N + 1) / 2;
@@ -381,7 +392,15 @@ int afqmc_create(const afqmc_ham* ham, const afqmc_trial* trial, const afqmc_opt
       for (int c = 0; c < n; c += afqmc::PROP_CH) h->chunks.push_back(PropChunk{off + c, std::min(afqmc::PROP_CH, n - c), b});
     }
     h->nchunks = (int)h->chunks.size();
+    for (int b = 0; b < nblk; ++b) {
+      const int off = b == 0 ? 0 : na, n = b == 0 ? na : nb;
+      for (int c = 0; c < n; c += 16) h->chunks32.push_back(PropChunk{off + c, std::min(16, n - c), b});
+    }
+    h->nchunks32 = (int)h->chunks32.size();
   }
+  const bool mixed = h->precision == AFQMC_PREC_MIXED;
+  h->kf_pad = (3 * h->nce * N + 63) / 64 * 64;
+  h->kv_pad = (3 * G + 63) / 64 * 64;
   h->nechunk = std::max(1, std::min(G, (4 * 152 + h->nwalk - 1) / h->nwalk));
 
   // --- device buffers ---
@@ -411,7 +430,18 @@ int afqmc_create(const afqmc_ham* ham, const afqmc_trial* trial, const afqmc_opt
   ALLOC(x, W * 2 * G);
   ALLOC(shift, W);
   ALLOC(fbterm, W);
-  ALLOC(V, W * h->nspV * 2 * NN);
+  if (!mixed) ALLOC(V, W * h->nspV * 2 * NN);
+  ALLOC(d_err, 1);
+  if (mixed) {
+    ALLOC(rotA, (size_t)G * h->kf_pad);
+    ALLOC(LTA, (size_t)nsp * T * h->kv_pad);
+    ALLOC(thetaB, W * 2 * h->kf_pad);
+    ALLOC(xB, W * 2 * h->kv_pad);
+    ALLOC(fb32, W * 2 * G);
+    ALLOC(V32, W * h->nspV * 2 * NN);
+    ALLOC(expm32, (size_t)nsp * 2 * NN);
+    ALLOC(d_chunks32, h->chunks32.size());
+  }
   ALLOC(qwork, W * h->ncw * N);
   ALLOC(epart, W * h->nechunk);
   ALLOC(eloc, W);
@@ -441,6 +471,28 @@ int afqmc_create(const afqmc_ham* ham, const afqmc_trial* trial, const afqmc_opt
   UP(expm, expm2);
   UP(mf, mf2);
   UP(d_chunks, h->chunks);
+  if (mixed) {
+    std::vector<float> e32((size_t)nsp * 2 * NN);
+    for (int s = 0; s < nsp; ++s)
+      for (size_t e = 0; e < NN; ++e) {
+        e32[(size_t)s * 2 * NN + e] = (float)expm_cm[(size_t)s * NN + e].real();
+        e32[(size_t)s * 2 * NN + NN + e] = (float)expm_cm[(size_t)s * NN + e].imag();
+      }
+    UP(expm32, e32);
+    UP(d_chunks32, h->chunks32);
+    ce = cudaMemsetAsync(h->xB, 0, W * 2 * h->kv_pad * sizeof(__nv_bfloat16), h->stream);
+    if (ce == cudaSuccess) ce = cudaMemsetAsync(h->thetaB, 0, W * 2 * h->kf_pad * sizeof(__nv_bfloat16), h->stream);
+    if (ce != cudaSuccess || !afqmc::setup_mixed(h)) {
+      g_create_err = ce != cudaSuccess ? cudaGetErrorString(ce) : "tensor map encoding failed";
+      release(h);
+      delete h;
+      return AFQMC_ERR_CUDA;
+    }
+  }
+  {
+    ce = cudaMemsetAsync(h->d_err, 0, sizeof(int), h->stream);
+    if (ce != cudaSuccess) { g_create_err = cudaGetErrorString(ce); release(h); delete h; return AFQMC_ERR_CUDA; }
+  }
   std::vector<double> sc(afqmc::S_NSLOTS, 0.0);
   UP(scal, sc);
   // walkers start at the trial determinant with unit weight
@@ -536,6 +588,7 @@ int afqmc_get_walkers(afqmc_handle* h, double* dets, double* overlaps, double* w
   const int N = h->N, na = h->na, nb = h->nb;
   const size_t W = h->nwalk, ser = (size_t)N * (na + nb);
   CK(cudaStreamSynchronize(h->stream));
+  if (int rc = device_error(h)) return rc;
   if (dets) {
     std::vector<double2> p((size_t)W * h->ncw * N);
     CK(cudaMemcpy(p.data(), h->psi, p.size() * sizeof(double2), cudaMemcpyDeviceToHost));
@@ -566,12 +619,23 @@ int afqmc_get_walkers(afqmc_handle* h, double* dets, double* overlaps, double* w
 int afqmc_force_bias(afqmc_handle* h, double* fb) {
   if (!h || !fb) return fail(h, AFQMC_ERR_ARG, "null argument");
   cudaSetDevice(h->device);
-  afqmc::launch_force_bias(h);
-  int rc = after_launch(h, "force_bias");
-  if (rc) return rc;
   std::vector<double> buf((size_t)h->nwalk * 2 * h->G);
-  CK(cudaMemcpyAsync(buf.data(), h->fb, buf.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
-  CK(cudaStreamSynchronize(h->stream));
+  if (h->precision == AFQMC_PREC_MIXED) {
+    afqmc::launch_force_bias_mixed(h);
+    int rc = after_launch(h, "force_bias");
+    if (rc) return rc;
+    std::vector<float> b32(buf.size());
+    CK(cudaMemcpyAsync(b32.data(), h->fb32, b32.size() * sizeof(float), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    for (size_t e = 0; e < buf.size(); ++e) buf[e] = b32[e];
+    if ((rc = device_error(h))) return rc;
+  } else {
+    afqmc::launch_force_bias(h);
+    int rc = after_launch(h, "force_bias");
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(buf.data(), h->fb, buf.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+  }
   for (int w = 0; w < h->nwalk; ++w)
     for (int g = 0; g < h->G; ++g) {
       fb[2 * ((size_t)w * h->G + g)] = buf[(size_t)(2 * w) * h->G + g];
@@ -596,16 +660,21 @@ int afqmc_step(afqmc_handle* h, const double* xi, const double* eshift) {
   }
   cudaEvent_t e0;
   stage_begin(h, afqmc::ST_FB, &e0);
-  afqmc::launch_force_bias(h);
+  const bool mixed = h->precision == AFQMC_PREC_MIXED;
+  if (mixed) afqmc::launch_force_bias_mixed(h);
+  else afqmc::launch_force_bias(h);
   stage_end(h, afqmc::ST_FB, e0);
   stage_begin(h, afqmc::ST_FIELDS, &e0);
-  afqmc::launch_fields(h, xi == nullptr);
+  if (mixed) afqmc::launch_fields_mixed(h, xi == nullptr);
+  else afqmc::launch_fields(h, xi == nullptr);
   stage_end(h, afqmc::ST_FIELDS, e0);
   stage_begin(h, afqmc::ST_VHS, &e0);
-  afqmc::launch_vhs(h);
+  if (mixed) afqmc::launch_vhs_mixed(h);
+  else afqmc::launch_vhs(h);
   stage_end(h, afqmc::ST_VHS, e0);
   stage_begin(h, afqmc::ST_PROP, &e0);
-  afqmc::launch_propagate(h);
+  if (mixed) afqmc::launch_propagate_mixed(h);
+  else afqmc::launch_propagate(h);
   stage_end(h, afqmc::ST_PROP, e0);
   stage_begin(h, afqmc::ST_OVERLAP, &e0);
   afqmc::launch_overlap_theta(h, true);
@@ -634,6 +703,7 @@ int afqmc_population(afqmc_handle* h, double* sum_w, double* eshift_next, long* 
   cudaSetDevice(h->device);
   double sc[afqmc::S_NSLOTS];
   CK(cudaStreamSynchronize(h->stream));
+  if (int rc = device_error(h)) return rc;
   CK(cudaMemcpy(sc, h->scal, sizeof(sc), cudaMemcpyDeviceToHost));
   if (sum_w) *sum_w = sc[afqmc::S_SUMW];
   if (eshift_next) *eshift_next = sc[afqmc::S_ESHIFT];
@@ -753,7 +823,7 @@ int afqmc_sync(afqmc_handle* h) {
   cudaSetDevice(h->device);
   CK(cudaStreamSynchronize(h->stream));
   CK(cudaGetLastError());
-  return AFQMC_OK;
+  return device_error(h);
 }
 
 }  // extern "C"

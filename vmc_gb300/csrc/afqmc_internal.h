@@ -1,5 +1,7 @@
 // Internal declarations shared by the C-ABI layer and the kernels.
 #pragma once
+#include <cuda.h>
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -48,7 +50,7 @@ struct afqmc_handle {
   int ncw = 0;          // walker det columns (na, or na + nb)
   int nchan = 0, mult = 1, nce = 0;
   afqmc::Channel chan[2];
-  std::vector<afqmc::PropChunk> chunks;
+  std::vector<afqmc::PropChunk> chunks, chunks32;
   int nspV = 1;         // distinct VHS matrices per walker (1 for INT_R, 2 for INT_U)
   double dt = 0, ecore = 0, weight_cap = 0, pop_target = 0;
   uint64_t seed = 0, step_counter = 0;
@@ -96,6 +98,20 @@ struct afqmc_handle {
   int nechunk = 0;
   afqmc::PropChunk* d_chunks = nullptr;
   int nchunks = 0;
+
+  // mixed-precision form
+  int* d_err = nullptr;              // error code of bounded device waits (0 = none)
+  int kf_pad = 0, kv_pad = 0;        // padded split-K lengths of the force-bias / VHS GEMMs
+  __nv_bfloat16* rotA = nullptr;     // [G][kf_pad]       [hi | hi | lo] of rot
+  __nv_bfloat16* LTA = nullptr;      // [nsp][T][kv_pad]  [hi | hi | lo] of LT
+  __nv_bfloat16* thetaB = nullptr;   // [2W][kf_pad]      [hi | lo | hi] of theta planes
+  __nv_bfloat16* xB = nullptr;       // [2W][kv_pad]      [hi | lo | hi] of field planes
+  float* fb32 = nullptr;             // [W][2][G]
+  float* V32 = nullptr;              // [W][nspV][2][N*N]
+  float* expm32 = nullptr;           // [nsp][2][N*N]     re / im planes, column-major
+  afqmc::PropChunk* d_chunks32 = nullptr;
+  int nchunks32 = 0;
+  CUtensorMap tm_rot, tm_theta, tm_x, tm_LT[2];
 };
 
 namespace afqmc {
@@ -110,6 +126,13 @@ void launch_weights(afqmc_handle* h);
 void launch_ortho(afqmc_handle* h);
 void launch_local_energy(afqmc_handle* h);
 void launch_init_overlap(afqmc_handle* h);
+
+// ---- kernels (kernels_mixed.cu) ----
+bool setup_mixed(afqmc_handle* h);
+void launch_force_bias_mixed(afqmc_handle* h);
+void launch_fields_mixed(afqmc_handle* h, bool device_rng);
+void launch_vhs_mixed(afqmc_handle* h);
+void launch_propagate_mixed(afqmc_handle* h);
 
 // error helper used by kernels' launchers
 bool check_launch(afqmc_handle* h, const char* what);

@@ -1,0 +1,327 @@
+// Mixed-precision form of the step: the two Cholesky contractions on tcgen05
+// tensor cores with split-BF16 operands, the propagator in FP32, and the FP64
+// kernels (overlap / inverse / theta, weights, QR) shared with the FP64 form.
+//
+// Split precision: a value x is carried as hi = bf16(x), lo = bf16(x - hi), and
+// a product sum_k a_k b_k as sum_k (a_hi b_hi + a_lo b_hi + a_hi b_lo) -- one
+// GEMM over the concatenated K axis [a_hi | a_lo | a_hi] . [b_hi | b_hi | b_lo],
+// accumulated in FP32 (relative error ~2^-16 of each term instead of 2^-8).
+#include <cuda.h>
+#include <cuda_runtime.h>
+#include <cuda_bf16.h>
+#include <math.h>
+
+#include <algorithm>
+
+#include "afqmc_internal.h"
+#include "device_common.cuh"
+#include "tcgen05.cuh"
+
+namespace afqmc {
+
+using tc::BK;
+
+// ---------------------------------------------------------------------------
+// tensor maps (driver entry point fetched through the runtime: no libcuda link)
+// ---------------------------------------------------------------------------
+typedef CUresult (*PFN_encodeTiled)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                    const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                    CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static PFN_encodeTiled encode_fn() {
+  static PFN_encodeTiled fn = nullptr;
+  if (!fn) {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = (PFN_encodeTiled)p;
+  }
+  return fn;
+}
+
+// 2-D BF16 tensor [rows][kpad] (kpad a multiple of 64), box = box_rows x 64, 128-byte swizzle
+bool make_tmap_bf16(CUtensorMap* tm, const void* base, int rows, int kpad, int box_rows) {
+  PFN_encodeTiled enc = encode_fn();
+  if (!enc) return false;
+  cuuint64_t dims[2] = {(cuuint64_t)kpad, (cuuint64_t)rows};
+  cuuint64_t strides[1] = {(cuuint64_t)kpad * 2};
+  cuuint32_t box[2] = {(cuuint32_t)BK, (cuuint32_t)box_rows};
+  cuuint32_t estr[2] = {1, 1};
+  CUresult r = enc(tm, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides, box, estr,
+                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS;
+}
+
+// ---------------------------------------------------------------------------
+// split-BF16 operand packing
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void split_bf16(double x, __nv_bfloat16& hi, __nv_bfloat16& lo) {
+  const float xf = (float)x;
+  hi = __float2bfloat16_rn(xf);
+  lo = __float2bfloat16_rn((float)(x - (double)__bfloat162float(hi)));
+}
+
+// dst[r][0:3K] = pattern of src[r][0:K] (FP64, row stride lds); pattern 0:
+// [hi | hi | lo] (the static side), 1: [hi | lo | hi] (the per-step side).
+// Columns K*3 .. kpad-1 are zero.
+__global__ void k_split_rows(const double* __restrict__ src, long lds, int rows, int K, int kpad, int pattern,
+                             __nv_bfloat16* __restrict__ dst) {
+  const long total = (long)rows * kpad;
+  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < total; e += (long)gridDim.x * blockDim.x) {
+    const int r = (int)(e / kpad), c = (int)(e % kpad);
+    __nv_bfloat16 v = __float2bfloat16_rn(0.f);
+    if (c < 3 * K) {
+      const int part = c / K, k = c % K;
+      __nv_bfloat16 hi, lo;
+      split_bf16(src[(long)r * lds + k], hi, lo);
+      const bool use_lo = pattern == 0 ? part == 2 : part == 1;
+      v = use_lo ? lo : hi;
+    }
+    dst[e] = v;
+  }
+}
+
+void split_rows(afqmc_handle* h, const double* src, long lds, int rows, int K, int kpad, int pattern,
+                __nv_bfloat16* dst) {
+  const long total = (long)rows * kpad;
+  const int blocks = (int)std::min<long>((total + 255) / 256, 152L * 16);
+  k_split_rows<<<blocks, 256, 0, h->stream>>>(src, lds, rows, K, kpad, pattern, dst);
+  h->launches++;
+}
+
+// ---------------------------------------------------------------------------
+// GEMM epilogues
+// ---------------------------------------------------------------------------
+// force bias: rows g, columns (walker, plane): fb32[(w, plane)][g] = mult * v
+struct EpiFB {
+  float* fb;
+  int G;
+  float mult;
+  __device__ __forceinline__ void operator()(int m, int n, float v) const { fb[(size_t)n * G + m] = mult * v; }
+};
+
+// VHS: rows t (packed index), columns (walker, plane) with plane 0 = L.Re(x),
+// plane 1 = L.Im(x); full symmetric V = sqrt(dt)(i L.Re(x) - L.Im(x)) in FP32
+// re / im planes, column-major (V(p, q) at q N + p).
+struct EpiV32 {
+  float* V;
+  const int2* tri;
+  int N, nspV, s;
+  float sdt;
+  __device__ __forceinline__ void operator()(int m, int n, float v) const {
+    const int w = n >> 1, plane = n & 1;
+    const int2 ij = tri[m];
+    const float val = plane == 0 ? sdt * v : -(sdt * v);
+    float* Vb = V + ((size_t)(w * nspV + s) * 2 + (plane == 0 ? 1 : 0)) * N * N;
+    Vb[(size_t)ij.y * N + ij.x] = val;
+    Vb[(size_t)ij.x * N + ij.y] = val;
+  }
+};
+
+template <class Epi>
+static void launch_tc(afqmc_handle* h, const CUtensorMap& ta, const CUtensorMap& tb, int M, int N, int K,
+                      const Epi& epi) {
+  constexpr int BN = 128, ST = 4;
+  const int smem = tc::GemmSmem<BN, ST>::TOTAL;
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(tc::k_tc_gemm<BN, ST, Epi>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    attr = true;
+  }
+  dim3 grid((N + BN - 1) / BN, (M + tc::BM - 1) / tc::BM);
+  tc::k_tc_gemm<BN, ST, Epi><<<grid, 128, smem, h->stream>>>(ta, tb, M, N, K, epi, h->d_err);
+  h->launches++;
+}
+
+// theta planes (FP64) -> split BF16 operand rows (w, plane)
+void launch_theta_split(afqmc_handle* h) {
+  const int K = h->nce * h->N;
+  split_rows(h, h->theta, K, 2 * h->nwalk, K, h->kf_pad, 1, h->thetaB);
+}
+
+void launch_force_bias_mixed(afqmc_handle* h) {
+  launch_theta_split(h);
+  EpiFB epi{h->fb32, h->G, (float)h->mult};
+  launch_tc(h, h->tm_rot, h->tm_theta, h->G, 2 * h->nwalk, h->kf_pad, epi);
+}
+
+void launch_vhs_mixed(afqmc_handle* h) {
+  for (int s = 0; s < h->nspV; ++s) {
+    EpiV32 epi{h->V32, h->tri, h->N, h->nspV, s, (float)sqrt(h->dt)};
+    launch_tc(h, h->tm_LT[s], h->tm_x, h->T, 2 * h->nwalk, h->kv_pad, epi);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// shifted fields from the FP32 force bias; x written as split BF16 rows
+// ---------------------------------------------------------------------------
+__global__ void k_fields_mixed(const float* __restrict__ fb, const double2* __restrict__ mf,
+                               const double* __restrict__ xi, __nv_bfloat16* __restrict__ xB, int kv_pad,
+                               double2* __restrict__ shift, double2* __restrict__ fbterm,
+                               const double* __restrict__ weights, int G, double sdt, int use_rng, uint64_t seed,
+                               uint64_t step) {
+  const int w = blockIdx.x;
+  const bool live = weights[w] > 1.0e-8;
+  double shr = 0.0, shi = 0.0, ftr = 0.0, fti = 0.0;
+  const float* fbr = fb + (size_t)(2 * w) * G;
+  const float* fbi = fbr + G;
+  __nv_bfloat16* xr_out = xB + (size_t)(2 * w) * kv_pad;
+  __nv_bfloat16* xi_out = xr_out + kv_pad;
+  for (int g = threadIdx.x; g < G; g += blockDim.x) {
+    const double xg = use_rng ? philox_normal(seed, step, (uint32_t)w, (uint32_t)g) : xi[(size_t)w * G + g];
+    const double2 m = mf[g];
+    const double fsr = -sdt * (-(double)fbi[g] - m.x);
+    const double fsi = -sdt * ((double)fbr[g] - m.y);
+    double xr = xg - fsr, xim = -fsi;
+    shr += xr * m.x - xim * m.y;
+    shi += xr * m.y + xim * m.x;
+    ftr += xg * fsr - 0.5 * (fsr * fsr - fsi * fsi);
+    fti += xg * fsi - 0.5 * (2.0 * fsr * fsi);
+    if (!live) { xr = 0.0; xim = 0.0; }
+    __nv_bfloat16 hi, lo;
+    split_bf16(xr, hi, lo);
+    xr_out[g] = hi; xr_out[G + g] = lo; xr_out[2 * G + g] = hi;
+    split_bf16(xim, hi, lo);
+    xi_out[g] = hi; xi_out[G + g] = lo; xi_out[2 * G + g] = hi;
+  }
+  shr = block_sum(shr);
+  shi = block_sum(shi);
+  ftr = block_sum(ftr);
+  fti = block_sum(fti);
+  if (threadIdx.x == 0) {
+    shift[w] = make_double2(shr, shi);
+    fbterm[w] = make_double2(ftr, fti);
+  }
+}
+
+void launch_fields_mixed(afqmc_handle* h, bool device_rng) {
+  k_fields_mixed<<<h->nwalk, 256, 0, h->stream>>>(h->fb32, h->mf, h->xi, h->xB, h->kv_pad, h->shift, h->fbterm,
+                                                  h->weights, h->G, sqrt(h->dt), device_rng ? 1 : 0, h->seed,
+                                                  h->step_counter);
+  h->launches++;
+}
+
+// ---------------------------------------------------------------------------
+// FP32 propagator: psi <- B (sum_{k<=5} V^k/k!) B psi, one CTA per (walker,
+// chunk of up to 16 columns); each thread owns one orbital row p and keeps the
+// Taylor sum of its row in registers; V streamed from L2 (column-major, so the
+// loads of a warp are contiguous).
+// ---------------------------------------------------------------------------
+constexpr int PCH32 = 16;
+
+__device__ __forceinline__ void apply_rows32(const float* __restrict__ Mr, const float* __restrict__ Mi,
+                                             const float2* in, int N, int nc, int p, float2* acc) {
+#pragma unroll
+  for (int j = 0; j < PCH32; ++j) acc[j] = make_float2(0.f, 0.f);
+  for (int q = 0; q < N; ++q) {
+    const float mr = Mr[(size_t)q * N + p], mi = Mi[(size_t)q * N + p];
+#pragma unroll
+    for (int j = 0; j < PCH32; ++j) {
+      if (j < nc) {
+        const float2 c = in[j * N + q];
+        acc[j].x = fmaf(mr, c.x, fmaf(-mi, c.y, acc[j].x));
+        acc[j].y = fmaf(mr, c.y, fmaf(mi, c.x, acc[j].y));
+      }
+    }
+  }
+}
+
+__global__ void k_propagate32(double2* __restrict__ psi, const float* __restrict__ V,
+                              const float* __restrict__ expm32, const double* __restrict__ weights,
+                              const PropChunk* __restrict__ chunks, int N, int ncw, int nspV, int nspB) {
+  const int w = blockIdx.x;
+  if (!(weights[w] > 1.0e-8)) return;
+  const PropChunk c = chunks[blockIdx.y];
+  extern __shared__ float2 sm32[];
+  float2* cur = sm32;
+  float2* nxt = sm32 + N * PCH32;
+  const int nc = c.nc;
+  const float* Br = expm32 + (size_t)(nspB == 1 ? 0 : c.spin) * 2 * N * N;
+  const float* Bi = Br + (size_t)N * N;
+  const float* Vr = V + ((size_t)(w * nspV + (nspV == 1 ? 0 : c.spin)) * 2) * N * N;
+  const float* Vi = Vr + (size_t)N * N;
+  double2* ps = psi + (size_t)w * ncw * N + (size_t)c.c0 * N;
+  for (int e = threadIdx.x; e < N * nc; e += blockDim.x) {
+    const double2 v = ps[e];
+    cur[e] = make_float2((float)v.x, (float)v.y);
+  }
+  __syncthreads();
+  float2 acc[PCH32], tmp[PCH32];
+  const int p = threadIdx.x;
+  const bool act = p < N;
+  if (act) apply_rows32(Br, Bi, cur, N, nc, p, tmp);  // B psi
+  __syncthreads();
+  if (act) {
+#pragma unroll
+    for (int j = 0; j < PCH32; ++j) {
+      acc[j] = tmp[j];
+      if (j < nc) nxt[j * N + p] = tmp[j];
+    }
+  }
+  __syncthreads();
+  float2* a = nxt;
+  float2* b = cur;
+  for (int k = 1; k <= 5; ++k) {
+    const float inv = 1.f / (float)k;
+    if (act) apply_rows32(Vr, Vi, a, N, nc, p, tmp);
+    __syncthreads();
+    if (act) {
+#pragma unroll
+      for (int j = 0; j < PCH32; ++j) {
+        tmp[j].x *= inv;
+        tmp[j].y *= inv;
+        acc[j].x += tmp[j].x;
+        acc[j].y += tmp[j].y;
+        if (j < nc) b[j * N + p] = tmp[j];
+      }
+    }
+    __syncthreads();
+    float2* t = a; a = b; b = t;
+  }
+  if (act) {
+#pragma unroll
+    for (int j = 0; j < PCH32; ++j)
+      if (j < nc) b[j * N + p] = acc[j];
+  }
+  __syncthreads();
+  if (act) {
+    apply_rows32(Br, Bi, b, N, nc, p, tmp);
+#pragma unroll
+    for (int j = 0; j < PCH32; ++j)
+      if (j < nc) ps[j * N + p] = make_double2((double)tmp[j].x, (double)tmp[j].y);
+  }
+}
+
+void launch_propagate_mixed(afqmc_handle* h) {
+  const size_t smem = 2 * (size_t)h->N * PCH32 * sizeof(float2);
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_propagate32, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    attr = true;
+  }
+  const int threads = ((h->N + 31) / 32) * 32;
+  dim3 grid(h->nwalk, h->nchunks32);
+  k_propagate32<<<grid, threads, smem, h->stream>>>(h->psi, h->V32, h->expm32, h->weights, h->d_chunks32, h->N,
+                                                    h->ncw, h->nspV, h->nsp);
+  h->launches++;
+}
+
+// static operands of the mixed form, from the FP64 device copies
+bool setup_mixed(afqmc_handle* h) {
+  const int Kf = h->nce * h->N;
+  split_rows(h, h->rot, Kf, h->G, Kf, h->kf_pad, 0, h->rotA);
+  for (int s = 0; s < h->nsp; ++s)
+    split_rows(h, h->LT + (size_t)s * h->T * h->G, h->G, h->T, h->G, h->kv_pad, 0,
+               h->LTA + (size_t)s * h->T * h->kv_pad);
+  bool ok = make_tmap_bf16(&h->tm_rot, h->rotA, h->G, h->kf_pad, tc::BM) &&
+            make_tmap_bf16(&h->tm_theta, h->thetaB, 2 * h->nwalk, h->kf_pad, 128) &&
+            make_tmap_bf16(&h->tm_x, h->xB, 2 * h->nwalk, h->kv_pad, 128);
+  for (int s = 0; s < h->nsp && ok; ++s)
+    ok = make_tmap_bf16(&h->tm_LT[s], h->LTA + (size_t)s * h->T * h->kv_pad, h->T, h->kv_pad, tc::BM);
+  return ok;
+}
+
+}  // namespace afqmc
