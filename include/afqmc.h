@@ -207,6 +207,7 @@ int afqmc_refrng_draw_step(afqmc_refrng* r, const double* weights, int nfields, 
 /* std::uniform_real_distribution<double>(0, 1) draw (the comb's zeta). */
 double afqmc_refrng_uniform(afqmc_refrng* r);
 
+
 #ifdef __cplusplus
 }
 #endif

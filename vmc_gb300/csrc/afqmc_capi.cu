@@ -184,6 +184,7 @@ void release(afqmc_handle* h) {
 
 namespace afqmc {
 bool check_launch(afqmc_handle* h, const char* what) { return after_launch(h, what) == AFQMC_OK; }
+void set_global_error(const std::string& msg) { g_create_err = msg; }
 }  // namespace afqmc
 
 extern "C" {

@@ -515,6 +515,7 @@ void launch_ortho(afqmc_handle* h) {
   h->launches++;
 }
 
+
 // ---------------------------------------------------------------------------
 // local energy (RHF.cpp:70-131, UHF.cpp:75-140):
 //   E = ecore + mult sum_s sum_{p,i} theta_s[p,i] (h1 Phi_s)[p,i]
