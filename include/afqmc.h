@@ -207,6 +207,27 @@ int afqmc_refrng_draw_step(afqmc_refrng* r, const double* weights, int nfields, 
 /* std::uniform_real_distribution<double>(0, 1) draw (the comb's zeta). */
 double afqmc_refrng_uniform(afqmc_refrng* r);
 
+/* ---- allocation-free orthonormalisation ----
+ * No counterpart in the reference.  For callers that cannot allocate GPU
+ * memory when they call it: code running under CUDA stream capture (where
+ * cudaMalloc is not allowed), hosts whose device memory belongs to another
+ * allocator, latency-bound loops that must not touch the allocator.  Same
+ * Householder QR as afqmc_orthonormalize, on caller-owned device buffers:
+ *   dets:     device, [nwalk][ncols][norb] complex double, column-major per walker
+ *             (ncols = nalpha for rhf_walker, else nalpha + nbeta, alpha first); in/out
+ *   overlaps: device, [nwalk] complex double; divided by prod diag(R) (squared
+ *             for the restricted walker); in/out
+ *   stream:   cudaStream_t to launch on (NULL: the default stream); asynchronous.
+ * The Q workspace is a fixed device array of 2^19 complex doubles (8 MiB) that
+ * every GPU loading the library keeps until exit; walkers go through it in
+ * batches, and one walker's det (norb x ncols) must fit, else AFQMC_ERR_ARG.
+ * The first call on a device looks up the array's address (with that device
+ * current) and must come before any stream capture.  All calls share the array:
+ * calls that overlap on the GPU race and must be serialised by the caller.
+ * Nothing is allocated (no cudaMalloc / cudaFree).  On failure the message is
+ * afqmc_last_error(NULL). */
+int afqmc_orthonormalize_noalloc(void* dets, void* overlaps, int nwalk, int norb, int nalpha, int nbeta,
+                                 int rhf_walker, void* stream);
 
 #ifdef __cplusplus
 }

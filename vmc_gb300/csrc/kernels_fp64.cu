@@ -515,6 +515,11 @@ void launch_ortho(afqmc_handle* h) {
   h->launches++;
 }
 
+// The same QR kernel on caller-supplied buffers (no handle).
+void launch_ortho_buffers(double2* psi, double2* qwork, double2* ovlp, int nwalk, int N, int ncw, int na, int nb,
+                          int rhf_walker, cudaStream_t stream) {
+  k_ortho<<<nwalk, 256, 0, stream>>>(psi, qwork, ovlp, N, ncw, na, nb, rhf_walker);
+}
 
 // ---------------------------------------------------------------------------
 // local energy (RHF.cpp:70-131, UHF.cpp:75-140):
