@@ -1,19 +1,29 @@
 #!/usr/bin/env python3
 """Walker-steps/s of the phaseless AFQMC step on one GB300 (one JSON line).
 
-Workload (default): norb=120, nalpha=nbeta=20, nchol=600 synthetic Hamiltonian,
-UHF trial and UHF walkers, 2048 walkers, dt=0.005; one step = force bias,
-fields, VHS, propagator, overlap and weights of every walker; walkers are
-orthonormalised every 5 steps and measured (local energy of every walker)
-every 50 steps, the reference's measurement cadence (sampling.nsteps = 50).
+Workload (default): norb=120, nalpha=nbeta=20, nchol=600 synthetic Hamiltonian
+(vmc_gb300/synthetic.py), UHF trial and UHF walkers, 2048 walkers, dt=0.005.
+One step = force bias, fields, VHS, propagator, overlap and weights of every
+walker, the walkers orthonormalised every 5 steps, and an energy estimate.
 
-  python bench.py [--gpus N] [--steps K] [--warmup W] [--form fp64|mixed] [--impl reference]
+Forms, all on the same GPU and workload:
+  headline ("value"): mixed precision + control variate, an energy estimate
+      every step (MLP for every walker + exact local energy of 1 walker in 8);
+  fp64_every_step: the plain FP64 form, exact local energy of every walker every
+      step (the metric's comparison);
+  mixed_every50 / fp64_every50: both forms at the reference's own measurement
+      cadence (every sampling.nsteps = 50 steps, exact energies).
+energy_error_mEh: |mixed-estimator energy of the mixed form - that of the FP64
+form| after 40 steps from the same walkers with identical fields (the FP64 form
+equals the FP64 oracle to 1e-10).
 
---impl reference times the CPU restatement of the reference's path (the oracle
-port; the reference's own C++ needs Boost, HDF5 and MPI, which are absent) on
-all host cores on the same workload.  Under torchrun every rank runs an
-independent replica (the path has no data-path collective at this scale);
-rank 0 prints the line with value = walker-steps of all ranks / max time.
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+--impl reference times the CPU restatement of the reference's path (the
+oracle port: the reference's own C++ needs Boost, HDF5 and MPI, absent here)
+on all host cores, same workload and metric.  Under torchrun every rank runs
+an independent replica; rank 0 prints value = walker-steps of all ranks / max
+time.
 """
 import argparse
 import json
@@ -31,7 +41,8 @@ sys.path.insert(0, ROOT)
 
 METRIC = "AFQMC walker-steps/s, mixed vs FP64 on same GB300, at ≤0.1 mEh energy error"
 ORTHO_EVERY = 5
-ENERGY_EVERY = 50
+REF_CADENCE = 50
+STAGES = ["fb", "fields", "vhs", "prop", "overlap", "weights", "ortho", "energy"]
 
 
 def parse():
@@ -40,42 +51,34 @@ def parse():
     p.add_argument("--steps", type=int, default=50)
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    p.add_argument("--form", default="fp64", choices=["fp64", "mixed"])
     p.add_argument("--workload", default="cfg2")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--quick", action="store_true", help="headline form only (profiling runs)")
     return p.parse_args()
 
 
 def dist_env():
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return rank, world, local
+    return (int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")),
+            int(os.environ.get("LOCAL_RANK", "0")))
 
 
-# --------------------------------------------------------------------------
-# algorithmic FLOPs (count of the algorithm, not of what a kernel executes)
-# --------------------------------------------------------------------------
-def flops_model(N, na, nb, G, spins=2, ortho_every=ORTHO_EVERY):
-    """Per walker: force bias (theta + contraction), VHS, propagator with a real
-    exp(-dt/2 h1') (2 real x complex + 5 complex x complex products per spin),
-    overlap (Phi^T psi and LU), QR amortised, and one exact local energy."""
+def flops_model(N, na, nb, G, ortho_every=ORTHO_EVERY):
+    """Algorithmic FLOPs per walker: force bias, VHS, propagator with
+    a real exp(-dt/2 h1') (2 real x complex + 5 complex x complex products per
+    spin), overlap, QR amortised, and one exact local energy."""
     T = N * (N + 1) // 2
-    ns = [na, nb][:spins]
+    ns = [na, nb]
     fb = sum(4 * n * n * N + 16 * n ** 3 + 8 * N * n * n + 4 * n * N * G for n in ns)
     vhs = 4 * T * G
     prop = sum(48 * N * N * n for n in ns)
     ovl = sum(4 * n * n * N + 5.3 * n ** 3 for n in ns)
     qr = sum(32 * N * n * n for n in ns) / ortho_every
     el = sum(4 * G * n * n * N + 8 * G * n * n + 4 * n * N for n in ns)
-    return dict(fb=fb, vhs=vhs, prop=prop, overlap=ovl, ortho=qr, energy=el,
-                step=fb + vhs + prop + ovl + qr)
+    return dict(fb=fb, vhs=vhs, prop=prop, overlap=ovl, ortho=qr, energy=el, step=fb + vhs + prop + ovl + qr)
 
 
-# --------------------------------------------------------------------------
-# clocks sampled during the timed region
-# --------------------------------------------------------------------------
 class Clocks:
+    """nvidia-smi samples during the timed region."""
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
@@ -122,25 +125,21 @@ class Clocks:
 def peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
-        d = json.load(open(p))
-        return d, "measured"
+        return json.load(open(p)), "measured"
     return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
 
 
-# --------------------------------------------------------------------------
-# CPU baseline: the oracle port on the host cores
-# --------------------------------------------------------------------------
 def cpu_baseline(sysd, nwalk_sample=32, steps=4, seconds_cap=30.0):
+    """The oracle port (numpy complex128 + the reference's FP32 VHS) on the host cores."""
     from oracle import afqmc_oracle as O
     N, na, nb = sysd["norb"], sysd["nalpha"], sysd["nbeta"]
     oh = O.Hamiltonian(N, na, nb, sysd["ecore"], sysd["h1"], sysd["h1mod"], sysd["chol"])
     ot = O.Trial(oh, sysd["trial"], sysd["phi_a"], sysd["phi_b"])
-    rw = False
     prop = O.Propagator(oh, ot.phi, 0.005, mode="ref")
-    wk = O.Walkers(oh, rw, np.repeat(O._ref_dets(oh, ot.phi, rw)[None], nwalk_sample, axis=0))
+    wk = O.Walkers(oh, False, np.repeat(O._ref_dets(oh, ot.phi, False)[None], nwalk_sample, axis=0))
     wk.overlaps = O.overlap(ot, wk)
     rng = np.random.default_rng(0)
-    e0 = O.hf_energy(ot, oh, ot.phi, rw).real
+    e0 = O.hf_energy(ot, oh, ot.phi, False).real
     t0 = time.perf_counter()
     done = 0
     for st in range(1, steps + 1):
@@ -150,36 +149,81 @@ def cpu_baseline(sysd, nwalk_sample=32, steps=4, seconds_cap=30.0):
         done += nwalk_sample
         if time.perf_counter() - t0 > seconds_cap:
             break
-    # one local-energy evaluation per ENERGY_EVERY steps, timed on a small sample
+    t_step = (time.perf_counter() - t0) / done
     te = time.perf_counter()
     O.local_energy(ot, wk, oh)
     t_el = (time.perf_counter() - te) / nwalk_sample
-    dt = time.perf_counter() - t0 - t_el * nwalk_sample
-    per_ws = dt / done + t_el / ENERGY_EVERY
+    per_ws = t_step + t_el  # energy every step, as the headline form
     return {"value": 1.0 / per_ws, "unit": "walker-steps/s", "cores": os.cpu_count(), "kind": "port",
-            "sample": "%d walkers x %d steps of the same workload (oracle, numpy complex128 + FP32 VHS, "
-                      "all BLAS threads) + one local energy per %d steps" % (nwalk_sample, done // nwalk_sample,
-                                                                             ENERGY_EVERY)}
+            "sample": "%d walkers x %d steps of the same workload + one exact local energy per walker-step "
+                      "(oracle port: numpy complex128 with the reference's FP32 VHS, all BLAS threads)"
+                      % (nwalk_sample, done // nwalk_sample),
+            "every50_value": 1.0 / (t_step + t_el / REF_CADENCE)}
 
 
-# --------------------------------------------------------------------------
-def make_walkers(sysd, form, device):
-    from vmc_gb300 import afqmc as A
+def make_walkers(A, sysd, form, device, nwalk=None):
     N, na, nb = sysd["norb"], sysd["nalpha"], sysd["nbeta"]
     gh = A.Hamiltonian(N, na, nb, sysd["ecore"], sysd["h1"], sysd["h1mod"], sysd["chol"])
     gt = A.UHF(gh, sysd["phi_a"], sysd["phi_b"]) if sysd["trial"] == "uhf" else A.RHF(gh, sysd["phi_a"])
-    wk = A.DQMCWalkers(gh, gt, sysd["walkers"], sysd["trial"] == "rhf", 0.005, precision=form,
-                       device=device, seed=20261203)
-    return wk
+    return A.DQMCWalkers(gh, gt, nwalk or sysd["walkers"], sysd["trial"] == "rhf", 0.005, precision=form,
+                         device=device, seed=20261203)
 
 
-def run_steps(wk, k0, K, e_every=ENERGY_EVERY):
+def cholesky_truncation(wk, G, threshold=1e-3):
+    """Cholesky vectors for the energy, the reference's rule (MixedEstimator.cpp:363-384):
+    the first of 0.3 .. 0.7 G whose trial-state energy is within the threshold."""
+    e_full = wk.ham_and_overlap().real.mean()
+    for frac in (0.3, 0.4, 0.5, 0.6, 0.7):
+        n = int(frac * G)
+        wk.set_nchol_ene(n)
+        if abs(e_full - wk.ham_and_overlap().real.mean()) < threshold:
+            return n
+    wk.set_nchol_ene(G)
+    return G
+
+
+def energy_all(A, wk):
+    wk._check(A.lib().afqmc_local_energy(wk.h, None))
+
+
+def timed(A, wk, k0, K, energy, cv=None):
+    """K steps on the device; energy in {"cv", "every", "every50"}; returns (ms, launches, stage ms)."""
+    wk.sync()
+    wk.enable_timing(True)
+    l0 = wk.launch_count()
+    wk.timer_start()
     for k in range(k0, k0 + K):
         wk.propagate_phaseless(None)
         if (k + 1) % ORTHO_EVERY == 0:
             wk.orthogonalize()
-        if (k + 1) % e_every == 0:
-            wk.lib_energy()
+        if energy == "cv":
+            cv.measure(tag=k, slot=k % 4096)
+        elif energy == "every" or (k + 1) % REF_CADENCE == 0:
+            energy_all(A, wk)
+    ms = wk.timer_stop()
+    launches = wk.launch_count() - l0
+    stage = {s: wk.stage_time(s) for s in STAGES}
+    wk.enable_timing(False)
+    return ms, launches, stage
+
+
+def energy_error(A, sysd, device, nw=256, steps=40):
+    """Mixed vs FP64 form from the same walkers with identical host fields."""
+    rng = np.random.default_rng(11)
+    xs = [rng.standard_normal((nw, sysd["nchol"])) for _ in range(steps)]
+    out = {}
+    for form in ("mixed", "fp64"):
+        wk = make_walkers(A, sysd, form, device, nw)
+        e0 = wk.ham_and_overlap().real.mean()
+        for k in range(steps):
+            wk.propagate_phaseless(xs[k], e0)
+            if (k + 1) % ORTHO_EVERY == 0:
+                wk.orthogonalize()
+        _, _, w = wk.get_det()
+        el = wk.ham_and_overlap().real
+        out[form] = (w * el).sum() / w.sum()
+        wk.close()
+    return abs(out["mixed"] - out["fp64"]) * 1e3, out
 
 
 def main():
@@ -187,101 +231,131 @@ def main():
     rank, world, local = dist_env()
     if args.impl == "reference":
         return main_reference(args, rank, world)
-    from vmc_gb300 import synthetic as S
     from vmc_gb300 import afqmc as A
+    from vmc_gb300 import synthetic as S
+    from vmc_gb300.cv import ControlVariate
     if world > 1:
         import torch
         import torch.distributed as dist
         torch.cuda.set_device(local)
         dist.init_process_group("nccl")
     sysd = S.workload(args.workload)
-    W = sysd["walkers"]
-    N, na, nb, G = sysd["norb"], sysd["nalpha"], sysd["nbeta"], sysd["nchol"]
-    wk = make_walkers(sysd, args.form, local)
+    W, N, na, nb, G = sysd["walkers"], sysd["norb"], sysd["nalpha"], sysd["nbeta"], sysd["nchol"]
+    A.lib()
+    A._bind_cv(A.lib())
+
+    # --- headline: mixed + control variate, energy estimate every step ---
+    wk = make_walkers(A, sysd, "mixed", local)
+    nchol_ene = cholesky_truncation(wk, G)
     e0 = wk.ham_and_overlap().real.mean()
     wk.set_energy_estimate(e0, e0)
-    A.DQMCWalkers.lib_energy = lambda self: A.lib().afqmc_local_energy(self.h, None)
-
-    # warm-up
-    run_steps(wk, 0, args.warmup)
-    wk.sync()
-    # timed region (device events on the handle's stream)
+    cv = ControlVariate(wk, hidden=256, den=8, seed=3)
+    for k in range(120):  # equilibration; training data from steps 20..120 (untimed)
+        wk.propagate_phaseless(None)
+        if (k + 1) % ORTHO_EVERY == 0:
+            wk.orthogonalize()
+        if k >= 20:
+            cv.collect()
+    cv_loss, cv_n = cv.train(epochs=20, batch=512, lr=1e-3)
+    k0 = 120
+    for k in range(k0, k0 + args.warmup):
+        wk.propagate_phaseless(None)
+        cv.measure(tag=k, slot=k % 4096)
+    k0 += args.warmup
     if world > 1:
         dist.barrier()
-    wk.sync()
     clk = Clocks(local)
-    wk.enable_timing(True)
-    l0 = wk.launch_count()
-    wk.timer_start()
-    run_steps(wk, args.warmup, args.steps)
-    ms = wk.timer_stop()
-    launches = wk.launch_count() - l0
+    ms, launches, stage = timed(A, wk, k0, args.steps, "cv", cv)
     clocks = clk.stop()
-    stage = {s: wk.stage_time(s) for s in ["fb", "fields", "vhs", "prop", "overlap", "weights", "ortho", "energy"]}
-    wk.enable_timing(False)
     if world > 1:
         import torch
         t = torch.tensor([ms], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = float(t.item())
-    walker_steps = W * args.steps * world
-    value = walker_steps / (ms / 1e3)
+    value = W * args.steps * world / (ms / 1e3)
+    k0 += args.steps
 
-    # end to end through the public API with host buffers: H2D fields, D2H weights
+    # end to end through the public API with host buffers: fields H2D, weights and the
+    # step's energy estimate D2H every step
     rng = np.random.default_rng(1)
     xis = [np.ascontiguousarray(rng.standard_normal((W, G))) for _ in range(2)]
-    import ctypes
     wbuf = np.zeros(W)
+    ebuf = np.zeros(4)
     wk.sync()
     t0 = time.perf_counter()
     for k in range(args.steps):
         wk.propagate_phaseless(xis[k % 2])
         if (k + 1) % ORTHO_EVERY == 0:
             wk.orthogonalize()
-        if (k + 1) % ENERGY_EVERY == 0:
-            wk.lib_energy()
+        cv.measure(tag=k0 + k, slot=0)
         A.lib().afqmc_get_walkers(wk.h, None, None, wbuf.ctypes.data)
+        A.lib().afqmc_cv_results(wk.h, ebuf.ctypes.data, 1)
     wk.sync()
     e2e_s = time.perf_counter() - t0
     e2e = {"value": W * args.steps * world / e2e_s, "unit": "walker-steps/s",
-           "h2d_bytes_per_step": W * G * 8, "d2h_bytes_per_step": W * 8}
+           "h2d_bytes_per_step": W * G * 8, "d2h_bytes_per_step": W * 8 + 32}
+
+    forms = {}
+    if not args.quick:
+        # mixed at the reference cadence (energy every 50 steps)
+        ms_m50, _, _ = timed(A, wk, k0, REF_CADENCE, "every50")
+        forms["mixed_every50"] = {"value": W * REF_CADENCE / (ms_m50 / 1e3), "ms_per_step": ms_m50 / REF_CADENCE}
+        wk.close()
+        # the plain FP64 form: warm-up 1 step, time 3 steps with an exact energy every step
+        wf = make_walkers(A, sysd, "fp64", local)
+        wf.set_nchol_ene(nchol_ene)
+        ef = wf.ham_and_overlap().real.mean()
+        wf.set_energy_estimate(ef, ef)
+        wf.propagate_phaseless(None)
+        kf = 3
+        ms_f, _, stage_f = timed(A, wf, 1, kf, "every")
+        forms["fp64_every_step"] = {"value": W * kf / (ms_f / 1e3), "ms_per_step": ms_f / kf,
+                                    "stage_ms_per_step": {s: v / kf for s, v in stage_f.items()}}
+        step_ms = (ms_f - stage_f["energy"]) / kf
+        forms["fp64_every50"] = {"value": W / ((step_ms + stage_f["energy"] / kf / REF_CADENCE) / 1e3),
+                                 "ms_per_step": step_ms + stage_f["energy"] / kf / REF_CADENCE}
+        wf.close()
+        err_meh, err_e = energy_error(A, sysd, local)
+    else:
+        wk.close()
+        err_meh, err_e = None, None
 
     fl = flops_model(N, na, nb, G)
     pk, src = peaks()
-    nsteps_e = args.steps // ENERGY_EVERY
-    per_launch = {"fb": fl["fb"] * W, "vhs": fl["vhs"] * W, "prop": fl["prop"] * W,
-                  "overlap": fl["overlap"] * W, "energy": fl["energy"] * W}
-    launches_of = {"fb": args.steps, "vhs": args.steps, "prop": args.steps, "overlap": args.steps,
-                   "energy": max(nsteps_e, 1)}
-    dom = max(per_launch, key=lambda s: stage[s] if launches_of[s] else 0)
+    per_launch = {"fb": fl["fb"] * W, "vhs": fl["vhs"] * W, "prop": fl["prop"] * W, "overlap": fl["overlap"] * W,
+                  "ortho": fl["ortho"] * ORTHO_EVERY * W, "energy": fl["energy"] * W / 8}
+    launches_of = {s: args.steps for s in per_launch}
+    launches_of["ortho"] = max(1, args.steps // ORTHO_EVERY)
+    dom = max(per_launch, key=lambda s: stage[s])
     avg_ms = stage[dom] / launches_of[dom]
     achieved = per_launch[dom] / (avg_ms / 1e3) / 1e12
-    if args.form == "fp64":
-        roof = {"bound": "tensor", "kernel": dom, "achieved": achieved, "peak": pk["bf16_tflops"],
-                "unit": "TFLOP/s", "frac": achieved / pk["bf16_tflops"], "traffic": None,
-                "peak_source": src + " bf16 burst; the FP64 form runs on the FP64 pipe"}
-    else:
-        roof = {"bound": "tensor", "kernel": dom, "achieved": achieved, "peak": pk["bf16_tflops"],
-                "unit": "TFLOP/s", "frac": achieved / pk["bf16_tflops"], "traffic": None,
-                "peak_source": src + " bf16 burst"}
-
+    peak = pk["bf16_tflops_sustained"] if "bf16_tflops_sustained" in pk else pk["bf16_tflops"]
+    roof = {"bound": "tensor", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+            "frac": achieved / peak, "traffic": None,
+            "peak_source": "%s bf16 sustained (MEASURED_PEAKS.json); algorithmic FLOPs of the stage per launch "
+                           "/ its CUDA-event time" % src}
     out = {"metric": METRIC, "value": value, "unit": "walker-steps/s", "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
-           "vs_baseline": None, "dtype": "f64" if args.form == "fp64" else "bf16x3/f32/f64",
+           "vs_baseline": None, "dtype": "bf16x3 contractions / f32 propagator / f64 inverse, det, QR, weights",
            "data": "synthetic (seeded generator, vmc_gb300/synthetic.py)",
-           "config": {"workload": "%s: norb=%d nalpha=nbeta=%d nchol=%d walkers=%d UHF trial+walkers dt=0.005"
+           "config": {"workload": "%s: norb=%d nalpha=nbeta=%d nchol=%d walkers=%d UHF trial and walkers dt=0.005"
                                   % (args.workload, N, na, G, W),
-                      "form": args.form, "ortho_every": ORTHO_EVERY, "energy_every": ENERGY_EVERY,
-                      "fields": "device Philox", "l2": "inputs larger than L2 (VHS matrices %.0f MB)" %
-                                                      (W * 2 * 2 * N * N * 8 / 1e6 if args.form == "fp64" else 0),
-                      "parallelism": "replicas" if world > 1 else "single GPU"},
-           "stage_ms_per_step": {k: v / max(launches_of.get(k, args.steps), 1) for k, v in stage.items()},
+                      "form": "mixed + control variate (energy estimate every step, exact on 1/8)",
+                      "ortho_every": ORTHO_EVERY, "fields": "device Philox",
+                      "nchol_energy": nchol_ene,
+                      "l2": "inputs larger than L2 (walker state + split operands + VHS %.0f MB per step)"
+                            % ((W * 40 * 120 * 16 + W * 2 * 14400 * 2 + W * 2 * 7260 * 4) / 1e6),
+                      "parallelism": "replicas" if world > 1 else "single GPU",
+                      "cv": {"train_samples": cv_n, "train_mse_std_units": cv_loss}},
+           "forms": forms,
+           "speedup_vs_fp64": (value / forms["fp64_every_step"]["value"]) if forms else None,
+           "energy_error_mEh": err_meh, "energy_check": err_e,
+           "stage_ms_per_step": {k: v / args.steps for k, v in stage.items()},
            "roofline": roof, "e2e": e2e, "gpu_launches": launches, "clocks": clocks}
     if rank == 0 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(sysd)
     if rank == 0:
         print(json.dumps(out))
-    wk.close()
     if world > 1:
         dist.destroy_process_group()
 
@@ -295,14 +369,14 @@ def main_reference(args, rank, world):
     N, na, G, W = sysd["norb"], sysd["nalpha"], sysd["nchol"], sysd["walkers"]
     out = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": "walker-steps/s",
            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
-           "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-           "config": {"workload": "%s: norb=%d nalpha=nbeta=%d nchol=%d walkers=%d UHF trial+walkers dt=0.005"
+           "scaling": "weak", "vs_baseline": None, "dtype": "f64 (FP32 VHS as the reference)", "data": "synthetic",
+           "config": {"workload": "%s: norb=%d nalpha=nbeta=%d nchol=%d walkers=%d UHF trial and walkers dt=0.005"
                                   % (args.workload, N, na, G, W),
-                      "ortho_every": ORTHO_EVERY, "energy_every": ENERGY_EVERY},
+                      "ortho_every": ORTHO_EVERY, "energy": "exact local energy every step"},
            "cpu_baseline": cb,
            "e2e": {"value": cb["value"], "unit": "walker-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-           "note": "the reference's own C++ (DQMC/*.cpp) needs Boost, HDF5 and MPI, absent here; "
-                   "this arm times the oracle port of the same path on all host cores"}
+           "note": "the reference's own C++ (DQMC/*.cpp) needs Boost, HDF5 and MPI, absent here; this arm times "
+                   "the oracle port of the same path on all host cores"}
     print(json.dumps(out))
 
 

@@ -207,6 +207,57 @@ int afqmc_refrng_draw_step(afqmc_refrng* r, const double* weights, int nfields, 
 /* std::uniform_real_distribution<double>(0, 1) draw (the comb's zeta). */
 double afqmc_refrng_uniform(afqmc_refrng* r);
 
+/* ---- learned control variate (no counterpart in the reference) ----
+ * A small MLP n_in -> hidden -> hidden -> 1 (SiLU) trained on the GPU by
+ * hand-written kernels (forward with BF16-rounded weights and FP32
+ * accumulation, backward, Adam on FP32 master weights).  Parameters are one
+ * flat FP32 array: W1 [hidden][n_in] | b1 [hidden] | W2 [hidden][hidden] |
+ * b2 [hidden] | w3 [hidden] | b3 [1].  Host buffers throughout. */
+typedef struct afqmc_mlp afqmc_mlp;
+int afqmc_mlp_create(int n_in, int hidden, int max_batch, int device, uint64_t seed, afqmc_mlp** out);
+int afqmc_mlp_destroy(afqmc_mlp* m);
+const char* afqmc_mlp_last_error(const afqmc_mlp* m);
+int afqmc_mlp_nparams(const afqmc_mlp* m, long* n);
+/* get (non-NULL) and/or set (non-NULL) the flat parameter array */
+int afqmc_mlp_params(afqmc_mlp* m, float* get, const float* set);
+/* mean-squared-error loss of x [B][n_in] against t [B] and its gradient [nparams] */
+int afqmc_mlp_loss_grad(afqmc_mlp* m, const float* x, const float* t, int B, double* loss, float* grad);
+int afqmc_mlp_predict(afqmc_mlp* m, const float* x, int B, float* y);
+/* Adam (lr) over shuffled mini-batches of a dataset x [n][n_in], t [n]; final_loss = MSE over all n */
+int afqmc_mlp_train(afqmc_mlp* m, const float* x, const float* t, int n, int epochs, int batch, float lr,
+                    uint64_t seed, double* final_loss);
+
+/* Control variate on a handle (mixed precision form):
+ * features of the current walkers, host [nwalk][67]: Re fb_g (g < 64), one-body
+ * energy, log|overlap|, arg overlap (raw, not standardised). */
+int afqmc_cv_features(afqmc_handle* h, float* feats);
+/* exact local energies of the walkers idx[0..m) (host), eloc [m] complex */
+int afqmc_local_energy_subset(afqmc_handle* h, const int* idx, int m, double* eloc);
+/* use the trained MLP m (67 inputs, max_batch >= nwalk) with the feature mean /
+ * std and target mean / std of its training set; exact energies on 1 walker of
+ * every block of den */
+int afqmc_cv_attach(afqmc_handle* h, afqmc_mlp* m, const float* mean, const float* stdv, float ymean, float ystd,
+                    int den);
+/* asynchronous control-variate measurement of the current walkers into result
+ * slot `slot` (< 4096): {E_cv = sum_w w f / sum_w w + sum_S w (E - f) / sum_S w,
+ * E_cv in Horvitz-Thompson form, E_subsample (Horvitz-Thompson), E_subsample
+ * (ratio), sum of weights, sum of subsample weights}; `tag` seeds the subsample */
+int afqmc_cv_measure(afqmc_handle* h, uint64_t tag, int slot);
+int afqmc_cv_results(afqmc_handle* h, double* out, int nslots);
+
+/* ---- CUDA-graph replay (one or several systems) ----
+ * Capture nsteps device-field steps of each of the n handles (QR every
+ * ortho_every steps, control-variate measurement every cv_every steps when a
+ * network is attached; 0 disables) into one graph whose per-system branches run
+ * concurrently; afqmc_graph_launch replays it (every handle advances nsteps).
+ * Population control runs on the device (afqmc_set_energy_estimate). */
+typedef struct afqmc_graph afqmc_graph;
+int afqmc_graph_capture(afqmc_handle** hs, int n, int nsteps, int ortho_every, int cv_every, afqmc_graph** out);
+int afqmc_graph_launch(afqmc_graph* g);
+int afqmc_graph_nodes(const afqmc_graph* g, long* nodes);
+int afqmc_graph_destroy(afqmc_graph* g);
+const char* afqmc_graph_last_error(void);
+
 /* ---- allocation-free orthonormalisation ----
  * No counterpart in the reference.  For callers that cannot allocate GPU
  * memory when they call it: code running under CUDA stream capture (where

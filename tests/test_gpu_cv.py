@@ -1,0 +1,94 @@
+"""Learned control variate: the GPU training kernels against the CPU oracle,
+and what the trained network gains over the method without it.
+
+* Gradient check: loss and every parameter gradient of the GPU forward /
+  backward kernels vs oracle/mlp_oracle.py (numpy, FP64 arithmetic, same BF16
+  weight rounding) within 2e-3 relative.
+* Training: Adam on a smooth regression lowers the loss by 10x.
+* Gain: on a small AFQMC system, after training on exact local energies from
+  equilibration, the control-variate estimate (exact energies on 1 of 8
+  walkers + MLP for all, corrected by the subsample's mean residual) tracks the exact
+  all-walker mixed energy with at least 2x smaller variance than the same 1/8
+  subsample without the network, and without a detectable bias.
+"""
+import numpy as np
+import pytest
+
+from oracle import afqmc_oracle as O
+from oracle import mlp_oracle as MO
+from vmc_gb300 import synthetic as S
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def A():
+    from vmc_gb300 import afqmc
+    afqmc.lib()
+    return afqmc
+
+
+def test_mlp_gradients_match_oracle(A):
+    m = A.MLP(67, 256, max_batch=512, seed=3)
+    rng = np.random.default_rng(0)
+    x = rng.standard_normal((200, 67)).astype(np.float32)
+    t = rng.standard_normal(200).astype(np.float32)
+    loss, g = m.loss_grad(x, t)
+    p = m.get_params()
+    params = [a.astype(np.float64) for a in m.split(p)]
+    params = [p_ if i not in (0, 2, 4) else m.split(p)[i] for i, p_ in enumerate(params)]
+    lo, go = MO.loss_and_grads(params, x.astype(np.float64), t.astype(np.float64))
+    assert abs(loss - lo) / lo < 1e-4
+    for gg, ref in zip(m.split(g), go):
+        assert np.abs(gg - ref).max() / (np.abs(ref).max() + 1e-30) < 2e-3
+
+
+def test_mlp_training_lowers_loss(A):
+    m = A.MLP(67, 256, max_batch=512, seed=4)
+    rng = np.random.default_rng(1)
+    x = rng.standard_normal((4096, 67)).astype(np.float32)
+    t = (np.sin(x[:, 0]) + 0.5 * x[:, 1] * x[:, 2] + 0.1 * (x[:, 3:10] ** 2).sum(1)).astype(np.float32)
+    t = (t - t.mean()) / t.std()
+    l0, _ = m.loss_grad(x[:512], t[:512])
+    l1 = m.train(x, t, epochs=15, batch=256, lr=1e-3, seed=0)
+    assert l1 < 0.1 * l0, (l0, l1)
+
+
+def test_control_variate_reduces_variance(A):
+    from vmc_gb300.cv import ControlVariate
+    s = S.make_system(30, 5, 90, 515, "uhf")
+    N, n = 30, 5
+    gh = A.Hamiltonian(N, n, n, 0.0, s["h1"], s["h1mod"], s["chol"])
+    gt = A.UHF(gh, s["phi_a"], s["phi_b"])
+    W = 1024
+    wk = A.DQMCWalkers(gh, gt, W, False, 0.005, precision="mixed", seed=99)
+    e0 = wk.ham_and_overlap().real.mean()
+    wk.set_energy_estimate(e0, e0)
+    cv = ControlVariate(wk, hidden=256, den=8, seed=5)
+    for st in range(1, 121):
+        wk.propagate_phaseless(None)
+        if st % 5 == 0:
+            wk.orthogonalize()
+        if st > 20:
+            cv.collect()
+    loss, nsamp = cv.train(epochs=40, batch=256, lr=1e-3)
+    assert nsamp > 5000
+    full, res = [], []
+    for st in range(80):
+        wk.propagate_phaseless(None)
+        if (st + 1) % 5 == 0:
+            wk.orthogonalize()
+        cv.measure(tag=1000 + st, slot=st)
+        el = wk.ham_and_overlap().real
+        _, _, w = wk.get_det()
+        full.append((w * el).sum() / w.sum())
+    res = cv.results(80)
+    full = np.array(full)
+    r_cv = res[:, 0] - full      # control variate, ratio correction
+    r_cv_ht = res[:, 1] - full   # control variate, Horvitz-Thompson correction
+    r_ht = res[:, 2] - full      # plain subsample, Horvitz-Thompson
+    r_ratio = res[:, 3] - full   # plain subsample, ratio
+    gain = r_ratio.var() / r_cv.var()
+    assert gain > 2.0, (gain, r_cv.std(), r_ratio.std(), r_cv_ht.std(), r_ht.std())
+    assert r_cv_ht.var() < r_ht.var()
+    assert abs(r_cv.mean()) < 4 * r_cv.std() / np.sqrt(len(r_cv)) + 1e-12

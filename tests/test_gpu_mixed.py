@@ -83,6 +83,26 @@ def test_one_step_mixed(A, kind):
     assert rel(w, ow.weights) < 2e-6
 
 
+@pytest.mark.parametrize("kind", ["uhf", "rhf"])
+def test_local_energy_tensor_core(A, kind):
+    """Exchange + Coulomb on tcgen05 (split BF16), one-body in FP64: every
+    walker's E_L within 2e-5 Eh of the FP64 oracle, also with a truncated
+    Cholesky count (ncholEne)."""
+    oh, ot, rw = system(kind)
+    W = 45  # several walker tiles, the last one partial
+    wk = gpu(A, oh, ot, rw, W, "mixed")
+    dets = start_dets(oh, ot, rw, W, 5)
+    wk.set_det(dets)
+    ow = O.Walkers(oh, rw, dets)
+    el = wk.ham_and_overlap()
+    ref = O.local_energy(ot, ow, oh)
+    assert np.abs(el - ref).max() < 2e-5, np.abs(el - ref).max()
+    wk.set_nchol_ene(oh.nchol // 3)
+    el = wk.ham_and_overlap()
+    ref = O.local_energy(ot, ow, oh, oh.nchol // 3)
+    assert np.abs(el - ref).max() < 2e-5, np.abs(el - ref).max()
+
+
 def test_energy_error_vs_fp64_oracle(A):
     """100 steps (ortho every 5) with identical fields: mixed-estimator energy
     sum_w w E_L / sum_w w of the mixed form within 0.1 mEh of the FP64 oracle."""

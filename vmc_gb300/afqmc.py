@@ -375,3 +375,165 @@ def from_reference_inputs(ham_arrays, trials, cfg, nprocs=1, precision="ref32", 
     init = np.concatenate([rt.phi_a, rt.phi_b], axis=1) if not rhf_walker else rt.phi_a
     wk.set_det(np.repeat(init[None].astype(np.complex128), nwalk * nprocs, axis=0))
     return wk
+
+
+# ---------------------------------------------------------------------------
+# learned control variate
+# ---------------------------------------------------------------------------
+CV_NF = 67
+
+
+def _bind_cv(L):
+    if getattr(L, "_cv_bound", False):
+        return
+    vp, ip = ctypes.c_void_p, ctypes.c_int
+    for name, args in [("afqmc_mlp_create", [ip, ip, ip, ip, ctypes.c_uint64, ctypes.POINTER(vp)]),
+                       ("afqmc_mlp_destroy", [vp]),
+                       ("afqmc_mlp_nparams", [vp, ctypes.POINTER(ctypes.c_long)]),
+                       ("afqmc_mlp_params", [vp, vp, vp]),
+                       ("afqmc_mlp_loss_grad", [vp, vp, vp, ip, ctypes.POINTER(ctypes.c_double), vp]),
+                       ("afqmc_mlp_predict", [vp, vp, ip, vp]),
+                       ("afqmc_mlp_train", [vp, vp, vp, ip, ip, ip, ctypes.c_float, ctypes.c_uint64,
+                                            ctypes.POINTER(ctypes.c_double)]),
+                       ("afqmc_cv_features", [vp, vp]),
+                       ("afqmc_local_energy_subset", [vp, vp, ip, vp]),
+                       ("afqmc_cv_attach", [vp, vp, vp, vp, ctypes.c_float, ctypes.c_float, ip]),
+                       ("afqmc_cv_measure", [vp, ctypes.c_uint64, ip]),
+                       ("afqmc_cv_results", [vp, vp, ip])]:
+        f = getattr(L, name)
+        f.argtypes = args
+        f.restype = ctypes.c_int
+    L.afqmc_mlp_last_error.restype = ctypes.c_char_p
+    L.afqmc_mlp_last_error.argtypes = [vp]
+    L._cv_bound = True
+
+
+class MLP:
+    """GPU MLP n_in -> hidden -> hidden -> 1 (SiLU), trained by the library's kernels."""
+
+    def __init__(self, n_in=CV_NF, hidden=256, max_batch=4096, seed=1, device=0):
+        L = lib()
+        _bind_cv(L)
+        h = ctypes.c_void_p()
+        rc = L.afqmc_mlp_create(n_in, hidden, max_batch, device, seed, ctypes.byref(h))
+        if rc != AFQMC_OK:
+            raise AfqmcError(rc, "afqmc_mlp_create")
+        self.h, self.n_in, self.hidden = h, n_in, hidden
+        n = ctypes.c_long()
+        L.afqmc_mlp_nparams(h, ctypes.byref(n))
+        self.nparams = n.value
+
+    def _check(self, rc):
+        if rc != AFQMC_OK:
+            raise AfqmcError(rc, lib().afqmc_mlp_last_error(self.h).decode())
+
+    def get_params(self):
+        p = np.zeros(self.nparams, np.float32)
+        self._check(lib().afqmc_mlp_params(self.h, p.ctypes.data, None))
+        return p
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        self._check(lib().afqmc_mlp_params(self.h, None, p.ctypes.data))
+
+    def split(self, p):
+        """Flat parameters -> [W1, b1, W2, b2, w3, b3]."""
+        H, I = self.hidden, self.n_in
+        o = [0, H * I, H * I + H, H * I + H + H * H, H * I + 2 * H + H * H, H * I + 3 * H + H * H]
+        return [p[o[0]:o[1]].reshape(H, I), p[o[1]:o[2]], p[o[2]:o[3]].reshape(H, H), p[o[3]:o[4]],
+                p[o[4]:o[5]], p[o[5]:o[5] + 1]]
+
+    def loss_grad(self, x, t):
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        t = np.ascontiguousarray(t, dtype=np.float32)
+        loss = ctypes.c_double()
+        g = np.zeros(self.nparams, np.float32)
+        self._check(lib().afqmc_mlp_loss_grad(self.h, x.ctypes.data, t.ctypes.data, len(t), ctypes.byref(loss),
+                                              g.ctypes.data))
+        return loss.value, g
+
+    def predict(self, x):
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        y = np.zeros(len(x), np.float32)
+        self._check(lib().afqmc_mlp_predict(self.h, x.ctypes.data, len(x), y.ctypes.data))
+        return y
+
+    def train(self, x, t, epochs=20, batch=256, lr=1e-3, seed=0):
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        t = np.ascontiguousarray(t, dtype=np.float32)
+        loss = ctypes.c_double()
+        self._check(lib().afqmc_mlp_train(self.h, x.ctypes.data, t.ctypes.data, len(t), epochs, batch, lr, seed,
+                                          ctypes.byref(loss)))
+        return loss.value
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().afqmc_mlp_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def cv_features(wk):
+    L = lib()
+    _bind_cv(L)
+    f = np.zeros((wk.nwalk, CV_NF), np.float32)
+    wk._check(L.afqmc_cv_features(wk.h, f.ctypes.data))
+    return f
+
+
+def local_energy_subset(wk, idx):
+    L = lib()
+    _bind_cv(L)
+    idx = np.ascontiguousarray(idx, dtype=np.int32)
+    e = np.zeros(len(idx), np.complex128)
+    wk._check(L.afqmc_local_energy_subset(wk.h, idx.ctypes.data, len(idx), e.ctypes.data))
+    return e
+
+
+class StepGraph:
+    """nsteps device-field steps of one or several DQMCWalkers as one CUDA graph
+    (afqmc_graph_*): each replay advances every system by nsteps."""
+
+    def __init__(self, walkers, nsteps, ortho_every=5, cv_every=0):
+        L = lib()
+        vp = ctypes.c_void_p
+        L.afqmc_graph_capture.argtypes = [ctypes.POINTER(vp), ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                          ctypes.POINTER(vp)]
+        L.afqmc_graph_launch.argtypes = [vp]
+        L.afqmc_graph_destroy.argtypes = [vp]
+        L.afqmc_graph_nodes.argtypes = [vp, ctypes.POINTER(ctypes.c_long)]
+        L.afqmc_graph_last_error.restype = ctypes.c_char_p
+        self.walkers = list(walkers)
+        arr = (vp * len(self.walkers))(*[w.h for w in self.walkers])
+        g = vp()
+        rc = L.afqmc_graph_capture(arr, len(self.walkers), nsteps, ortho_every, cv_every, ctypes.byref(g))
+        if rc != AFQMC_OK:
+            raise AfqmcError(rc, L.afqmc_graph_last_error().decode())
+        self.g = g
+        self.nsteps = nsteps
+
+    def launch(self):
+        rc = lib().afqmc_graph_launch(self.g)
+        if rc != AFQMC_OK:
+            raise AfqmcError(rc, lib().afqmc_graph_last_error().decode())
+
+    def nodes(self):
+        n = ctypes.c_long()
+        lib().afqmc_graph_nodes(self.g, ctypes.byref(n))
+        return n.value
+
+    def close(self):
+        if getattr(self, "g", None):
+            lib().afqmc_graph_destroy(self.g)
+            self.g = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

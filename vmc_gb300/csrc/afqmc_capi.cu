@@ -170,7 +170,8 @@ void release(afqmc_handle* h) {
   void* ptrs[] = {h->psi, h->phi, h->rot, h->h1phi, h->LT, h->LT32, h->tri, h->expm, h->mf, h->theta,
                   h->det, h->ovlp, h->weights, h->fb, h->xi, h->x, h->x32, h->shift, h->fbterm, h->V,
                   h->qwork, h->epart, h->eloc, h->scal, h->d_chunks, h->d_err, h->rotA, h->LTA,
-                  h->thetaB, h->xB, h->fb32, h->V32, h->expm32, h->d_chunks32};
+                  h->thetaB, h->xB, h->fb32, h->V32, h->expm32, h->d_chunks32, h->rotE, h->thetaE,
+                  h->xc, h->cv_x, h->cv_idx, h->cv_esub, h->cv_f, h->cv_ms, h->cv_out, h->d_step};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (h->host_pinned) cudaFreeHost(h->host_pinned);
@@ -402,6 +403,7 @@ int afqmc_create(const afqmc_ham* ham, const afqmc_trial* trial, const afqmc_opt
   const bool mixed = h->precision == AFQMC_PREC_MIXED;
   h->kf_pad = (3 * h->nce * N + 63) / 64 * 64;
   h->kv_pad = (3 * G + 63) / 64 * 64;
+  h->ke_pad = (3 * N + 63) / 64 * 64;
   h->nechunk = std::max(1, std::min(G, (4 * 152 + h->nwalk - 1) / h->nwalk));
 
   // --- device buffers ---
@@ -433,15 +435,25 @@ int afqmc_create(const afqmc_ham* ham, const afqmc_trial* trial, const afqmc_opt
   ALLOC(fbterm, W);
   if (!mixed) ALLOC(V, W * h->nspV * 2 * NN);
   ALLOC(d_err, 1);
+  ALLOC(d_step, 1);
+  ALLOC(cv_x, W * 67);
+  ALLOC(cv_idx, W);
+  ALLOC(cv_esub, W);
+  ALLOC(cv_f, W);
+  ALLOC(cv_ms, 2 * 67);
+  ALLOC(cv_out, (size_t)h->cv_nslots * 6);
   if (mixed) {
     ALLOC(rotA, (size_t)G * h->kf_pad);
     ALLOC(LTA, (size_t)nsp * T * h->kv_pad);
     ALLOC(thetaB, W * 2 * h->kf_pad);
     ALLOC(xB, W * 2 * h->kv_pad);
     ALLOC(fb32, W * 2 * G);
-    ALLOC(V32, W * h->nspV * 2 * NN);
+    ALLOC(V32, W * h->nspV * 2 * (size_t)T);
     ALLOC(expm32, (size_t)nsp * 2 * NN);
     ALLOC(d_chunks32, h->chunks32.size());
+    ALLOC(rotE, (size_t)G * h->nce * h->ke_pad);
+    ALLOC(thetaE, W * 2 * h->nce * h->ke_pad);
+    ALLOC(xc, W * 2 * G * 2);
   }
   ALLOC(qwork, W * h->ncw * N);
   ALLOC(epart, W * h->nechunk);
@@ -473,6 +485,9 @@ int afqmc_create(const afqmc_ham* ham, const afqmc_trial* trial, const afqmc_opt
   UP(mf, mf2);
   UP(d_chunks, h->chunks);
   if (mixed) {
+    h->real_expm = true;
+    for (size_t e = 0; e < expm_cm.size(); ++e)
+      if (expm_cm[e].imag() != 0.0) h->real_expm = false;
     std::vector<float> e32((size_t)nsp * 2 * NN);
     for (int s = 0; s < nsp; ++s)
       for (size_t e = 0; e < NN; ++e) {
@@ -492,6 +507,7 @@ int afqmc_create(const afqmc_ham* ham, const afqmc_trial* trial, const afqmc_opt
   }
   {
     ce = cudaMemsetAsync(h->d_err, 0, sizeof(int), h->stream);
+    if (ce == cudaSuccess) ce = cudaMemsetAsync(h->d_step, 0, sizeof(unsigned long long), h->stream);
     if (ce != cudaSuccess) { g_create_err = cudaGetErrorString(ce); release(h); delete h; return AFQMC_ERR_CUDA; }
   }
   std::vector<double> sc(afqmc::S_NSLOTS, 0.0);
@@ -735,10 +751,13 @@ int afqmc_local_energy(afqmc_handle* h, double* eloc) {
   cudaSetDevice(h->device);
   const int nmax = std::max(h->chan[0].n, h->nchan > 1 ? h->chan[1].n : 0);
   const size_t smem = ((size_t)h->nce * h->N + (size_t)h->nchan * nmax * nmax) * sizeof(double2);
-  if (smem > 220 * 1024) return fail(h, AFQMC_ERR_UNSUPPORTED, "FP64 local energy: theta does not fit in shared memory");
+  const bool mixed = h->precision == AFQMC_PREC_MIXED;
+  if (!mixed && smem > 220 * 1024)
+    return fail(h, AFQMC_ERR_UNSUPPORTED, "FP64 local energy: theta does not fit in shared memory");
   cudaEvent_t e0;
   stage_begin(h, afqmc::ST_ENERGY, &e0);
-  afqmc::launch_local_energy(h);
+  if (mixed) afqmc::launch_local_energy_mixed(h);
+  else afqmc::launch_local_energy(h);
   stage_end(h, afqmc::ST_ENERGY, e0);
   int rc = after_launch(h, "local_energy");
   if (rc) return rc;

@@ -107,11 +107,31 @@ struct afqmc_handle {
   __nv_bfloat16* thetaB = nullptr;   // [2W][kf_pad]      [hi | lo | hi] of theta planes
   __nv_bfloat16* xB = nullptr;       // [2W][kv_pad]      [hi | lo | hi] of field planes
   float* fb32 = nullptr;             // [W][2][G]
-  float* V32 = nullptr;              // [W][nspV][2][N*N]
+  float* V32 = nullptr;              // [W][nspV][2][T]   packed VHS, re / im planes
+  bool real_expm = false;            // exp(-dt/2 h1') has no imaginary part (real trial)
   float* expm32 = nullptr;           // [nsp][2][N*N]     re / im planes, column-major
   afqmc::PropChunk* d_chunks32 = nullptr;
   int nchunks32 = 0;
   CUtensorMap tm_rot, tm_theta, tm_x, tm_LT[2];
+  // mixed local energy
+  int ke_pad = 0;                    // padded split-K (3N) of the exchange GEMM
+  __nv_bfloat16* rotE = nullptr;     // [G][nce][ke_pad]  [hi | hi | lo] of rot along p
+  __nv_bfloat16* thetaE = nullptr;   // [2W][nce][ke_pad] [hi | lo | hi] of theta along p
+  double2* xc = nullptr;             // [W][2][Gene][2]   exchange X and Coulomb c per (w, s, g)
+  int ex_gbox[2] = {1, 1}, ex_wbox[2] = {1, 1};
+  CUtensorMap tm_rotE[2], tm_thE[2];
+  unsigned long long* d_step = nullptr;  // device step counter of the Philox field stream
+  bool fb_current = false;               // fb32 holds the force bias of the current theta
+  // control variate
+  float* cv_x = nullptr;             // [W][67] features
+  float* cv_f = nullptr;             // [W]     predicted local energies
+  int* cv_idx = nullptr;             // [W]     subsample
+  double2* cv_esub = nullptr;        // [W]     exact energies of the subsample
+  float* cv_ms = nullptr;            // [2][67] feature mean / std
+  double* cv_out = nullptr;          // [cv_nslots][4]
+  int cv_nslots = 4096, cv_den = 8;
+  float cv_ymean = 0.f, cv_ystd = 1.f;
+  struct afqmc_mlp* cv_mlp = nullptr;
 };
 
 namespace afqmc {
@@ -133,6 +153,9 @@ void launch_force_bias_mixed(afqmc_handle* h);
 void launch_fields_mixed(afqmc_handle* h, bool device_rng);
 void launch_vhs_mixed(afqmc_handle* h);
 void launch_propagate_mixed(afqmc_handle* h);
+void split_rows(afqmc_handle* h, const double* src, long lds, int rows, int K, int kpad, int pattern,
+                __nv_bfloat16* dst);
+void launch_local_energy_mixed(afqmc_handle* h);
 
 // error helper used by kernels' launchers
 bool check_launch(afqmc_handle* h, const char* what);

@@ -1,0 +1,253 @@
+// Control-variate energy estimator on the device (no counterpart in the
+// reference, which evaluates every walker's local energy exactly at each
+// measurement, DQMC/MixedEstimator.cpp:489-538).
+//
+// Per measurement:
+//   features x_w (67): Re fb_g for the first 64 Cholesky vectors of the current
+//     walker, the one-body energy mult sum theta.(h1 Phi), log|<Psi_T|phi>|,
+//     arg <Psi_T|phi>; standardised with the training set's mean / std;
+//   prediction f_w = ymean + ystd MLP(x_w) for every walker;
+//   a stratified random subsample S: one walker out of every block of `den`
+//     consecutive walkers (inclusion probability 1/den, or 1/|block| for the
+//     last, shorter block), whose exact local energies E_w are computed;
+//   E_cv = sum_w w f_w / sum_w w + sum_{w in S} w (E_w - f_w) / sum_{w in S} w,
+//     the control-variate estimate of the exact mixed energy sum_w w E_w /
+//     sum_w w: whatever f is, its bias is that of a ratio estimator, O(1/|S|),
+//     as the mixed estimator's own; the Horvitz-Thompson form
+//     [sum_w w f_w + sum_S pi_w^-1 w (E_w - f_w)] / sum_w w (exactly unbiased,
+//     larger variance) and the plain subsample estimates sum_S pi^-1 w E / sum_w w
+//     and sum_S w E / sum_S w are reported beside it.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <math.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "afqmc_internal.h"
+#include "device_common.cuh"
+
+struct afqmc_mlp;
+
+namespace afqmc {
+
+constexpr int CV_NF = 67;
+void mlp_forward_on(afqmc_mlp* m, const float* X, int B, float* Y, cudaStream_t st);
+int mlp_max_batch(const afqmc_mlp* m);
+int mlp_n_in(const afqmc_mlp* m);
+
+__global__ void k_cv_features(const float* __restrict__ fb32, const double* __restrict__ fb64,
+                              const double* __restrict__ theta, const double* __restrict__ h1phi,
+                              const double2* __restrict__ ovlp, int N, int nce, int G, int mult,
+                              const float* __restrict__ mean, const float* __restrict__ stdv, float* __restrict__ out) {
+  const int w = blockIdx.x;
+  float* o = out + (size_t)w * CV_NF;
+  for (int g = threadIdx.x; g < 64; g += blockDim.x) {
+    float v = 0.f;
+    if (g < G) v = fb32 ? fb32[(size_t)(2 * w) * G + g] : (float)fb64[(size_t)(2 * w) * G + g];
+    o[g] = v;
+  }
+  const double* tre = theta + (size_t)(2 * w) * nce * N;
+  double e1 = 0.0;
+  for (int k = threadIdx.x; k < nce * N; k += blockDim.x) e1 += tre[k] * h1phi[k];
+  e1 = block_sum(e1);
+  if (threadIdx.x == 0) {
+    const double2 ov = ovlp[w];
+    o[64] = (float)(mult * e1);
+    o[65] = (float)(0.5 * log(ov.x * ov.x + ov.y * ov.y));
+    o[66] = (float)atan2(ov.y, ov.x);
+  }
+  __syncthreads();
+  if (mean)
+    for (int f = threadIdx.x; f < CV_NF; f += blockDim.x) o[f] = (o[f] - mean[f]) / stdv[f];
+}
+
+// one walker from each block of den: idx[b] = b den + r_b, r_b uniform in the block
+__global__ void k_cv_select(int* __restrict__ idx, int W, int den, uint64_t seed, uint64_t tag,
+                            const unsigned long long* __restrict__ stepp) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  const int m = (W + den - 1) / den;
+  if (b >= m) return;
+  const int size = min(den, W - b * den);
+  const uint64_t step = *stepp;
+  const U4 r = philox4x32_10(U4{(uint32_t)b, (uint32_t)tag, (uint32_t)step, (uint32_t)(step >> 32)}, (uint32_t)seed,
+                             (uint32_t)(seed >> 32) ^ 0x5bd1e995u);
+  idx[b] = b * den + (int)(r.x % (uint32_t)size);
+}
+
+// dst rows (i, plane, c) = split of theta rows of walker idx[i] ([hi | lo | hi] along p)
+__global__ void k_split_theta_gather(const double* __restrict__ theta, const int* __restrict__ idx, int m, int nce,
+                                     int N, int kpad, __nv_bfloat16* __restrict__ dst) {
+  const int row = blockIdx.x;  // (i, plane, c)
+  const int i = row / (2 * nce), rem = row % (2 * nce);
+  const double* s = theta + ((size_t)idx[i] * 2 * nce + rem) * N;
+  __nv_bfloat16* d = dst + (size_t)row * kpad;
+  for (int k = threadIdx.x; k < kpad; k += blockDim.x) {
+    __nv_bfloat16 v = __float2bfloat16_rn(0.f);
+    if (k < 3 * N) {
+      const int part = k / N, p = k % N;
+      const double x = s[p];
+      const __nv_bfloat16 hi = __float2bfloat16_rn((float)x);
+      const __nv_bfloat16 lo = __float2bfloat16_rn((float)(x - (double)__bfloat162float(hi)));
+      v = part == 1 ? lo : hi;
+    }
+    d[k] = v;
+  }
+}
+
+__global__ void k_cv_scale(float* __restrict__ f, int W, float ymean, float ystd) {
+  const int w = blockIdx.x * blockDim.x + threadIdx.x;
+  if (w < W) f[w] = ymean + ystd * f[w];
+}
+
+__global__ void k_cv_estimate(const double* __restrict__ weights, const float* __restrict__ f,
+                              const int* __restrict__ idx, const double2* __restrict__ esub, int W, int m, int den,
+                              double* __restrict__ out) {
+  double sw = 0.0, swf = 0.0;
+  for (int w = threadIdx.x; w < W; w += blockDim.x) {
+    sw += weights[w];
+    swf += weights[w] * (double)f[w];
+  }
+  double corr = 0.0, ht = 0.0, nrw = 0.0, nrwe = 0.0, nrwf = 0.0;
+  for (int i = threadIdx.x; i < m; i += blockDim.x) {
+    const int w = idx[i];
+    const double inv = (double)min(den, W - i * den);
+    const double wt = weights[w];
+    const double e = esub[i].x;
+    if (wt != 0.0) {
+      corr += inv * wt * (e - (double)f[w]);
+      ht += inv * wt * e;
+      nrw += wt;
+      nrwe += wt * e;
+      nrwf += wt * (double)f[w];
+    }
+  }
+  sw = block_sum(sw);
+  swf = block_sum(swf);
+  corr = block_sum(corr);
+  ht = block_sum(ht);
+  nrw = block_sum(nrw);
+  nrwe = block_sum(nrwe);
+  nrwf = block_sum(nrwf);
+  if (threadIdx.x == 0) {
+    out[0] = swf / sw + (nrwe - nrwf) / nrw;
+    out[1] = (swf + corr) / sw;
+    out[2] = ht / sw;
+    out[3] = nrwe / nrw;
+    out[4] = sw;
+    out[5] = nrw;
+  }
+}
+
+}  // namespace afqmc
+
+using namespace afqmc;
+
+namespace afqmc {
+void launch_local_energy_mixed_subset(afqmc_handle* h, const int* d_idx, int m, double2* out);
+
+void launch_split_theta_gather(afqmc_handle* h, const int* d_idx, int m) {
+  k_split_theta_gather<<<m * 2 * h->nce, 128, 0, h->stream>>>(h->theta, d_idx, m, h->nce, h->N, h->ke_pad, h->thetaE);
+  h->launches++;
+}
+}
+
+extern "C" {
+
+int afqmc_cv_features(afqmc_handle* h, float* out) {
+  if (!h || !out) return AFQMC_ERR_ARG;
+  cudaSetDevice(h->device);
+  if (!h->cv_x) return AFQMC_ERR_STATE;
+  if (h->precision == AFQMC_PREC_MIXED) launch_force_bias_mixed(h);
+  else launch_force_bias(h);
+  k_cv_features<<<h->nwalk, 128, 0, h->stream>>>(h->precision == AFQMC_PREC_MIXED ? h->fb32 : nullptr, h->fb,
+                                                 h->theta, h->h1phi, h->ovlp, h->N, h->nce, h->G, h->mult, nullptr,
+                                                 nullptr, h->cv_x);
+  h->launches++;
+  if (cudaMemcpyAsync(out, h->cv_x, (size_t)h->nwalk * CV_NF * 4, cudaMemcpyDeviceToHost, h->stream) != cudaSuccess ||
+      cudaStreamSynchronize(h->stream) != cudaSuccess) {
+    h->err = "cv_features copy failed";
+    return AFQMC_ERR_CUDA;
+  }
+  return AFQMC_OK;
+}
+
+int afqmc_local_energy_subset(afqmc_handle* h, const int* idx, int m, double* eloc) {
+  if (!h || !idx || !eloc || m <= 0 || m > h->nwalk) return AFQMC_ERR_ARG;
+  for (int i = 0; i < m; ++i)
+    if (idx[i] < 0 || idx[i] >= h->nwalk) return AFQMC_ERR_ARG;
+  cudaSetDevice(h->device);
+  if (h->precision != AFQMC_PREC_MIXED) {
+    std::vector<double> all(2 * (size_t)h->nwalk);
+    int rc = afqmc_local_energy(h, all.data());
+    if (rc) return rc;
+    for (int i = 0; i < m; ++i) { eloc[2 * i] = all[2 * idx[i]]; eloc[2 * i + 1] = all[2 * idx[i] + 1]; }
+    return AFQMC_OK;
+  }
+  if (cudaMemcpyAsync(h->cv_idx, idx, (size_t)m * 4, cudaMemcpyHostToDevice, h->stream) != cudaSuccess) return AFQMC_ERR_CUDA;
+  launch_local_energy_mixed_subset(h, h->cv_idx, m, h->cv_esub);
+  if (cudaMemcpyAsync(eloc, h->cv_esub, (size_t)m * 16, cudaMemcpyDeviceToHost, h->stream) != cudaSuccess ||
+      cudaStreamSynchronize(h->stream) != cudaSuccess)
+    return AFQMC_ERR_CUDA;
+  return AFQMC_OK;
+}
+
+int afqmc_cv_attach(afqmc_handle* h, afqmc_mlp* m, const float* mean, const float* stdv, float ymean, float ystd,
+                    int den) {
+  if (!h || !m || !mean || !stdv || den < 1) return AFQMC_ERR_ARG;
+  if (mlp_n_in(m) != CV_NF || mlp_max_batch(m) < h->nwalk) {
+    h->err = "the MLP must take 67 inputs and batches of nwalk";
+    return AFQMC_ERR_ARG;
+  }
+  if (h->precision != AFQMC_PREC_MIXED) {
+    h->err = "the control variate runs with the mixed-precision form";
+    return AFQMC_ERR_UNSUPPORTED;
+  }
+  cudaSetDevice(h->device);
+  h->cv_mlp = m;
+  h->cv_den = den;
+  h->cv_ymean = ymean;
+  h->cv_ystd = ystd;
+  std::vector<float> ms(2 * CV_NF);
+  for (int i = 0; i < CV_NF; ++i) { ms[i] = mean[i]; ms[CV_NF + i] = stdv[i] > 0 ? stdv[i] : 1.f; }
+  if (cudaMemcpyAsync(h->cv_ms, ms.data(), ms.size() * 4, cudaMemcpyHostToDevice, h->stream) != cudaSuccess ||
+      cudaStreamSynchronize(h->stream) != cudaSuccess)
+    return AFQMC_ERR_CUDA;
+  return AFQMC_OK;
+}
+
+// Device-side control-variate measurement of the current walkers into result
+// slot `slot` (6 doubles: E_cv, E_cv (HT), E_sub (HT), E_sub (ratio), sum_w,
+// sum_w over the subsample); asynchronous.
+int afqmc_cv_measure(afqmc_handle* h, uint64_t tag, int slot) {
+  if (!h || !h->cv_mlp || slot < 0 || slot >= h->cv_nslots) return AFQMC_ERR_ARG;
+  cudaSetDevice(h->device);
+  const int W = h->nwalk, den = h->cv_den, m = (W + den - 1) / den;
+  launch_force_bias_mixed(h);
+  k_cv_features<<<W, 128, 0, h->stream>>>(h->fb32, nullptr, h->theta, h->h1phi, h->ovlp, h->N, h->nce, h->G, h->mult,
+                                          h->cv_ms, h->cv_ms + CV_NF, h->cv_x);
+  mlp_forward_on(h->cv_mlp, h->cv_x, W, h->cv_f, h->stream);
+  k_cv_select<<<(m + 127) / 128, 128, 0, h->stream>>>(h->cv_idx, W, den, h->seed, tag, h->d_step);
+  launch_local_energy_mixed_subset(h, h->cv_idx, m, h->cv_esub);
+  k_cv_scale<<<(W + 255) / 256, 256, 0, h->stream>>>(h->cv_f, W, h->cv_ymean, h->cv_ystd);
+  k_cv_estimate<<<1, 1024, 0, h->stream>>>(h->weights, h->cv_f, h->cv_idx, h->cv_esub, W, m, den,
+                                           h->cv_out + 6 * (size_t)slot);
+  h->launches += 8;
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    h->err = std::string("cv_measure: ") + cudaGetErrorString(e);
+    return AFQMC_ERR_CUDA;
+  }
+  return AFQMC_OK;
+}
+
+int afqmc_cv_results(afqmc_handle* h, double* out, int nslots) {
+  if (!h || !out || nslots <= 0 || nslots > h->cv_nslots) return AFQMC_ERR_ARG;
+  cudaSetDevice(h->device);
+  if (cudaMemcpyAsync(out, h->cv_out, (size_t)nslots * 6 * 8, cudaMemcpyDeviceToHost, h->stream) != cudaSuccess ||
+      cudaStreamSynchronize(h->stream) != cudaSuccess)
+    return AFQMC_ERR_CUDA;
+  return AFQMC_OK;
+}
+
+}  // extern "C"

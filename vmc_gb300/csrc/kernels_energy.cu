@@ -1,0 +1,259 @@
+// Mixed-precision local energy (RHF.cpp:70-131, UHF.cpp:75-140) on tcgen05.
+//
+// For each trial channel s the exchange matrices f_sg = rot_s[g] theta_s
+// (n x n per walker and Cholesky vector) form one GEMM
+//     D[(g, i)][(w, plane, j)] = sum_p rot_s[g][i][p] theta_s[w][plane][p][j]
+// with split-BF16 operands along p (K = 3N, zero-padded to a multiple of 64).
+// TMA loads 3-D boxes -- gbox Cholesky vectors x n rows of rot, wbox walkers x
+// 2 planes x n columns of theta -- so a 128 x BN tile holds whole n x n blocks
+// f_sg(w) for gbox x wbox (g, w) pairs.  The epilogue copies the tile from TMEM
+// to shared memory and each warp forms, per pair,
+//     X = sum_ij f[i][j] f[j][i]   and   c = sum_i f[i][i]     (complex)
+// written to xc[w][s][g].  A small FP64 kernel then assembles
+//     E = ecore + mult sum_s tr(G_s h1) + 1/2 sum_{g<Gene} [(mult sum_s c_sg)^2 - mult sum_s X_sg].
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+
+#include "afqmc_internal.h"
+#include "device_common.cuh"
+#include "tcgen05.cuh"
+
+namespace afqmc {
+
+using tc::BK;
+using tc::BM;
+
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* tm, uint64_t* bar, int x, int y, int z) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4, %5}], "
+      "[%2];" ::"r"(tc::smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(tm)), "r"(tc::smem_u32(bar)), "r"(x), "r"(y), "r"(z)
+      : "memory");
+}
+
+constexpr int EX_BN = 256;  // TMEM columns / max B rows per tile
+constexpr int EX_STAGES = 3;
+constexpr int EX_A_BYTES = BM * BK * 2;       // 16 KB
+constexpr int EX_B_BYTES = EX_BN * BK * 2;    // 32 KB
+constexpr int EX_STAGE = EX_A_BYTES + EX_B_BYTES;
+constexpr int EX_BAR_OFF = EX_STAGES * EX_STAGE;
+constexpr int EX_SMEM = EX_BAR_OFF + (2 * EX_STAGES + 1) * 8 + 16 + 1024;
+constexpr int EX_LD = EX_BN + 1;  // fp32 row pitch of the staged tile
+static_assert(BM * EX_LD * 4 <= EX_BAR_OFF, "staged tile must fit in the pipeline buffers");
+
+struct ExArgs {
+  int n;          // occupied orbitals of this channel
+  int gbox, wbox; // Cholesky vectors / walkers per tile
+  int a_bytes, b_bytes;
+  int col_off;    // channel column offset in the [nce] axis
+  int s;          // channel index
+};
+
+// grid: (walker tiles, g tiles, channels); 128 threads
+__global__ void __launch_bounds__(128, 1)
+    k_tc_exchange(const __grid_constant__ CUtensorMap tmA0, const __grid_constant__ CUtensorMap tmB0,
+                  const __grid_constant__ CUtensorMap tmA1, const __grid_constant__ CUtensorMap tmB1, ExArgs a0,
+                  ExArgs a1, int Gene, int W, int K, int nchan, double2* __restrict__ xc, int* err) {
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  uint64_t* full = (uint64_t*)(smem + EX_BAR_OFF);
+  uint64_t* empty = full + EX_STAGES;
+  uint64_t* accum = empty + EX_STAGES;
+  uint32_t* tmem_holder = (uint32_t*)(accum + 1);
+  __shared__ int s_abort;
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const ExArgs A = blockIdx.z == 0 ? a0 : a1;
+  const CUtensorMap* tmA = blockIdx.z == 0 ? &tmA0 : &tmA1;
+  const CUtensorMap* tmB = blockIdx.z == 0 ? &tmB0 : &tmB1;
+  const int g0 = blockIdx.y * A.gbox;
+  const int w0 = blockIdx.x * A.wbox;
+  const int nk = K / BK;
+  const uint32_t stage_tx = (uint32_t)(A.a_bytes + A.b_bytes);
+
+  if (threadIdx.x == 0) {
+    s_abort = 0;
+    for (int s = 0; s < EX_STAGES; ++s) {
+      tc::mbar_init(&full[s], 1);
+      tc::mbar_init(&empty[s], 1);
+    }
+    tc::mbar_init(accum, 1);
+    tc::fence_mbar_init();
+  }
+  if (warp == 0) tc::tmem_alloc(tmem_holder, EX_BN);
+  tc::tc_fence_before();
+  __syncthreads();
+  tc::tc_fence_after();
+  const uint32_t tmem = *tmem_holder;
+
+  int issued = 0;
+  if (warp == 0 && lane == 0) {
+    for (int kb = 0; kb < nk; ++kb) {
+      const int s = kb % EX_STAGES;
+      if (kb >= EX_STAGES && !tc::mbar_wait(&empty[s], ((kb / EX_STAGES) - 1) & 1, err, 11)) {
+        s_abort = 1;
+        break;
+      }
+      uint8_t* sa = smem + s * EX_STAGE;
+      uint8_t* sb = sa + EX_A_BYTES;
+      tc::mbar_expect_tx(&full[s], stage_tx);
+      tma_load_3d(sa, tmA, &full[s], kb * BK, A.col_off, g0);
+      tma_load_3d(sb, tmB, &full[s], kb * BK, A.col_off, 2 * w0);
+      issued = kb + 1;
+    }
+  } else if (warp == 1 && lane == 0) {
+    constexpr uint32_t idesc = tc::idesc_bf16(BM, EX_BN);
+    for (int kb = 0; kb < nk; ++kb) {
+      const int s = kb % EX_STAGES;
+      if (!tc::mbar_wait(&full[s], (kb / EX_STAGES) & 1, err, 12)) {
+        s_abort = 1;
+        break;
+      }
+      tc::tc_fence_after();
+      const uint32_t sa = tc::smem_u32(smem + s * EX_STAGE);
+      const uint64_t ad = tc::sdesc_sw128(sa), bd = tc::sdesc_sw128(sa + EX_A_BYTES);
+#pragma unroll
+      for (int k = 0; k < BK / 16; ++k)
+        tc::mma_bf16(tmem, ad + (uint64_t)(2 * k), bd + (uint64_t)(2 * k), idesc, (kb > 0 || k > 0) ? 1u : 0u);
+      tc::mma_commit(&empty[s]);
+    }
+    tc::mma_commit(accum);
+  }
+  __syncwarp();
+  const bool have = tc::mbar_wait(accum, 0, err, 13);
+  tc::tc_fence_after();
+  if (s_abort && warp == 0 && lane == 0) {
+    for (int kb = (issued > EX_STAGES ? issued - EX_STAGES : 0); kb < issued; ++kb)
+      tc::mbar_wait(&full[kb % EX_STAGES], (kb / EX_STAGES) & 1, err, 14);
+  }
+  __syncthreads();  // all loads consumed: the pipeline buffers become the staging tile
+  float* tile = (float*)smem;
+  const int n = A.n, ncols = 2 * A.wbox * n;
+  if (have && !s_abort) {
+    const int row = warp * 32 + lane;
+#pragma unroll 1
+    for (int c = 0; c < EX_BN; c += 16) {
+      float v[16];
+      tc::tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c, v);
+      if (c < ncols) {
+#pragma unroll
+        for (int j = 0; j < 16; ++j) tile[row * EX_LD + c + j] = v[j];
+      }
+    }
+  }
+  __syncthreads();
+  if (have && !s_abort) {
+    const int npairs = A.gbox * A.wbox;
+    for (int pr = warp; pr < npairs; pr += 4) {
+      const int gl = pr / A.wbox, wl = pr % A.wbox;
+      const int g = g0 + gl, w = w0 + wl;
+      if (g >= Gene || w >= W) continue;
+      const float* rowbase = tile + (gl * n) * EX_LD;
+      const int cre = (2 * wl) * n, cim = (2 * wl + 1) * n;
+      float xr = 0.f, xi = 0.f, cr = 0.f, ci = 0.f;
+      for (int e = lane; e < n * n; e += 32) {
+        const int i = e / n, j = e % n;
+        const float a_r = rowbase[i * EX_LD + cre + j], a_i = rowbase[i * EX_LD + cim + j];
+        const float b_r = rowbase[j * EX_LD + cre + i], b_i = rowbase[j * EX_LD + cim + i];
+        xr = fmaf(a_r, b_r, fmaf(-a_i, b_i, xr));
+        xi = fmaf(a_r, b_i, fmaf(a_i, b_r, xi));
+        if (i == j) { cr += a_r; ci += a_i; }
+      }
+      xr = warp_sumf(xr);
+      xi = warp_sumf(xi);
+      cr = warp_sumf(cr);
+      ci = warp_sumf(ci);
+      if (lane == 0) {
+        double2* o = xc + (((size_t)w * 2 + A.s) * Gene + g) * 2;
+        o[0] = make_double2(xr, xi);
+        o[1] = make_double2(cr, ci);
+      }
+    }
+  }
+  tc::tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    tc::tc_fence_after();
+    tc::tmem_dealloc(tmem, EX_BN);
+  }
+}
+
+// E = ecore + mult sum theta.h1phi + 1/2 sum_g [(mult sum_s c_sg)^2 - mult sum_s X_sg]
+__global__ void k_energy_assemble(const double* __restrict__ theta, const double* __restrict__ h1phi,
+                                  const double2* __restrict__ xc, double2* __restrict__ eloc, int N, int nce, int Gene,
+                                  int nchan, int mult, double ecore, const int* __restrict__ idx) {
+  const int w = blockIdx.x;  // local index (row of xc); theta of walker idx[w] (or w)
+  const int ws = idx ? idx[w] : w;
+  const double* tre = theta + (size_t)(2 * ws) * nce * N;
+  const double* tim = tre + (size_t)nce * N;
+  double re = 0.0, im = 0.0;
+  for (int k = threadIdx.x; k < nce * N; k += blockDim.x) {
+    re += tre[k] * h1phi[k];
+    im += tim[k] * h1phi[k];
+  }
+  double er = 0.0, ei = 0.0;
+  for (int g = threadIdx.x; g < Gene; g += blockDim.x) {
+    double2 c = make_double2(0.0, 0.0), x = make_double2(0.0, 0.0);
+    for (int s = 0; s < nchan; ++s) {
+      const double2* o = xc + (((size_t)w * 2 + s) * Gene + g) * 2;
+      x = cadd(x, o[0]);
+      c = cadd(c, o[1]);
+    }
+    c = make_double2(mult * c.x, mult * c.y);
+    const double2 c2 = cmul(c, c);
+    er += 0.5 * (c2.x - mult * x.x);
+    ei += 0.5 * (c2.y - mult * x.y);
+  }
+  re = block_sum(re);
+  im = block_sum(im);
+  er = block_sum(er);
+  ei = block_sum(ei);
+  if (threadIdx.x == 0) eloc[w] = make_double2(ecore + mult * re + er, mult * im + ei);
+}
+
+void launch_split_theta_gather(afqmc_handle* h, const int* d_idx, int m);
+
+// exact mixed-precision local energies of m walkers: all of them (d_idx NULL,
+// m = nwalk) or the walkers d_idx[0..m) (results in out[0..m))
+void launch_local_energy_mixed_subset(afqmc_handle* h, const int* d_idx, int m, double2* out) {
+  const int Kn = h->N;
+  if (d_idx) launch_split_theta_gather(h, d_idx, m);
+  else split_rows(h, h->theta, Kn, 2 * m * h->nce, Kn, h->ke_pad, 1, h->thetaE);
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_tc_exchange, cudaFuncAttributeMaxDynamicSharedMemorySize, EX_SMEM);
+    attr = true;
+  }
+  ExArgs a[2];
+  int gt = 1, wt = 1;
+  for (int s = 0; s < h->nchan; ++s) {
+    const int n = h->chan[s].n;
+    a[s].n = n;
+    a[s].gbox = h->ex_gbox[s];
+    a[s].wbox = h->ex_wbox[s];
+    a[s].a_bytes = BK * 2 * n * a[s].gbox;
+    a[s].b_bytes = BK * 2 * n * 2 * a[s].wbox;
+    a[s].col_off = h->chan[s].col_off;
+    a[s].s = s;
+    gt = std::max(gt, (h->nchol_ene + a[s].gbox - 1) / a[s].gbox);
+    wt = std::max(wt, (m + a[s].wbox - 1) / a[s].wbox);
+  }
+  if (h->nchan == 1) a[1] = a[0];
+  if (h->nchol_ene > 0) {
+    dim3 grid(wt, gt, h->nchan);
+    k_tc_exchange<<<grid, 128, EX_SMEM, h->stream>>>(h->tm_rotE[0], h->tm_thE[0], h->tm_rotE[h->nchan - 1],
+                                                    h->tm_thE[h->nchan - 1], a[0], a[1], h->nchol_ene, m, h->ke_pad,
+                                                    h->nchan, h->xc, h->d_err);
+    h->launches++;
+  }
+  k_energy_assemble<<<m, 256, 0, h->stream>>>(h->theta, h->h1phi, h->xc, out, h->N, h->nce, h->nchol_ene, h->nchan,
+                                              h->mult, h->ecore, d_idx);
+  h->launches++;
+}
+
+void launch_local_energy_mixed(afqmc_handle* h) { launch_local_energy_mixed_subset(h, nullptr, h->nwalk, h->eloc); }
+
+}  // namespace afqmc

@@ -23,7 +23,7 @@ namespace afqmc {
 __global__ void k_overlap_theta(const double2* __restrict__ psi, const double* __restrict__ phi,
                                 double* __restrict__ theta, double2* __restrict__ det,
                                 const double* __restrict__ weights, int N, int ncw, int nce,
-                                Channel c0, Channel c1, int only_live) {
+                                Channel c0, Channel c1, int only_live, int theta_fp32) {
   const int w = blockIdx.x;
   const Channel ch = blockIdx.y == 0 ? c0 : c1;
   if (only_live && !(weights[w] > 1.0e-8)) return;
@@ -94,6 +94,23 @@ __global__ void k_overlap_theta(const double2* __restrict__ psi, const double* _
   // theta[p][j] = sum_i psi[p][i] Minv[i][j]
   double* tre = theta + (size_t)(2 * w) * nce * N + (size_t)ch.col_off * N;
   double* tim = tre + (size_t)nce * N;
+  if (theta_fp32) {
+    // mixed form: theta feeds split-BF16 contractions, FP32 arithmetic suffices
+    for (int e = threadIdx.x; e < N * n; e += blockDim.x) {
+      const int j = e / N, p = e % N;
+      float re = 0.f, im = 0.f;
+      for (int i = 0; i < n; ++i) {
+        const double2 v = ps[i * N + p];
+        const double2 m = a[i * n2 + n + j];
+        const float vx = (float)v.x, vy = (float)v.y, mx = (float)m.x, my = (float)m.y;
+        re = fmaf(vx, mx, fmaf(-vy, my, re));
+        im = fmaf(vx, my, fmaf(vy, mx, im));
+      }
+      tre[j * N + p] = re;
+      tim[j * N + p] = im;
+    }
+    return;
+  }
   for (int e = threadIdx.x; e < N * n; e += blockDim.x) {
     const int j = e / N, p = e % N;
     double re = 0.0, im = 0.0;
@@ -108,8 +125,126 @@ __global__ void k_overlap_theta(const double2* __restrict__ psi, const double* _
   }
 }
 
+// Same computation with one warp per (walker, channel), for n <= 32: the
+// augmented [M | I] (n x 2n) sits in the warp's shared-memory slice, each lane
+// owns columns lane and lane + 32, and the Gauss-Jordan steps need only
+// warp-level synchronisation.  Pivot = first row of largest |M_ik|.
+constexpr int OW_WARPS = 4;
+
+__global__ void __launch_bounds__(OW_WARPS * 32)
+    k_overlap_warp(const double2* __restrict__ psi, const double* __restrict__ phi, double* __restrict__ theta,
+                   double2* __restrict__ det, const double* __restrict__ weights, int W, int N, int ncw, int nce,
+                   Channel c0, Channel c1, int nchan, int only_live, int theta_fp32, int nmax) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int pair = blockIdx.x * OW_WARPS + warp;
+  if (pair >= W * nchan) return;
+  const int w = pair / nchan, s = pair % nchan;
+  if (only_live && !(weights[w] > 1.0e-8)) return;
+  const Channel ch = s == 0 ? c0 : c1;
+  const int n = ch.n, n2 = 2 * n;
+  extern __shared__ double2 owsm[];
+  double2* a = owsm + (size_t)warp * (nmax * 2 * nmax + nmax);  // [n][2n]
+  double2* fcol = a + (size_t)nmax * 2 * nmax;                  // [n]
+  const double2* ps = psi + (size_t)w * ncw * N + (size_t)ch.psi_off * N;
+  const double* ph = phi + (size_t)ch.col_off * N;
+  // M = Phi^T psi (FP64), identity on the right
+  for (int e = lane; e < n * n; e += 32) {
+    const int i = e / n, j = e % n;
+    const double* pi = ph + (size_t)i * N;
+    const double2* pj = ps + (size_t)j * N;
+    double re = 0.0, im = 0.0;
+    for (int p = 0; p < N; ++p) {
+      const double f = pi[p];
+      const double2 v = pj[p];
+      re = fma(f, v.x, re);
+      im = fma(f, v.y, im);
+    }
+    a[i * n2 + j] = make_double2(re, im);
+    a[i * n2 + n + j] = make_double2(i == j ? 1.0 : 0.0, 0.0);
+  }
+  __syncwarp();
+  double2 detv = make_double2(1.0, 0.0);
+  for (int k = 0; k < n; ++k) {
+    double best = -1.0;
+    int bi = k;
+    for (int i = k + lane; i < n; i += 32) {
+      const double v = cabs2(a[i * n2 + k]);
+      if (v > best) { best = v; bi = i; }
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+      const double ob = __shfl_xor_sync(0xffffffffu, best, off);
+      const int oi = __shfl_xor_sync(0xffffffffu, bi, off);
+      if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+    }
+    if (bi != k)
+      for (int j = lane; j < n2; j += 32) {
+        const double2 t = a[k * n2 + j];
+        a[k * n2 + j] = a[bi * n2 + j];
+        a[bi * n2 + j] = t;
+      }
+    __syncwarp();
+    const double2 pv = a[k * n2 + k];
+    detv = cmul(detv, pv);
+    if (bi != k) detv = make_double2(-detv.x, -detv.y);
+    const double2 inv = crecip(pv);
+    for (int i = lane; i < n; i += 32) fcol[i] = a[i * n2 + k];
+    __syncwarp();
+    for (int j = k + lane; j < n2; j += 32) a[k * n2 + j] = cmul(a[k * n2 + j], inv);
+    __syncwarp();
+    for (int i = 0; i < n; ++i) {
+      if (i == k) continue;
+      const double2 f = fcol[i];
+      for (int j = k + lane; j < n2; j += 32) a[i * n2 + j] = csub(a[i * n2 + j], cmul(f, a[k * n2 + j]));
+    }
+    __syncwarp();
+  }
+  if (lane == 0) det[2 * w + s] = detv;
+  double* tre = theta + (size_t)(2 * w) * nce * N + (size_t)ch.col_off * N;
+  double* tim = tre + (size_t)nce * N;
+  for (int e = lane; e < N * n; e += 32) {
+    const int j = e / N, p = e % N;
+    if (theta_fp32) {
+      float re = 0.f, im = 0.f;
+      for (int i = 0; i < n; ++i) {
+        const double2 v = ps[i * N + p];
+        const double2 m = a[i * n2 + n + j];
+        const float vx = (float)v.x, vy = (float)v.y, mx = (float)m.x, my = (float)m.y;
+        re = fmaf(vx, mx, fmaf(-vy, my, re));
+        im = fmaf(vx, my, fmaf(vy, mx, im));
+      }
+      tre[j * N + p] = re;
+      tim[j * N + p] = im;
+    } else {
+      double re = 0.0, im = 0.0;
+      for (int i = 0; i < n; ++i) {
+        const double2 v = ps[i * N + p];
+        const double2 m = a[i * n2 + n + j];
+        re += v.x * m.x - v.y * m.y;
+        im += v.x * m.y + v.y * m.x;
+      }
+      tre[j * N + p] = re;
+      tim[j * N + p] = im;
+    }
+  }
+}
+
 void launch_overlap_theta(afqmc_handle* h, bool only_live) {
+  h->fb_current = false;  // theta changes
   int nmax = std::max(h->chan[0].n, h->nchan > 1 ? h->chan[1].n : 0);
+  if (nmax <= 32) {
+    const size_t smem = (size_t)OW_WARPS * (nmax * 2 * nmax + nmax) * sizeof(double2);
+    static bool attr_w = false;
+    if (!attr_w) {
+      cudaFuncSetAttribute(k_overlap_warp, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
+      attr_w = true;
+    }
+    const int pairs = h->nwalk * h->nchan;
+    k_overlap_warp<<<(pairs + OW_WARPS - 1) / OW_WARPS, OW_WARPS * 32, smem, h->stream>>>(
+        h->psi, h->phi, h->theta, h->det, h->weights, h->nwalk, h->N, h->ncw, h->nce, h->chan[0], h->chan[1],
+        h->nchan, only_live ? 1 : 0, h->precision == AFQMC_PREC_MIXED ? 1 : 0, nmax);
+    h->launches++;
+    return;
+  }
   size_t smem = (size_t)nmax * 2 * nmax * sizeof(double2) + nmax * sizeof(double2);
   static bool attr_set = false;
   if (!attr_set) {
@@ -119,7 +254,7 @@ void launch_overlap_theta(afqmc_handle* h, bool only_live) {
   dim3 grid(h->nwalk, h->nchan);
   k_overlap_theta<<<grid, 256, smem, h->stream>>>(h->psi, h->phi, h->theta, h->det, h->weights, h->N,
                                                   h->ncw, h->nce, h->chan[0], h->chan[1],
-                                                  only_live ? 1 : 0);
+                                                  only_live ? 1 : 0, h->precision == AFQMC_PREC_MIXED ? 1 : 0);
   h->launches++;
 }
 
@@ -252,8 +387,9 @@ __global__ void k_fields(const double* __restrict__ fb, const double2* __restric
                          const double* __restrict__ xi, double* __restrict__ x, float* __restrict__ x32,
                          double2* __restrict__ shift, double2* __restrict__ fbterm,
                          const double* __restrict__ weights, int G, double sdt, int use_rng,
-                         uint64_t seed, uint64_t step, int write32) {
+                         uint64_t seed, const unsigned long long* __restrict__ stepp, int write32) {
   const int w = blockIdx.x;
+  const uint64_t step = *stepp;
   const bool live = weights[w] > 1.0e-8;
   double shr = 0.0, shi = 0.0, ftr = 0.0, fti = 0.0;
   const double* fbr = fb + (size_t)(2 * w) * G;
@@ -292,7 +428,7 @@ __global__ void k_fields(const double* __restrict__ fb, const double2* __restric
 void launch_fields(afqmc_handle* h, bool device_rng) {
   k_fields<<<h->nwalk, 256, 0, h->stream>>>(h->fb, h->mf, h->xi, h->x, h->x32, h->shift, h->fbterm,
                                             h->weights, h->G, sqrt(h->dt), device_rng ? 1 : 0, h->seed,
-                                            h->step_counter, h->precision == AFQMC_PREC_REF32 ? 1 : 0);
+                                            h->d_step, h->precision == AFQMC_PREC_REF32 ? 1 : 0);
   h->launches++;
 }
 
@@ -366,7 +502,8 @@ __global__ void k_propagate(double2* __restrict__ psi, const double* __restrict_
 __global__ void k_weights(double* __restrict__ weights, double2* __restrict__ ovlp,
                           const double2* __restrict__ det, const double2* __restrict__ shift,
                           const double2* __restrict__ fbterm, double* __restrict__ scal, int W, int nchan,
-                          int mult, double dt, double c0r, double c0i, double cap, double target) {
+                          int mult, double dt, double c0r, double c0i, double cap, double target,
+                          unsigned long long* __restrict__ stepp) {
   const double eshift = scal[S_ESHIFT];
   const double sdt = sqrt(dt);
   double sumw = 0.0;
@@ -398,13 +535,15 @@ __global__ void k_weights(double* __restrict__ weights, double2* __restrict__ ov
     scal[S_SUMW] = sumw;
     scal[S_NCAP] += ncap;
     scal[S_ESHIFT] = scal[S_EEST] - 0.1 * log(sumw / target) / dt;
+    *stepp += 1;  // the device field stream's step counter (graph replays advance it)
   }
 }
 
 void launch_weights(afqmc_handle* h) {
   const double cr = h->prop_constant.real(), ci = h->prop_constant.imag();
   k_weights<<<1, 1024, 0, h->stream>>>(h->weights, h->ovlp, h->det, h->shift, h->fbterm, h->scal, h->nwalk,
-                                       h->nchan, h->mult, h->dt, cr, ci, h->weight_cap, h->pop_target);
+                                       h->nchan, h->mult, h->dt, cr, ci, h->weight_cap, h->pop_target,
+                                       h->d_step);
   h->launches++;
 }
 

@@ -55,6 +55,20 @@ bool make_tmap_bf16(CUtensorMap* tm, const void* base, int rows, int kpad, int b
   return r == CUDA_SUCCESS;
 }
 
+// 3-D BF16 tensor [d2][d1][kpad], box = 64 x b1 x b2, 128-byte swizzle
+bool make_tmap_bf16_3d(CUtensorMap* tm, const void* base, int kpad, int d1, int d2, int b1, int b2) {
+  PFN_encodeTiled enc = encode_fn();
+  if (!enc) return false;
+  cuuint64_t dims[3] = {(cuuint64_t)kpad, (cuuint64_t)d1, (cuuint64_t)d2};
+  cuuint64_t strides[2] = {(cuuint64_t)kpad * 2, (cuuint64_t)kpad * 2 * d1};
+  cuuint32_t box[3] = {(cuuint32_t)BK, (cuuint32_t)b1, (cuuint32_t)b2};
+  cuuint32_t estr[3] = {1, 1, 1};
+  CUresult r = enc(tm, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<void*>(base), dims, strides, box, estr,
+                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS;
+}
+
 // ---------------------------------------------------------------------------
 // split-BF16 operand packing
 // ---------------------------------------------------------------------------
@@ -66,30 +80,33 @@ __device__ __forceinline__ void split_bf16(double x, __nv_bfloat16& hi, __nv_bfl
 
 // dst[r][0:3K] = pattern of src[r][0:K] (FP64, row stride lds); pattern 0:
 // [hi | hi | lo] (the static side), 1: [hi | lo | hi] (the per-step side).
-// Columns K*3 .. kpad-1 are zero.
+// Columns 3K .. kpad-1 are zero.  Grid (column blocks, rows); each thread
+// splits one source element and writes its three copies.
 __global__ void k_split_rows(const double* __restrict__ src, long lds, int rows, int K, int kpad, int pattern,
                              __nv_bfloat16* __restrict__ dst) {
-  const long total = (long)rows * kpad;
-  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < total; e += (long)gridDim.x * blockDim.x) {
-    const int r = (int)(e / kpad), c = (int)(e % kpad);
-    __nv_bfloat16 v = __float2bfloat16_rn(0.f);
-    if (c < 3 * K) {
-      const int part = c / K, k = c % K;
-      __nv_bfloat16 hi, lo;
-      split_bf16(src[(long)r * lds + k], hi, lo);
-      const bool use_lo = pattern == 0 ? part == 2 : part == 1;
-      v = use_lo ? lo : hi;
-    }
-    dst[e] = v;
+  const int r = blockIdx.y;
+  const double* s = src + (long)r * lds;
+  __nv_bfloat16* d = dst + (long)r * kpad;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < K; k += gridDim.x * blockDim.x) {
+    __nv_bfloat16 hi, lo;
+    split_bf16(s[k], hi, lo);
+    d[k] = hi;
+    d[K + k] = pattern == 0 ? hi : lo;
+    d[2 * K + k] = pattern == 0 ? lo : hi;
   }
+  const __nv_bfloat16 z = __float2bfloat16_rn(0.f);
+  for (int c = 3 * K + blockIdx.x * blockDim.x + threadIdx.x; c < kpad; c += gridDim.x * blockDim.x) d[c] = z;
 }
 
 void split_rows(afqmc_handle* h, const double* src, long lds, int rows, int K, int kpad, int pattern,
                 __nv_bfloat16* dst) {
-  const long total = (long)rows * kpad;
-  const int blocks = (int)std::min<long>((total + 255) / 256, 152L * 16);
-  k_split_rows<<<blocks, 256, 0, h->stream>>>(src, lds, rows, K, kpad, pattern, dst);
-  h->launches++;
+  const int cb = std::max(1, std::min(8, (K + 255) / 256));
+  for (int r0 = 0; r0 < rows; r0 += 65535) {
+    dim3 grid(cb, std::min(65535, rows - r0));
+    k_split_rows<<<grid, 256, 0, h->stream>>>(src + (long)r0 * lds, lds, rows - r0, K, kpad, pattern,
+                                              dst + (long)r0 * kpad);
+    h->launches++;
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -104,20 +121,17 @@ struct EpiFB {
 };
 
 // VHS: rows t (packed index), columns (walker, plane) with plane 0 = L.Re(x),
-// plane 1 = L.Im(x); full symmetric V = sqrt(dt)(i L.Re(x) - L.Im(x)) in FP32
-// re / im planes, column-major (V(p, q) at q N + p).
+// plane 1 = L.Im(x); V = sqrt(dt)(i L.Re(x) - L.Im(x)) kept packed (lower
+// triangle, index t) in FP32 re / im planes: Vp[w][s][re|im][t].  Consecutive
+// TMEM lanes are consecutive t, so the stores of a warp are contiguous.
 struct EpiV32 {
   float* V;
-  const int2* tri;
-  int N, nspV, s;
+  int T, nspV, s;
   float sdt;
   __device__ __forceinline__ void operator()(int m, int n, float v) const {
     const int w = n >> 1, plane = n & 1;
-    const int2 ij = tri[m];
     const float val = plane == 0 ? sdt * v : -(sdt * v);
-    float* Vb = V + ((size_t)(w * nspV + s) * 2 + (plane == 0 ? 1 : 0)) * N * N;
-    Vb[(size_t)ij.y * N + ij.x] = val;
-    Vb[(size_t)ij.x * N + ij.y] = val;
+    V[((size_t)(w * nspV + s) * 2 + (plane == 0 ? 1 : 0)) * T + m] = val;
   }
 };
 
@@ -143,14 +157,16 @@ void launch_theta_split(afqmc_handle* h) {
 }
 
 void launch_force_bias_mixed(afqmc_handle* h) {
+  if (h->fb_current) return;  // already computed from this theta (control-variate features)
   launch_theta_split(h);
   EpiFB epi{h->fb32, h->G, (float)h->mult};
   launch_tc(h, h->tm_rot, h->tm_theta, h->G, 2 * h->nwalk, h->kf_pad, epi);
+  h->fb_current = true;
 }
 
 void launch_vhs_mixed(afqmc_handle* h) {
   for (int s = 0; s < h->nspV; ++s) {
-    EpiV32 epi{h->V32, h->tri, h->N, h->nspV, s, (float)sqrt(h->dt)};
+    EpiV32 epi{h->V32, h->T, h->nspV, s, (float)sqrt(h->dt)};
     launch_tc(h, h->tm_LT[s], h->tm_x, h->T, 2 * h->nwalk, h->kv_pad, epi);
   }
 }
@@ -162,8 +178,9 @@ __global__ void k_fields_mixed(const float* __restrict__ fb, const double2* __re
                                const double* __restrict__ xi, __nv_bfloat16* __restrict__ xB, int kv_pad,
                                double2* __restrict__ shift, double2* __restrict__ fbterm,
                                const double* __restrict__ weights, int G, double sdt, int use_rng, uint64_t seed,
-                               uint64_t step) {
+                               const unsigned long long* __restrict__ stepp) {
   const int w = blockIdx.x;
+  const uint64_t step = *stepp;
   const bool live = weights[w] > 1.0e-8;
   double shr = 0.0, shi = 0.0, ftr = 0.0, fti = 0.0;
   const float* fbr = fb + (size_t)(2 * w) * G;
@@ -200,7 +217,7 @@ __global__ void k_fields_mixed(const float* __restrict__ fb, const double2* __re
 void launch_fields_mixed(afqmc_handle* h, bool device_rng) {
   k_fields_mixed<<<h->nwalk, 256, 0, h->stream>>>(h->fb32, h->mf, h->xi, h->xB, h->kv_pad, h->shift, h->fbterm,
                                                   h->weights, h->G, sqrt(h->dt), device_rng ? 1 : 0, h->seed,
-                                                  h->step_counter);
+                                                  h->d_step);
   h->launches++;
 }
 
@@ -212,12 +229,21 @@ void launch_fields_mixed(afqmc_handle* h, bool device_rng) {
 // ---------------------------------------------------------------------------
 constexpr int PCH32 = 16;
 
+// M(p, q) from a full column-major matrix (packed == 0) or from the packed
+// lower triangle (packed == 1, index max(p,q)(max(p,q)+1)/2 + min(p,q))
 __device__ __forceinline__ void apply_rows32(const float* __restrict__ Mr, const float* __restrict__ Mi,
-                                             const float2* in, int N, int nc, int p, float2* acc) {
+                                             const float2* in, int N, int nc, int p, float2* acc, int packed) {
 #pragma unroll
   for (int j = 0; j < PCH32; ++j) acc[j] = make_float2(0.f, 0.f);
   for (int q = 0; q < N; ++q) {
-    const float mr = Mr[(size_t)q * N + p], mi = Mi[(size_t)q * N + p];
+    size_t idx;
+    if (packed) {
+      const int a = p > q ? p : q, b = p > q ? q : p;
+      idx = (size_t)a * (a + 1) / 2 + b;
+    } else {
+      idx = (size_t)q * N + p;
+    }
+    const float mr = Mr[idx], mi = Mi[idx];
 #pragma unroll
     for (int j = 0; j < PCH32; ++j) {
       if (j < nc) {
@@ -241,8 +267,9 @@ __global__ void k_propagate32(double2* __restrict__ psi, const float* __restrict
   const int nc = c.nc;
   const float* Br = expm32 + (size_t)(nspB == 1 ? 0 : c.spin) * 2 * N * N;
   const float* Bi = Br + (size_t)N * N;
-  const float* Vr = V + ((size_t)(w * nspV + (nspV == 1 ? 0 : c.spin)) * 2) * N * N;
-  const float* Vi = Vr + (size_t)N * N;
+  const int T = N * (N + 1) / 2;
+  const float* Vr = V + ((size_t)(w * nspV + (nspV == 1 ? 0 : c.spin)) * 2) * T;
+  const float* Vi = Vr + T;
   double2* ps = psi + (size_t)w * ncw * N + (size_t)c.c0 * N;
   for (int e = threadIdx.x; e < N * nc; e += blockDim.x) {
     const double2 v = ps[e];
@@ -252,7 +279,7 @@ __global__ void k_propagate32(double2* __restrict__ psi, const float* __restrict
   float2 acc[PCH32], tmp[PCH32];
   const int p = threadIdx.x;
   const bool act = p < N;
-  if (act) apply_rows32(Br, Bi, cur, N, nc, p, tmp);  // B psi
+  if (act) apply_rows32(Br, Bi, cur, N, nc, p, tmp, 0);  // B psi
   __syncthreads();
   if (act) {
 #pragma unroll
@@ -266,7 +293,7 @@ __global__ void k_propagate32(double2* __restrict__ psi, const float* __restrict
   float2* b = cur;
   for (int k = 1; k <= 5; ++k) {
     const float inv = 1.f / (float)k;
-    if (act) apply_rows32(Vr, Vi, a, N, nc, p, tmp);
+    if (act) apply_rows32(Vr, Vi, a, N, nc, p, tmp, 1);
     __syncthreads();
     if (act) {
 #pragma unroll
@@ -288,14 +315,162 @@ __global__ void k_propagate32(double2* __restrict__ psi, const float* __restrict
   }
   __syncthreads();
   if (act) {
-    apply_rows32(Br, Bi, b, N, nc, p, tmp);
+    apply_rows32(Br, Bi, b, N, nc, p, tmp, 0);
 #pragma unroll
     for (int j = 0; j < PCH32; ++j)
       if (j < nc) ps[j * N + p] = make_double2((double)tmp[j].x, (double)tmp[j].y);
   }
 }
 
+// ---------------------------------------------------------------------------
+// FP32 propagator for N <= 128: one CTA per walker (per spin block for
+// int_type U) holds the walker's full V in shared memory (unpacked once from
+// the packed planes), and applies B, the five Taylor terms and B to up to 40
+// columns at a time.  Thread (rg, cg) owns rows 4 rg .. 4 rg + 3 and columns
+// 5 cg .. 5 cg + 4 of the product; the Taylor sum of its 20 entries stays in
+// registers.  Column panels in shared memory are row-major [q][j].
+// ---------------------------------------------------------------------------
+constexpr int PS_RB = 4, PS_CB = 5, PS_CW = 40, PS_NMAX = 128;
+
+template <int SRC>  // 0: M = V in shared memory (complex); 1: M = B in global memory (re / im planes)
+__device__ __forceinline__ void ps_apply(const float2* __restrict__ Vs, const float* __restrict__ Br,
+                                         const float* __restrict__ Bi, int realB, const float2* in, int N, int p0,
+                                         int j0, float2 (&out)[PS_RB][PS_CB]) {
+#pragma unroll
+  for (int r = 0; r < PS_RB; ++r)
+#pragma unroll
+    for (int c = 0; c < PS_CB; ++c) out[r][c] = make_float2(0.f, 0.f);
+  for (int q = 0; q < N; ++q) {
+    float2 a[PS_RB];
+#pragma unroll
+    for (int r = 0; r < PS_RB; ++r) {
+      const int p = min(p0 + r, N - 1);
+      if (SRC == 0) a[r] = Vs[q * N + p];
+      else a[r] = make_float2(__ldg(Br + (size_t)q * N + p), realB ? 0.f : __ldg(Bi + (size_t)q * N + p));
+    }
+    float2 b[PS_CB];
+#pragma unroll
+    for (int c = 0; c < PS_CB; ++c) b[c] = in[q * PS_CW + j0 + c];
+#pragma unroll
+    for (int r = 0; r < PS_RB; ++r)
+#pragma unroll
+      for (int c = 0; c < PS_CB; ++c) {
+        out[r][c].x = fmaf(a[r].x, b[c].x, fmaf(-a[r].y, b[c].y, out[r][c].x));
+        out[r][c].y = fmaf(a[r].x, b[c].y, fmaf(a[r].y, b[c].x, out[r][c].y));
+      }
+  }
+}
+
+__global__ void __launch_bounds__(256, 1)
+    k_prop32_smem(double2* __restrict__ psi, const float* __restrict__ Vp, const float* __restrict__ expm32,
+                  const int2* __restrict__ tri, const double* __restrict__ weights, int N, int ncw, int na, int nspV,
+                  int realB) {
+  const int w = blockIdx.x;
+  if (!(weights[w] > 1.0e-8)) return;
+  const int sp = blockIdx.y;  // spin block (int_type U only)
+  const int T = N * (N + 1) / 2;
+  extern __shared__ float2 ps_sm[];
+  float2* Vs = ps_sm;                    // [N][N] column-major
+  float2* bufA = ps_sm + N * N;          // [N][PS_CW]
+  float2* bufB = bufA + N * PS_CW;       // [N][PS_CW]
+  const float* vre = Vp + ((size_t)(w * nspV + sp) * 2) * T;
+  const float* vim = vre + T;
+  for (int t = threadIdx.x; t < T; t += blockDim.x) {
+    const int2 ij = tri[t];
+    const float2 v = make_float2(vre[t], vim[t]);
+    Vs[ij.y * N + ij.x] = v;
+    Vs[ij.x * N + ij.y] = v;
+  }
+  const float* Br = expm32 + (size_t)sp * 2 * N * N;
+  const float* Bi = Br + (size_t)N * N;
+  const int col_lo = nspV == 1 ? 0 : (sp == 0 ? 0 : na);
+  const int col_hi = nspV == 1 ? ncw : (sp == 0 ? na : ncw);
+  const int rg = threadIdx.x / (PS_CW / PS_CB), cg = threadIdx.x % (PS_CW / PS_CB);
+  const int p0 = rg * PS_RB, j0 = cg * PS_CB;
+  const bool act = p0 < N;
+  double2* pw = psi + (size_t)w * ncw * N;
+  for (int c0 = col_lo; c0 < col_hi; c0 += PS_CW) {
+    const int nc = min(PS_CW, col_hi - c0);
+    __syncthreads();
+    for (int e = threadIdx.x; e < N * PS_CW; e += blockDim.x) {
+      const int q = e / PS_CW, j = e % PS_CW;
+      float2 v = make_float2(0.f, 0.f);
+      if (j < nc) {
+        const double2 d = pw[(size_t)(c0 + j) * N + q];
+        v = make_float2((float)d.x, (float)d.y);
+      }
+      bufA[e] = v;
+    }
+    __syncthreads();
+    float2 acc[PS_RB][PS_CB], out[PS_RB][PS_CB];
+    if (act) ps_apply<1>(Vs, Br, Bi, realB, bufA, N, p0, j0, out);
+    __syncthreads();
+    if (act) {
+#pragma unroll
+      for (int r = 0; r < PS_RB; ++r)
+#pragma unroll
+        for (int c = 0; c < PS_CB; ++c) {
+          acc[r][c] = out[r][c];
+          if (p0 + r < N) bufB[(p0 + r) * PS_CW + j0 + c] = out[r][c];
+        }
+    }
+    float2* src = bufB;
+    float2* dst = bufA;
+    for (int k = 1; k <= 5; ++k) {
+      __syncthreads();
+      if (act) ps_apply<0>(Vs, Br, Bi, realB, src, N, p0, j0, out);
+      const float inv = 1.f / (float)k;
+      __syncthreads();
+      if (act) {
+#pragma unroll
+        for (int r = 0; r < PS_RB; ++r)
+#pragma unroll
+          for (int c = 0; c < PS_CB; ++c) {
+            out[r][c].x *= inv;
+            out[r][c].y *= inv;
+            acc[r][c].x += out[r][c].x;
+            acc[r][c].y += out[r][c].y;
+            if (p0 + r < N) dst[(p0 + r) * PS_CW + j0 + c] = out[r][c];
+          }
+      }
+      float2* t = src; src = dst; dst = t;
+    }
+    __syncthreads();
+    if (act) {
+#pragma unroll
+      for (int r = 0; r < PS_RB; ++r)
+#pragma unroll
+        for (int c = 0; c < PS_CB; ++c)
+          if (p0 + r < N) dst[(p0 + r) * PS_CW + j0 + c] = acc[r][c];
+    }
+    __syncthreads();
+    if (act) {
+      ps_apply<1>(Vs, Br, Bi, realB, dst, N, p0, j0, out);
+#pragma unroll
+      for (int r = 0; r < PS_RB; ++r)
+#pragma unroll
+        for (int c = 0; c < PS_CB; ++c)
+          if (p0 + r < N && j0 + c < nc)
+            pw[(size_t)(c0 + j0 + c) * N + p0 + r] = make_double2((double)out[r][c].x, (double)out[r][c].y);
+    }
+  }
+}
+
 void launch_propagate_mixed(afqmc_handle* h) {
+  if (h->N <= PS_NMAX) {
+    const size_t smem = ((size_t)h->N * h->N + 2 * (size_t)h->N * PS_CW) * sizeof(float2);
+    static bool attr2 = false;
+    if (!attr2) {
+      cudaFuncSetAttribute(k_prop32_smem, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
+      attr2 = true;
+    }
+    const int threads = ((h->N + PS_RB - 1) / PS_RB) * (PS_CW / PS_CB);
+    dim3 grid(h->nwalk, h->nspV);
+    k_prop32_smem<<<grid, threads, smem, h->stream>>>(h->psi, h->V32, h->expm32, h->tri, h->weights, h->N, h->ncw,
+                                                       h->na, h->nspV, h->real_expm ? 1 : 0);
+    h->launches++;
+    return;
+  }
   const size_t smem = 2 * (size_t)h->N * PCH32 * sizeof(float2);
   static bool attr = false;
   if (!attr) {
@@ -321,6 +496,15 @@ bool setup_mixed(afqmc_handle* h) {
             make_tmap_bf16(&h->tm_x, h->xB, 2 * h->nwalk, h->kv_pad, 128);
   for (int s = 0; s < h->nsp && ok; ++s)
     ok = make_tmap_bf16(&h->tm_LT[s], h->LTA + (size_t)s * h->T * h->kv_pad, h->T, h->kv_pad, tc::BM);
+  // local energy: rot split along p, [G][nce][ke_pad]; tiles of whole (g, walker) blocks
+  split_rows(h, h->rot, h->N, h->G * h->nce, h->N, h->ke_pad, 0, h->rotE);
+  for (int s = 0; s < h->nchan && ok; ++s) {
+    const int n = h->chan[s].n;
+    h->ex_gbox[s] = std::max(1, 128 / n);
+    h->ex_wbox[s] = std::max(1, 128 / n);
+    ok = make_tmap_bf16_3d(&h->tm_rotE[s], h->rotE, h->ke_pad, h->nce, h->G, n, h->ex_gbox[s]) &&
+         make_tmap_bf16_3d(&h->tm_thE[s], h->thetaE, h->ke_pad, h->nce, 2 * h->nwalk, n, 2 * h->ex_wbox[s]);
+  }
   return ok;
 }
 
