@@ -53,8 +53,14 @@ def parse():
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--workload", default="cfg2")
     p.add_argument("--no-cpu-baseline", action="store_true")
-    p.add_argument("--quick", action="store_true", help="headline form only (profiling runs)")
-    return p.parse_args()
+    p.add_argument("--quick", action="store_true", help="headline form only")
+    p.add_argument("--profile", action="store_true",
+                   help="for ncu: headline form only, short training, no e2e / CPU legs (numbers not reported)")
+    a = p.parse_args()
+    if a.profile:
+        a.quick = True
+        a.no_cpu_baseline = True
+    return a
 
 
 def dist_env():
@@ -129,8 +135,9 @@ def peaks():
     return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
 
 
-def cpu_baseline(sysd, nwalk_sample=32, steps=4, seconds_cap=30.0):
-    """The oracle port (numpy complex128 + the reference's FP32 VHS) on the host cores."""
+def cpu_baseline(sysd, nwalk_sample=32, steps=4, seconds_cap=30.0, nchol_ene=None):
+    """The oracle port (numpy complex128 + the reference's FP32 VHS) on the host cores;
+    local energies with the same Cholesky truncation as the GPU run."""
     from oracle import afqmc_oracle as O
     N, na, nb = sysd["norb"], sysd["nalpha"], sysd["nbeta"]
     oh = O.Hamiltonian(N, na, nb, sysd["ecore"], sysd["h1"], sysd["h1mod"], sysd["chol"])
@@ -151,7 +158,7 @@ def cpu_baseline(sysd, nwalk_sample=32, steps=4, seconds_cap=30.0):
             break
     t_step = (time.perf_counter() - t0) / done
     te = time.perf_counter()
-    O.local_energy(ot, wk, oh)
+    O.local_energy(ot, wk, oh, nchol_ene)
     t_el = (time.perf_counter() - te) / nwalk_sample
     per_ws = t_step + t_el  # energy every step, as the headline form
     return {"value": 1.0 / per_ws, "unit": "walker-steps/s", "cores": os.cpu_count(), "kind": "port",
@@ -226,11 +233,60 @@ def energy_error(A, sysd, device, nw=256, steps=40):
     return abs(out["mixed"] - out["fp64"]) * 1e3, out
 
 
+def main_multisystem(args, local):
+    """Uneven multi-system batch: 16 synthetic systems, norb ~ U[40, 200],
+    nocc = round(norb / 6), nchol = 5 norb, 256 walkers each, mixed form,
+    each system autotuned for its size class, all advanced by one CUDA graph
+    (10 steps + QR every 5 per replay)."""
+    from vmc_gb300 import afqmc as A
+    from vmc_gb300 import synthetic as S
+    systems = S.multi_system_batch()
+    cache = os.environ.get("AFQMC_TUNE_CACHE", os.path.join(os.path.expanduser("~"), ".cache", "vmc_gb300",
+                                                            "autotune.txt"))
+    os.makedirs(os.path.dirname(cache), exist_ok=True)
+    hs, flops = [], 0.0
+    for sd in systems:
+        n = sd["nalpha"]
+        gh = A.Hamiltonian(sd["norb"], n, n, sd["ecore"], sd["h1"], sd["h1mod"], sd["chol"])
+        gt = A.UHF(gh, sd["phi_a"], sd["phi_b"])
+        wk = A.DQMCWalkers(gh, gt, sd["walkers"], False, 0.005, precision="mixed", device=local, seed=7 + len(hs))
+        A.autotune(wk, cache)
+        e0 = wk.ham_and_overlap().real.mean()
+        wk.set_energy_estimate(e0, e0)
+        hs.append(wk)
+        flops += flops_model(sd["norb"], n, n, sd["nchol"])["step"] * sd["walkers"]
+    g = A.StepGraph(hs, 10, ortho_every=5)
+    for _ in range(max(1, args.warmup // 10 + 1)):
+        g.launch()
+    reps = max(1, args.steps // 10)
+    for h in hs:
+        h.sync()
+    t0 = time.perf_counter()
+    hs[0].timer_start()
+    for _ in range(reps):
+        g.launch()
+    ms = hs[0].timer_stop()
+    for h in hs:
+        h.sync()
+    wall = time.perf_counter() - t0
+    W = sum(sd["walkers"] for sd in systems)
+    out = {"metric": METRIC, "value": W * 10 * reps / (ms / 1e3), "unit": "walker-steps/s", "n_gpus": 1,
+           "steps": 10 * reps, "warmup": args.warmup, "ms_per_step": ms / (10 * reps), "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "bf16x3 / f32 / f64", "data": "synthetic",
+           "config": {"workload": "cfg3: 16 systems, norb %s, 256 walkers each, UHF, mixed form, one CUDA graph"
+                                  % sorted(sd["norb"] for sd in systems),
+                      "graph_nodes": g.nodes(), "ortho_every": 5, "energy": "none in the timed region"},
+           "achieved_tflops_algorithmic": flops * 10 * reps / (ms / 1e3) / 1e12, "wall_s": wall}
+    print(json.dumps(out))
+
+
 def main():
     args = parse()
     rank, world, local = dist_env()
     if args.impl == "reference":
         return main_reference(args, rank, world)
+    if args.workload == "cfg3":
+        return main_multisystem(args, local)
     from vmc_gb300 import afqmc as A
     from vmc_gb300 import synthetic as S
     from vmc_gb300.cv import ControlVariate
@@ -246,18 +302,23 @@ def main():
 
     # --- headline: mixed + control variate, energy estimate every step ---
     wk = make_walkers(A, sysd, "mixed", local)
+    cache = os.environ.get("AFQMC_TUNE_CACHE", os.path.join(os.path.expanduser("~"), ".cache", "vmc_gb300",
+                                                            "autotune.txt"))
+    os.makedirs(os.path.dirname(cache), exist_ok=True)
+    tuned, tune_report = A.autotune(wk, cache)
     nchol_ene = cholesky_truncation(wk, G)
     e0 = wk.ham_and_overlap().real.mean()
     wk.set_energy_estimate(e0, e0)
     cv = ControlVariate(wk, hidden=256, den=8, seed=3)
-    for k in range(120):  # equilibration; training data from steps 20..120 (untimed)
+    n_eq, n_skip = (25, 20) if args.profile else (120, 20)
+    for k in range(n_eq):  # equilibration; training data from steps 20.. (untimed)
         wk.propagate_phaseless(None)
         if (k + 1) % ORTHO_EVERY == 0:
             wk.orthogonalize()
-        if k >= 20:
+        if k >= n_skip:
             cv.collect()
-    cv_loss, cv_n = cv.train(epochs=20, batch=512, lr=1e-3)
-    k0 = 120
+    cv_loss, cv_n = cv.train(epochs=1 if args.profile else 20, batch=512, lr=1e-3)
+    k0 = n_eq
     for k in range(k0, k0 + args.warmup):
         wk.propagate_phaseless(None)
         cv.measure(tag=k, slot=k % 4096)
@@ -275,6 +336,9 @@ def main():
     value = W * args.steps * world / (ms / 1e3)
     k0 += args.steps
 
+    if args.profile:
+        print(json.dumps({"profile_run": True, "ms_per_step": ms / args.steps}))
+        return
     # end to end through the public API with host buffers: fields H2D, weights and the
     # step's energy estimate D2H every step
     rng = np.random.default_rng(1)
@@ -342,7 +406,7 @@ def main():
                                   % (args.workload, N, na, G, W),
                       "form": "mixed + control variate (energy estimate every step, exact on 1/8)",
                       "ortho_every": ORTHO_EVERY, "fields": "device Philox",
-                      "nchol_energy": nchol_ene,
+                      "nchol_energy": nchol_ene, "autotune": tuned, "autotune_report": tune_report,
                       "l2": "inputs larger than L2 (walker state + split operands + VHS %.0f MB per step)"
                             % ((W * 40 * 120 * 16 + W * 2 * 14400 * 2 + W * 2 * 7260 * 4) / 1e6),
                       "parallelism": "replicas" if world > 1 else "single GPU",
@@ -353,11 +417,20 @@ def main():
            "stage_ms_per_step": {k: v / args.steps for k, v in stage.items()},
            "roofline": roof, "e2e": e2e, "gpu_launches": launches, "clocks": clocks}
     if rank == 0 and not args.no_cpu_baseline:
-        out["cpu_baseline"] = cpu_baseline(sysd)
+        out["cpu_baseline"] = cpu_baseline(sysd, nchol_ene=nchol_ene)
     if rank == 0:
         print(json.dumps(out))
     if world > 1:
         dist.destroy_process_group()
+
+
+def reference_truncation(sysd, threshold=1e-3):
+    """The reference's energy Cholesky truncation (MixedEstimator.cpp:363-384), on the oracle."""
+    from oracle import afqmc_oracle as O
+    N, na, nb = sysd["norb"], sysd["nalpha"], sysd["nbeta"]
+    oh = O.Hamiltonian(N, na, nb, sysd["ecore"], sysd["h1"], sysd["h1mod"], sysd["chol"])
+    ot = O.Trial(oh, sysd["trial"], sysd["phi_a"], sysd["phi_b"])
+    return O.truncate_cholesky(ot, oh, ot.phi, sysd["trial"] == "rhf", threshold)[0]
 
 
 def main_reference(args, rank, world):
@@ -365,7 +438,7 @@ def main_reference(args, rank, world):
         return
     from vmc_gb300 import synthetic as S
     sysd = S.workload(args.workload)
-    cb = cpu_baseline(sysd, nwalk_sample=32, steps=max(2, min(args.steps, 6)))
+    cb = cpu_baseline(sysd, nwalk_sample=32, steps=max(2, min(args.steps, 6)), nchol_ene=reference_truncation(sysd))
     N, na, G, W = sysd["norb"], sysd["nalpha"], sysd["nchol"], sysd["walkers"]
     out = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": "walker-steps/s",
            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,

@@ -245,6 +245,16 @@ int afqmc_cv_attach(afqmc_handle* h, afqmc_mlp* m, const float* mean, const floa
 int afqmc_cv_measure(afqmc_handle* h, uint64_t tag, int slot);
 int afqmc_cv_results(afqmc_handle* h, double* out, int nslots);
 
+/* ---- autotuner ----
+ * Time the candidate tile shapes and kernel variants of this handle's size class
+ * on its own data (tensor-core GEMM N-tiles 64/128/256 for the force bias and
+ * the VHS, propagator with V in shared memory or column-chunked, overlap with a
+ * warp or a CTA per matrix) and keep the fastest.  cache_path (nullable): text
+ * file of earlier choices, read first and appended to.  report (nullable)
+ * receives the timings. */
+int afqmc_autotune(afqmc_handle* h, const char* cache_path, char* report, int report_len);
+int afqmc_tuning(const afqmc_handle* h, int* bn_fb, int* bn_vhs, int* prop, int* ovl);
+
 /* ---- CUDA-graph replay (one or several systems) ----
  * Capture nsteps device-field steps of each of the n handles (QR every
  * ortho_every steps, control-variate measurement every cv_every steps when a

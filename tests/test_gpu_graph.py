@@ -61,3 +61,25 @@ def test_uneven_systems_in_one_graph(A):
         assert np.array_equal(da, db) and np.array_equal(wa, wb)
         assert np.all(np.isfinite(da))
     g.close()
+
+
+def test_autotune_choices_and_cache(A, tmp_path):
+    """The autotuner picks valid variants, caches them, and the tuned handle
+    steps like an untuned one (same fields) within the mixed form's tolerance."""
+    s = S.make_system(48, 8, 160, 41, "uhf")
+    a = make(A, s, 300, "mixed", 3)
+    b = make(A, s, 300, "mixed", 3)
+    cache = str(tmp_path / "tune.txt")
+    ch, rep = A.autotune(b, cache)
+    assert ch["bn_fb"] in (64, 128, 256) and ch["bn_vhs"] in (64, 128, 256)
+    assert ch["prop"] in (1, 2) and ch["ovl"] in (1, 2)
+    c = make(A, s, 300, "mixed", 3)
+    ch2, rep2 = A.autotune(c, cache)
+    assert ch2 == ch and rep2.startswith("cached")
+    for k in range(6):
+        a.propagate_phaseless(None)
+        b.propagate_phaseless(None)
+    da, oa, wa = a.get_det()
+    db, ob, wb = b.get_det()
+    assert np.abs(da - db).max() / np.abs(da).max() < 1e-5
+    assert np.abs(wa - wb).max() / np.abs(wa).max() < 1e-5

@@ -537,3 +537,15 @@ class StepGraph:
             self.close()
         except Exception:
             pass
+
+
+def autotune(wk, cache_path=None):
+    """Run the library's autotuner on a DQMCWalkers handle; returns (choices, report)."""
+    L = lib()
+    L.afqmc_autotune.argtypes = [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int]
+    L.afqmc_tuning.argtypes = [ctypes.c_void_p] + [ctypes.POINTER(ctypes.c_int)] * 4
+    buf = ctypes.create_string_buffer(2048)
+    wk._check(L.afqmc_autotune(wk.h, cache_path.encode() if cache_path else None, buf, 2048))
+    v = [ctypes.c_int() for _ in range(4)]
+    L.afqmc_tuning(wk.h, *[ctypes.byref(x) for x in v])
+    return dict(bn_fb=v[0].value, bn_vhs=v[1].value, prop=v[2].value, ovl=v[3].value), buf.value.decode()

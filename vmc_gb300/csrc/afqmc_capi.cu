@@ -171,7 +171,7 @@ void release(afqmc_handle* h) {
                   h->det, h->ovlp, h->weights, h->fb, h->xi, h->x, h->x32, h->shift, h->fbterm, h->V,
                   h->qwork, h->epart, h->eloc, h->scal, h->d_chunks, h->d_err, h->rotA, h->LTA,
                   h->thetaB, h->xB, h->fb32, h->V32, h->expm32, h->d_chunks32, h->rotE, h->thetaE,
-                  h->xc, h->cv_x, h->cv_idx, h->cv_esub, h->cv_f, h->cv_ms, h->cv_out, h->d_step};
+                  h->xc, h->cv_x, h->cv_idx, h->cv_esub, h->cv_f, h->cv_ms, h->cv_out, h->d_step, h->psi32};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (h->host_pinned) cudaFreeHost(h->host_pinned);
@@ -452,6 +452,7 @@ int afqmc_create(const afqmc_ham* ham, const afqmc_trial* trial, const afqmc_opt
     ALLOC(expm32, (size_t)nsp * 2 * NN);
     ALLOC(d_chunks32, h->chunks32.size());
     ALLOC(rotE, (size_t)G * h->nce * h->ke_pad);
+    ALLOC(psi32, W * h->ncw * N);
     ALLOC(thetaE, W * 2 * h->nce * h->ke_pad);
     ALLOC(xc, W * 2 * G * 2);
   }
@@ -529,6 +530,7 @@ int afqmc_create(const afqmc_ham* ham, const afqmc_trial* trial, const afqmc_opt
   }
 #undef UP
   k_fill<<<64, 256, 0, h->stream>>>(h->weights, W, 1.0);
+  afqmc::launch_psi_to_f32(h);
   afqmc::launch_overlap_theta(h, false);
   afqmc::launch_init_overlap(h);
   ce = cudaStreamSynchronize(h->stream);
@@ -586,6 +588,7 @@ int afqmc_set_walkers(afqmc_handle* h, const double* dets, const double* overlap
     k_fill<<<64, 256, 0, h->stream>>>(h->weights, W, 1.0);
     h->launches++;
   }
+  afqmc::launch_psi_to_f32(h);
   afqmc::launch_overlap_theta(h, false);
   if (overlaps) {
     std::vector<double2> o(W);

@@ -112,7 +112,12 @@ struct afqmc_handle {
   float* expm32 = nullptr;           // [nsp][2][N*N]     re / im planes, column-major
   afqmc::PropChunk* d_chunks32 = nullptr;
   int nchunks32 = 0;
-  CUtensorMap tm_rot, tm_theta, tm_x, tm_LT[2];
+  CUtensorMap tm_rot, tm_LT[2];
+  CUtensorMap tm_theta_bn[3], tm_x_bn[3];  // B operands with box heights 64, 128, 256
+  // autotuned choices (afqmc_autotune): GEMM N-tiles; propagator 0 auto / 1 SMEM / 2 chunked / 3 tcgen05;
+  // overlap 0 auto / 1 warp per matrix / 2 block per matrix
+  int tune_bn_fb = 128, tune_bn_vhs = 128, tune_prop = 0, tune_ovl = 0;
+  int tune_prop_best = 0, tune_ovl_best = 0;
   // mixed local energy
   int ke_pad = 0;                    // padded split-K (3N) of the exchange GEMM
   __nv_bfloat16* rotE = nullptr;     // [G][nce][ke_pad]  [hi | hi | lo] of rot along p
@@ -122,6 +127,7 @@ struct afqmc_handle {
   CUtensorMap tm_rotE[2], tm_thE[2];
   unsigned long long* d_step = nullptr;  // device step counter of the Philox field stream
   bool fb_current = false;               // fb32 holds the force bias of the current theta
+  float2* psi32 = nullptr;               // [W][ncw][N] FP32 copy of psi (mixed form)
   // control variate
   float* cv_x = nullptr;             // [W][67] features
   float* cv_f = nullptr;             // [W]     predicted local energies
@@ -146,6 +152,7 @@ void launch_weights(afqmc_handle* h);
 void launch_ortho(afqmc_handle* h);
 void launch_local_energy(afqmc_handle* h);
 void launch_init_overlap(afqmc_handle* h);
+void launch_psi_to_f32(afqmc_handle* h);
 
 // ---- kernels (kernels_mixed.cu) ----
 bool setup_mixed(afqmc_handle* h);

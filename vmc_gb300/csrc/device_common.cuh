@@ -95,17 +95,18 @@ __device__ __forceinline__ U4 philox4x32_10(U4 c, uint32_t k0, uint32_t k1) {
 }
 
 // Standard normal for (step, walker, field): one Philox block gives the
-// Box-Muller pair of fields (2m, 2m+1).
+// Box-Muller pair of fields (2m, 2m+1).  The transform runs in FP32 (24-bit
+// uniforms; the FP64 pipe of this GPU is ~60x slower than its FP32 pipe).
 __device__ __forceinline__ double philox_normal(uint64_t seed, uint64_t step, uint32_t w, uint32_t g) {
   const U4 r = philox4x32_10(U4{g >> 1, w, (uint32_t)step, (uint32_t)(step >> 32)}, (uint32_t)seed,
                              (uint32_t)(seed >> 32));
-  const double two53 = 1.0 / 9007199254740992.0;
-  const double u1 = ((double)(((uint64_t)r.x << 21) | (r.y >> 11)) + 0.5) * two53;
-  const double u2 = ((double)(((uint64_t)r.z << 21) | (r.w >> 11)) + 0.5) * two53;
-  const double rad = sqrt(-2.0 * log(u1));
-  double s, c;
-  sincospi(2.0 * u2, &s, &c);
-  return (g & 1u) ? rad * s : rad * c;
+  const float two24 = 1.0f / 16777216.0f;
+  const float u1 = ((float)(r.x >> 8) + 0.5f) * two24;
+  const float u2 = ((float)(r.z >> 8) + 0.5f) * two24;
+  const float rad = sqrtf(-2.0f * logf(u1));
+  float s, c;
+  sincospif(2.0f * u2, &s, &c);
+  return (double)((g & 1u) ? rad * s : rad * c);
 }
 
 }  // namespace afqmc

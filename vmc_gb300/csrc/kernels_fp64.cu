@@ -125,50 +125,84 @@ __global__ void k_overlap_theta(const double2* __restrict__ psi, const double* _
   }
 }
 
-// Same computation with one warp per (walker, channel), for n <= 32: the
-// augmented [M | I] (n x 2n) sits in the warp's shared-memory slice, each lane
-// owns columns lane and lane + 32, and the Gauss-Jordan steps need only
-// warp-level synchronisation.  Pivot = first row of largest |M_ik|.
+// Same results with one warp per (walker, channel), for n <= 32, and an LU
+// instead of Gauss-Jordan: M = Phi^T psi (FP64, register-tiled: lane
+// (li, lj) owns rows li + 4a and columns lj + 8b), partial-pivot LU of M in FP64
+// (pivot = first row of largest |M_ik|, det = sign * prod U_kk), then every
+// row p of theta from psi[p] . M^-1 by two triangular solves with the LU
+// factors (P M = L U => theta = psi U^-1 L^-1 P).  In the mixed form the solves
+// run in FP32 from the FP32 copy of the walkers.  A CTA holds OW_WARPS walkers
+// of one channel and stages that channel's Phi in shared memory.
 constexpr int OW_WARPS = 4;
 
+// NM: n rounded up to a multiple of 4 (<= 32); lane (li, lj) of the M product
+// owns rows li + 4a (a < NM/4) and columns lj + 8b (b < ceil(NM/8)).
+template <bool F32, int NM>
 __global__ void __launch_bounds__(OW_WARPS * 32)
-    k_overlap_warp(const double2* __restrict__ psi, const double* __restrict__ phi, double* __restrict__ theta,
-                   double2* __restrict__ det, const double* __restrict__ weights, int W, int N, int ncw, int nce,
-                   Channel c0, Channel c1, int nchan, int only_live, int theta_fp32, int nmax) {
+    k_overlap_lu(const double2* __restrict__ psi, const float2* __restrict__ psi32, const double* __restrict__ phi,
+                 double* __restrict__ theta, double2* __restrict__ det, const double* __restrict__ weights, int W,
+                 int N, int ncw, int nce, Channel c0, Channel c1, int only_live, int nmax) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int pair = blockIdx.x * OW_WARPS + warp;
-  if (pair >= W * nchan) return;
-  const int w = pair / nchan, s = pair % nchan;
-  if (only_live && !(weights[w] > 1.0e-8)) return;
+  const int s = blockIdx.y;
   const Channel ch = s == 0 ? c0 : c1;
-  const int n = ch.n, n2 = 2 * n;
-  extern __shared__ double2 owsm[];
-  double2* a = owsm + (size_t)warp * (nmax * 2 * nmax + nmax);  // [n][2n]
-  double2* fcol = a + (size_t)nmax * 2 * nmax;                  // [n]
-  const double2* ps = psi + (size_t)w * ncw * N + (size_t)ch.psi_off * N;
+  const int n = ch.n;
+  extern __shared__ __align__(16) unsigned char ow_raw[];
+  double* phs = (double*)ow_raw;  // [n][N] channel orbitals (column i at i N)
+  const size_t per_warp = ((size_t)nmax * nmax * (sizeof(double2) + sizeof(float2)) + nmax * sizeof(int) + 15) & ~(size_t)15;
+  unsigned char* wbase = ow_raw + (((size_t)nmax * N * sizeof(double) + 15) & ~(size_t)15) + warp * per_warp;
+  double2* a = (double2*)wbase;                                     // [n][n] LU, row-major
+  float2* af = (float2*)(wbase + (size_t)nmax * nmax * sizeof(double2));  // FP32 copy of the factors
+  int* perm = (int*)(wbase + (size_t)nmax * nmax * (sizeof(double2) + sizeof(float2)));
   const double* ph = phi + (size_t)ch.col_off * N;
-  // M = Phi^T psi (FP64), identity on the right
-  for (int e = lane; e < n * n; e += 32) {
-    const int i = e / n, j = e % n;
-    const double* pi = ph + (size_t)i * N;
-    const double2* pj = ps + (size_t)j * N;
-    double re = 0.0, im = 0.0;
+  for (int e = threadIdx.x; e < n * N; e += blockDim.x) phs[e] = ph[e];
+  __syncthreads();
+  const int w = blockIdx.x * OW_WARPS + warp;
+  if (w >= W) return;
+  if (only_live && !(weights[w] > 1.0e-8)) return;
+  const double2* ps = psi + (size_t)w * ncw * N + (size_t)ch.psi_off * N;
+  // M = Phi^T psi
+  {
+    constexpr int OW_RI = NM / 4, OW_RJ = (NM + 7) / 8;
+    const int li = lane >> 3, lj = lane & 7;
+    double2 acc[OW_RI][OW_RJ];
+#pragma unroll
+    for (int x = 0; x < OW_RI; ++x)
+#pragma unroll
+      for (int y = 0; y < OW_RJ; ++y) acc[x][y] = make_double2(0.0, 0.0);
     for (int p = 0; p < N; ++p) {
-      const double f = pi[p];
-      const double2 v = pj[p];
-      re = fma(f, v.x, re);
-      im = fma(f, v.y, im);
+      double2 v[OW_RJ];
+#pragma unroll
+      for (int y = 0; y < OW_RJ; ++y) {
+        const int j = lj + 8 * y;
+        v[y] = j < n ? ps[(size_t)j * N + p] : make_double2(0.0, 0.0);
+      }
+#pragma unroll
+      for (int x = 0; x < OW_RI; ++x) {
+        const int i = li + 4 * x;
+        const double f = i < n ? phs[i * N + p] : 0.0;
+#pragma unroll
+        for (int y = 0; y < OW_RJ; ++y) {
+          acc[x][y].x = fma(f, v[y].x, acc[x][y].x);
+          acc[x][y].y = fma(f, v[y].y, acc[x][y].y);
+        }
+      }
     }
-    a[i * n2 + j] = make_double2(re, im);
-    a[i * n2 + n + j] = make_double2(i == j ? 1.0 : 0.0, 0.0);
+#pragma unroll
+    for (int x = 0; x < OW_RI; ++x)
+#pragma unroll
+      for (int y = 0; y < OW_RJ; ++y) {
+        const int i = li + 4 * x, j = lj + 8 * y;
+        if (i < n && j < n) a[i * n + j] = acc[x][y];
+      }
   }
   __syncwarp();
+  // LU with partial pivoting (FP64)
   double2 detv = make_double2(1.0, 0.0);
   for (int k = 0; k < n; ++k) {
     double best = -1.0;
     int bi = k;
     for (int i = k + lane; i < n; i += 32) {
-      const double v = cabs2(a[i * n2 + k]);
+      const double v = cabs2(a[i * n + k]);
       if (v > best) { best = v; bi = i; }
     }
     for (int off = 16; off > 0; off >>= 1) {
@@ -176,72 +210,181 @@ __global__ void __launch_bounds__(OW_WARPS * 32)
       const int oi = __shfl_xor_sync(0xffffffffu, bi, off);
       if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
     }
+    if (lane == 0) perm[k] = bi;
     if (bi != k)
-      for (int j = lane; j < n2; j += 32) {
-        const double2 t = a[k * n2 + j];
-        a[k * n2 + j] = a[bi * n2 + j];
-        a[bi * n2 + j] = t;
+      for (int j = lane; j < n; j += 32) {
+        const double2 t = a[k * n + j];
+        a[k * n + j] = a[bi * n + j];
+        a[bi * n + j] = t;
       }
     __syncwarp();
-    const double2 pv = a[k * n2 + k];
+    const double2 pv = a[k * n + k];
     detv = cmul(detv, pv);
     if (bi != k) detv = make_double2(-detv.x, -detv.y);
     const double2 inv = crecip(pv);
-    for (int i = lane; i < n; i += 32) fcol[i] = a[i * n2 + k];
+    for (int i = k + 1 + lane; i < n; i += 32) a[i * n + k] = cmul(a[i * n + k], inv);
     __syncwarp();
-    for (int j = k + lane; j < n2; j += 32) a[k * n2 + j] = cmul(a[k * n2 + j], inv);
-    __syncwarp();
-    for (int i = 0; i < n; ++i) {
-      if (i == k) continue;
-      const double2 f = fcol[i];
-      for (int j = k + lane; j < n2; j += 32) a[i * n2 + j] = csub(a[i * n2 + j], cmul(f, a[k * n2 + j]));
+    const int rem = n - k - 1;
+    for (int e = lane; e < rem * rem; e += 32) {
+      const int i = k + 1 + e / rem, j = k + 1 + e % rem;
+      a[i * n + j] = csub(a[i * n + j], cmul(a[i * n + k], a[k * n + j]));
     }
     __syncwarp();
   }
   if (lane == 0) det[2 * w + s] = detv;
+  // perm[k]: row swapped with k at step k -> final row order of P M
+  if (lane == 0) {
+    int order[NM];
+    for (int i = 0; i < n; ++i) order[i] = i;
+    for (int k = 0; k < n; ++k) {
+      const int t = order[k];
+      order[k] = order[perm[k]];
+      order[perm[k]] = t;
+    }
+    for (int k = 0; k < n; ++k) perm[k] = order[k];
+  }
+  if (F32)
+    for (int e = lane; e < n * n; e += 32) af[e] = make_float2((float)a[e].x, (float)a[e].y);
+  __syncwarp();
+  // theta[p][:] = psi[p][:] M^-1 ; with P M = L U: solve w U = psi[p], z L = w, theta[perm[k]] = z[k]
   double* tre = theta + (size_t)(2 * w) * nce * N + (size_t)ch.col_off * N;
   double* tim = tre + (size_t)nce * N;
-  for (int e = lane; e < N * n; e += 32) {
-    const int j = e / N, p = e % N;
-    if (theta_fp32) {
-      float re = 0.f, im = 0.f;
-      for (int i = 0; i < n; ++i) {
-        const double2 v = ps[i * N + p];
-        const double2 m = a[i * n2 + n + j];
-        const float vx = (float)v.x, vy = (float)v.y, mx = (float)m.x, my = (float)m.y;
-        re = fmaf(vx, mx, fmaf(-vy, my, re));
-        im = fmaf(vx, my, fmaf(vy, mx, im));
+  for (int p = lane; p < N; p += 32) {
+    if (F32) {
+      const float2* p32 = psi32 + (size_t)w * ncw * N + (size_t)ch.psi_off * N;
+      float2 r[NM];
+#pragma unroll
+      for (int j = 0; j < NM; ++j)
+        if (j < n) r[j] = p32[(size_t)j * N + p];
+      // w U = r (forward over columns)
+#pragma unroll
+      for (int j = 0; j < NM; ++j) {
+        if (j < n) {
+          float2 t = r[j];
+#pragma unroll
+          for (int i = 0; i < NM; ++i)
+            if (i < j) {
+              const float2 u = af[i * n + j];
+              t.x -= r[i].x * u.x - r[i].y * u.y;
+              t.y -= r[i].x * u.y + r[i].y * u.x;
+            }
+          const float2 d = af[j * n + j];
+          const float den = d.x * d.x + d.y * d.y;
+          r[j] = make_float2((t.x * d.x + t.y * d.y) / den, (t.y * d.x - t.x * d.y) / den);
+        }
       }
-      tre[j * N + p] = re;
-      tim[j * N + p] = im;
+      // z L = w (backward, L unit lower)
+#pragma unroll
+      for (int jj = NM - 1; jj >= 0; --jj) {
+        if (jj < n) {
+          float2 t = r[jj];
+#pragma unroll
+          for (int i = 0; i < NM; ++i)
+            if (i > jj && i < n) {
+              const float2 l = af[i * n + jj];
+              t.x -= r[i].x * l.x - r[i].y * l.y;
+              t.y -= r[i].x * l.y + r[i].y * l.x;
+            }
+          r[jj] = t;
+        }
+      }
+#pragma unroll
+      for (int k = 0; k < NM; ++k)
+        if (k < n) {
+          const int c = perm[k];
+          tre[(size_t)c * N + p] = r[k].x;
+          tim[(size_t)c * N + p] = r[k].y;
+        }
     } else {
-      double re = 0.0, im = 0.0;
-      for (int i = 0; i < n; ++i) {
-        const double2 v = ps[i * N + p];
-        const double2 m = a[i * n2 + n + j];
-        re += v.x * m.x - v.y * m.y;
-        im += v.x * m.y + v.y * m.x;
+      double2 r[NM];
+#pragma unroll
+      for (int j = 0; j < NM; ++j)
+        if (j < n) r[j] = ps[(size_t)j * N + p];
+#pragma unroll
+      for (int j = 0; j < NM; ++j) {
+        if (j < n) {
+          double2 t = r[j];
+#pragma unroll
+          for (int i = 0; i < NM; ++i)
+            if (i < j) t = csub(t, cmul(r[i], a[i * n + j]));
+          r[j] = cdiv(t, a[j * n + j]);
+        }
       }
-      tre[j * N + p] = re;
-      tim[j * N + p] = im;
+#pragma unroll
+      for (int jj = NM - 1; jj >= 0; --jj) {
+        if (jj < n) {
+          double2 t = r[jj];
+#pragma unroll
+          for (int i = 0; i < NM; ++i)
+            if (i > jj && i < n) t = csub(t, cmul(r[i], a[i * n + jj]));
+          r[jj] = t;
+        }
+      }
+#pragma unroll
+      for (int k = 0; k < NM; ++k)
+        if (k < n) {
+          const int c = perm[k];
+          tre[(size_t)c * N + p] = r[k].x;
+          tim[(size_t)c * N + p] = r[k].y;
+        }
     }
   }
+}
+
+// FP32 copy of the walker dets (mixed form; read by the FP32 theta solves)
+__global__ void k_psi_to_f32(const double2* __restrict__ psi, float2* __restrict__ psi32, size_t n) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const double2 v = psi[i];
+    psi32[i] = make_float2((float)v.x, (float)v.y);
+  }
+}
+
+void launch_psi_to_f32(afqmc_handle* h) {
+  if (!h->psi32) return;
+  k_psi_to_f32<<<1024, 256, 0, h->stream>>>(h->psi, h->psi32, (size_t)h->nwalk * h->ncw * h->N);
+  h->launches++;
 }
 
 void launch_overlap_theta(afqmc_handle* h, bool only_live) {
   h->fb_current = false;  // theta changes
   int nmax = std::max(h->chan[0].n, h->nchan > 1 ? h->chan[1].n : 0);
-  if (nmax <= 32) {
-    const size_t smem = (size_t)OW_WARPS * (nmax * 2 * nmax + nmax) * sizeof(double2);
-    static bool attr_w = false;
-    if (!attr_w) {
-      cudaFuncSetAttribute(k_overlap_warp, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
-      attr_w = true;
+  const size_t smem_lu = (((size_t)nmax * h->N * sizeof(double) + 15) & ~(size_t)15) +
+                         OW_WARPS * (((size_t)nmax * nmax * (sizeof(double2) + sizeof(float2)) + nmax * sizeof(int) + 15) &
+                                     ~(size_t)15);
+  if (nmax <= 32 && h->tune_ovl != 2 && smem_lu <= 160 * 1024) {
+    const size_t smem = smem_lu;
+    const bool f32 = h->precision == AFQMC_PREC_MIXED && h->psi32;
+    dim3 grid((h->nwalk + OW_WARPS - 1) / OW_WARPS, h->nchan);
+    const int nm = (nmax + 3) / 4 * 4;
+#define OW_LAUNCH(F, NMV)                                                                                     \
+  {                                                                                                          \
+    static bool attr = false;                                                                                \
+    if (!attr) {                                                                                             \
+      cudaFuncSetAttribute(k_overlap_lu<F, NMV>, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);   \
+      attr = true;                                                                                           \
+    }                                                                                                        \
+    k_overlap_lu<F, NMV><<<grid, OW_WARPS * 32, smem, h->stream>>>(h->psi, h->psi32, h->phi, h->theta, h->det, \
+                                                                  h->weights, h->nwalk, h->N, h->ncw, h->nce, \
+                                                                  h->chan[0], h->chan[1], only_live ? 1 : 0, nmax); \
+  }
+#define OW_NM(F)                          \
+  switch (nm) {                           \
+    case 4: OW_LAUNCH(F, 4) break;        \
+    case 8: OW_LAUNCH(F, 8) break;        \
+    case 12: OW_LAUNCH(F, 12) break;      \
+    case 16: OW_LAUNCH(F, 16) break;      \
+    case 20: OW_LAUNCH(F, 20) break;      \
+    case 24: OW_LAUNCH(F, 24) break;      \
+    case 28: OW_LAUNCH(F, 28) break;      \
+    default: OW_LAUNCH(F, 32) break;      \
+  }
+    if (f32) {
+      OW_NM(true)
+    } else {
+      OW_NM(false)
     }
-    const int pairs = h->nwalk * h->nchan;
-    k_overlap_warp<<<(pairs + OW_WARPS - 1) / OW_WARPS, OW_WARPS * 32, smem, h->stream>>>(
-        h->psi, h->phi, h->theta, h->det, h->weights, h->nwalk, h->N, h->ncw, h->nce, h->chan[0], h->chan[1],
-        h->nchan, only_live ? 1 : 0, h->precision == AFQMC_PREC_MIXED ? 1 : 0, nmax);
+#undef OW_NM
+#undef OW_LAUNCH
     h->launches++;
     return;
   }
@@ -555,8 +698,10 @@ void launch_weights(afqmc_handle* h) {
 // psi <- Q = prod_k (I - conj(tau_k) v_k v_k^H) I,  overlap /= prod beta_k.
 // One CTA per walker; columns are worked in place in global memory (L2).
 // ---------------------------------------------------------------------------
+template <bool SMEM>
 __global__ void k_ortho(double2* __restrict__ psi, double2* __restrict__ qwork, double2* __restrict__ ovlp,
                         int N, int ncw, int na, int nb, int rhf_walker) {
+  extern __shared__ double2 qr_sm[];  // SMEM variant: [N][nmax] working block + [N][nmax] Q
   const int w = blockIdx.x;
   __shared__ double2 s_tau[QR_MAXN];
   __shared__ double s_beta[QR_MAXN];
@@ -567,8 +712,15 @@ __global__ void k_ortho(double2* __restrict__ psi, double2* __restrict__ qwork, 
   const int nblk = rhf_walker ? 1 : 2;
   for (int b = 0; b < nblk; ++b) {
     const int off = b == 0 ? 0 : na, n = b == 0 ? na : nb;
-    double2* A = psi + (size_t)w * ncw * N + (size_t)off * N;
+    double2* Ag = psi + (size_t)w * ncw * N + (size_t)off * N;
+    double2* A = Ag;
     double2* Q = qwork + (size_t)w * ncw * N + (size_t)off * N;
+    if (SMEM) {
+      A = qr_sm;
+      Q = qr_sm + (size_t)N * max(na, nb);
+      for (int e = threadIdx.x; e < N * n; e += blockDim.x) A[e] = Ag[e];
+      __syncthreads();
+    }
     for (int k = 0; k < n; ++k) {
       double2* col = A + (size_t)k * N;
       double t = 0.0;
@@ -637,7 +789,7 @@ __global__ void k_ortho(double2* __restrict__ psi, double2* __restrict__ qwork, 
       }
       __syncthreads();
     }
-    for (int e = threadIdx.x; e < N * n; e += blockDim.x) A[e] = Q[e];
+    for (int e = threadIdx.x; e < N * n; e += blockDim.x) Ag[e] = Q[e];
     __syncthreads();
     if (threadIdx.x == 0)
       for (int k = 0; k < n; ++k) fac = cmul(fac, make_double2(s_beta[k], 0.0));
@@ -648,16 +800,37 @@ __global__ void k_ortho(double2* __restrict__ psi, double2* __restrict__ qwork, 
   }
 }
 
+// QR with the walker's spin block and Q in shared memory when they fit
+// (2 N nocc complex <= 200 KB), else worked in global memory (L2)
+void launch_ortho_core(afqmc_handle* h);
+void launch_psi_to_f32(afqmc_handle* h);
+
 void launch_ortho(afqmc_handle* h) {
-  k_ortho<<<h->nwalk, 256, 0, h->stream>>>(h->psi, h->qwork, h->ovlp, h->N, h->ncw, h->na, h->nb,
-                                           h->rhf_walker);
+  launch_ortho_core(h);
+  launch_psi_to_f32(h);
+}
+
+void launch_ortho_core(afqmc_handle* h) {
+  const size_t smem = 2 * (size_t)h->N * std::max(h->na, h->nb) * sizeof(double2);
+  if (smem <= 200 * 1024) {
+    static bool attr = false;
+    if (!attr) {
+      cudaFuncSetAttribute(k_ortho<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+      attr = true;
+    }
+    k_ortho<true><<<h->nwalk, 256, smem, h->stream>>>(h->psi, h->qwork, h->ovlp, h->N, h->ncw, h->na, h->nb,
+                                                      h->rhf_walker);
+  } else {
+    k_ortho<false><<<h->nwalk, 256, 0, h->stream>>>(h->psi, h->qwork, h->ovlp, h->N, h->ncw, h->na, h->nb,
+                                                    h->rhf_walker);
+  }
   h->launches++;
 }
 
 // The same QR kernel on caller-supplied buffers (no handle).
 void launch_ortho_buffers(double2* psi, double2* qwork, double2* ovlp, int nwalk, int N, int ncw, int na, int nb,
                           int rhf_walker, cudaStream_t stream) {
-  k_ortho<<<nwalk, 256, 0, stream>>>(psi, qwork, ovlp, N, ncw, na, nb, rhf_walker);
+  k_ortho<false><<<nwalk, 256, 0, stream>>>(psi, qwork, ovlp, N, ncw, na, nb, rhf_walker);
 }
 
 // ---------------------------------------------------------------------------

@@ -135,10 +135,10 @@ struct EpiV32 {
   }
 };
 
-template <class Epi>
-static void launch_tc(afqmc_handle* h, const CUtensorMap& ta, const CUtensorMap& tb, int M, int N, int K,
-                      const Epi& epi) {
-  constexpr int BN = 128, ST = 4;
+template <int BN, class Epi>
+static void launch_tc_bn(afqmc_handle* h, const CUtensorMap& ta, const CUtensorMap& tb, int M, int N, int K,
+                         const Epi& epi) {
+  constexpr int ST = 4;
   const int smem = tc::GemmSmem<BN, ST>::TOTAL;
   static bool attr = false;
   if (!attr) {
@@ -148,6 +148,16 @@ static void launch_tc(afqmc_handle* h, const CUtensorMap& ta, const CUtensorMap&
   dim3 grid((N + BN - 1) / BN, (M + tc::BM - 1) / tc::BM);
   tc::k_tc_gemm<BN, ST, Epi><<<grid, 128, smem, h->stream>>>(ta, tb, M, N, K, epi, h->d_err);
   h->launches++;
+}
+
+// N-tile of the tensor-core GEMM chosen by the autotuner (64, 128 or 256);
+// tbs holds the B-operand tensor maps of the three box heights.
+template <class Epi>
+static void launch_tc(afqmc_handle* h, const CUtensorMap& ta, const CUtensorMap* tbs, int bn, int M, int N, int K,
+                      const Epi& epi) {
+  if (bn == 64) launch_tc_bn<64>(h, ta, tbs[0], M, N, K, epi);
+  else if (bn == 256) launch_tc_bn<256>(h, ta, tbs[2], M, N, K, epi);
+  else launch_tc_bn<128>(h, ta, tbs[1], M, N, K, epi);
 }
 
 // theta planes (FP64) -> split BF16 operand rows (w, plane)
@@ -160,14 +170,14 @@ void launch_force_bias_mixed(afqmc_handle* h) {
   if (h->fb_current) return;  // already computed from this theta (control-variate features)
   launch_theta_split(h);
   EpiFB epi{h->fb32, h->G, (float)h->mult};
-  launch_tc(h, h->tm_rot, h->tm_theta, h->G, 2 * h->nwalk, h->kf_pad, epi);
+  launch_tc(h, h->tm_rot, h->tm_theta_bn, h->tune_bn_fb, h->G, 2 * h->nwalk, h->kf_pad, epi);
   h->fb_current = true;
 }
 
 void launch_vhs_mixed(afqmc_handle* h) {
   for (int s = 0; s < h->nspV; ++s) {
     EpiV32 epi{h->V32, h->T, h->nspV, s, (float)sqrt(h->dt)};
-    launch_tc(h, h->tm_LT[s], h->tm_x, h->T, 2 * h->nwalk, h->kv_pad, epi);
+    launch_tc(h, h->tm_LT[s], h->tm_x_bn, h->tune_bn_vhs, h->T, 2 * h->nwalk, h->kv_pad, epi);
   }
 }
 
@@ -255,7 +265,7 @@ __device__ __forceinline__ void apply_rows32(const float* __restrict__ Mr, const
   }
 }
 
-__global__ void k_propagate32(double2* __restrict__ psi, const float* __restrict__ V,
+__global__ void k_propagate32(double2* __restrict__ psi, float2* __restrict__ psi32, const float* __restrict__ V,
                               const float* __restrict__ expm32, const double* __restrict__ weights,
                               const PropChunk* __restrict__ chunks, int N, int ncw, int nspV, int nspB) {
   const int w = blockIdx.x;
@@ -318,7 +328,10 @@ __global__ void k_propagate32(double2* __restrict__ psi, const float* __restrict
     apply_rows32(Br, Bi, b, N, nc, p, tmp, 0);
 #pragma unroll
     for (int j = 0; j < PCH32; ++j)
-      if (j < nc) ps[j * N + p] = make_double2((double)tmp[j].x, (double)tmp[j].y);
+      if (j < nc) {
+        ps[j * N + p] = make_double2((double)tmp[j].x, (double)tmp[j].y);
+        if (psi32) psi32[(size_t)w * ncw * N + (size_t)c.c0 * N + j * N + p] = tmp[j];
+      }
   }
 }
 
@@ -362,9 +375,9 @@ __device__ __forceinline__ void ps_apply(const float2* __restrict__ Vs, const fl
 }
 
 __global__ void __launch_bounds__(256, 1)
-    k_prop32_smem(double2* __restrict__ psi, const float* __restrict__ Vp, const float* __restrict__ expm32,
-                  const int2* __restrict__ tri, const double* __restrict__ weights, int N, int ncw, int na, int nspV,
-                  int realB) {
+    k_prop32_smem(double2* __restrict__ psi, float2* __restrict__ psi32, const float* __restrict__ Vp,
+                  const float* __restrict__ expm32, const int2* __restrict__ tri, const double* __restrict__ weights,
+                  int N, int ncw, int na, int nspV, int realB) {
   const int w = blockIdx.x;
   if (!(weights[w] > 1.0e-8)) return;
   const int sp = blockIdx.y;  // spin block (int_type U only)
@@ -450,14 +463,23 @@ __global__ void __launch_bounds__(256, 1)
       for (int r = 0; r < PS_RB; ++r)
 #pragma unroll
         for (int c = 0; c < PS_CB; ++c)
-          if (p0 + r < N && j0 + c < nc)
-            pw[(size_t)(c0 + j0 + c) * N + p0 + r] = make_double2((double)out[r][c].x, (double)out[r][c].y);
+          if (p0 + r < N && j0 + c < nc) {
+            const size_t o = (size_t)(c0 + j0 + c) * N + p0 + r;
+            pw[o] = make_double2((double)out[r][c].x, (double)out[r][c].y);
+            if (psi32) psi32[(size_t)w * ncw * N + o] = out[r][c];
+          }
     }
   }
 }
 
+void launch_propagate_tc(afqmc_handle* h);
+
 void launch_propagate_mixed(afqmc_handle* h) {
-  if (h->N <= PS_NMAX) {
+  if (h->N <= 128 && h->tune_prop == 3) {
+    launch_propagate_tc(h);
+    return;
+  }
+  if (h->N <= PS_NMAX && h->tune_prop != 2) {
     const size_t smem = ((size_t)h->N * h->N + 2 * (size_t)h->N * PS_CW) * sizeof(float2);
     static bool attr2 = false;
     if (!attr2) {
@@ -466,8 +488,8 @@ void launch_propagate_mixed(afqmc_handle* h) {
     }
     const int threads = ((h->N + PS_RB - 1) / PS_RB) * (PS_CW / PS_CB);
     dim3 grid(h->nwalk, h->nspV);
-    k_prop32_smem<<<grid, threads, smem, h->stream>>>(h->psi, h->V32, h->expm32, h->tri, h->weights, h->N, h->ncw,
-                                                       h->na, h->nspV, h->real_expm ? 1 : 0);
+    k_prop32_smem<<<grid, threads, smem, h->stream>>>(h->psi, h->psi32, h->V32, h->expm32, h->tri, h->weights, h->N,
+                                                       h->ncw, h->na, h->nspV, h->real_expm ? 1 : 0);
     h->launches++;
     return;
   }
@@ -479,7 +501,7 @@ void launch_propagate_mixed(afqmc_handle* h) {
   }
   const int threads = ((h->N + 31) / 32) * 32;
   dim3 grid(h->nwalk, h->nchunks32);
-  k_propagate32<<<grid, threads, smem, h->stream>>>(h->psi, h->V32, h->expm32, h->weights, h->d_chunks32, h->N,
+  k_propagate32<<<grid, threads, smem, h->stream>>>(h->psi, h->psi32, h->V32, h->expm32, h->weights, h->d_chunks32, h->N,
                                                     h->ncw, h->nspV, h->nsp);
   h->launches++;
 }
@@ -491,9 +513,11 @@ bool setup_mixed(afqmc_handle* h) {
   for (int s = 0; s < h->nsp; ++s)
     split_rows(h, h->LT + (size_t)s * h->T * h->G, h->G, h->T, h->G, h->kv_pad, 0,
                h->LTA + (size_t)s * h->T * h->kv_pad);
-  bool ok = make_tmap_bf16(&h->tm_rot, h->rotA, h->G, h->kf_pad, tc::BM) &&
-            make_tmap_bf16(&h->tm_theta, h->thetaB, 2 * h->nwalk, h->kf_pad, 128) &&
-            make_tmap_bf16(&h->tm_x, h->xB, 2 * h->nwalk, h->kv_pad, 128);
+  bool ok = make_tmap_bf16(&h->tm_rot, h->rotA, h->G, h->kf_pad, tc::BM);
+  const int bns[3] = {64, 128, 256};
+  for (int i = 0; i < 3 && ok; ++i)
+    ok = make_tmap_bf16(&h->tm_theta_bn[i], h->thetaB, 2 * h->nwalk, h->kf_pad, bns[i]) &&
+         make_tmap_bf16(&h->tm_x_bn[i], h->xB, 2 * h->nwalk, h->kv_pad, bns[i]);
   for (int s = 0; s < h->nsp && ok; ++s)
     ok = make_tmap_bf16(&h->tm_LT[s], h->LTA + (size_t)s * h->T * h->kv_pad, h->T, h->kv_pad, tc::BM);
   // local energy: rot split along p, [G][nce][ke_pad]; tiles of whole (g, walker) blocks
@@ -508,4 +532,18 @@ bool setup_mixed(afqmc_handle* h) {
   return ok;
 }
 
+}  // namespace afqmc
+
+namespace afqmc {
+// single GEMMs for the autotuner (operands must be current)
+void launch_fb_gemm(afqmc_handle* h, int bn) {
+  EpiFB epi{h->fb32, h->G, (float)h->mult};
+  launch_tc(h, h->tm_rot, h->tm_theta_bn, bn, h->G, 2 * h->nwalk, h->kf_pad, epi);
+}
+void launch_vhs_gemm(afqmc_handle* h, int bn) {
+  for (int s = 0; s < h->nspV; ++s) {
+    EpiV32 epi{h->V32, h->T, h->nspV, s, (float)sqrt(h->dt)};
+    launch_tc(h, h->tm_LT[s], h->tm_x_bn, bn, h->T, 2 * h->nwalk, h->kv_pad, epi);
+  }
+}
 }  // namespace afqmc
