@@ -182,6 +182,9 @@ typedef struct afqmc_run_opts {
   int comb;          /* 1: comb reconfiguration after every measurement (as the reference) */
   double cholesky_threshold;  /* sampling.choleskyThreshold (energy Cholesky truncation) */
   long max_steps;    /* > 0: stop after this many steps */
+  int device_blocks; /* 1 (field_source 1 only): each block -- its steps, QR cadence, measurement and
+                        comb -- is one CUDA-graph replay with all scalars on the device; needs
+                        nsteps to be a multiple of ortho_steps */
 } afqmc_run_opts;
 
 typedef struct afqmc_run_stats {
@@ -253,7 +256,38 @@ int afqmc_cv_results(afqmc_handle* h, double* out, int nslots);
  * file of earlier choices, read first and appended to.  report (nullable)
  * receives the timings. */
 int afqmc_autotune(afqmc_handle* h, const char* cache_path, char* report, int report_len);
-int afqmc_tuning(const afqmc_handle* h, int* bn_fb, int* bn_vhs, int* prop, int* ovl);
+int afqmc_tuning(const afqmc_handle* h, int* bn_fb, int* bn_vhs, int* prop, int* ovl, int* qr);
+/* Set the choices directly (a value <= 0 keeps the current one).  bn_*: 64, 128
+ * or 256; prop: 1 V in shared memory (N <= 128), 2 column-chunked, 3 tensor
+ * core (N <= 128); ovl: 1 warp per matrix, 2 CTA per matrix; qr (walker
+ * orthonormalisation): 1 Householder with the reference's (Eigen's) column
+ * signs, 2 Cholesky-QR in FP64 (mixed form; the same Q up to column signs,
+ * which the overlaps carry, so every physical result is unchanged; the
+ * default there).  An unavailable choice is AFQMC_ERR_ARG. */
+int afqmc_set_tuning(afqmc_handle* h, int bn_fb, int bn_vhs, int prop, int ovl, int qr);
+
+/* ---- device-resident blocks (MixedEstimator.cpp:483-635 without the host) ----
+ * afqmc_block_setup starts a run's device state: nprocs emulated ranks (the
+ * comb's P), nsteps per block, the energy estimate and running average the
+ * driver starts from, the truncation correction delta, burn_steps (steps
+ * measured into the equilibration average besides those with step*dt < 10),
+ * and optionally the comb zetas of the first nzeta blocks (the reference draws
+ * them from rank 0's generator); later blocks draw zeta from the device Philox
+ * stream.  Steps are counted from this call. */
+int afqmc_block_setup(afqmc_handle* h, int nprocs, int nsteps, double e_estimate, double avg_e, double delta,
+                      long burn_steps, const double* zetas, int nzeta);
+/* End of a block, enqueued on the handle's stream (capturable, no host sync):
+ * exact local energies of all walkers, the clamped weighted block energy into
+ * the block ring, the running averages and energy estimate, and with comb != 0
+ * the comb reconfiguration.  A non-finite energy of a live walker is reported
+ * as AFQMC_ERR_NAN by the next call that reads device state. */
+int afqmc_block_end(afqmc_handle* h, int comb);
+/* The first nblocks ring entries (total weight, block energy: samples.dat rows
+ * 1..nblocks) and the clamped local energies counted since afqmc_block_setup. */
+int afqmc_block_results(afqmc_handle* h, int nblocks, double* total_weights, double* total_energies, long* n_large);
+/* Comb reconfiguration alone, on the device, with the given zeta in [0, 1) over
+ * nprocs emulated ranks (MixedEstimator.cpp:583-621). */
+int afqmc_comb(afqmc_handle* h, double zeta, int nprocs);
 
 /* ---- CUDA-graph replay (one or several systems) ----
  * Capture nsteps device-field steps of each of the n handles (QR every
@@ -263,6 +297,9 @@ int afqmc_tuning(const afqmc_handle* h, int* bn_fb, int* bn_vhs, int* prop, int*
  * Population control runs on the device (afqmc_set_energy_estimate). */
 typedef struct afqmc_graph afqmc_graph;
 int afqmc_graph_capture(afqmc_handle** hs, int n, int nsteps, int ortho_every, int cv_every, afqmc_graph** out);
+/* As afqmc_graph_capture, and each handle's branch ends with afqmc_block_end
+ * (comb as given): one replay is one whole block of the run. */
+int afqmc_graph_capture_blocks(afqmc_handle** hs, int n, int nsteps, int ortho_every, int comb, afqmc_graph** out);
 int afqmc_graph_launch(afqmc_graph* g);
 int afqmc_graph_nodes(const afqmc_graph* g, long* nodes);
 int afqmc_graph_destroy(afqmc_graph* g);

@@ -1,0 +1,77 @@
+"""Cholesky-QR orthonormalisation of the mixed form against the Householder QR
+with the reference's (Eigen's) column convention.
+
+The two factorisations give the same Q up to the sign of each column, and the
+overlaps differ by the product of those signs (squared for the restricted
+walker): checked to 1e-12.  Every physical quantity is unchanged: local
+energies after the QR agree to 1e-5 Eh (the mixed form keeps the pre-QR theta,
+which is invariant, where the Householder path recomputes it in FP32), and one
+further step with identical fields gives the same weights to 1e-6 relative.
+"""
+import numpy as np
+import pytest
+
+from oracle import afqmc_oracle as O
+from vmc_gb300 import synthetic as S
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def A():
+    from vmc_gb300 import afqmc
+    afqmc.lib()
+    return afqmc
+
+
+@pytest.mark.parametrize("kind", ["uhf", "rhf"])
+def test_cholesky_qr_equals_householder_up_to_column_signs(A, kind):
+    if kind == "uhf":
+        s = S.make_system(40, 7, 150, 4242, "uhf")
+        na, nb, rw = 7, 6, False
+    else:
+        s = S.make_system(36, 6, 130, 4343, "rhf")
+        na = nb = 6
+        rw = True
+    N = s["norb"]
+    oh = O.Hamiltonian(N, na, nb, s["ecore"], s["h1"], s["h1mod"], s["chol"])
+    ot = O.Trial(oh, s["trial"], s["phi_a"][:, :na], s["phi_b"][:, :nb])
+    W = 48
+    rng = np.random.default_rng(5)
+    base = O._ref_dets(oh, ot.phi, rw)
+    dets = base[None] + 0.3 * (rng.standard_normal((W,) + base.shape) + 1j * rng.standard_normal((W,) + base.shape))
+    out = {}
+    for qr in ("householder", "cholesky"):
+        gh = A.Hamiltonian(N, na, nb, oh.ecore, oh.h1, oh.h1mod, oh.chol)
+        gt = A.RHF(gh, ot.phi[0]) if ot.kind == "rhf" else A.UHF(gh, ot.phi[0], ot.phi[1])
+        wk = A.DQMCWalkers(gh, gt, W, rw, 0.005, precision="mixed")
+        A.set_tuning(wk, qr=qr)
+        wk.set_det(dets)
+        wk.orthogonalize()
+        d, o, w = wk.get_det()
+        el = wk.ham_and_overlap().real
+        xi = np.random.default_rng(9).standard_normal((W, oh.nchol))
+        e0 = O.hf_energy(ot, oh, ot.phi, rw).real
+        wk.propagate_phaseless(xi, e0)
+        _, _, w1 = wk.get_det()
+        out[qr] = (d, o, el, w1)
+    dh, oh_, elh, w1h = out["householder"]
+    dc, oc, elc, w1c = out["cholesky"]
+    def blocks_of(d):  # serial layout: alpha N x na row-major, then beta N x nb (a copy for the RHF walker)
+        a = d[:, :N * na].reshape(W, N, na)
+        return a if rw else np.concatenate([a, d[:, N * na:].reshape(W, N, nb)], axis=2)
+
+    qh, qc = blocks_of(dh), blocks_of(dc)
+    for w in range(W):
+        sgn = np.sign(np.einsum("pj,pj->j", qh[w].conj(), qc[w]).real)
+        assert np.all(np.abs(sgn) == 1)
+        assert np.abs(qc[w] - qh[w] * sgn[None]).max() < 1e-12
+        # orthonormal columns per spin block
+        blocks = [(0, na)] if rw else [(0, na), (na, na + nb)]
+        for a, b in blocks:
+            g = qc[w][:, a:b].conj().T @ qc[w][:, a:b]
+            assert np.abs(g - np.eye(b - a)).max() < 1e-12
+        fac = np.prod(sgn) ** (2 if rw else 1)
+        assert abs(oc[w] - fac * oh_[w]) <= 1e-12 * abs(oh_[w])
+    assert np.abs(elc - elh).max() < 1e-5
+    assert np.abs(w1c - w1h).max() <= 1e-6 * np.abs(w1h).max()

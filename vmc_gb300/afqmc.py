@@ -100,7 +100,8 @@ class _RunOpts(ctypes.Structure):
     _fields_ = [("nprocs", ctypes.c_int), ("nsteps", ctypes.c_int), ("nsweeps", ctypes.c_int),
                 ("ortho_steps", ctypes.c_int), ("burn_iter", ctypes.c_int), ("seed", ctypes.c_uint),
                 ("field_source", ctypes.c_int), ("comb", ctypes.c_int),
-                ("cholesky_threshold", ctypes.c_double), ("max_steps", ctypes.c_long)]
+                ("cholesky_threshold", ctypes.c_double), ("max_steps", ctypes.c_long),
+                ("device_blocks", ctypes.c_int)]
 
 
 class _RunStats(ctypes.Structure):
@@ -282,6 +283,37 @@ class DQMCWalkers:
     def orthogonalize(self):
         self._check(lib().afqmc_orthonormalize(self.h))
 
+    def comb(self, zeta, nprocs=1):
+        """Comb reconfiguration on the device (MixedEstimator.cpp:583-621)."""
+        L = lib()
+        L.afqmc_comb.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_int]
+        self._check(L.afqmc_comb(self.h, float(zeta), int(nprocs)))
+
+    def block_setup(self, nsteps, e_est, avg_e=None, delta=0.0, burn_steps=0, zetas=None, nprocs=1):
+        """Start device-resident blocks (afqmc_block_setup)."""
+        L = lib()
+        L.afqmc_block_setup.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                        ctypes.c_double, ctypes.c_double, ctypes.c_long, ctypes.c_void_p,
+                                        ctypes.c_int]
+        z = None if zetas is None else np.ascontiguousarray(zetas, dtype=np.float64)
+        self._check(L.afqmc_block_setup(self.h, int(nprocs), int(nsteps), float(e_est),
+                                        float(e_est if avg_e is None else avg_e), float(delta), int(burn_steps),
+                                        _ptr(z), 0 if z is None else len(z)))
+
+    def block_end(self, comb=True):
+        L = lib()
+        L.afqmc_block_end.argtypes = [ctypes.c_void_p, ctypes.c_int]
+        self._check(L.afqmc_block_end(self.h, int(bool(comb))))
+
+    def block_results(self, nblocks):
+        """(total_weights, block energies, clamped local energies) of the first nblocks blocks."""
+        L = lib()
+        L.afqmc_block_results.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
+                                          ctypes.POINTER(ctypes.c_long)]
+        tw, te, n = np.zeros(nblocks), np.zeros(nblocks), ctypes.c_long()
+        self._check(L.afqmc_block_results(self.h, int(nblocks), tw.ctypes.data, te.ctypes.data, ctypes.byref(n)))
+        return tw, te, n.value
+
     def set_energy_estimate(self, e_est, eshift=None):
         e = None if eshift is None else np.array([eshift], dtype=np.float64)
         self._check(lib().afqmc_set_energy_estimate(self.h, float(e_est), _ptr(e)))
@@ -325,13 +357,13 @@ class DQMCWalkers:
         return ms.value
 
     def run(self, nsteps=50, nsweeps=50, ortho_steps=20, seed=4321, nprocs=1, burn_iter=0,
-            field_source="reference", comb=True, cholesky_threshold=1e-3, max_steps=0):
+            field_source="reference", comb=True, cholesky_threshold=1e-3, max_steps=0, device_blocks=False):
         """calcMixedEstimatorLongProp from the current walkers (DQMC/MixedEstimator.cpp:309-660).
 
         Returns (total_weights, total_energies, stats) -- the samples.dat columns."""
         o = _RunOpts(int(nprocs), int(nsteps), int(nsweeps), int(ortho_steps), int(burn_iter), int(seed),
                      0 if field_source == "reference" else 1, int(bool(comb)), float(cholesky_threshold),
-                     int(max_steps))
+                     int(max_steps), int(bool(device_blocks)))
         tw = np.zeros(nsweeps)
         te = np.zeros(nsweeps)
         st = _RunStats()
@@ -499,11 +531,14 @@ class StepGraph:
     """nsteps device-field steps of one or several DQMCWalkers as one CUDA graph
     (afqmc_graph_*): each replay advances every system by nsteps."""
 
-    def __init__(self, walkers, nsteps, ortho_every=5, cv_every=0):
+    def __init__(self, walkers, nsteps, ortho_every=5, cv_every=0, block_end=None):
+        """block_end: None (steps only), or "measure" / "comb" to end each
+        replay with the device-resident block end (afqmc_graph_capture_blocks)."""
         L = lib()
         vp = ctypes.c_void_p
         L.afqmc_graph_capture.argtypes = [ctypes.POINTER(vp), ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                           ctypes.POINTER(vp)]
+        L.afqmc_graph_capture_blocks.argtypes = L.afqmc_graph_capture.argtypes
         L.afqmc_graph_launch.argtypes = [vp]
         L.afqmc_graph_destroy.argtypes = [vp]
         L.afqmc_graph_nodes.argtypes = [vp, ctypes.POINTER(ctypes.c_long)]
@@ -511,7 +546,11 @@ class StepGraph:
         self.walkers = list(walkers)
         arr = (vp * len(self.walkers))(*[w.h for w in self.walkers])
         g = vp()
-        rc = L.afqmc_graph_capture(arr, len(self.walkers), nsteps, ortho_every, cv_every, ctypes.byref(g))
+        if block_end is None:
+            rc = L.afqmc_graph_capture(arr, len(self.walkers), nsteps, ortho_every, cv_every, ctypes.byref(g))
+        else:
+            rc = L.afqmc_graph_capture_blocks(arr, len(self.walkers), nsteps, ortho_every,
+                                              1 if block_end == "comb" else 0, ctypes.byref(g))
         if rc != AFQMC_OK:
             raise AfqmcError(rc, L.afqmc_graph_last_error().decode())
         self.g = g
@@ -543,9 +582,25 @@ def autotune(wk, cache_path=None):
     """Run the library's autotuner on a DQMCWalkers handle; returns (choices, report)."""
     L = lib()
     L.afqmc_autotune.argtypes = [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int]
-    L.afqmc_tuning.argtypes = [ctypes.c_void_p] + [ctypes.POINTER(ctypes.c_int)] * 4
+    L.afqmc_tuning.argtypes = [ctypes.c_void_p] + [ctypes.POINTER(ctypes.c_int)] * 5
     buf = ctypes.create_string_buffer(2048)
     wk._check(L.afqmc_autotune(wk.h, cache_path.encode() if cache_path else None, buf, 2048))
-    v = [ctypes.c_int() for _ in range(4)]
+    v = [ctypes.c_int() for _ in range(5)]
     L.afqmc_tuning(wk.h, *[ctypes.byref(x) for x in v])
-    return dict(bn_fb=v[0].value, bn_vhs=v[1].value, prop=v[2].value, ovl=v[3].value), buf.value.decode()
+    return (dict(bn_fb=v[0].value, bn_vhs=v[1].value, prop=v[2].value, ovl=v[3].value, qr=v[4].value),
+            buf.value.decode())
+
+
+PROP_VARIANTS = {"smem": 1, "chunked": 2, "tensor": 3}
+QR_VARIANTS = {"householder": 1, "cholesky": 2}
+
+
+def set_tuning(wk, bn_fb=0, bn_vhs=0, prop=0, ovl=0, qr=0):
+    """Choose kernel variants directly (0 keeps the current choice); `prop` and
+    `qr` may be names of PROP_VARIANTS / QR_VARIANTS.  Raises on a choice the
+    handle cannot run."""
+    L = lib()
+    L.afqmc_set_tuning.argtypes = [ctypes.c_void_p] + [ctypes.c_int] * 5
+    prop = PROP_VARIANTS.get(prop, prop)
+    qr = QR_VARIANTS.get(qr, qr)
+    wk._check(L.afqmc_set_tuning(wk.h, bn_fb, bn_vhs, prop, ovl, qr))

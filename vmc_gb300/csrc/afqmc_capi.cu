@@ -139,6 +139,11 @@ int upload(afqmc_handle* h, T* d, const std::vector<T>& v) {
 int device_error(afqmc_handle* h) {
   int e = 0;
   CK(cudaMemcpy(&e, h->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+  if (e == afqmc::DERR_NAN_ENERGY) {
+    h->err = "non-finite local energy of a live walker (device block)";
+    cudaMemset(h->d_err, 0, sizeof(int));
+    return AFQMC_ERR_NAN;
+  }
   if (e != 0) {
     h->err = "a tensor-core pipeline wait timed out (stage code " + std::to_string(e) + ")";
     cudaMemset(h->d_err, 0, sizeof(int));
@@ -171,7 +176,8 @@ void release(afqmc_handle* h) {
                   h->det, h->ovlp, h->weights, h->fb, h->xi, h->x, h->x32, h->shift, h->fbterm, h->V,
                   h->qwork, h->epart, h->eloc, h->scal, h->d_chunks, h->d_err, h->rotA, h->LTA,
                   h->thetaB, h->xB, h->fb32, h->V32, h->expm32, h->d_chunks32, h->rotE, h->thetaE,
-                  h->xc, h->cv_x, h->cv_idx, h->cv_esub, h->cv_f, h->cv_ms, h->cv_out, h->d_step, h->psi32};
+                  h->xc, h->cv_x, h->cv_idx, h->cv_esub, h->cv_f, h->cv_ms, h->cv_out, h->d_step, h->psi32,
+                  h->pt_img, h->comb_cum, h->comb_idx, h->comb_ovl, h->blk, h->blk_zeta};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (h->host_pinned) cudaFreeHost(h->host_pinned);
@@ -186,6 +192,7 @@ void release(afqmc_handle* h) {
 namespace afqmc {
 bool check_launch(afqmc_handle* h, const char* what) { return after_launch(h, what) == AFQMC_OK; }
 void set_global_error(const std::string& msg) { g_create_err = msg; }
+int take_device_error(afqmc_handle* h) { return device_error(h); }
 }  // namespace afqmc
 
 extern "C" {
@@ -453,6 +460,7 @@ int afqmc_create(const afqmc_ham* ham, const afqmc_trial* trial, const afqmc_opt
     ALLOC(d_chunks32, h->chunks32.size());
     ALLOC(rotE, (size_t)G * h->nce * h->ke_pad);
     ALLOC(psi32, W * h->ncw * N);
+    if (N <= 128) ALLOC(pt_img, (size_t)nsp * 2 * 128 * 256);
     ALLOC(thetaE, W * 2 * h->nce * h->ke_pad);
     ALLOC(xc, W * 2 * G * 2);
   }
@@ -461,6 +469,11 @@ int afqmc_create(const afqmc_ham* ham, const afqmc_trial* trial, const afqmc_opt
   ALLOC(eloc, W);
   ALLOC(scal, (size_t)afqmc::S_NSLOTS);
   ALLOC(d_chunks, (size_t)h->nchunks);
+  ALLOC(comb_cum, W);
+  ALLOC(comb_idx, W);
+  ALLOC(comb_ovl, W);
+  ALLOC(blk, 2 * (size_t)afqmc::BLK_MAX);
+  ALLOC(blk_zeta, (size_t)afqmc::BLK_MAX);
 #undef ALLOC
   ce = cudaMallocHost((void**)&h->host_pinned, W * G * sizeof(double));
   if (ce != cudaSuccess) { g_create_err = cudaGetErrorString(ce); release(h); delete h; return AFQMC_ERR_CUDA; }
@@ -512,6 +525,7 @@ int afqmc_create(const afqmc_ham* ham, const afqmc_trial* trial, const afqmc_opt
     if (ce != cudaSuccess) { g_create_err = cudaGetErrorString(ce); release(h); delete h; return AFQMC_ERR_CUDA; }
   }
   std::vector<double> sc(afqmc::S_NSLOTS, 0.0);
+  sc[afqmc::S_NPROCS] = 1.0;
   UP(scal, sc);
   // walkers start at the trial determinant with unit weight
   {
@@ -737,8 +751,7 @@ int afqmc_orthonormalize(afqmc_handle* h) {
   if (h->ncw > 0 && std::max(h->na, h->nb) > afqmc::QR_MAXN) return fail(h, AFQMC_ERR_UNSUPPORTED, "nocc too large for QR");
   cudaEvent_t e0;
   stage_begin(h, afqmc::ST_ORTHO, &e0);
-  afqmc::launch_ortho(h);
-  afqmc::launch_overlap_theta(h, false);
+  afqmc::launch_ortho_refresh(h);
   stage_end(h, afqmc::ST_ORTHO, e0);
   return after_launch(h, "orthonormalize");
 }

@@ -135,7 +135,47 @@ int afqmc_run(afqmc_handle* h, const afqmc_run_opts* o, double* total_weights, d
   const long last = o->max_steps > 0 ? std::min<long>((long)nsweeps * nsteps, (long)o->max_steps + 1)
                                      : (long)nsweeps * nsteps;
   RUN(afqmc_get_walkers(h, nullptr, nullptr, wts.data()));
-  for (long step = 1; step < last; ++step) {
+  if (o->device_blocks) {
+    // Whole blocks as graph replays with the device-resident block end; the
+    // comb zetas are drawn here in the reference's order (rank 0's generator,
+    // one per measurement) and handed to the device up front.
+    if (o->field_source != 1 || nsteps % o->ortho_steps != 0) {
+      h->err = "device_blocks needs field_source 1 and nsteps a multiple of ortho_steps";
+      return AFQMC_ERR_ARG;
+    }
+    const long nblk = (last - 1) / nsteps;  // measured blocks: steps nsteps, 2 nsteps, ... < last
+    if (nblk > afqmc::BLK_MAX) {
+      h->err = "device_blocks: too many blocks";
+      return AFQMC_ERR_ARG;
+    }
+    std::vector<double> zetas(o->comb ? nblk : 0);
+    for (auto& z : zetas) z = afqmc_refrng_uniform(rngs[0]);
+    RUN(afqmc_block_setup(h, P, nsteps, e_est, avg_e, delta, (long)o->burn_iter * nsteps, zetas.data(),
+                          (int)zetas.size()));
+    if (nblk > 0) {
+      afqmc_graph* g = nullptr;
+      afqmc_handle* hs[1] = {h};
+      RUN(afqmc_graph_capture_blocks(hs, 1, nsteps, o->ortho_steps, o->comb, &g));
+      for (long b = 0; b < nblk && rc == AFQMC_OK; ++b) rc = afqmc_graph_launch(g);
+      afqmc_graph_destroy(g);
+      if (rc != AFQMC_OK) {
+        h->err = afqmc_graph_last_error();
+        return rc;
+      }
+    }
+    for (long step = nblk * nsteps + 1; step < last; ++step) {  // steps after the last measurement
+      RUN(afqmc_step(h, nullptr, nullptr));
+      if (step % o->ortho_steps == 0) RUN(afqmc_orthonormalize(h));
+    }
+    std::vector<double> bw(nblk), be(nblk);
+    RUN(afqmc_block_results(h, (int)nblk, bw.data(), be.data(), &nlarge));
+    for (long b = 0; b < nblk; ++b)
+      if (b + 1 < nsweeps) {
+        total_weights[b + 1] = bw[b];
+        total_energies[b + 1] = be[b];
+      }
+  }
+  for (long step = o->device_blocks ? last : 1; step < last; ++step) {
     if (step * dt < 10.0) avg_e = avg_e_eql;
     if (o->field_source == 0) {
       for (int r = 0; r < P; ++r)

@@ -4,7 +4,8 @@
 // A graph holds `nsteps` device-field steps of every handle (force bias,
 // fields, VHS, propagator, overlap, weights; QR every `ortho_every` steps; the
 // control-variate measurement every `cv_every` steps when a network is
-// attached).  Each handle's kernels run on its own stream, forked from and
+// attached), optionally followed by the device-resident block end
+// (measurement, energy estimate, comb).  Each handle's kernels run on its own stream, forked from and
 // joined to the first handle's stream during capture, so the systems' kernels
 // are independent branches of the one graph and run concurrently; a replay is
 // one cudaGraphLaunch.  The device step counter of the Philox field stream
@@ -50,10 +51,7 @@ void enqueue_step(afqmc_handle* h) {
   launch_weights(h);
 }
 
-void enqueue_ortho(afqmc_handle* h) {
-  launch_ortho(h);
-  launch_overlap_theta(h, false);
-}
+void enqueue_ortho(afqmc_handle* h) { launch_ortho_refresh(h); }
 
 }  // namespace afqmc
 
@@ -63,7 +61,11 @@ int afqmc_cv_measure(afqmc_handle* h, uint64_t tag, int slot);
 
 const char* afqmc_graph_last_error(void) { return g_graph_err.c_str(); }
 
-int afqmc_graph_capture(afqmc_handle** hs, int n, int nsteps, int ortho_every, int cv_every, afqmc_graph** out) {
+}  // extern "C"
+
+namespace {
+// block_end < 0: steps only; 0 / 1: each branch ends with the block end without / with the comb
+int capture(afqmc_handle** hs, int n, int nsteps, int ortho_every, int cv_every, int block_end, afqmc_graph** out) {
   if (!hs || n <= 0 || nsteps <= 0 || !out) {
     g_graph_err = "bad arguments";
     return AFQMC_ERR_ARG;
@@ -108,6 +110,7 @@ int afqmc_graph_capture(afqmc_handle** hs, int n, int nsteps, int ortho_every, i
       if (ortho_every > 0 && (k + 1) % ortho_every == 0) afqmc::enqueue_ortho(h);
       if (cv_every > 0 && h->cv_mlp && (k + 1) % cv_every == 0) afqmc_cv_measure(h, (uint64_t)k, k % h->cv_nslots);
     }
+    if (block_end >= 0) afqmc::launch_block_end(h, block_end);
     if (i > 0) {
       cudaEventRecord(g->evs[i], h->stream);
       cudaStreamWaitEvent(s0, g->evs[i], 0);
@@ -121,6 +124,17 @@ int afqmc_graph_capture(afqmc_handle** hs, int n, int nsteps, int ortho_every, i
   cudaGraphGetNodes(g->graph, nullptr, &g->nodes);
   *out = g;
   return AFQMC_OK;
+}
+}  // namespace
+
+extern "C" {
+
+int afqmc_graph_capture(afqmc_handle** hs, int n, int nsteps, int ortho_every, int cv_every, afqmc_graph** out) {
+  return capture(hs, n, nsteps, ortho_every, cv_every, -1, out);
+}
+
+int afqmc_graph_capture_blocks(afqmc_handle** hs, int n, int nsteps, int ortho_every, int comb, afqmc_graph** out) {
+  return capture(hs, n, nsteps, ortho_every, 0, comb ? 1 : 0, out);
 }
 
 // One replay: every handle advances nsteps steps.  Ordered after each handle's

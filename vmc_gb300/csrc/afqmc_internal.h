@@ -35,8 +35,20 @@ struct PropChunk {
 constexpr int PROP_CH = 8;   // walker-det columns per propagator CTA
 constexpr int QR_MAXN = 128; // largest nocc the QR kernel handles
 
-// Device scalars of the population control (slots of Handle::scal).
-enum { S_ESHIFT = 0, S_EEST = 1, S_SUMW = 2, S_NCAP = 3, S_NSLOTS = 8 };
+// Device scalars of the population control and of device-resident blocks
+// (slots of Handle::scal): energy shift, energy estimate, sum of weights after
+// the last step, capped weights; running block averages (production / before
+// the end of equilibration), truncation correction delta, clamped local
+// energies, step counter at the start of the run, equilibration steps, the
+// next block slot, emulated ranks, and the number of host-given comb zetas.
+enum {
+  S_ESHIFT = 0, S_EEST = 1, S_SUMW = 2, S_NCAP = 3,
+  S_AVGE = 4, S_AVGE_EQL = 5, S_NUM = 6, S_DEN = 7, S_NUM_EQL = 8, S_DEN_EQL = 9,
+  S_DELTA = 10, S_NLARGE = 11, S_STEP0 = 12, S_BURN = 13, S_BLOCK = 14, S_NPROCS = 15, S_NZETA = 16,
+  S_NSLOTS = 24
+};
+constexpr int BLK_MAX = 65536;  // block ring capacity (samples of one run)
+constexpr int DERR_NAN_ENERGY = 100;  // d_err code: non-finite local energy in a device block
 
 // Stage names for timing.
 enum Stage { ST_FB = 0, ST_FIELDS, ST_VHS, ST_PROP, ST_OVERLAP, ST_WEIGHTS, ST_ORTHO, ST_ENERGY, ST_N };
@@ -117,6 +129,7 @@ struct afqmc_handle {
   // autotuned choices (afqmc_autotune): GEMM N-tiles; propagator 0 auto / 1 SMEM / 2 chunked / 3 tcgen05;
   // overlap 0 auto / 1 warp per matrix / 2 block per matrix
   int tune_bn_fb = 128, tune_bn_vhs = 128, tune_prop = 0, tune_ovl = 0;
+  int tune_qr = 0;  // walker QR: 0 auto (Cholesky-QR in the mixed form when it fits), 1 Householder, 2 Cholesky-QR
   int tune_prop_best = 0, tune_ovl_best = 0;
   // mixed local energy
   int ke_pad = 0;                    // padded split-K (3N) of the exchange GEMM
@@ -128,6 +141,13 @@ struct afqmc_handle {
   unsigned long long* d_step = nullptr;  // device step counter of the Philox field stream
   bool fb_current = false;               // fb32 holds the force bias of the current theta
   float2* psi32 = nullptr;               // [W][ncw][N] FP32 copy of psi (mixed form)
+  // device-resident blocks: comb scratch, the block ring and host-given zetas
+  double* comb_cum = nullptr;   // [W]
+  int* comb_idx = nullptr;      // [W]
+  double2* comb_ovl = nullptr;  // [W]
+  double* blk = nullptr;        // [BLK_MAX][2] total weight, block energy
+  double* blk_zeta = nullptr;   // [BLK_MAX]
+  __nv_bfloat16* pt_img = nullptr;       // [nsp][hi, lo][128 x 256] swizzled A image of B (tensor-core propagator, N <= 128)
   // control variate
   float* cv_x = nullptr;             // [W][67] features
   float* cv_f = nullptr;             // [W]     predicted local energies
@@ -156,6 +176,15 @@ void launch_psi_to_f32(afqmc_handle* h);
 
 // ---- kernels (kernels_mixed.cu) ----
 bool setup_mixed(afqmc_handle* h);
+bool setup_prop_tc(afqmc_handle* h);
+bool prop_tc_available(const afqmc_handle* h);
+void launch_propagate_tc(afqmc_handle* h);
+void launch_block_end(afqmc_handle* h, int comb);
+bool ortho_chol_available(const afqmc_handle* h);
+void launch_ortho_chol(afqmc_handle* h);
+// the step's orthonormalisation: QR of every walker and whatever it invalidates
+void launch_ortho_refresh(afqmc_handle* h);
+int take_device_error(afqmc_handle* h);  // AFQMC_OK, or the status of a recorded device error (cleared)
 void launch_force_bias_mixed(afqmc_handle* h);
 void launch_fields_mixed(afqmc_handle* h, bool device_rng);
 void launch_vhs_mixed(afqmc_handle* h);

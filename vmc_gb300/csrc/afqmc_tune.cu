@@ -2,8 +2,8 @@
 // blocks, precision) it times the candidate tile shapes and kernel variants
 // on the handle's own data and keeps the fastest:
 //   * N-tile (64 / 128 / 256) of the tensor-core force-bias and VHS GEMMs,
-//   * propagator: walker V resident in shared memory, or column-chunked with V
-//     streamed from L2,
+//   * propagator: tensor core (tcgen05, split BF16), walker V resident in
+//     shared memory (FP32), or column-chunked with V streamed from L2 (FP32),
 //   * overlap / inverse: one warp per matrix, or one CTA per matrix.
 // Choices are cached in a text file (one "key value..." line per size class),
 // so later handles of the same class skip the timing.
@@ -100,9 +100,9 @@ int afqmc_autotune(afqmc_handle* h, const char* cache_path, char* report, int re
     const size_t bytes = (size_t)h->nwalk * h->ncw * h->N * sizeof(double2);
     cudaMemcpyAsync(h->qwork, h->psi, bytes, cudaMemcpyDeviceToDevice, h->stream);
     best = 1e30f;
-    const int cands[2] = {1, 2};
+    const int cands[3] = {3, 1, 2};
     for (int c : cands) {
-      if ((c == 1 || c == 3) && h->N > 128) continue;
+      if ((c == 1 && h->N > 128) || (c == 3 && !afqmc::prop_tc_available(h))) continue;
       h->tune_prop = c;
       const float t = time_ms(h, [&] {
         afqmc::launch_propagate_mixed(h);
@@ -145,12 +145,39 @@ int afqmc_autotune(afqmc_handle* h, const char* cache_path, char* report, int re
   return AFQMC_OK;
 }
 
-int afqmc_tuning(const afqmc_handle* h, int* bn_fb, int* bn_vhs, int* prop, int* ovl) {
+int afqmc_set_tuning(afqmc_handle* h, int bn_fb, int bn_vhs, int prop, int ovl, int qr) {
+  if (!h) return AFQMC_ERR_ARG;
+  auto bn_ok = [](int b) { return b <= 0 || b == 64 || b == 128 || b == 256; };
+  const bool mixed = h->precision == AFQMC_PREC_MIXED;
+  if (!bn_ok(bn_fb) || !bn_ok(bn_vhs) || prop > 3 || ovl > 2 || ((bn_fb > 0 || bn_vhs > 0 || prop > 0) && !mixed) ||
+      ((prop == 1) && h->N > 128) || (prop == 3 && !afqmc::prop_tc_available(h)) || qr > 2 ||
+      (qr == 2 && !afqmc::ortho_chol_available(h))) {
+    h->err = "afqmc_set_tuning: choice not available for this handle";
+    return AFQMC_ERR_ARG;
+  }
+  if (ovl == 1) {
+    const int nmax = std::max(h->chan[0].n, h->nchan > 1 ? h->chan[1].n : 0);
+    if (nmax > 32) {
+      h->err = "afqmc_set_tuning: warp overlap needs at most 32 electrons per channel";
+      return AFQMC_ERR_ARG;
+    }
+  }
+  if (bn_fb > 0) h->tune_bn_fb = bn_fb;
+  if (bn_vhs > 0) h->tune_bn_vhs = bn_vhs;
+  if (prop > 0) h->tune_prop = prop;
+  if (ovl > 0) h->tune_ovl = ovl;
+  if (qr > 0) h->tune_qr = qr;
+  h->fb_current = false;
+  return AFQMC_OK;
+}
+
+int afqmc_tuning(const afqmc_handle* h, int* bn_fb, int* bn_vhs, int* prop, int* ovl, int* qr) {
   if (!h) return AFQMC_ERR_ARG;
   if (bn_fb) *bn_fb = h->tune_bn_fb;
   if (bn_vhs) *bn_vhs = h->tune_bn_vhs;
   if (prop) *prop = h->tune_prop;
   if (ovl) *ovl = h->tune_ovl;
+  if (qr) *qr = h->tune_qr == 2 ? 2 : 1;
   return AFQMC_OK;
 }
 

@@ -472,10 +472,8 @@ __global__ void __launch_bounds__(256, 1)
   }
 }
 
-void launch_propagate_tc(afqmc_handle* h);
-
 void launch_propagate_mixed(afqmc_handle* h) {
-  if (h->N <= 128 && h->tune_prop == 3) {
+  if (h->tune_prop == 3 && prop_tc_available(h)) {
     launch_propagate_tc(h);
     return;
   }
@@ -513,7 +511,7 @@ bool setup_mixed(afqmc_handle* h) {
   for (int s = 0; s < h->nsp; ++s)
     split_rows(h, h->LT + (size_t)s * h->T * h->G, h->G, h->T, h->G, h->kv_pad, 0,
                h->LTA + (size_t)s * h->T * h->kv_pad);
-  bool ok = make_tmap_bf16(&h->tm_rot, h->rotA, h->G, h->kf_pad, tc::BM);
+  bool ok = setup_prop_tc(h) && make_tmap_bf16(&h->tm_rot, h->rotA, h->G, h->kf_pad, tc::BM);
   const int bns[3] = {64, 128, 256};
   for (int i = 0; i < 3 && ok; ++i)
     ok = make_tmap_bf16(&h->tm_theta_bn[i], h->thetaB, 2 * h->nwalk, h->kf_pad, bns[i]) &&

@@ -1,18 +1,31 @@
-// Tensor-core (tcgen05, kind::tf32) propagator of the mixed form:
+// Tensor-core (tcgen05) propagator of the mixed form:
 //     psi <- B (sum_{k=0}^{5} V^k / k!) B psi          (DQMCWalker.cpp:424-431, :482-491)
-// for N <= 128.  One CTA (4 warps) per walker and V block; every complex
+// for N <= 128.  One CTA (4 warps) per walker and V block.  Every complex
 // product M X is one real GEMM
-//     [Re MX | Im MX] = [Mr | Mi] . [[Xr, Xi], [-Xi, Xr]]      (K = 2N, padded to 256)
-// with the 128 x 256 A operand ([Mr | Mi]: B = exp(-dt/2 h1') or the walker's V;
-// K columns [0, N) real part, [128, 128 + N) imaginary part, the rest zero)
-// and the NC x 256 B operand (NC = 2 x columns: rows (j, re) and (j, im)) in
-// shared memory, K-major with the 128-byte swizzle (8 panels of 32 TF32 per
-// row), and the 128 x NC FP32 accumulator in TMEM.  Thread p (TMEM lane p)
-// owns orbital row p: it reads its row of the product with tcgen05.ld, keeps
-// the Taylor sum of its row in registers and writes its row back as column p
-// (and N + p) of the next B operand.  Seven products per walker: B, five
-// Taylor terms, B.
+//     [Re MX | Im MX] = [Mr | Mi] . [[Xr, Xi], [-Xi, Xr]]
+// with K = 256: K columns [0, N) carry the real part of M, [128, 128 + N) the
+// imaginary part, the rest are zero.  A = M is 128 x 256 (rows >= N zero), the
+// B operand holds NC = 2 x (columns of X) rows: row (j, re) = [Xr(:, j) | -Xi(:, j)],
+// row (j, im) = [Xi(:, j) | Xr(:, j)].  Both operands are split into BF16
+// high and low parts (x = hi + lo) and the product is accumulated in FP32 in
+// TMEM from three MMA passes hi.hi + lo.hi + hi.lo (the dropped lo.lo term is
+// 2^-16 of the product), which keeps the propagator close to FP32 accuracy.
+//
+// Shared memory: A (hi, lo; 64 KB each) and B (hi, lo; up to 80 rows, 40 KB
+// each), K-major with the 128-byte swizzle (4 panels of 64 BF16 per row).
+// B = exp(-dt/2 h1') is the same for every walker, so an error in its split
+// would bias every walker's overlap the same way; the tensor core therefore
+// multiplies by B - I (entries of order dt, whose split error is ~1e-8 of B)
+// and each thread adds its own row of X in FP32.  The split, swizzled A image of
+// B - I is built once per handle in global memory and copied in with
+// cp.async.bulk.
+// V comes from the packed lower triangle written by the VHS GEMM and is
+// scattered into A by the CTA.  Thread p (TMEM lane p) owns orbital row p: it
+// reads its row of each product with tcgen05.ld, keeps the Taylor sum of its
+// row in registers and writes its row back as K column p (and 128 + p) of the
+// next B operand.  Seven products per walker: B, five Taylor terms, B.
 #include <cuda.h>
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -22,154 +35,216 @@
 
 namespace afqmc {
 
-constexpr int PT_K = 256;            // padded K = 2N
-constexpr int PT_PANELS = PT_K / 32;  // 128-byte rows of 32 TF32
-constexpr int PT_A_BYTES = 128 * PT_K * 4;
-constexpr int PT_NCMAX = 80;         // max B rows (2 x 40 columns) per pass
-constexpr int PT_B_BYTES = PT_NCMAX * PT_K * 4;
-constexpr int PT_SMEM = PT_A_BYTES + PT_B_BYTES + 64 + 1024;
+constexpr int PT_K = 256;                          // K: real block [0, 128), imaginary block [128, 256)
+constexpr int PT_A_BYTES = 128 * PT_K * 2;         // one BF16 half of A
+constexpr int PT_NCMAX = 80;                       // max B rows (2 x 40 columns) per pass
+constexpr int PT_B_BYTES = PT_NCMAX * PT_K * 2;    // one BF16 half of B
+constexpr int PT_SMEM = 2 * PT_A_BYTES + 2 * PT_B_BYTES + 64 + 1024;
+constexpr int PT_IMG = 128 * PT_K;                 // BF16 elements of one half of the B image
+constexpr int PT_COPY = 16384;                     // bytes per bulk copy
 
-// byte offset of element (row r, k) in a K-major SW128 operand of R rows
-__device__ __forceinline__ uint32_t sw_off(int r, int k, int R) {
-  const int kb = k >> 5, kk = k & 31;
-  const int chunk = (kk >> 2) ^ (r & 7);
-  return (uint32_t)(kb * R * 128 + r * 128 + chunk * 16 + (kk & 3) * 4);
+// byte offset of element (row r, k) in a K-major SW128 BF16 operand of R rows
+// (R a multiple of 8; panels of 64 K-elements are R x 128 bytes apart)
+__host__ __device__ __forceinline__ uint32_t pt_off(int r, int k, int R) {
+  const int kb = k >> 6, kk = k & 63;
+  const int chunk = (kk >> 3) ^ (r & 7);
+  return (uint32_t)(kb * R * 128 + r * 128 + chunk * 16 + (kk & 7) * 2);
 }
 
-// Instruction descriptor, kind::tf32: D FP32 (bits 4-5 = 1), A and B TF32
-// (bits 7-9 = 2, 10-12 = 2), K-major, N >> 3 at 17-22, M >> 4 at 24-28.
-__host__ __device__ constexpr uint32_t idesc_tf32(int M, int N) {
-  return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+__device__ __forceinline__ void pt_split(float v, __nv_bfloat16& hi, __nv_bfloat16& lo) {
+  hi = __float2bfloat16_rn(v);
+  lo = __float2bfloat16_rn(v - __bfloat162float(hi));
 }
 
-__device__ __forceinline__ void mma_tf32(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
-                                         uint32_t accumulate) {
-  asm volatile(
-      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
-      " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
-      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
-      : "memory");
+// 1-D bulk copy global -> shared, completing on an mbarrier (16-byte aligned, size % 16 == 0)
+__device__ __forceinline__ void pt_bulk(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   tc::smem_u32(dst)),
+               "l"(src), "r"(bytes), "r"(tc::smem_u32(bar))
+               : "memory");
 }
 
-__device__ __forceinline__ void fence_proxy_async() {
+__device__ __forceinline__ void pt_fence_proxy() {
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }
 
-// out[c] = (M X)[row p][c] for c < nc (FP32), computed by the tensor core.
-// Issued by thread 0; every thread waits on the barrier (bounded).
-__device__ __forceinline__ bool pt_product(uint8_t* sA, uint8_t* sB, int nc, uint32_t tmem, uint64_t* bar,
+// The split, swizzled A image of B - I for each spin block: img[s][half][pt_off / 2].
+__global__ void k_pt_image(const float* __restrict__ expm32, __nv_bfloat16* __restrict__ img, int N) {
+  const int s = blockIdx.y;
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= 128 * PT_K) return;
+  const int r = e / PT_K, k = e % PT_K;
+  const float* Br = expm32 + (size_t)s * 2 * N * N;
+  const float* Bi = Br + (size_t)N * N;
+  float v = 0.f;
+  if (r < N) {
+    if (k < N) v = Br[(size_t)k * N + r] - (k == r ? 1.f : 0.f);  // B(r, q) column-major
+    else if (k >= 128 && k < 128 + N) v = Bi[(size_t)(k - 128) * N + r];
+  }
+  __nv_bfloat16 hi, lo;
+  pt_split(v, hi, lo);
+  const uint32_t o = pt_off(r, k, 128) / 2;
+  img[(size_t)(2 * s) * PT_IMG + o] = hi;
+  img[(size_t)(2 * s + 1) * PT_IMG + o] = lo;
+}
+
+// Start the copy of one spin block's B - I image (hi and lo, 128 KB) into A.
+__device__ __forceinline__ void pt_issue_image(uint8_t* sA, const __nv_bfloat16* img, uint64_t* bar) {
+  if (threadIdx.x == 0) {
+    tc::mbar_expect_tx(bar, 2 * PT_A_BYTES);
+    const uint8_t* src = (const uint8_t*)img;
+#pragma unroll 1
+    for (int o = 0; o < 2 * PT_A_BYTES; o += PT_COPY) pt_bulk(sA + o, src + o, PT_COPY, bar);
+  }
+}
+
+// All threads agree whether the wait succeeded.
+__device__ __forceinline__ bool pt_wait(uint64_t* bar, uint32_t& phase, int* err, int code) {
+  const bool ok = tc::mbar_wait(bar, phase, err, code);
+  phase ^= 1u;
+  return __syncthreads_and(ok ? 1 : 0) != 0;
+}
+
+// TMEM[128 x nc] = A . B^T over the first ns K-steps of 16, three split passes.
+__device__ __forceinline__ bool pt_product(uint8_t* sA, uint8_t* sB, int nc, int ns, uint32_t tmem, uint64_t* bar,
                                            uint32_t& phase, int* err) {
-  fence_proxy_async();
+  pt_fence_proxy();  // this thread's generic writes to A / B -> visible to the tensor core
+  tc::tc_fence_before();
   __syncthreads();
   if (threadIdx.x == 0) {
     tc::tc_fence_after();
-    const uint32_t idesc = idesc_tf32(128, nc);
-    const uint32_t a0 = tc::smem_u32(sA), b0 = tc::smem_u32(sB);
+    const uint32_t idesc = tc::idesc_bf16(128, nc);
+    const uint32_t a_hi = tc::smem_u32(sA), a_lo = a_hi + PT_A_BYTES;
+    const uint32_t b_hi = tc::smem_u32(sB), b_lo = b_hi + PT_B_BYTES;
 #pragma unroll 1
-    for (int s = 0; s < PT_K / 8; ++s) {
-      const uint32_t ao = (uint32_t)((s >> 2) * 128 * 128 + (s & 3) * 32);
-      const uint32_t bo = (uint32_t)((s >> 2) * nc * 128 + (s & 3) * 32);
-      mma_tf32(tmem, tc::sdesc_sw128(a0 + ao), tc::sdesc_sw128(b0 + bo), idesc, s > 0 ? 1u : 0u);
+    for (int pass = 0; pass < 3; ++pass) {
+      const uint32_t a0 = pass == 1 ? a_lo : a_hi;
+      const uint32_t b0 = pass == 2 ? b_lo : b_hi;
+#pragma unroll 1
+      for (int s = 0; s < ns; ++s) {
+        const uint32_t ao = (uint32_t)((s >> 2) * 128 * 128 + (s & 3) * 32);
+        const uint32_t bo = (uint32_t)((s >> 2) * nc * 128 + (s & 3) * 32);
+        tc::mma_bf16(tmem, tc::sdesc_sw128(a0 + ao), tc::sdesc_sw128(b0 + bo), idesc,
+                     (pass > 0 || s > 0) ? 1u : 0u);
+      }
     }
     tc::mma_commit(bar);
   }
-  const bool ok = tc::mbar_wait(bar, phase, err, 21);
-  phase ^= 1u;
+  const bool ok = pt_wait(bar, phase, err, 21);
   tc::tc_fence_after();
   return ok;
 }
 
-// load [Mr | Mi] rows p < N (zero rows N..127, zero K padding) into A
-__device__ __forceinline__ void pt_load_B(uint8_t* sA, const float* __restrict__ Br, const float* __restrict__ Bi,
-                                          int N, int realB) {
-  // thread p writes row p; B(p, q) = Br[q N + p] (column-major) -> coalesced over p
-  const int p = threadIdx.x;
-  for (int k = 0; k < PT_K; ++k) {
-    float v = 0.f;
-    if (p < N) {
-      if (k < N) v = __ldg(Br + (size_t)k * N + p);
-      else if (k >= 128 && k < 128 + N && !realB) v = __ldg(Bi + (size_t)(k - 128) * N + p);
-    }
-    *(float*)(sA + sw_off(p, k, 128)) = v;
-  }
-}
-
-__device__ __forceinline__ void pt_load_V(uint8_t* sA, const float* __restrict__ vre, const float* __restrict__ vim,
-                                          const int2* __restrict__ tri, int N) {
-  const int T = N * (N + 1) / 2;
-  // zero the padding rows / columns first
-  for (int e = threadIdx.x; e < 128 * PT_K; e += blockDim.x) {
-    const int r = e / PT_K, k = e % PT_K;
-    if (r >= N || (k >= N && k < 128) || k >= 128 + N) *(float*)(sA + sw_off(r, k, 128)) = 0.f;
-  }
-  // V(i, j) = V(j, i): row i gets Re at k = j and Im at k = 128 + j
-  for (int t = threadIdx.x; t < T; t += blockDim.x) {
-    const int2 ij = tri[t];
-    const float re = vre[t], im = vim[t];
-    *(float*)(sA + sw_off(ij.x, ij.y, 128)) = re;
-    *(float*)(sA + sw_off(ij.x, 128 + ij.y, 128)) = im;
-    *(float*)(sA + sw_off(ij.y, ij.x, 128)) = re;
-    *(float*)(sA + sw_off(ij.y, 128 + ij.x, 128)) = im;
-  }
-}
-
-// write row p of X (x[c], c = 2j + {0 re, 1 im}) as column p / 128 + p of the B operand:
-// row (j, re) = [Xr(:, j) | -Xi(:, j)], row (j, im) = [Xi(:, j) | Xr(:, j)]
-__device__ __forceinline__ void pt_store_X(uint8_t* sB, const float* x, int nc, int p) {
-#pragma unroll 4
+// Row p of X (x[2j] = Re X(p, j), x[2j+1] = Im X(p, j)) into K column p (and
+// 128 + p when `both`) of the B operand rows (j, re) and (j, im), split in BF16.
+__device__ __forceinline__ void pt_store_X(uint8_t* sB, const float* x, int nc, int p, bool both) {
+  uint8_t* sBl = sB + PT_B_BYTES;
+#pragma unroll
   for (int j2 = 0; j2 < PT_NCMAX; j2 += 2) {
     if (j2 < nc) {
-      const float xr = x[j2], xi = x[j2 + 1];
-      *(float*)(sB + sw_off(j2, p, nc)) = xr;
-      *(float*)(sB + sw_off(j2, 128 + p, nc)) = -xi;
-      *(float*)(sB + sw_off(j2 + 1, p, nc)) = xi;
-      *(float*)(sB + sw_off(j2 + 1, 128 + p, nc)) = xr;
+      __nv_bfloat16 rh, rl, ih, il;
+      pt_split(x[j2], rh, rl);
+      pt_split(x[j2 + 1], ih, il);
+      const uint32_t o0 = pt_off(j2, p, nc), o1 = pt_off(j2 + 1, p, nc);
+      *(__nv_bfloat16*)(sB + o0) = rh;
+      *(__nv_bfloat16*)(sBl + o0) = rl;
+      *(__nv_bfloat16*)(sB + o1) = ih;
+      *(__nv_bfloat16*)(sBl + o1) = il;
+      if (both) {
+        const uint32_t q0 = pt_off(j2, 128 + p, nc), q1 = pt_off(j2 + 1, 128 + p, nc);
+        *(__nv_bfloat16*)(sB + q0) = __hneg(ih);
+        *(__nv_bfloat16*)(sBl + q0) = __hneg(il);
+        *(__nv_bfloat16*)(sB + q1) = rh;
+        *(__nv_bfloat16*)(sBl + q1) = rl;
+      }
     }
+  }
+}
+
+// Scatter the walker's V (packed lower triangle, V(i, j) = V(j, i)) into A,
+// split in BF16: row i gets Re V(i, j) at K = j and Im V(i, j) at K = 128 + j.
+// Positions outside [0, N) x ([0, N) U [128, 128 + N)) keep the image's zeros.
+__device__ __forceinline__ void pt_load_V(uint8_t* sA, const float* __restrict__ vre, const float* __restrict__ vim,
+                                          const int2* __restrict__ tri, int T) {
+  uint8_t* sAl = sA + PT_A_BYTES;
+  for (int t = threadIdx.x; t < T; t += blockDim.x) {
+    const int2 ij = __ldg(tri + t);
+    __nv_bfloat16 rh, rl, ih, il;
+    pt_split(__ldg(vre + t), rh, rl);
+    pt_split(__ldg(vim + t), ih, il);
+    uint32_t o = pt_off(ij.x, ij.y, 128);
+    *(__nv_bfloat16*)(sA + o) = rh;
+    *(__nv_bfloat16*)(sAl + o) = rl;
+    o = pt_off(ij.x, 128 + ij.y, 128);
+    *(__nv_bfloat16*)(sA + o) = ih;
+    *(__nv_bfloat16*)(sAl + o) = il;
+    o = pt_off(ij.y, ij.x, 128);
+    *(__nv_bfloat16*)(sA + o) = rh;
+    *(__nv_bfloat16*)(sAl + o) = rl;
+    o = pt_off(ij.y, 128 + ij.x, 128);
+    *(__nv_bfloat16*)(sA + o) = ih;
+    *(__nv_bfloat16*)(sAl + o) = il;
   }
 }
 
 __device__ __forceinline__ void pt_read(uint32_t tmem, int nc, float* y) {
-  const int warp = threadIdx.x >> 5;
+  const uint32_t lane_base = (uint32_t)((threadIdx.x >> 5) * 32) << 16;
 #pragma unroll
-  for (int c = 0; c < PT_NCMAX; c += 16) {
-    if (c < nc) tc::tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c, y + c);
-  }
+  for (int c = 0; c < PT_NCMAX; c += 16)
+    if (c < nc) tc::tmem_ld16(tmem + lane_base + (uint32_t)c, y + c);
+}
+
+// y += this thread's row of the product (the identity part of B X = X + (B - I) X)
+__device__ __forceinline__ void pt_read_add(uint32_t tmem, int nc, float* y) {
+  const uint32_t lane_base = (uint32_t)((threadIdx.x >> 5) * 32) << 16;
+#pragma unroll
+  for (int c = 0; c < PT_NCMAX; c += 16)
+    if (c < nc) {
+      float t[16];
+      tc::tmem_ld16(tmem + lane_base + (uint32_t)c, t);
+#pragma unroll
+      for (int i = 0; i < 16; ++i) y[c + i] += t[i];
+    }
 }
 
 __global__ void __launch_bounds__(128, 1)
     k_prop_tc(double2* __restrict__ psi, float2* __restrict__ psi32, const float* __restrict__ Vp,
-              const float* __restrict__ expm32, const int2* __restrict__ tri, const double* __restrict__ weights,
-              int N, int ncw, int na, int nspV, int realB, int* err) {
+              const __nv_bfloat16* __restrict__ img, const int2* __restrict__ tri,
+              const double* __restrict__ weights, int N, int ncw, int na, int nspV, int realB, int* err) {
   const int w = blockIdx.x;
   if (!(weights[w] > 1.0e-8)) return;
   const int sp = blockIdx.y;
   extern __shared__ uint8_t pt_raw[];
   uint8_t* smem = (uint8_t*)(((uintptr_t)pt_raw + 1023) & ~(uintptr_t)1023);
-  uint8_t* sA = smem;
-  uint8_t* sB = smem + PT_A_BYTES;
-  uint64_t* bar = (uint64_t*)(sB + PT_B_BYTES);
-  uint32_t* tmem_holder = (uint32_t*)(bar + 1);
+  uint8_t* sA = smem;                    // hi at 0, lo at PT_A_BYTES
+  uint8_t* sB = smem + 2 * PT_A_BYTES;   // hi at 0, lo at PT_B_BYTES
+  uint64_t* bar_ld = (uint64_t*)(sB + 2 * PT_B_BYTES);
+  uint64_t* bar_mma = bar_ld + 1;
+  uint32_t* tmem_holder = (uint32_t*)(bar_mma + 1);
   const int warp = threadIdx.x >> 5;
   if (threadIdx.x == 0) {
-    tc::mbar_init(bar, 1);
+    tc::mbar_init(bar_ld, 1);
+    tc::mbar_init(bar_mma, 1);
     tc::fence_mbar_init();
   }
   if (warp == 0) tc::tmem_alloc(tmem_holder, 128);
+  // B operand: K positions no row of X is written to stay zero
+  for (int e = threadIdx.x; e < 2 * PT_B_BYTES / 16; e += blockDim.x) ((uint4*)sB)[e] = make_uint4(0, 0, 0, 0);
   tc::tc_fence_before();
   __syncthreads();
   tc::tc_fence_after();
   const uint32_t tmem = *tmem_holder;
-  uint32_t phase = 0;
+  uint32_t ph_ld = 0, ph_mma = 0;
   bool ok = true;
 
   const int T = N * (N + 1) / 2;
   const float* vre = Vp + ((size_t)(w * nspV + sp) * 2) * T;
   const float* vim = vre + T;
-  const float* Br = expm32 + (size_t)sp * 2 * N * N;
-  const float* Bi = Br + (size_t)N * N;
+  const __nv_bfloat16* im = img + (size_t)sp * 2 * PT_IMG;
   const int col_lo = nspV == 1 ? 0 : (sp == 0 ? 0 : na);
   const int col_hi = nspV == 1 ? ncw : (sp == 0 ? na : ncw);
   const int p = threadIdx.x;
+  const int nsB = realB ? 8 : 16;  // K-steps of a product with B (imaginary block all zero when real)
   double2* pw = psi + (size_t)w * ncw * N;
   float2* pw32 = psi32 + (size_t)w * ncw * N;
 
@@ -177,34 +252,30 @@ __global__ void __launch_bounds__(128, 1)
     const int ncols = min(PT_NCMAX / 2, col_hi - c0);
     const int nc = ((2 * ncols + 15) / 16) * 16;
     float x[PT_NCMAX], acc[PT_NCMAX];
-    // zero the whole B operand (padding rows and K beyond 2N stay zero)
     __syncthreads();
-    for (int e = threadIdx.x; e < nc * PT_K; e += blockDim.x) ((float*)sB)[e] = 0.f;
-    __syncthreads();
+    pt_issue_image(sA, im, bar_ld);
 #pragma unroll
-    for (int c = 0; c < PT_NCMAX; ++c) x[c] = 0.f;
-    if (p < N)
-      for (int j = 0; j < ncols; ++j) {
-        const float2 v = pw32[(size_t)(c0 + j) * N + p];
-        x[2 * j] = v.x;
-        x[2 * j + 1] = v.y;
+    for (int j = 0; j < PT_NCMAX / 2; ++j) {
+      float2 v = make_float2(0.f, 0.f);
+      if (j < ncols && p < N) {
+        const double2 d = pw[(size_t)(c0 + j) * N + p];
+        v = make_float2((float)d.x, (float)d.y);
       }
-    // B psi
-    pt_load_B(sA, Br, Bi, N, realB);
-    if (p < N) pt_store_X(sB, x, nc, p);
-    ok = pt_product(sA, sB, nc, tmem, bar, phase, err);
-    if (!ok) break;
-    pt_read(tmem, nc, x);
+      x[2 * j] = v.x;
+      x[2 * j + 1] = v.y;
+    }
+    if (p < N) pt_store_X(sB, x, nc, p, !realB);
+    if (!(ok = pt_wait(bar_ld, ph_ld, err, 22))) break;
+    // B psi = psi + (B - I) psi
+    if (!(ok = pt_product(sA, sB, nc, nsB, tmem, bar_mma, ph_mma, err))) break;
+    pt_read_add(tmem, nc, x);
 #pragma unroll
     for (int c = 0; c < PT_NCMAX; ++c) acc[c] = x[c];
     // Taylor terms with V
-    __syncthreads();
-    pt_load_V(sA, vre, vim, tri, N);
+    pt_load_V(sA, vre, vim, tri, T);
     for (int k = 1; k <= 5 && ok; ++k) {
-      __syncthreads();
-      if (p < N) pt_store_X(sB, x, nc, p);
-      ok = pt_product(sA, sB, nc, tmem, bar, phase, err);
-      if (!ok) break;
+      if (p < N) pt_store_X(sB, x, nc, p, true);
+      if (!(ok = pt_product(sA, sB, nc, 16, tmem, bar_mma, ph_mma, err))) break;
       pt_read(tmem, nc, x);
       const float inv = 1.f / (float)k;
 #pragma unroll
@@ -215,18 +286,20 @@ __global__ void __launch_bounds__(128, 1)
     }
     if (!ok) break;
     // B (sum)
-    __syncthreads();
-    pt_load_B(sA, Br, Bi, N, realB);
-    if (p < N) pt_store_X(sB, acc, nc, p);
-    ok = pt_product(sA, sB, nc, tmem, bar, phase, err);
-    if (!ok) break;
-    pt_read(tmem, nc, x);
-    if (p < N)
-      for (int j = 0; j < ncols; ++j) {
-        const size_t o = (size_t)(c0 + j) * N + p;
-        pw[o] = make_double2((double)x[2 * j], (double)x[2 * j + 1]);
-        pw32[o] = make_float2(x[2 * j], x[2 * j + 1]);
-      }
+    pt_issue_image(sA, im, bar_ld);
+    if (p < N) pt_store_X(sB, acc, nc, p, !realB);
+    if (!(ok = pt_wait(bar_ld, ph_ld, err, 22))) break;
+    if (!(ok = pt_product(sA, sB, nc, nsB, tmem, bar_mma, ph_mma, err))) break;
+    pt_read_add(tmem, nc, acc);
+    if (p < N) {
+#pragma unroll
+      for (int j = 0; j < PT_NCMAX / 2; ++j)
+        if (j < ncols) {
+          const size_t o = (size_t)(c0 + j) * N + p;
+          pw[o] = make_double2((double)acc[2 * j], (double)acc[2 * j + 1]);
+          pw32[o] = make_float2(acc[2 * j], acc[2 * j + 1]);
+        }
+    }
   }
   tc::tc_fence_before();
   __syncthreads();
@@ -236,6 +309,15 @@ __global__ void __launch_bounds__(128, 1)
   }
 }
 
+bool setup_prop_tc(afqmc_handle* h) {
+  if (h->N > 128 || !h->pt_img) return true;
+  dim3 grid(128 * PT_K / 256, h->nsp);
+  k_pt_image<<<grid, 256, 0, h->stream>>>(h->expm32, h->pt_img, h->N);
+  return cudaGetLastError() == cudaSuccess;
+}
+
+bool prop_tc_available(const afqmc_handle* h) { return h->N <= 128 && h->pt_img != nullptr; }
+
 void launch_propagate_tc(afqmc_handle* h) {
   static bool attr = false;
   if (!attr) {
@@ -243,8 +325,8 @@ void launch_propagate_tc(afqmc_handle* h) {
     attr = true;
   }
   dim3 grid(h->nwalk, h->nspV);
-  k_prop_tc<<<grid, 128, PT_SMEM, h->stream>>>(h->psi, h->psi32, h->V32, h->expm32, h->tri, h->weights, h->N, h->ncw,
-                                               h->na, h->nspV, h->real_expm ? 1 : 0, h->d_err);
+  k_prop_tc<<<grid, 128, PT_SMEM, h->stream>>>(h->psi, h->psi32, h->V32, h->pt_img, h->tri, h->weights, h->N,
+                                               h->ncw, h->na, h->nspV, h->real_expm ? 1 : 0, h->d_err);
   h->launches++;
 }
 
