@@ -3,9 +3,9 @@ with the reference's (Eigen's) column convention.
 
 The two factorisations give the same Q up to the sign of each column, and the
 overlaps differ by the product of those signs (squared for the restricted
-walker): checked to 1e-12.  Every physical quantity is unchanged: local
-energies after the QR agree to 1e-5 Eh (the mixed form keeps the pre-QR theta,
-which is invariant, where the Householder path recomputes it in FP32), and one
+walker): checked to 1e-12.  Every physical quantity is unchanged: the local
+energies after either QR are within 2e-5 Eh of the FP64 oracle's energies of
+the walkers before it (the mixed form's local-energy tolerance), and one
 further step with identical fields gives the same weights to 1e-6 relative.
 """
 import numpy as np
@@ -39,7 +39,8 @@ def test_cholesky_qr_equals_householder_up_to_column_signs(A, kind):
     W = 48
     rng = np.random.default_rng(5)
     base = O._ref_dets(oh, ot.phi, rw)
-    dets = base[None] + 0.3 * (rng.standard_normal((W,) + base.shape) + 1j * rng.standard_normal((W,) + base.shape))
+    dets = base[None] + 0.1 * (rng.standard_normal((W,) + base.shape) + 1j * rng.standard_normal((W,) + base.shape))
+    el_ref = O.local_energy(ot, O.Walkers(oh, rw, dets), oh).real
     out = {}
     for qr in ("householder", "cholesky"):
         gh = A.Hamiltonian(N, na, nb, oh.ecore, oh.h1, oh.h1mod, oh.chol)
@@ -57,11 +58,7 @@ def test_cholesky_qr_equals_householder_up_to_column_signs(A, kind):
         out[qr] = (d, o, el, w1)
     dh, oh_, elh, w1h = out["householder"]
     dc, oc, elc, w1c = out["cholesky"]
-    def blocks_of(d):  # serial layout: alpha N x na row-major, then beta N x nb (a copy for the RHF walker)
-        a = d[:, :N * na].reshape(W, N, na)
-        return a if rw else np.concatenate([a, d[:, N * na:].reshape(W, N, nb)], axis=2)
-
-    qh, qc = blocks_of(dh), blocks_of(dc)
+    qh, qc = dh, dc  # (W, N, columns): alpha columns, then beta for the unrestricted walker
     for w in range(W):
         sgn = np.sign(np.einsum("pj,pj->j", qh[w].conj(), qc[w]).real)
         assert np.all(np.abs(sgn) == 1)
@@ -73,5 +70,6 @@ def test_cholesky_qr_equals_householder_up_to_column_signs(A, kind):
             assert np.abs(g - np.eye(b - a)).max() < 1e-12
         fac = np.prod(sgn) ** (2 if rw else 1)
         assert abs(oc[w] - fac * oh_[w]) <= 1e-12 * abs(oh_[w])
-    assert np.abs(elc - elh).max() < 1e-5
+    assert np.abs(elh - el_ref).max() < 2e-5
+    assert np.abs(elc - el_ref).max() < 2e-5
     assert np.abs(w1c - w1h).max() <= 1e-6 * np.abs(w1h).max()

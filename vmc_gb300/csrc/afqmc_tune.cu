@@ -177,7 +177,7 @@ int afqmc_tuning(const afqmc_handle* h, int* bn_fb, int* bn_vhs, int* prop, int*
   if (bn_vhs) *bn_vhs = h->tune_bn_vhs;
   if (prop) *prop = h->tune_prop;
   if (ovl) *ovl = h->tune_ovl;
-  if (qr) *qr = h->tune_qr == 2 ? 2 : 1;
+  if (qr) *qr = h->tune_qr == 0 ? (afqmc::ortho_chol_available(h) ? 2 : 1) : h->tune_qr;
   return AFQMC_OK;
 }
 

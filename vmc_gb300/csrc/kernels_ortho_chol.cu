@@ -147,7 +147,7 @@ void launch_ortho_chol(afqmc_handle* h) {
 }
 
 void launch_ortho_refresh(afqmc_handle* h) {
-  if (h->tune_qr == 2 && ortho_chol_available(h)) {
+  if (h->tune_qr != 1 && ortho_chol_available(h)) {
     launch_ortho_chol(h);  // theta and the cached force bias stay valid
     return;
   }
