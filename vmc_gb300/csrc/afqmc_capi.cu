@@ -177,7 +177,7 @@ void release(afqmc_handle* h) {
                   h->qwork, h->epart, h->eloc, h->scal, h->d_chunks, h->d_err, h->rotA, h->LTA,
                   h->thetaB, h->xB, h->fb32, h->V32, h->expm32, h->d_chunks32, h->rotE, h->thetaE,
                   h->xc, h->cv_x, h->cv_idx, h->cv_esub, h->cv_f, h->cv_ms, h->cv_out, h->d_step, h->psi32,
-                  h->pt_img, h->comb_cum, h->comb_idx, h->comb_ovl, h->blk, h->blk_zeta};
+                  h->pt_img, h->comb_cum, h->comb_idx, h->comb_ovl, h->blk, h->blk_zeta, h->wpart};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (h->host_pinned) cudaFreeHost(h->host_pinned);
@@ -469,6 +469,7 @@ int afqmc_create(const afqmc_ham* ham, const afqmc_trial* trial, const afqmc_opt
   ALLOC(eloc, W);
   ALLOC(scal, (size_t)afqmc::S_NSLOTS);
   ALLOC(d_chunks, (size_t)h->nchunks);
+  ALLOC(wpart, 2 * (size_t)afqmc::WT_MAXPARTS);
   ALLOC(comb_cum, W);
   ALLOC(comb_idx, W);
   ALLOC(comb_ovl, W);

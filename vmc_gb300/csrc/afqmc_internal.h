@@ -48,6 +48,7 @@ enum {
   S_NSLOTS = 24
 };
 constexpr int BLK_MAX = 65536;  // block ring capacity (samples of one run)
+constexpr int WT_MAXPARTS = 1024;  // CTAs of the weight update (partial sums)
 constexpr int DERR_NAN_ENERGY = 100;  // d_err code: non-finite local energy in a device block
 
 // Stage names for timing.
@@ -142,6 +143,7 @@ struct afqmc_handle {
   bool fb_current = false;               // fb32 holds the force bias of the current theta
   float2* psi32 = nullptr;               // [W][ncw][N] FP32 copy of psi (mixed form)
   // device-resident blocks: comb scratch, the block ring and host-given zetas
+  double* wpart = nullptr;      // [WT_MAXPARTS][2] partial sums of the weight update
   double* comb_cum = nullptr;   // [W]
   int* comb_idx = nullptr;      // [W]
   double2* comb_ovl = nullptr;  // [W]

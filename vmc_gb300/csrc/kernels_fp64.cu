@@ -642,16 +642,20 @@ __global__ void k_propagate(double2* __restrict__ psi, const double* __restrict_
 // weights (DQMCWalker.cpp:495-502, MixedEstimator.cpp:461-475): importance
 // function, phaseless projection, cap, sum of weights, next eshift.  One CTA.
 // ---------------------------------------------------------------------------
-__global__ void k_weights(double* __restrict__ weights, double2* __restrict__ ovlp,
-                          const double2* __restrict__ det, const double2* __restrict__ shift,
-                          const double2* __restrict__ fbterm, double* __restrict__ scal, int W, int nchan,
-                          int mult, double dt, double c0r, double c0i, double cap, double target,
-                          unsigned long long* __restrict__ stepp) {
+// Per-walker part over many CTAs (the FP64 transcendentals of one walker are
+// the cost; one SM would take ~0.1 ms for 2048 walkers); each CTA writes its
+// partial sums, which k_weights_final adds in CTA order.
+constexpr int WT_THREADS = 128;
+__global__ void __launch_bounds__(WT_THREADS)
+    k_weights(double* __restrict__ weights, double2* __restrict__ ovlp, const double2* __restrict__ det,
+              const double2* __restrict__ shift, const double2* __restrict__ fbterm, const double* __restrict__ scal,
+              int W, int nchan, int mult, double dt, double c0r, double c0i, double cap,
+              double* __restrict__ part) {
   const double eshift = scal[S_ESHIFT];
   const double sdt = sqrt(dt);
   double sumw = 0.0;
   double ncap = 0.0;
-  for (int w = threadIdx.x; w < W; w += blockDim.x) {
+  for (int w = blockIdx.x * WT_THREADS + threadIdx.x; w < W; w += gridDim.x * WT_THREADS) {
     double wt = weights[w];
     if (wt > 1.0e-8) {
       double2 on = det[2 * w];
@@ -675,6 +679,21 @@ __global__ void k_weights(double* __restrict__ weights, double2* __restrict__ ov
   sumw = block_sum(sumw);
   ncap = block_sum(ncap);
   if (threadIdx.x == 0) {
+    part[2 * blockIdx.x] = sumw;
+    part[2 * blockIdx.x + 1] = ncap;
+  }
+}
+
+__global__ void k_weights_final(const double* __restrict__ part, int nparts, double* __restrict__ scal, double dt,
+                                double target, unsigned long long* __restrict__ stepp) {
+  double sumw = 0.0, ncap = 0.0;
+  for (int b = threadIdx.x; b < nparts; b += blockDim.x) {
+    sumw += part[2 * b];
+    ncap += part[2 * b + 1];
+  }
+  sumw = block_sum(sumw);
+  ncap = block_sum(ncap);
+  if (threadIdx.x == 0) {
     scal[S_SUMW] = sumw;
     scal[S_NCAP] += ncap;
     scal[S_ESHIFT] = scal[S_EEST] - 0.1 * log(sumw / target) / dt;
@@ -682,12 +701,15 @@ __global__ void k_weights(double* __restrict__ weights, double2* __restrict__ ov
   }
 }
 
+int weights_parts(const afqmc_handle* h) { return std::min(WT_MAXPARTS, (h->nwalk + WT_THREADS - 1) / WT_THREADS); }
+
 void launch_weights(afqmc_handle* h) {
   const double cr = h->prop_constant.real(), ci = h->prop_constant.imag();
-  k_weights<<<1, 1024, 0, h->stream>>>(h->weights, h->ovlp, h->det, h->shift, h->fbterm, h->scal, h->nwalk,
-                                       h->nchan, h->mult, h->dt, cr, ci, h->weight_cap, h->pop_target,
-                                       h->d_step);
-  h->launches++;
+  const int nb = weights_parts(h);
+  k_weights<<<nb, WT_THREADS, 0, h->stream>>>(h->weights, h->ovlp, h->det, h->shift, h->fbterm, h->scal, h->nwalk,
+                                               h->nchan, h->mult, h->dt, cr, ci, h->weight_cap, h->wpart);
+  k_weights_final<<<1, 256, 0, h->stream>>>(h->wpart, nb, h->scal, h->dt, h->pop_target, h->d_step);
+  h->launches += 2;
 }
 
 // ---------------------------------------------------------------------------
