@@ -4,7 +4,8 @@
 //   * N-tile (64 / 128 / 256) of the tensor-core force-bias and VHS GEMMs,
 //   * propagator: tensor core (tcgen05, split BF16), walker V resident in
 //     shared memory (FP32), or column-chunked with V streamed from L2 (FP32),
-//   * overlap / inverse: one warp per matrix, or one CTA per matrix.
+//   * overlap / inverse: one warp per matrix with M = Phi^T psi in FP64 or on
+//     the tensor cores (exact BF16 slices), or one CTA per matrix.
 // Choices are cached in a text file (one "key value..." line per size class),
 // so later handles of the same class skip the timing.
 #include <cuda_runtime.h>
@@ -117,13 +118,14 @@ int afqmc_autotune(afqmc_handle* h, const char* cache_path, char* report, int re
   {
     const int nmax = std::max(h->chan[0].n, h->nchan > 1 ? h->chan[1].n : 0);
     float best = 1e30f;
-    const int cands[2] = {1, 2};
+    const int cands[3] = {3, 1, 2};
     for (int c : cands) {
       if (c == 1 && (nmax > 32 || (size_t)nmax * h->N * 8 + 4 * ((size_t)nmax * nmax * 24 + 4 * nmax + 16) > 160 * 1024))
         continue;
+      if (c == 3 && !afqmc::ovl_tc_available(h)) continue;
       h->tune_ovl = c;
       const float t = time_ms(h, [&] { afqmc::launch_overlap_theta(h, false); }, 3);
-      rep << "ovl" << (c == 1 ? "_warp" : "_block") << "=" << t << "ms ";
+      rep << "ovl" << (c == 1 ? "_warp" : c == 2 ? "_block" : "_tc") << "=" << t << "ms ";
       if (t < best) { best = t; h->tune_ovl_best = c; }
     }
     h->tune_ovl = h->tune_ovl_best;
@@ -149,13 +151,14 @@ int afqmc_set_tuning(afqmc_handle* h, int bn_fb, int bn_vhs, int prop, int ovl, 
   if (!h) return AFQMC_ERR_ARG;
   auto bn_ok = [](int b) { return b <= 0 || b == 64 || b == 128 || b == 256; };
   const bool mixed = h->precision == AFQMC_PREC_MIXED;
-  if (!bn_ok(bn_fb) || !bn_ok(bn_vhs) || prop > 3 || ovl > 2 || ((bn_fb > 0 || bn_vhs > 0 || prop > 0) && !mixed) ||
+  if (!bn_ok(bn_fb) || !bn_ok(bn_vhs) || prop > 3 || ovl > 3 || ((bn_fb > 0 || bn_vhs > 0 || prop > 0) && !mixed) ||
+      (ovl == 3 && !afqmc::ovl_tc_available(h)) ||
       ((prop == 1) && h->N > 128) || (prop == 3 && !afqmc::prop_tc_available(h)) || qr > 2 ||
       (qr == 2 && !afqmc::ortho_chol_available(h))) {
     h->err = "afqmc_set_tuning: choice not available for this handle";
     return AFQMC_ERR_ARG;
   }
-  if (ovl == 1) {
+  if (ovl == 1 || ovl == 3) {
     const int nmax = std::max(h->chan[0].n, h->nchan > 1 ? h->chan[1].n : 0);
     if (nmax > 32) {
       h->err = "afqmc_set_tuning: warp overlap needs at most 32 electrons per channel";

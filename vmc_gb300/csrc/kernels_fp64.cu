@@ -137,11 +137,14 @@ constexpr int OW_WARPS = 4;
 
 // NM: n rounded up to a multiple of 4 (<= 32); lane (li, lj) of the M product
 // owns rows li + 4a (a < NM/4) and columns lj + 8b (b < ceil(NM/8)).
-template <bool F32, int NM>
+// MB: M was formed beforehand (tensor-core overlap, mbuf[w][channel][i][j],
+// row stride n) and is read instead of computed here.
+template <bool F32, int NM, bool MB>
 __global__ void __launch_bounds__(OW_WARPS * 32)
     k_overlap_lu(const double2* __restrict__ psi, const float2* __restrict__ psi32, const double* __restrict__ phi,
                  double* __restrict__ theta, double2* __restrict__ det, const double* __restrict__ weights, int W,
-                 int N, int ncw, int nce, Channel c0, Channel c1, int only_live, int nmax) {
+                 int N, int ncw, int nce, Channel c0, Channel c1, int only_live, int nmax,
+                 const double2* __restrict__ mbuf) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int s = blockIdx.y;
   const Channel ch = s == 0 ? c0 : c1;
@@ -149,19 +152,25 @@ __global__ void __launch_bounds__(OW_WARPS * 32)
   extern __shared__ __align__(16) unsigned char ow_raw[];
   double* phs = (double*)ow_raw;  // [n][N] channel orbitals (column i at i N)
   const size_t per_warp = ((size_t)nmax * nmax * (sizeof(double2) + sizeof(float2)) + nmax * sizeof(int) + 15) & ~(size_t)15;
-  unsigned char* wbase = ow_raw + (((size_t)nmax * N * sizeof(double) + 15) & ~(size_t)15) + warp * per_warp;
+  const size_t phs_bytes = MB ? 0 : (((size_t)nmax * N * sizeof(double) + 15) & ~(size_t)15);
+  unsigned char* wbase = ow_raw + phs_bytes + warp * per_warp;
   double2* a = (double2*)wbase;                                     // [n][n] LU, row-major
   float2* af = (float2*)(wbase + (size_t)nmax * nmax * sizeof(double2));  // FP32 copy of the factors
   int* perm = (int*)(wbase + (size_t)nmax * nmax * (sizeof(double2) + sizeof(float2)));
-  const double* ph = phi + (size_t)ch.col_off * N;
-  for (int e = threadIdx.x; e < n * N; e += blockDim.x) phs[e] = ph[e];
-  __syncthreads();
+  if (!MB) {
+    const double* ph = phi + (size_t)ch.col_off * N;
+    for (int e = threadIdx.x; e < n * N; e += blockDim.x) phs[e] = ph[e];
+    __syncthreads();
+  }
   const int w = blockIdx.x * OW_WARPS + warp;
   if (w >= W) return;
   if (only_live && !(weights[w] > 1.0e-8)) return;
   const double2* ps = psi + (size_t)w * ncw * N + (size_t)ch.psi_off * N;
-  // M = Phi^T psi
-  {
+  if (MB) {
+    const double2* mb = mbuf + ((size_t)w * 2 + s) * nmax * nmax;
+    for (int e = lane; e < n * n; e += 32) a[e] = mb[e];
+  } else {  // M = Phi^T psi
+
     constexpr int OW_RI = NM / 4, OW_RJ = (NM + 7) / 8;
     const int li = lane >> 3, lj = lane & 7;
     double2 acc[OW_RI][OW_RJ];
@@ -348,40 +357,44 @@ void launch_psi_to_f32(afqmc_handle* h) {
 void launch_overlap_theta(afqmc_handle* h, bool only_live) {
   h->fb_current = false;  // theta changes
   int nmax = std::max(h->chan[0].n, h->nchan > 1 ? h->chan[1].n : 0);
-  const size_t smem_lu = (((size_t)nmax * h->N * sizeof(double) + 15) & ~(size_t)15) +
-                         OW_WARPS * (((size_t)nmax * nmax * (sizeof(double2) + sizeof(float2)) + nmax * sizeof(int) + 15) &
-                                     ~(size_t)15);
-  if (nmax <= 32 && h->tune_ovl != 2 && smem_lu <= 160 * 1024) {
-    const size_t smem = smem_lu;
+  const size_t per_warp =
+      ((size_t)nmax * nmax * (sizeof(double2) + sizeof(float2)) + nmax * sizeof(int) + 15) & ~(size_t)15;
+  const size_t smem_lu = (((size_t)nmax * h->N * sizeof(double) + 15) & ~(size_t)15) + OW_WARPS * per_warp;
+  const bool mtc = h->tune_ovl == 3 && ovl_tc_available(h);  // M on the tensor cores
+  if (nmax <= 32 && h->tune_ovl != 2 && (mtc || smem_lu <= 160 * 1024)) {
+    const size_t smem = mtc ? OW_WARPS * per_warp : smem_lu;
     const bool f32 = h->precision == AFQMC_PREC_MIXED && h->psi32;
+    if (mtc) launch_overlap_m_tc(h);
     dim3 grid((h->nwalk + OW_WARPS - 1) / OW_WARPS, h->nchan);
     const int nm = (nmax + 3) / 4 * 4;
-#define OW_LAUNCH(F, NMV)                                                                                     \
+#define OW_LAUNCH(F, NMV, MBV)                                                                                \
   {                                                                                                          \
     static bool attr = false;                                                                                \
     if (!attr) {                                                                                             \
-      cudaFuncSetAttribute(k_overlap_lu<F, NMV>, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);   \
+      cudaFuncSetAttribute(k_overlap_lu<F, NMV, MBV>, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024); \
       attr = true;                                                                                           \
     }                                                                                                        \
-    k_overlap_lu<F, NMV><<<grid, OW_WARPS * 32, smem, h->stream>>>(h->psi, h->psi32, h->phi, h->theta, h->det, \
-                                                                  h->weights, h->nwalk, h->N, h->ncw, h->nce, \
-                                                                  h->chan[0], h->chan[1], only_live ? 1 : 0, nmax); \
+    k_overlap_lu<F, NMV, MBV><<<grid, OW_WARPS * 32, smem, h->stream>>>(                                     \
+        h->psi, h->psi32, h->phi, h->theta, h->det, h->weights, h->nwalk, h->N, h->ncw, h->nce, h->chan[0],  \
+        h->chan[1], only_live ? 1 : 0, nmax, h->ovl_M);                                                       \
   }
-#define OW_NM(F)                          \
-  switch (nm) {                           \
-    case 4: OW_LAUNCH(F, 4) break;        \
-    case 8: OW_LAUNCH(F, 8) break;        \
-    case 12: OW_LAUNCH(F, 12) break;      \
-    case 16: OW_LAUNCH(F, 16) break;      \
-    case 20: OW_LAUNCH(F, 20) break;      \
-    case 24: OW_LAUNCH(F, 24) break;      \
-    case 28: OW_LAUNCH(F, 28) break;      \
-    default: OW_LAUNCH(F, 32) break;      \
+#define OW_NM(F, MBV)                          \
+  switch (nm) {                                \
+    case 4: OW_LAUNCH(F, 4, MBV) break;        \
+    case 8: OW_LAUNCH(F, 8, MBV) break;        \
+    case 12: OW_LAUNCH(F, 12, MBV) break;      \
+    case 16: OW_LAUNCH(F, 16, MBV) break;      \
+    case 20: OW_LAUNCH(F, 20, MBV) break;      \
+    case 24: OW_LAUNCH(F, 24, MBV) break;      \
+    case 28: OW_LAUNCH(F, 28, MBV) break;      \
+    default: OW_LAUNCH(F, 32, MBV) break;      \
   }
-    if (f32) {
-      OW_NM(true)
+    if (mtc) {
+      OW_NM(true, true)
+    } else if (f32) {
+      OW_NM(true, false)
     } else {
-      OW_NM(false)
+      OW_NM(false, false)
     }
 #undef OW_NM
 #undef OW_LAUNCH

@@ -511,7 +511,7 @@ bool setup_mixed(afqmc_handle* h) {
   for (int s = 0; s < h->nsp; ++s)
     split_rows(h, h->LT + (size_t)s * h->T * h->G, h->G, h->T, h->G, h->kv_pad, 0,
                h->LTA + (size_t)s * h->T * h->kv_pad);
-  bool ok = setup_prop_tc(h) && make_tmap_bf16(&h->tm_rot, h->rotA, h->G, h->kf_pad, tc::BM);
+  bool ok = setup_prop_tc(h) && setup_ovl_tc(h) && make_tmap_bf16(&h->tm_rot, h->rotA, h->G, h->kf_pad, tc::BM);
   const int bns[3] = {64, 128, 256};
   for (int i = 0; i < 3 && ok; ++i)
     ok = make_tmap_bf16(&h->tm_theta_bn[i], h->thetaB, 2 * h->nwalk, h->kf_pad, bns[i]) &&
