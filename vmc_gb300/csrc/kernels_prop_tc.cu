@@ -21,9 +21,10 @@
 // cp.async.bulk.
 // V comes from the packed lower triangle written by the VHS GEMM and is
 // scattered into A by the CTA.  Thread p (TMEM lane p) owns orbital row p: it
-// reads its row of each product with tcgen05.ld, keeps the Taylor sum of its
-// row in registers and writes its row back as K column p (and 128 + p) of the
-// next B operand.  Seven products per walker: B, five Taylor terms, B.
+// reads its row of each product with tcgen05.ld, keeps its row of the Taylor
+// sum in TMEM (columns 128.., its own lane) and writes its row back as K
+// column p (and 128 + p) of the next B operand.  Seven products per walker: B,
+// five Taylor terms, B.
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -167,23 +168,38 @@ __device__ __forceinline__ void pt_store_X(uint8_t* sB, const float* x, int nc, 
 __device__ __forceinline__ void pt_load_V(uint8_t* sA, const float* __restrict__ vre, const float* __restrict__ vim,
                                           const int2* __restrict__ tri, int T) {
   uint8_t* sAl = sA + PT_A_BYTES;
-  for (int t = threadIdx.x; t < T; t += blockDim.x) {
-    const int2 ij = __ldg(tri + t);
-    __nv_bfloat16 rh, rl, ih, il;
-    pt_split(__ldg(vre + t), rh, rl);
-    pt_split(__ldg(vim + t), ih, il);
-    uint32_t o = pt_off(ij.x, ij.y, 128);
-    *(__nv_bfloat16*)(sA + o) = rh;
-    *(__nv_bfloat16*)(sAl + o) = rl;
-    o = pt_off(ij.x, 128 + ij.y, 128);
-    *(__nv_bfloat16*)(sA + o) = ih;
-    *(__nv_bfloat16*)(sAl + o) = il;
-    o = pt_off(ij.y, ij.x, 128);
-    *(__nv_bfloat16*)(sA + o) = rh;
-    *(__nv_bfloat16*)(sAl + o) = rl;
-    o = pt_off(ij.y, 128 + ij.x, 128);
-    *(__nv_bfloat16*)(sA + o) = ih;
-    *(__nv_bfloat16*)(sAl + o) = il;
+  constexpr int VB = 8;  // loads of VB entries in flight per thread before their stores
+  for (int t0 = threadIdx.x; t0 < T; t0 += VB * blockDim.x) {
+    int2 ij[VB];
+    float re[VB], im[VB];
+#pragma unroll
+    for (int u = 0; u < VB; ++u) {
+      const int t = t0 + u * blockDim.x;
+      if (t < T) {
+        ij[u] = __ldg(tri + t);
+        re[u] = __ldg(vre + t);
+        im[u] = __ldg(vim + t);
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < VB; ++u) {
+      if (t0 + u * blockDim.x >= T) break;
+      __nv_bfloat16 rh, rl, ih, il;
+      pt_split(re[u], rh, rl);
+      pt_split(im[u], ih, il);
+      uint32_t o = pt_off(ij[u].x, ij[u].y, 128);
+      *(__nv_bfloat16*)(sA + o) = rh;
+      *(__nv_bfloat16*)(sAl + o) = rl;
+      o = pt_off(ij[u].x, 128 + ij[u].y, 128);
+      *(__nv_bfloat16*)(sA + o) = ih;
+      *(__nv_bfloat16*)(sAl + o) = il;
+      o = pt_off(ij[u].y, ij[u].x, 128);
+      *(__nv_bfloat16*)(sA + o) = rh;
+      *(__nv_bfloat16*)(sAl + o) = rl;
+      o = pt_off(ij[u].y, 128 + ij[u].x, 128);
+      *(__nv_bfloat16*)(sA + o) = ih;
+      *(__nv_bfloat16*)(sAl + o) = il;
+    }
   }
 }
 
@@ -192,6 +208,44 @@ __device__ __forceinline__ void pt_read(uint32_t tmem, int nc, float* y) {
 #pragma unroll
   for (int c = 0; c < PT_NCMAX; c += 16)
     if (c < nc) tc::tmem_ld16(tmem + lane_base + (uint32_t)c, y + c);
+}
+
+// The Taylor sum lives in TMEM columns [PT_ACC, PT_ACC + nc) of the thread's
+// own lane (registers hold only the current term).
+constexpr int PT_ACC = 128;
+constexpr int PT_TMEM_COLS = 256;
+
+__device__ __forceinline__ void pt_tmem_st16(uint32_t taddr, const float* v) {
+  asm volatile(
+      "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16};" ::"r"(
+          taddr),
+      "r"(__float_as_uint(v[0])), "r"(__float_as_uint(v[1])), "r"(__float_as_uint(v[2])), "r"(__float_as_uint(v[3])),
+      "r"(__float_as_uint(v[4])), "r"(__float_as_uint(v[5])), "r"(__float_as_uint(v[6])), "r"(__float_as_uint(v[7])),
+      "r"(__float_as_uint(v[8])), "r"(__float_as_uint(v[9])), "r"(__float_as_uint(v[10])),
+      "r"(__float_as_uint(v[11])), "r"(__float_as_uint(v[12])), "r"(__float_as_uint(v[13])),
+      "r"(__float_as_uint(v[14])), "r"(__float_as_uint(v[15]))
+      : "memory");
+  asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+}
+
+// acc = x (mode 0), acc += x (mode 1), x = acc (mode 2)
+__device__ __forceinline__ void pt_acc(uint32_t tmem, int nc, float* x, int mode) {
+  const uint32_t base = tmem + ((uint32_t)((threadIdx.x >> 5) * 32) << 16) + PT_ACC;
+#pragma unroll
+  for (int c = 0; c < PT_NCMAX; c += 16)
+    if (c < nc) {
+      if (mode == 0) {
+        pt_tmem_st16(base + c, x + c);
+      } else if (mode == 1) {
+        float t[16];
+        tc::tmem_ld16(base + c, t);
+#pragma unroll
+        for (int i = 0; i < 16; ++i) t[i] += x[c + i];
+        pt_tmem_st16(base + c, t);
+      } else {
+        tc::tmem_ld16(base + c, x + c);
+      }
+    }
 }
 
 // y += this thread's row of the product (the identity part of B X = X + (B - I) X)
@@ -227,7 +281,7 @@ __global__ void __launch_bounds__(128, 1)
     tc::mbar_init(bar_mma, 1);
     tc::fence_mbar_init();
   }
-  if (warp == 0) tc::tmem_alloc(tmem_holder, 128);
+  if (warp == 0) tc::tmem_alloc(tmem_holder, PT_TMEM_COLS);
   // B operand: K positions no row of X is written to stay zero
   for (int e = threadIdx.x; e < 2 * PT_B_BYTES / 16; e += blockDim.x) ((uint4*)sB)[e] = make_uint4(0, 0, 0, 0);
   tc::tc_fence_before();
@@ -251,7 +305,7 @@ __global__ void __launch_bounds__(128, 1)
   for (int c0 = col_lo; c0 < col_hi && ok; c0 += PT_NCMAX / 2) {
     const int ncols = min(PT_NCMAX / 2, col_hi - c0);
     const int nc = ((2 * ncols + 15) / 16) * 16;
-    float x[PT_NCMAX], acc[PT_NCMAX];
+    float x[PT_NCMAX];
     __syncthreads();
     pt_issue_image(sA, im, bar_ld);
 #pragma unroll
@@ -269,8 +323,7 @@ __global__ void __launch_bounds__(128, 1)
     // B psi = psi + (B - I) psi
     if (!(ok = pt_product(sA, sB, nc, nsB, tmem, bar_mma, ph_mma, err))) break;
     pt_read_add(tmem, nc, x);
-#pragma unroll
-    for (int c = 0; c < PT_NCMAX; ++c) acc[c] = x[c];
+    pt_acc(tmem, nc, x, 0);  // the Taylor sum starts from B psi
     // Taylor terms with V
     pt_load_V(sA, vre, vim, tri, T);
     for (int k = 1; k <= 5 && ok; ++k) {
@@ -279,25 +332,24 @@ __global__ void __launch_bounds__(128, 1)
       pt_read(tmem, nc, x);
       const float inv = 1.f / (float)k;
 #pragma unroll
-      for (int c = 0; c < PT_NCMAX; ++c) {
-        x[c] *= inv;
-        acc[c] += x[c];
-      }
+      for (int c = 0; c < PT_NCMAX; ++c) x[c] *= inv;
+      pt_acc(tmem, nc, x, 1);
     }
     if (!ok) break;
     // B (sum)
     pt_issue_image(sA, im, bar_ld);
-    if (p < N) pt_store_X(sB, acc, nc, p, !realB);
+    pt_acc(tmem, nc, x, 2);
+    if (p < N) pt_store_X(sB, x, nc, p, !realB);
     if (!(ok = pt_wait(bar_ld, ph_ld, err, 22))) break;
     if (!(ok = pt_product(sA, sB, nc, nsB, tmem, bar_mma, ph_mma, err))) break;
-    pt_read_add(tmem, nc, acc);
+    pt_read_add(tmem, nc, x);
     if (p < N) {
 #pragma unroll
       for (int j = 0; j < PT_NCMAX / 2; ++j)
         if (j < ncols) {
           const size_t o = (size_t)(c0 + j) * N + p;
-          pw[o] = make_double2((double)acc[2 * j], (double)acc[2 * j + 1]);
-          pw32[o] = make_float2(acc[2 * j], acc[2 * j + 1]);
+          pw[o] = make_double2((double)x[2 * j], (double)x[2 * j + 1]);
+          pw32[o] = make_float2(x[2 * j], x[2 * j + 1]);
         }
     }
   }
@@ -305,7 +357,7 @@ __global__ void __launch_bounds__(128, 1)
   __syncthreads();
   if (warp == 0) {
     tc::tc_fence_after();
-    tc::tmem_dealloc(tmem, 128);
+    tc::tmem_dealloc(tmem, PT_TMEM_COLS);
   }
 }
 
