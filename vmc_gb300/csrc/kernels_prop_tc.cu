@@ -21,13 +21,10 @@
 // cp.async.bulk.
 // V comes from the packed lower triangle written by the VHS GEMM and is
 // scattered into A by the CTA.  Thread p (TMEM lane p) owns orbital row p: it
-// reads its row of each product with tcgen05.ld and writes it back as K
-// column p (and 128 + p) of the next B operand.  The additions stay on the
-// tensor core: for a product with B the row of X is stored into the TMEM tile
-// first and the MMAs of B - I accumulate onto it, and every Taylor term's MMAs
-// are issued a second time into the Taylor-sum tile (TMEM columns 128..),
-// with the 1/k of the term applied to X before it is stored; each thread keeps
-// one row in registers.  Seven products per walker: B, five Taylor terms, B.
+// reads its row of each product with tcgen05.ld, keeps its row of the Taylor
+// sum in TMEM (columns 128.., its own lane; the additions are its own, in
+// FP32 round-to-nearest) and writes its row back as K column p (and 128 + p)
+// of the next B operand.  Seven products per walker: B, five Taylor terms, B.
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -112,12 +109,9 @@ __device__ __forceinline__ bool pt_wait(uint64_t* bar, uint32_t& phase, int* err
 constexpr int PT_ACC = 128;        // TMEM column of the Taylor sum (the product tile is at 0)
 constexpr int PT_TMEM_COLS = 256;
 
-// TMEM[128 x nc] (+)= A . B^T over the first ns K-steps of 16, three split
-// passes.  onto: the tile already holds an addend (B X = X + (B - I) X with X
-// stored there first).  dual: the same product is also added to the Taylor sum
-// at column PT_ACC.
+// TMEM[128 x nc] = A . B^T over the first ns K-steps of 16, three split passes.
 __device__ __forceinline__ bool pt_product(uint8_t* sA, uint8_t* sB, int nc, int ns, uint32_t tmem, uint64_t* bar,
-                                           uint32_t& phase, int* err, bool onto, bool dual) {
+                                           uint32_t& phase, int* err) {
   pt_fence_proxy();  // this thread's generic writes to A / B -> visible to the tensor core
   tc::tc_fence_before();
   __syncthreads();
@@ -134,9 +128,8 @@ __device__ __forceinline__ bool pt_product(uint8_t* sA, uint8_t* sB, int nc, int
       for (int s = 0; s < ns; ++s) {
         const uint32_t ao = (uint32_t)((s >> 2) * 128 * 128 + (s & 3) * 32);
         const uint32_t bo = (uint32_t)((s >> 2) * nc * 128 + (s & 3) * 32);
-        const uint64_t ad = tc::sdesc_sw128(a0 + ao), bd = tc::sdesc_sw128(b0 + bo);
-        tc::mma_bf16(tmem, ad, bd, idesc, (onto || pass > 0 || s > 0) ? 1u : 0u);
-        if (dual) tc::mma_bf16(tmem + PT_ACC, ad, bd, idesc, 1u);
+        tc::mma_bf16(tmem, tc::sdesc_sw128(a0 + ao), tc::sdesc_sw128(b0 + bo), idesc,
+                     (pass > 0 || s > 0) ? 1u : 0u);
       }
     }
     tc::mma_commit(bar);
@@ -213,7 +206,7 @@ __device__ __forceinline__ void pt_load_V(uint8_t* sA, const float* __restrict__
   }
 }
 
-// 80 columns (5 x 16) of this thread's TMEM lane from taddr, one wait for all
+// this thread's TMEM lane, 80 / 48 / 32 columns from taddr, one wait per call
 __device__ __forceinline__ void pt_tmem_ld80(uint32_t taddr, float* v) {
   uint32_t u[80];
   asm volatile(
@@ -224,16 +217,44 @@ __device__ __forceinline__ void pt_tmem_ld80(uint32_t taddr, float* v) {
       "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%64,%65,%66,%67,%68,%69,%70,%71,%72,%73,%74,%75,%76,%77,%78,%79}, [%84];\n"
       "tcgen05.wait::ld.sync.aligned;\n"
       : "=r"(u[0]), "=r"(u[1]), "=r"(u[2]), "=r"(u[3]), "=r"(u[4]), "=r"(u[5]), "=r"(u[6]), "=r"(u[7]), "=r"(u[8]), "=r"(u[9]), "=r"(u[10]), "=r"(u[11]), "=r"(u[12]), "=r"(u[13]), "=r"(u[14]), "=r"(u[15]), "=r"(u[16]), "=r"(u[17]), "=r"(u[18]), "=r"(u[19]), "=r"(u[20]), "=r"(u[21]), "=r"(u[22]), "=r"(u[23]), "=r"(u[24]), "=r"(u[25]), "=r"(u[26]), "=r"(u[27]), "=r"(u[28]), "=r"(u[29]), "=r"(u[30]), "=r"(u[31]), "=r"(u[32]), "=r"(u[33]), "=r"(u[34]), "=r"(u[35]), "=r"(u[36]), "=r"(u[37]), "=r"(u[38]), "=r"(u[39]), "=r"(u[40]), "=r"(u[41]), "=r"(u[42]), "=r"(u[43]), "=r"(u[44]), "=r"(u[45]), "=r"(u[46]), "=r"(u[47]), "=r"(u[48]), "=r"(u[49]), "=r"(u[50]), "=r"(u[51]), "=r"(u[52]), "=r"(u[53]), "=r"(u[54]), "=r"(u[55]), "=r"(u[56]), "=r"(u[57]), "=r"(u[58]), "=r"(u[59]), "=r"(u[60]), "=r"(u[61]), "=r"(u[62]), "=r"(u[63]), "=r"(u[64]), "=r"(u[65]), "=r"(u[66]), "=r"(u[67]), "=r"(u[68]), "=r"(u[69]), "=r"(u[70]), "=r"(u[71]), "=r"(u[72]), "=r"(u[73]), "=r"(u[74]), "=r"(u[75]), "=r"(u[76]), "=r"(u[77]), "=r"(u[78]), "=r"(u[79])
-      : "r"(taddr), "r"(taddr + 16), "r"(taddr + 32), "r"(taddr + 48), "r"(taddr + 64)
+      : "r"(taddr + 0), "r"(taddr + 16), "r"(taddr + 32), "r"(taddr + 48), "r"(taddr + 64)
       : "memory");
 #pragma unroll
   for (int i = 0; i < 80; ++i) v[i] = __uint_as_float(u[i]);
 }
 
-// 80 columns to this thread's TMEM lane at taddr, one wait for all
-__device__ __forceinline__ void pt_tmem_st80(uint32_t taddr, const float* v) {
+__device__ __forceinline__ void pt_tmem_ld48(uint32_t taddr, float* v) {
+  uint32_t u[48];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%48];\n"
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%49];\n"
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%32,%33,%34,%35,%36,%37,%38,%39,%40,%41,%42,%43,%44,%45,%46,%47}, [%50];\n"
+      "tcgen05.wait::ld.sync.aligned;\n"
+      : "=r"(u[0]), "=r"(u[1]), "=r"(u[2]), "=r"(u[3]), "=r"(u[4]), "=r"(u[5]), "=r"(u[6]), "=r"(u[7]), "=r"(u[8]), "=r"(u[9]), "=r"(u[10]), "=r"(u[11]), "=r"(u[12]), "=r"(u[13]), "=r"(u[14]), "=r"(u[15]), "=r"(u[16]), "=r"(u[17]), "=r"(u[18]), "=r"(u[19]), "=r"(u[20]), "=r"(u[21]), "=r"(u[22]), "=r"(u[23]), "=r"(u[24]), "=r"(u[25]), "=r"(u[26]), "=r"(u[27]), "=r"(u[28]), "=r"(u[29]), "=r"(u[30]), "=r"(u[31]), "=r"(u[32]), "=r"(u[33]), "=r"(u[34]), "=r"(u[35]), "=r"(u[36]), "=r"(u[37]), "=r"(u[38]), "=r"(u[39]), "=r"(u[40]), "=r"(u[41]), "=r"(u[42]), "=r"(u[43]), "=r"(u[44]), "=r"(u[45]), "=r"(u[46]), "=r"(u[47])
+      : "r"(taddr + 0), "r"(taddr + 16), "r"(taddr + 32)
+      : "memory");
 #pragma unroll
-  for (int k = 0; k < 5; ++k) {
+  for (int i = 0; i < 48; ++i) v[i] = __uint_as_float(u[i]);
+}
+
+__device__ __forceinline__ void pt_tmem_ld32(uint32_t taddr, float* v) {
+  uint32_t u[32];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%32];\n"
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%33];\n"
+      "tcgen05.wait::ld.sync.aligned;\n"
+      : "=r"(u[0]), "=r"(u[1]), "=r"(u[2]), "=r"(u[3]), "=r"(u[4]), "=r"(u[5]), "=r"(u[6]), "=r"(u[7]), "=r"(u[8]), "=r"(u[9]), "=r"(u[10]), "=r"(u[11]), "=r"(u[12]), "=r"(u[13]), "=r"(u[14]), "=r"(u[15]), "=r"(u[16]), "=r"(u[17]), "=r"(u[18]), "=r"(u[19]), "=r"(u[20]), "=r"(u[21]), "=r"(u[22]), "=r"(u[23]), "=r"(u[24]), "=r"(u[25]), "=r"(u[26]), "=r"(u[27]), "=r"(u[28]), "=r"(u[29]), "=r"(u[30]), "=r"(u[31])
+      : "r"(taddr + 0), "r"(taddr + 16)
+      : "memory");
+#pragma unroll
+  for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(u[i]);
+}
+
+// NCH x 16 columns to this thread's TMEM lane at taddr, one wait
+template <int NCH>
+__device__ __forceinline__ void pt_tmem_st(uint32_t taddr, const float* v) {
+#pragma unroll
+  for (int k = 0; k < NCH; ++k) {
     const float* w = v + 16 * k;
     asm volatile(
         "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16};" ::"r"(
@@ -248,12 +269,39 @@ __device__ __forceinline__ void pt_tmem_st80(uint32_t taddr, const float* v) {
   asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
 }
 
-static_assert(PT_NCMAX == 80, "the TMEM row helpers move 80 columns");
+static_assert(PT_NCMAX == 80, "the TMEM row helpers move 80 columns (48 + 32)");
 
-// Row traffic to TMEM moves all PT_NCMAX columns in one batch with one wait;
-// columns >= nc carry values that only ever feed padding columns.
+// Row traffic to TMEM moves all PT_NCMAX columns in batches with one wait each;
+// columns >= nc carry values that only ever feed padding columns.  Additions
+// are made by the threads (round to nearest): the tensor core's accumulation
+// of small products onto a stored O(1) value was measured to shrink it
+// systematically, which biased every walker's overlap.
 __device__ __forceinline__ uint32_t pt_lane(uint32_t tmem) {
   return tmem + ((uint32_t)((threadIdx.x >> 5) * 32) << 16);
+}
+
+// y += the row at taddr (48 + 32 columns, so one extra half row is live)
+__device__ __forceinline__ void pt_add_row(uint32_t taddr, float* y) {
+  float t[48];
+  pt_tmem_ld48(taddr, t);
+#pragma unroll
+  for (int i = 0; i < 48; ++i) y[i] += t[i];
+  pt_tmem_ld32(taddr + 48, t);
+#pragma unroll
+  for (int i = 0; i < 32; ++i) y[48 + i] += t[i];
+}
+
+// row at taddr += x (48 + 32 columns)
+__device__ __forceinline__ void pt_acc_add(uint32_t taddr, const float* x) {
+  float t[48];
+  pt_tmem_ld48(taddr, t);
+#pragma unroll
+  for (int i = 0; i < 48; ++i) t[i] += x[i];
+  pt_tmem_st<3>(taddr, t);
+  pt_tmem_ld32(taddr + 48, t);
+#pragma unroll
+  for (int i = 0; i < 32; ++i) t[i] += x[48 + i];
+  pt_tmem_st<2>(taddr + 48, t);
 }
 
 __global__ void __launch_bounds__(128, 1)
@@ -313,32 +361,31 @@ __global__ void __launch_bounds__(128, 1)
       x[2 * j] = v.x;
       x[2 * j + 1] = v.y;
     }
-    // B psi = psi + (B - I) psi, psi stored into the product tile first
-    pt_tmem_st80(pt_lane(tmem), x);
     if (p < N) pt_store_X(sB, x, nc, p, !realB);
     if (!(ok = pt_wait(bar_ld, ph_ld, err, 22))) break;
-    if (!(ok = pt_product(sA, sB, nc, nsB, tmem, bar_mma, ph_mma, err, true, false))) break;
-    pt_tmem_ld80(pt_lane(tmem), x);
-    pt_tmem_st80(pt_lane(tmem) + PT_ACC, x);  // the Taylor sum starts from B psi
-    // Taylor terms: term_k = V (term_{k-1} / k), added to the sum by the tensor core
+    // B psi = psi + (B - I) psi
+    if (!(ok = pt_product(sA, sB, nc, nsB, tmem, bar_mma, ph_mma, err))) break;
+    pt_add_row(pt_lane(tmem), x);
+    pt_tmem_st<5>(pt_lane(tmem) + PT_ACC, x);  // the Taylor sum starts from B psi
+    // Taylor terms with V: term_k = V term_{k-1} / k, added to the sum in TMEM
     pt_load_V(sA, vre, vim, tri, T);
     for (int k = 1; k <= 5 && ok; ++k) {
+      if (p < N) pt_store_X(sB, x, nc, p, true);
+      if (!(ok = pt_product(sA, sB, nc, 16, tmem, bar_mma, ph_mma, err))) break;
+      pt_tmem_ld80(pt_lane(tmem), x);
       const float inv = 1.f / (float)k;
 #pragma unroll
       for (int c = 0; c < PT_NCMAX; ++c) x[c] *= inv;
-      if (p < N) pt_store_X(sB, x, nc, p, true);
-      if (!(ok = pt_product(sA, sB, nc, 16, tmem, bar_mma, ph_mma, err, false, true))) break;
-      if (k < 5) pt_tmem_ld80(pt_lane(tmem), x);
+      pt_acc_add(pt_lane(tmem) + PT_ACC, x);
     }
     if (!ok) break;
     // B (sum) = sum + (B - I) sum
     pt_issue_image(sA, im, bar_ld);
     pt_tmem_ld80(pt_lane(tmem) + PT_ACC, x);
-    pt_tmem_st80(pt_lane(tmem), x);
     if (p < N) pt_store_X(sB, x, nc, p, !realB);
     if (!(ok = pt_wait(bar_ld, ph_ld, err, 22))) break;
-    if (!(ok = pt_product(sA, sB, nc, nsB, tmem, bar_mma, ph_mma, err, true, false))) break;
-    pt_tmem_ld80(pt_lane(tmem), x);
+    if (!(ok = pt_product(sA, sB, nc, nsB, tmem, bar_mma, ph_mma, err))) break;
+    pt_add_row(pt_lane(tmem), x);
     if (p < N) {
 #pragma unroll
       for (int j = 0; j < PT_NCMAX / 2; ++j)
