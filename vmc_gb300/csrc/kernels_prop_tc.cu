@@ -1,6 +1,6 @@
 // Tensor-core (tcgen05) propagator of the mixed form:
 //     psi <- B (sum_{k=0}^{5} V^k / k!) B psi          (DQMCWalker.cpp:424-431, :482-491)
-// for N <= 128.  One CTA (4 warps) per walker and V block.  Every complex
+// for N <= 128.  One CTA (16 warps) per walker and V block.  Every complex
 // product M X is one real GEMM
 //     [Re MX | Im MX] = [Mr | Mi] . [[Xr, Xi], [-Xi, Xr]]
 // with K = 256: K columns [0, N) carry the real part of M, [128, 128 + N) the
@@ -20,11 +20,14 @@
 // B - I is built once per handle in global memory and copied in with
 // cp.async.bulk.
 // V comes from the packed lower triangle written by the VHS GEMM and is
-// scattered into A by the CTA.  Thread p (TMEM lane p) owns orbital row p: it
-// reads its row of each product with tcgen05.ld, keeps its row of the Taylor
-// sum in TMEM (columns 128.., its own lane; the additions are its own, in
-// FP32 round-to-nearest) and writes its row back as K column p (and 128 + p)
-// of the next B operand.  Seven products per walker: B, five Taylor terms, B.
+// scattered into A by the CTA.  Thread (p, g) owns 20 columns (group g of 4)
+// of orbital row p = TMEM lane p: it reads them from each product with
+// tcgen05.ld, keeps them of the Taylor sum in TMEM (columns 128.., its own
+// lane; the additions are its own, in FP32 round-to-nearest) and writes them
+// back as K column p (and 128 + p) of the next B operand.  Four warps share
+// each TMEM lane quadrant, so one 214 KB CTA per SM still keeps four warps per
+// scheduler to hide the load and barrier latencies.  Seven products per walker:
+// B, five Taylor terms, B.
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -39,6 +42,9 @@ namespace afqmc {
 constexpr int PT_K = 256;                          // K: real block [0, 128), imaginary block [128, 256)
 constexpr int PT_A_BYTES = 128 * PT_K * 2;         // one BF16 half of A
 constexpr int PT_NCMAX = 80;                       // max B rows (2 x 40 columns) per pass
+constexpr int PT_NG = 4;                           // column groups: 4 warps per TMEM lane quadrant
+constexpr int PT_CW = PT_NCMAX / PT_NG;            // B rows (product columns) per thread
+constexpr int PT_THREADS = 128 * PT_NG;
 constexpr int PT_B_BYTES = PT_NCMAX * PT_K * 2;    // one BF16 half of B
 constexpr int PT_SMEM = 2 * PT_A_BYTES + 2 * PT_B_BYTES + 64 + 1024;
 constexpr int PT_IMG = 128 * PT_K;                 // BF16 elements of one half of the B image
@@ -139,16 +145,18 @@ __device__ __forceinline__ bool pt_product(uint8_t* sA, uint8_t* sB, int nc, int
   return ok;
 }
 
-// Row p of X (x[2j] = Re X(p, j), x[2j+1] = Im X(p, j)) into K column p (and
-// 128 + p when `both`) of the B operand rows (j, re) and (j, im), split in BF16.
-__device__ __forceinline__ void pt_store_X(uint8_t* sB, const float* x, int nc, int p, bool both) {
+// This thread's part of row p of X (x[2jj] = Re X(p, j), x[2jj+1] = Im X(p, j)
+// for the columns j of group g) into K column p (and 128 + p when `both`) of
+// the B operand rows (j, re) and (j, im), split in BF16.
+__device__ __forceinline__ void pt_store_X(uint8_t* sB, const float* x, int nc, int p, bool both, int g) {
   uint8_t* sBl = sB + PT_B_BYTES;
 #pragma unroll
-  for (int j2 = 0; j2 < PT_NCMAX; j2 += 2) {
+  for (int jj = 0; jj < PT_CW; jj += 2) {
+    const int j2 = g * PT_CW + jj;
     if (j2 < nc) {
       __nv_bfloat16 rh, rl, ih, il;
-      pt_split(x[j2], rh, rl);
-      pt_split(x[j2 + 1], ih, il);
+      pt_split(x[jj], rh, rl);
+      pt_split(x[jj + 1], ih, il);
       const uint32_t o0 = pt_off(j2, p, nc), o1 = pt_off(j2 + 1, p, nc);
       *(__nv_bfloat16*)(sB + o0) = rh;
       *(__nv_bfloat16*)(sBl + o0) = rl;
@@ -206,105 +214,59 @@ __device__ __forceinline__ void pt_load_V(uint8_t* sA, const float* __restrict__
   }
 }
 
-// this thread's TMEM lane, 80 / 48 / 32 columns from taddr, one wait per call
-__device__ __forceinline__ void pt_tmem_ld80(uint32_t taddr, float* v) {
-  uint32_t u[80];
+// PT_CW = 20 columns of this thread's TMEM lane from taddr (x16 + x4), one wait
+__device__ __forceinline__ void pt_tmem_ld(uint32_t taddr, float* v) {
+  uint32_t u[PT_CW];
   asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%80];\n"
-      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%81];\n"
-      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%32,%33,%34,%35,%36,%37,%38,%39,%40,%41,%42,%43,%44,%45,%46,%47}, [%82];\n"
-      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%48,%49,%50,%51,%52,%53,%54,%55,%56,%57,%58,%59,%60,%61,%62,%63}, [%83];\n"
-      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%64,%65,%66,%67,%68,%69,%70,%71,%72,%73,%74,%75,%76,%77,%78,%79}, [%84];\n"
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%20];\n"
+      "tcgen05.ld.sync.aligned.32x32b.x4.b32 {%16,%17,%18,%19}, [%21];\n"
       "tcgen05.wait::ld.sync.aligned;\n"
-      : "=r"(u[0]), "=r"(u[1]), "=r"(u[2]), "=r"(u[3]), "=r"(u[4]), "=r"(u[5]), "=r"(u[6]), "=r"(u[7]), "=r"(u[8]), "=r"(u[9]), "=r"(u[10]), "=r"(u[11]), "=r"(u[12]), "=r"(u[13]), "=r"(u[14]), "=r"(u[15]), "=r"(u[16]), "=r"(u[17]), "=r"(u[18]), "=r"(u[19]), "=r"(u[20]), "=r"(u[21]), "=r"(u[22]), "=r"(u[23]), "=r"(u[24]), "=r"(u[25]), "=r"(u[26]), "=r"(u[27]), "=r"(u[28]), "=r"(u[29]), "=r"(u[30]), "=r"(u[31]), "=r"(u[32]), "=r"(u[33]), "=r"(u[34]), "=r"(u[35]), "=r"(u[36]), "=r"(u[37]), "=r"(u[38]), "=r"(u[39]), "=r"(u[40]), "=r"(u[41]), "=r"(u[42]), "=r"(u[43]), "=r"(u[44]), "=r"(u[45]), "=r"(u[46]), "=r"(u[47]), "=r"(u[48]), "=r"(u[49]), "=r"(u[50]), "=r"(u[51]), "=r"(u[52]), "=r"(u[53]), "=r"(u[54]), "=r"(u[55]), "=r"(u[56]), "=r"(u[57]), "=r"(u[58]), "=r"(u[59]), "=r"(u[60]), "=r"(u[61]), "=r"(u[62]), "=r"(u[63]), "=r"(u[64]), "=r"(u[65]), "=r"(u[66]), "=r"(u[67]), "=r"(u[68]), "=r"(u[69]), "=r"(u[70]), "=r"(u[71]), "=r"(u[72]), "=r"(u[73]), "=r"(u[74]), "=r"(u[75]), "=r"(u[76]), "=r"(u[77]), "=r"(u[78]), "=r"(u[79])
-      : "r"(taddr + 0), "r"(taddr + 16), "r"(taddr + 32), "r"(taddr + 48), "r"(taddr + 64)
+      : "=r"(u[0]), "=r"(u[1]), "=r"(u[2]), "=r"(u[3]), "=r"(u[4]), "=r"(u[5]), "=r"(u[6]), "=r"(u[7]), "=r"(u[8]), "=r"(u[9]), "=r"(u[10]), "=r"(u[11]), "=r"(u[12]), "=r"(u[13]), "=r"(u[14]), "=r"(u[15]), "=r"(u[16]), "=r"(u[17]), "=r"(u[18]), "=r"(u[19])
+      : "r"(taddr), "r"(taddr + 16)
       : "memory");
 #pragma unroll
-  for (int i = 0; i < 80; ++i) v[i] = __uint_as_float(u[i]);
+  for (int i = 0; i < PT_CW; ++i) v[i] = __uint_as_float(u[i]);
 }
 
-__device__ __forceinline__ void pt_tmem_ld48(uint32_t taddr, float* v) {
-  uint32_t u[48];
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%48];\n"
-      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%49];\n"
-      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%32,%33,%34,%35,%36,%37,%38,%39,%40,%41,%42,%43,%44,%45,%46,%47}, [%50];\n"
-      "tcgen05.wait::ld.sync.aligned;\n"
-      : "=r"(u[0]), "=r"(u[1]), "=r"(u[2]), "=r"(u[3]), "=r"(u[4]), "=r"(u[5]), "=r"(u[6]), "=r"(u[7]), "=r"(u[8]), "=r"(u[9]), "=r"(u[10]), "=r"(u[11]), "=r"(u[12]), "=r"(u[13]), "=r"(u[14]), "=r"(u[15]), "=r"(u[16]), "=r"(u[17]), "=r"(u[18]), "=r"(u[19]), "=r"(u[20]), "=r"(u[21]), "=r"(u[22]), "=r"(u[23]), "=r"(u[24]), "=r"(u[25]), "=r"(u[26]), "=r"(u[27]), "=r"(u[28]), "=r"(u[29]), "=r"(u[30]), "=r"(u[31]), "=r"(u[32]), "=r"(u[33]), "=r"(u[34]), "=r"(u[35]), "=r"(u[36]), "=r"(u[37]), "=r"(u[38]), "=r"(u[39]), "=r"(u[40]), "=r"(u[41]), "=r"(u[42]), "=r"(u[43]), "=r"(u[44]), "=r"(u[45]), "=r"(u[46]), "=r"(u[47])
-      : "r"(taddr + 0), "r"(taddr + 16), "r"(taddr + 32)
-      : "memory");
-#pragma unroll
-  for (int i = 0; i < 48; ++i) v[i] = __uint_as_float(u[i]);
-}
-
-__device__ __forceinline__ void pt_tmem_ld32(uint32_t taddr, float* v) {
-  uint32_t u[32];
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%32];\n"
-      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%33];\n"
-      "tcgen05.wait::ld.sync.aligned;\n"
-      : "=r"(u[0]), "=r"(u[1]), "=r"(u[2]), "=r"(u[3]), "=r"(u[4]), "=r"(u[5]), "=r"(u[6]), "=r"(u[7]), "=r"(u[8]), "=r"(u[9]), "=r"(u[10]), "=r"(u[11]), "=r"(u[12]), "=r"(u[13]), "=r"(u[14]), "=r"(u[15]), "=r"(u[16]), "=r"(u[17]), "=r"(u[18]), "=r"(u[19]), "=r"(u[20]), "=r"(u[21]), "=r"(u[22]), "=r"(u[23]), "=r"(u[24]), "=r"(u[25]), "=r"(u[26]), "=r"(u[27]), "=r"(u[28]), "=r"(u[29]), "=r"(u[30]), "=r"(u[31])
-      : "r"(taddr + 0), "r"(taddr + 16)
-      : "memory");
-#pragma unroll
-  for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(u[i]);
-}
-
-// NCH x 16 columns to this thread's TMEM lane at taddr, one wait
-template <int NCH>
+// PT_CW = 20 columns to this thread's TMEM lane at taddr, one wait
 __device__ __forceinline__ void pt_tmem_st(uint32_t taddr, const float* v) {
-#pragma unroll
-  for (int k = 0; k < NCH; ++k) {
-    const float* w = v + 16 * k;
-    asm volatile(
-        "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16};" ::"r"(
-            taddr + 16 * k),
-        "r"(__float_as_uint(w[0])), "r"(__float_as_uint(w[1])), "r"(__float_as_uint(w[2])), "r"(__float_as_uint(w[3])),
-        "r"(__float_as_uint(w[4])), "r"(__float_as_uint(w[5])), "r"(__float_as_uint(w[6])), "r"(__float_as_uint(w[7])),
-        "r"(__float_as_uint(w[8])), "r"(__float_as_uint(w[9])), "r"(__float_as_uint(w[10])),
-        "r"(__float_as_uint(w[11])), "r"(__float_as_uint(w[12])), "r"(__float_as_uint(w[13])),
-        "r"(__float_as_uint(w[14])), "r"(__float_as_uint(w[15]))
-        : "memory");
-  }
-  asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+  asm volatile(
+      "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17};\n"
+      "tcgen05.st.sync.aligned.32x32b.x4.b32 [%1], {%18,%19,%20,%21};\n"
+      "tcgen05.wait::st.sync.aligned;\n" ::"r"(taddr),
+      "r"(taddr + 16), "r"(__float_as_uint(v[0])), "r"(__float_as_uint(v[1])), "r"(__float_as_uint(v[2])),
+      "r"(__float_as_uint(v[3])), "r"(__float_as_uint(v[4])), "r"(__float_as_uint(v[5])), "r"(__float_as_uint(v[6])),
+      "r"(__float_as_uint(v[7])), "r"(__float_as_uint(v[8])), "r"(__float_as_uint(v[9])),
+      "r"(__float_as_uint(v[10])), "r"(__float_as_uint(v[11])), "r"(__float_as_uint(v[12])),
+      "r"(__float_as_uint(v[13])), "r"(__float_as_uint(v[14])), "r"(__float_as_uint(v[15])),
+      "r"(__float_as_uint(v[16])), "r"(__float_as_uint(v[17])), "r"(__float_as_uint(v[18])),
+      "r"(__float_as_uint(v[19]))
+      : "memory");
 }
 
-static_assert(PT_NCMAX == 80, "the TMEM row helpers move 80 columns (48 + 32)");
+static_assert(PT_CW == 20 && PT_NG * PT_CW == PT_NCMAX, "the TMEM row helpers move 20 columns (x16 + x4)");
 
-// Row traffic to TMEM moves all PT_NCMAX columns in batches with one wait each;
-// columns >= nc carry values that only ever feed padding columns.  Additions
-// are made by the threads (round to nearest): the tensor core's accumulation
-// of small products onto a stored O(1) value was measured to shrink it
-// systematically, which biased every walker's overlap.
-__device__ __forceinline__ uint32_t pt_lane(uint32_t tmem) {
-  return tmem + ((uint32_t)((threadIdx.x >> 5) * 32) << 16);
-}
-
-// y += the row at taddr (48 + 32 columns, so one extra half row is live)
+// Additions are made by the threads (round to nearest): the tensor core's
+// accumulation of small products onto a stored O(1) value was measured to
+// shrink it systematically, which biased every walker's overlap.
+// y += the 20 columns at taddr
 __device__ __forceinline__ void pt_add_row(uint32_t taddr, float* y) {
-  float t[48];
-  pt_tmem_ld48(taddr, t);
+  float t[PT_CW];
+  pt_tmem_ld(taddr, t);
 #pragma unroll
-  for (int i = 0; i < 48; ++i) y[i] += t[i];
-  pt_tmem_ld32(taddr + 48, t);
-#pragma unroll
-  for (int i = 0; i < 32; ++i) y[48 + i] += t[i];
+  for (int i = 0; i < PT_CW; ++i) y[i] += t[i];
 }
 
-// row at taddr += x (48 + 32 columns)
+// the 20 columns at taddr += x
 __device__ __forceinline__ void pt_acc_add(uint32_t taddr, const float* x) {
-  float t[48];
-  pt_tmem_ld48(taddr, t);
+  float t[PT_CW];
+  pt_tmem_ld(taddr, t);
 #pragma unroll
-  for (int i = 0; i < 48; ++i) t[i] += x[i];
-  pt_tmem_st<3>(taddr, t);
-  pt_tmem_ld32(taddr + 48, t);
-#pragma unroll
-  for (int i = 0; i < 32; ++i) t[i] += x[48 + i];
-  pt_tmem_st<2>(taddr + 48, t);
+  for (int i = 0; i < PT_CW; ++i) t[i] += x[i];
+  pt_tmem_st(taddr, t);
 }
 
-__global__ void __launch_bounds__(128, 1)
+__global__ void __launch_bounds__(PT_THREADS, 1)
     k_prop_tc(double2* __restrict__ psi, float2* __restrict__ psi32, const float* __restrict__ Vp,
               const __nv_bfloat16* __restrict__ img, const int2* __restrict__ tri,
               const double* __restrict__ weights, int N, int ncw, int na, int nspV, int realB, int* err) {
@@ -318,7 +280,7 @@ __global__ void __launch_bounds__(128, 1)
   uint64_t* bar_ld = (uint64_t*)(sB + 2 * PT_B_BYTES);
   uint64_t* bar_mma = bar_ld + 1;
   uint32_t* tmem_holder = (uint32_t*)(bar_mma + 1);
-  const int warp = threadIdx.x >> 5;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (threadIdx.x == 0) {
     tc::mbar_init(bar_ld, 1);
     tc::mbar_init(bar_mma, 1);
@@ -334,13 +296,20 @@ __global__ void __launch_bounds__(128, 1)
   uint32_t ph_ld = 0, ph_mma = 0;
   bool ok = true;
 
+  // thread = (orbital row p = TMEM lane, column group g): warp w reaches lanes
+  // 32 (w % 4) .. + 31, and the warps with the same w % 4 split the columns
+  const int p = ((warp & 3) << 5) | lane;
+  const int g = warp >> 2;
+  const uint32_t trow = tmem + ((uint32_t)((warp & 3) * 32) << 16);
+  const uint32_t tcol = trow + (uint32_t)(g * PT_CW);            // product columns of this thread
+  const uint32_t tacc = trow + (uint32_t)(PT_ACC + g * PT_CW);   // Taylor-sum columns of this thread
+
   const int T = N * (N + 1) / 2;
   const float* vre = Vp + ((size_t)(w * nspV + sp) * 2) * T;
   const float* vim = vre + T;
   const __nv_bfloat16* im = img + (size_t)sp * 2 * PT_IMG;
   const int col_lo = nspV == 1 ? 0 : (sp == 0 ? 0 : na);
   const int col_hi = nspV == 1 ? ncw : (sp == 0 ? na : ncw);
-  const int p = threadIdx.x;
   const int nsB = realB ? 8 : 16;  // K-steps of a product with B (imaginary block all zero when real)
   double2* pw = psi + (size_t)w * ncw * N;
   float2* pw32 = psi32 + (size_t)w * ncw * N;
@@ -348,52 +317,55 @@ __global__ void __launch_bounds__(128, 1)
   for (int c0 = col_lo; c0 < col_hi && ok; c0 += PT_NCMAX / 2) {
     const int ncols = min(PT_NCMAX / 2, col_hi - c0);
     const int nc = ((2 * ncols + 15) / 16) * 16;
-    float x[PT_NCMAX];
+    float x[PT_CW];
     __syncthreads();
     pt_issue_image(sA, im, bar_ld);
 #pragma unroll
-    for (int j = 0; j < PT_NCMAX / 2; ++j) {
+    for (int jj = 0; jj < PT_CW / 2; ++jj) {
+      const int j = g * (PT_CW / 2) + jj;
       float2 v = make_float2(0.f, 0.f);
       if (j < ncols && p < N) {
         const double2 d = pw[(size_t)(c0 + j) * N + p];
         v = make_float2((float)d.x, (float)d.y);
       }
-      x[2 * j] = v.x;
-      x[2 * j + 1] = v.y;
+      x[2 * jj] = v.x;
+      x[2 * jj + 1] = v.y;
     }
-    if (p < N) pt_store_X(sB, x, nc, p, !realB);
+    if (p < N) pt_store_X(sB, x, nc, p, !realB, g);
     if (!(ok = pt_wait(bar_ld, ph_ld, err, 22))) break;
     // B psi = psi + (B - I) psi
     if (!(ok = pt_product(sA, sB, nc, nsB, tmem, bar_mma, ph_mma, err))) break;
-    pt_add_row(pt_lane(tmem), x);
-    pt_tmem_st<5>(pt_lane(tmem) + PT_ACC, x);  // the Taylor sum starts from B psi
+    pt_add_row(tcol, x);
+    pt_tmem_st(tacc, x);  // the Taylor sum starts from B psi
     // Taylor terms with V: term_k = V term_{k-1} / k, added to the sum in TMEM
     pt_load_V(sA, vre, vim, tri, T);
     for (int k = 1; k <= 5 && ok; ++k) {
-      if (p < N) pt_store_X(sB, x, nc, p, true);
+      if (p < N) pt_store_X(sB, x, nc, p, true, g);
       if (!(ok = pt_product(sA, sB, nc, 16, tmem, bar_mma, ph_mma, err))) break;
-      pt_tmem_ld80(pt_lane(tmem), x);
+      pt_tmem_ld(tcol, x);
       const float inv = 1.f / (float)k;
 #pragma unroll
-      for (int c = 0; c < PT_NCMAX; ++c) x[c] *= inv;
-      pt_acc_add(pt_lane(tmem) + PT_ACC, x);
+      for (int c = 0; c < PT_CW; ++c) x[c] *= inv;
+      pt_acc_add(tacc, x);
     }
     if (!ok) break;
     // B (sum) = sum + (B - I) sum
     pt_issue_image(sA, im, bar_ld);
-    pt_tmem_ld80(pt_lane(tmem) + PT_ACC, x);
-    if (p < N) pt_store_X(sB, x, nc, p, !realB);
+    pt_tmem_ld(tacc, x);
+    if (p < N) pt_store_X(sB, x, nc, p, !realB, g);
     if (!(ok = pt_wait(bar_ld, ph_ld, err, 22))) break;
     if (!(ok = pt_product(sA, sB, nc, nsB, tmem, bar_mma, ph_mma, err))) break;
-    pt_add_row(pt_lane(tmem), x);
+    pt_add_row(tcol, x);
     if (p < N) {
 #pragma unroll
-      for (int j = 0; j < PT_NCMAX / 2; ++j)
+      for (int jj = 0; jj < PT_CW / 2; ++jj) {
+        const int j = g * (PT_CW / 2) + jj;
         if (j < ncols) {
           const size_t o = (size_t)(c0 + j) * N + p;
-          pw[o] = make_double2((double)x[2 * j], (double)x[2 * j + 1]);
-          pw32[o] = make_float2(x[2 * j], x[2 * j + 1]);
+          pw[o] = make_double2((double)x[2 * jj], (double)x[2 * jj + 1]);
+          pw32[o] = make_float2(x[2 * jj], x[2 * jj + 1]);
         }
+      }
     }
   }
   tc::tc_fence_before();
@@ -420,7 +392,7 @@ void launch_propagate_tc(afqmc_handle* h) {
     attr = true;
   }
   dim3 grid(h->nwalk, h->nspV);
-  k_prop_tc<<<grid, 128, PT_SMEM, h->stream>>>(h->psi, h->psi32, h->V32, h->pt_img, h->tri, h->weights, h->N,
+  k_prop_tc<<<grid, PT_THREADS, PT_SMEM, h->stream>>>(h->psi, h->psi32, h->V32, h->pt_img, h->tri, h->weights, h->N,
                                                h->ncw, h->na, h->nspV, h->real_expm ? 1 : 0, h->d_err);
   h->launches++;
 }
