@@ -18,9 +18,10 @@
 // solves then run as before (DQMC/RHF.cpp:52-64, DQMC/UHF.cpp:57-68 for the
 // overlap; the force-bias theta of :71-91), reading M.
 //
-// The slices are cut with integer arithmetic from the bits of each double:
-// the FP64 pipe of this GPU is its scarce unit, and cutting seven slices with
-// FP64 rint / multiply costs more than the FP64 product it replaces.
+// The slices are cut with 32-bit integer arithmetic from the bits of each
+// double: the FP64 pipe of this GPU is its scarce unit (64-bit integer work
+// runs there too), and cutting seven slices with FP64 rint / multiply costs
+// more than the FP64 product it replaces.
 //
 // k_ovl_slice writes the slices of psi as a BF16 operand [rows][7 x KP], one
 // block of rows per channel (row = (walker, channel column, re / im), each
@@ -49,32 +50,56 @@ constexpr int OZ_STAGES = 3;   // A-tile ring
 constexpr int OZ_TILE = 128 * 64 * 2;  // one 128 x 64 BF16 A tile
 
 // Slices of x for the row scale sigma = 2^e (|x| < sigma), from the bits of x
-// with integer arithmetic only: T = x 2^(55 - e) as a fixed-point integer
-// (|T| < 2^55; bits of x below 2^(e - 55) are dropped, ~2^-55 sigma), then
-// balanced base-256 digits T = sum_s a_s 2^(8 (6 - s)) with a_1..a_6 in
-// [-128, 127] and |a_0| <= 128, so x = sigma 2^-7 sum_s a_s 2^-8s.  Zero and
-// subnormal x give zero slices.
+// with 32-bit integer arithmetic only (on this GPU 64-bit integer and FP64
+// work share the small FP64 pipe): T = x 2^(55 - e) as a fixed-point integer
+// (|T| < 2^55; bits of x below 2^(e - 55) are dropped, ~2^-55 sigma), held as
+// two's-complement words (hi, lo), then balanced base-256 digits: with
+// U = T + 128, d = (U & 255) - 128 and T <- U >> 8 (the low byte of U - 128 - d
+// is zero), giving T = sum_s a_s 2^(8 (6 - s)) with a_1..a_6 in [-128, 127] and
+// |a_0| <= 128, so x = sigma 2^-7 sum_s a_s 2^-8s.  Zero and subnormal x give
+// zero slices.
 __device__ __forceinline__ void oz_slices_bits(double x, int e, float* a) {
-  const long long bits = __double_as_longlong(x);
-  const int biased = (int)((bits >> 52) & 0x7FF);
-  long long T = 0;
+  const uint32_t whi = (uint32_t)__double2hiint(x), wlo = (uint32_t)__double2loint(x);
+  const int biased = (int)((whi >> 20) & 0x7FF);
+  uint32_t hi = 0, lo = 0;
   if (biased != 0) {
-    const unsigned long long m = ((unsigned long long)bits & 0xFFFFFFFFFFFFFull) | (1ull << 52);
-    const int sh = (biased - 1023) - e + 3;  // x = m 2^(E - 52), T = m 2^(E - e + 3)
-    const unsigned long long u = sh >= 0 ? (m << sh) : (-sh < 64 ? (m >> -sh) : 0ull);
-    T = bits < 0 ? -(long long)u : (long long)u;
+    // m = 2^52 + fraction as (mh, ml), then u = m shifted left by sh (|sh| < 64)
+    const uint32_t mh = (whi & 0xFFFFFu) | 0x100000u, ml = wlo;
+    const int sh = (biased - 1023) - e + 3;  // x = m 2^(E - 52), T = m 2^(E - e + 3); sh <= 2
+    uint32_t uh, ul;
+    if (sh >= 0) {
+      uh = (mh << sh) | (sh ? (ml >> (32 - sh)) : 0u);
+      ul = ml << sh;
+    } else if (-sh < 32) {
+      const int r = -sh;
+      ul = (ml >> r) | (r ? (mh << (32 - r)) : 0u);
+      uh = mh >> r;
+    } else if (-sh < 64) {
+      ul = mh >> (-sh - 32);
+      uh = 0u;
+    } else {
+      ul = uh = 0u;
+    }
+    if ((int)whi < 0) {  // two's-complement negation of (uh, ul)
+      ul = ~ul + 1u;
+      uh = ~uh + (ul == 0u ? 1u : 0u);
+    }
+    hi = uh;
+    lo = ul;
   }
 #pragma unroll
   for (int s = OZ_S - 1; s >= 1; --s) {
-    const int d = (int)((T + 128) & 255) - 128;
-    a[s] = (float)d;
-    T = (T - d) >> 8;  // exact: T - d is a multiple of 256
+    const uint32_t nlo = lo + 128u;
+    const uint32_t nhi = hi + (nlo < lo ? 1u : 0u);
+    a[s] = (float)((int)(nlo & 255u) - 128);
+    lo = (nlo >> 8) | (nhi << 24);
+    hi = (uint32_t)((int)nhi >> 8);
   }
-  a[0] = (float)T;
+  a[0] = (float)(int)lo;  // |a_0| <= 128: the value fits the low word
 }
 
 // biased FP64 exponent of x (0 for zero and subnormals)
-__device__ __forceinline__ int oz_biased(double x) { return (int)((__double_as_longlong(x) >> 52) & 0x7FF); }
+__device__ __forceinline__ int oz_biased(double x) { return (__double2hiint(x) >> 20) & 0x7FF; }
 // row scale sigma = 2^e, e = 1 + the largest unbiased exponent of the row (0 if all zero)
 __device__ __forceinline__ int oz_row_e(int max_biased) { return max_biased > 0 ? max_biased - 1022 : 0; }
 
