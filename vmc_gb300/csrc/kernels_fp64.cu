@@ -255,17 +255,20 @@ __global__ void __launch_bounds__(OW_WARPS * 32)
   if (F32)
     for (int e = lane; e < n * n; e += 32) af[e] = make_float2((float)a[e].x, (float)a[e].y);
   __syncwarp();
-  // theta[p][:] = psi[p][:] M^-1 ; with P M = L U: solve w U = psi[p], z L = w, theta[perm[k]] = z[k]
+  // theta[p][:] = psi[p][:] M^-1 ; with P M = L U: w U = psi[p], z L = w, theta[perm[k]] = z[k]
   double* tre = theta + (size_t)(2 * w) * nce * N + (size_t)ch.col_off * N;
   double* tim = tre + (size_t)nce * N;
-  for (int p = lane; p < N; p += 32) {
-    if (F32) {
-      const float2* p32 = psi32 + (size_t)w * ncw * N + (size_t)ch.psi_off * N;
+  if (F32) {
+    // FP32: lane j < n forms row j of G = U^-1 L^-1 (the same two solves with
+    // psi[p] = e_j), stored with its columns in theta order, G[j][perm[k]] =
+    // z[k], over the FP64 factors (no longer needed); then every orbital row
+    // of theta is psi32[p][:] G.  n solves instead of N, and the row products
+    // read G by broadcast.
+    float2* G = reinterpret_cast<float2*>(a);  // [n][n]
+    if (lane < n) {
       float2 r[NM];
 #pragma unroll
-      for (int j = 0; j < NM; ++j)
-        if (j < n) r[j] = p32[(size_t)j * N + p];
-      // w U = r (forward over columns)
+      for (int j = 0; j < NM; ++j) r[j] = make_float2(j == lane ? 1.f : 0.f, 0.f);
 #pragma unroll
       for (int j = 0; j < NM; ++j) {
         if (j < n) {
@@ -282,7 +285,6 @@ __global__ void __launch_bounds__(OW_WARPS * 32)
           r[j] = make_float2((t.x * d.x + t.y * d.y) / den, (t.y * d.x - t.x * d.y) / den);
         }
       }
-      // z L = w (backward, L unit lower)
 #pragma unroll
       for (int jj = NM - 1; jj >= 0; --jj) {
         if (jj < n) {
@@ -299,12 +301,37 @@ __global__ void __launch_bounds__(OW_WARPS * 32)
       }
 #pragma unroll
       for (int k = 0; k < NM; ++k)
-        if (k < n) {
-          const int c = perm[k];
-          tre[(size_t)c * N + p] = r[k].x;
-          tim[(size_t)c * N + p] = r[k].y;
+        if (k < n) G[lane * n + perm[k]] = r[k];
+    }
+    __syncwarp();
+    const float2* p32 = psi32 + (size_t)w * ncw * N + (size_t)ch.psi_off * N;
+    for (int p = lane; p < N; p += 32) {
+      float2 acc[NM];
+#pragma unroll
+      for (int c = 0; c < NM; ++c) acc[c] = make_float2(0.f, 0.f);
+#pragma unroll 2
+      for (int j = 0; j < n; ++j) {
+        const float2 x = p32[(size_t)j * N + p];
+        const float2* gj = G + j * n;
+#pragma unroll
+        for (int c = 0; c < NM; ++c)
+          if (c < n) {
+            const float2 gv = gj[c];
+            acc[c].x += x.x * gv.x - x.y * gv.y;
+            acc[c].y += x.x * gv.y + x.y * gv.x;
+          }
+      }
+#pragma unroll
+      for (int c = 0; c < NM; ++c)
+        if (c < n) {
+          tre[(size_t)c * N + p] = acc[c].x;
+          tim[(size_t)c * N + p] = acc[c].y;
         }
-    } else {
+    }
+    return;
+  }
+  for (int p = lane; p < N; p += 32) {
+    {
       double2 r[NM];
 #pragma unroll
       for (int j = 0; j < NM; ++j)
