@@ -1,12 +1,15 @@
 """Cholesky-QR orthonormalisation of the mixed form against the Householder QR
 with the reference's (Eigen's) column convention.
 
-The two factorisations give the same Q up to the sign of each column, and the
-overlaps differ by the product of those signs (squared for the restricted
-walker): checked to 1e-12.  Every physical quantity is unchanged: the local
-energies after either QR are within 2e-5 Eh of the FP64 oracle's energies of
-the walkers before it (the mixed form's local-energy tolerance), and one
-further step with identical fields gives the same weights to 1e-6 relative.
+The two factorisations give the same Q up to the sign of each column: the
+Cholesky-QR's Gram matrix is formed in FP32, so its Q is orthonormal to ~1e-7
+and is checked against Householder's to 1e-6.  What keeps the walk exact is
+that the stored overlap is the overlap of the returned Q: checked against the
+FP64 oracle's overlap of those dets to 1e-10.  Every physical quantity is
+unchanged: the local energies after either QR are within 2e-5 Eh of the FP64
+oracle's energies of the walkers before it (the mixed form's local-energy
+tolerance), and one further step with identical fields gives the same weights
+to 1e-6 relative.
 """
 import numpy as np
 import pytest
@@ -62,14 +65,16 @@ def test_cholesky_qr_equals_householder_up_to_column_signs(A, kind):
     for w in range(W):
         sgn = np.sign(np.einsum("pj,pj->j", qh[w].conj(), qc[w]).real)
         assert np.all(np.abs(sgn) == 1)
-        assert np.abs(qc[w] - qh[w] * sgn[None]).max() < 1e-12
+        assert np.abs(qc[w] - qh[w] * sgn[None]).max() < 1e-6
         # orthonormal columns per spin block
         blocks = [(0, na)] if rw else [(0, na), (na, na + nb)]
         for a, b in blocks:
             g = qc[w][:, a:b].conj().T @ qc[w][:, a:b]
-            assert np.abs(g - np.eye(b - a)).max() < 1e-12
-        fac = np.prod(sgn) ** (2 if rw else 1)
-        assert abs(oc[w] - fac * oh_[w]) <= 1e-12 * abs(oh_[w])
+            assert np.abs(g - np.eye(b - a)).max() < 1e-6
+    ref_o = O.overlap(ot, O.Walkers(oh, rw, dc))
+    assert np.abs(oc / ref_o - 1).max() < 1e-10
+    ref_h = O.overlap(ot, O.Walkers(oh, rw, dh))
+    assert np.abs(oh_ / ref_h - 1).max() < 1e-10
     assert np.abs(elh - el_ref).max() < 2e-5
     assert np.abs(elc - el_ref).max() < 2e-5
     assert np.abs(w1c - w1h).max() <= 1e-6 * np.abs(w1h).max()

@@ -1,4 +1,4 @@
-// Cholesky-QR orthonormalisation of the walkers (mixed form), in FP64:
+// Cholesky-QR orthonormalisation of the walkers (mixed form):
 //     G = psi_s^H psi_s,   G = R^H R (R upper triangular, positive real diagonal),
 //     psi_s <- psi_s R^-1,  overlap /= prod_s prod_k R_kk  (squared for the restricted walker)
 // per spin block s.  This is the reference's orthogonalize
@@ -13,6 +13,12 @@
 // multiply.  theta = psi (Phi^T psi)^-1 is invariant under psi -> psi R^-1, so
 // no overlap or theta recompute follows; the per-channel determinants are
 // recomputed by the next step before they are used.
+//
+// Precision: R only has to make Q well conditioned -- whatever R is used, the
+// walker stays the same as long as psi R^-1 and overlap / det R are formed
+// with that same R.  So the Gram matrix is formed in FP32 from the FP32 copy of
+// psi (Q orthonormal to ~1e-7), while the Cholesky factor, R^-1, Q = psi R^-1
+// and det R are FP64: the stored overlap stays det(Phi^T Q) to FP64 accuracy.
 //
 // One CTA (256 threads) per walker, both spin blocks in turn; the block, the
 // Gram/R matrix and R^-1 live in shared memory.  Dead walkers (weight <= 1e-8)
@@ -39,6 +45,7 @@ __global__ void __launch_bounds__(OC_THREADS)
   double2* A = oc_sm;                          // [nmax][N]     spin block, column-major
   double2* R = A + (size_t)nmax * N;           // [nmax][nmax]  Gram, then R in its upper triangle (R[i * n + j])
   double2* Ri = R + (size_t)nmax * nmax;       // [nmax][nmax]  R^-1, upper (Ri[i * n + j])
+  float2* A32 = reinterpret_cast<float2*>(Ri + (size_t)nmax * nmax);  // [nmax][N] FP32 copy of the block
   __shared__ int s_bad;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   double fac = 1.0;  // thread 0
@@ -47,25 +54,35 @@ __global__ void __launch_bounds__(OC_THREADS)
     const int off = b == 0 ? 0 : na, n = b == 0 ? na : nb;
     if (n == 0) continue;
     double2* Ag = psi + ((size_t)w * ncw + off) * N;
-    float2* A32 = psi32 ? psi32 + ((size_t)w * ncw + off) * N : nullptr;
+    float2* Ag32 = psi32 + ((size_t)w * ncw + off) * N;
     __syncthreads();  // A, R, Ri free (previous block done)
-    for (int e = tid; e < n * N; e += OC_THREADS) A[e] = Ag[e];
+    for (int e = tid; e < n * N; e += OC_THREADS) {
+      A[e] = Ag[e];
+      A32[e] = Ag32[e];
+    }
     if (tid == 0) s_bad = 0;
     __syncthreads();
-    // Gram matrix, upper triangle: R[i][j] = sum_p conj(A_i[p]) A_j[p], i <= j
+    // Gram matrix (FP32), upper triangle: R[i][j] = sum_p conj(A_i[p]) A_j[p], i <= j
     for (int e = tid; e < n * n; e += OC_THREADS) {
       const int i = e / n, j = e % n;
       if (i > j) continue;
-      const double2* ai = A + (size_t)i * N;
-      const double2* aj = A + (size_t)j * N;
-      double2 s0 = make_double2(0.0, 0.0), s1 = make_double2(0.0, 0.0);
+      const float2* ai = A32 + (size_t)i * N;
+      const float2* aj = A32 + (size_t)j * N;
+      float sr = 0.f, si = 0.f, tr = 0.f, ti = 0.f;
       int p = 0;
       for (; p + 1 < N; p += 2) {
-        s0 = cfma(cconj(ai[p]), aj[p], s0);
-        s1 = cfma(cconj(ai[p + 1]), aj[p + 1], s1);
+        const float2 x0 = ai[p], y0 = aj[p], x1 = ai[p + 1], y1 = aj[p + 1];
+        sr += x0.x * y0.x + x0.y * y0.y;
+        si += x0.x * y0.y - x0.y * y0.x;
+        tr += x1.x * y1.x + x1.y * y1.y;
+        ti += x1.x * y1.y - x1.y * y1.x;
       }
-      if (p < N) s0 = cfma(cconj(ai[p]), aj[p], s0);
-      R[i * n + j] = cadd(s0, s1);
+      if (p < N) {
+        const float2 x0 = ai[p], y0 = aj[p];
+        sr += x0.x * y0.x + x0.y * y0.y;
+        si += x0.x * y0.y - x0.y * y0.x;
+      }
+      R[i * n + j] = make_double2((double)(sr + tr), (double)(si + ti));
     }
     __syncthreads();
     // Cholesky (warp 0): row k of R from G and rows m < k
@@ -113,7 +130,7 @@ __global__ void __launch_bounds__(OC_THREADS)
       double2 q = make_double2(0.0, 0.0);
       for (int i = 0; i <= j; ++i) q = cfma(A[(size_t)i * N + p], Ri[i * n + j], q);
       Ag[e] = q;
-      if (A32) A32[e] = make_float2((float)q.x, (float)q.y);
+      Ag32[e] = make_float2((float)q.x, (float)q.y);
     }
     if (tid == 0)
       for (int k = 0; k < n; ++k) fac *= R[k * n + k].x;
@@ -127,11 +144,11 @@ __global__ void __launch_bounds__(OC_THREADS)
 
 size_t ortho_chol_smem(const afqmc_handle* h) {
   const size_t nmax = (size_t)std::max(h->na, h->rhf_walker ? 0 : h->nb);
-  return (nmax * h->N + 2 * nmax * nmax) * sizeof(double2);
+  return (nmax * h->N + 2 * nmax * nmax) * sizeof(double2) + nmax * h->N * sizeof(float2);
 }
 
 bool ortho_chol_available(const afqmc_handle* h) {
-  return h->precision == AFQMC_PREC_MIXED && ortho_chol_smem(h) <= 200 * 1024;
+  return h->precision == AFQMC_PREC_MIXED && h->psi32 && ortho_chol_smem(h) <= 200 * 1024;
 }
 
 void launch_ortho_chol(afqmc_handle* h) {
