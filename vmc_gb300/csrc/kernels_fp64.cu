@@ -227,10 +227,17 @@ __global__ void __launch_bounds__(OW_WARPS * 32)
         a[bi * n + j] = t;
       }
     __syncwarp();
-    const double2 pv = a[k * n + k];
-    detv = cmul(detv, pv);
-    if (bi != k) detv = make_double2(-detv.x, -detv.y);
-    const double2 inv = crecip(pv);
+    // the pivot's reciprocal and the determinant on lane 0 only (FP64 is this
+    // GPU's scarce pipe), the reciprocal broadcast to the lanes that scale
+    double2 inv = make_double2(0.0, 0.0);
+    if (lane == 0) {
+      const double2 pv = a[k * n + k];
+      detv = cmul(detv, pv);
+      if (bi != k) detv = make_double2(-detv.x, -detv.y);
+      inv = crecip(pv);
+    }
+    inv.x = __shfl_sync(0xffffffffu, inv.x, 0);
+    inv.y = __shfl_sync(0xffffffffu, inv.y, 0);
     for (int i = k + 1 + lane; i < n; i += 32) a[i * n + k] = cmul(a[i * n + k], inv);
     __syncwarp();
     const int rem = n - k - 1;
