@@ -129,10 +129,12 @@ __global__ void k_overlap_theta(const double2* __restrict__ psi, const double* _
 // instead of Gauss-Jordan: M = Phi^T psi (FP64, register-tiled: lane
 // (li, lj) owns rows li + 4a and columns lj + 8b), partial-pivot LU of M in FP64
 // (pivot = first row of largest |M_ik|, det = sign * prod U_kk), then every
-// row p of theta from psi[p] . M^-1 by two triangular solves with the LU
-// factors (P M = L U => theta = psi U^-1 L^-1 P).  In the mixed form the solves
-// run in FP32 from the FP32 copy of the walkers.  A CTA holds OW_WARPS walkers
-// of one channel and stages that channel's Phi in shared memory.
+// row p of theta from psi[p] . M^-1 with the LU factors (P M = L U => theta =
+// psi U^-1 L^-1 P): in the FP64 form by two triangular solves per row; in the
+// mixed form (FP32 from the FP32 copy of the walkers) by forming the n rows of
+// U^-1 L^-1 once and one row product per orbital.  A CTA holds OW_WARPS walkers
+// of one channel and stages that channel's Phi in shared memory (unless M is
+// formed beforehand).
 constexpr int OW_WARPS = 4;
 
 // NM: n rounded up to a multiple of 4 (<= 32); lane (li, lj) of the M product
