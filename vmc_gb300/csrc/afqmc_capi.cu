@@ -178,7 +178,7 @@ void release(afqmc_handle* h) {
                   h->thetaB, h->xB, h->fb32, h->V32, h->expm32, h->d_chunks32, h->rotE, h->thetaE,
                   h->xc, h->cv_x, h->cv_idx, h->cv_esub, h->cv_f, h->cv_ms, h->cv_out, h->d_step, h->psi32,
                   h->pt_img, h->comb_cum, h->comb_idx, h->comb_ovl, h->blk, h->blk_zeta, h->wpart,
-                  h->ovl_A, h->ovl_sig, h->ovl_tau, h->ovl_bimg, h->ovl_M};
+                  h->ovl_A, h->ovl_sig, h->ovl_tau, h->ovl_bimg, h->ovl_M, h->theta32};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (h->host_pinned) cudaFreeHost(h->host_pinned);
@@ -432,7 +432,11 @@ int afqmc_create(const afqmc_ham* ham, const afqmc_trial* trial, const afqmc_opt
   ALLOC(tri, (size_t)T);
   ALLOC(expm, (size_t)nsp * NN);
   ALLOC(mf, (size_t)G);
-  ALLOC(theta, W * 2 * h->nce * N);
+  if (mixed) {
+    ALLOC(theta32, W * 2 * h->nce * N);
+  } else {
+    ALLOC(theta, W * 2 * h->nce * N);
+  }
   ALLOC(det, W * 2);
   ALLOC(ovlp, W);
   ALLOC(weights, W);

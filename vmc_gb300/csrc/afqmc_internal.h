@@ -91,7 +91,8 @@ struct afqmc_handle {
   int2* tri = nullptr;        // [T]                  packed index -> (i, j), j <= i
   double2* expm = nullptr;    // [nsp][N][N]          column-major exp(-dt/2 h1'_s)
   double2* mf = nullptr;      // [G]
-  double* theta = nullptr;    // [W][2][nce*N]        re / im planes
+  double* theta = nullptr;    // [W][2][nce*N]        re / im planes (FP64 and reference forms)
+  float* theta32 = nullptr;   // [W][2][nce*N]        the same in FP32 (mixed form, where it is formed in FP32)
   double2* det = nullptr;     // [W][2]               det(Phi_s^T psi_s) per channel
   double2* ovlp = nullptr;    // [W]
   double* weights = nullptr;  // [W]
@@ -210,6 +211,8 @@ void launch_fields_mixed(afqmc_handle* h, bool device_rng);
 void launch_vhs_mixed(afqmc_handle* h);
 void launch_propagate_mixed(afqmc_handle* h);
 void split_rows(afqmc_handle* h, const double* src, long lds, int rows, int K, int kpad, int pattern,
+                __nv_bfloat16* dst);
+void split_rows(afqmc_handle* h, const float* src, long lds, int rows, int K, int kpad, int pattern,
                 __nv_bfloat16* dst);
 void launch_local_energy_mixed(afqmc_handle* h);
 

@@ -36,8 +36,9 @@ void mlp_forward_on(afqmc_mlp* m, const float* X, int B, float* Y, cudaStream_t 
 int mlp_max_batch(const afqmc_mlp* m);
 int mlp_n_in(const afqmc_mlp* m);
 
+template <class T>
 __global__ void k_cv_features(const float* __restrict__ fb32, const double* __restrict__ fb64,
-                              const double* __restrict__ theta, const double* __restrict__ h1phi,
+                              const T* __restrict__ theta, const double* __restrict__ h1phi,
                               const double2* __restrict__ ovlp, int N, int nce, int G, int mult,
                               const float* __restrict__ mean, const float* __restrict__ stdv, float* __restrict__ out) {
   const int w = blockIdx.x;
@@ -47,9 +48,9 @@ __global__ void k_cv_features(const float* __restrict__ fb32, const double* __re
     if (g < G) v = fb32 ? fb32[(size_t)(2 * w) * G + g] : (float)fb64[(size_t)(2 * w) * G + g];
     o[g] = v;
   }
-  const double* tre = theta + (size_t)(2 * w) * nce * N;
+  const T* tre = theta + (size_t)(2 * w) * nce * N;
   double e1 = 0.0;
-  for (int k = threadIdx.x; k < nce * N; k += blockDim.x) e1 += tre[k] * h1phi[k];
+  for (int k = threadIdx.x; k < nce * N; k += blockDim.x) e1 += (double)tre[k] * h1phi[k];
   e1 = block_sum(e1);
   if (threadIdx.x == 0) {
     const double2 ov = ovlp[w];
@@ -76,19 +77,19 @@ __global__ void k_cv_select(int* __restrict__ idx, int W, int den, uint64_t seed
 }
 
 // dst rows (i, plane, c) = split of theta rows of walker idx[i] ([hi | lo | hi] along p)
-__global__ void k_split_theta_gather(const double* __restrict__ theta, const int* __restrict__ idx, int m, int nce,
+__global__ void k_split_theta_gather(const float* __restrict__ theta, const int* __restrict__ idx, int m, int nce,
                                      int N, int kpad, __nv_bfloat16* __restrict__ dst) {
   const int row = blockIdx.x;  // (i, plane, c)
   const int i = row / (2 * nce), rem = row % (2 * nce);
-  const double* s = theta + ((size_t)idx[i] * 2 * nce + rem) * N;
+  const float* s = theta + ((size_t)idx[i] * 2 * nce + rem) * N;
   __nv_bfloat16* d = dst + (size_t)row * kpad;
   for (int k = threadIdx.x; k < kpad; k += blockDim.x) {
     __nv_bfloat16 v = __float2bfloat16_rn(0.f);
     if (k < 3 * N) {
       const int part = k / N, p = k % N;
-      const double x = s[p];
-      const __nv_bfloat16 hi = __float2bfloat16_rn((float)x);
-      const __nv_bfloat16 lo = __float2bfloat16_rn((float)(x - (double)__bfloat162float(hi)));
+      const float x = s[p];
+      const __nv_bfloat16 hi = __float2bfloat16_rn(x);
+      const __nv_bfloat16 lo = __float2bfloat16_rn(x - __bfloat162float(hi));
       v = part == 1 ? lo : hi;
     }
     d[k] = v;
@@ -147,7 +148,7 @@ namespace afqmc {
 void launch_local_energy_mixed_subset(afqmc_handle* h, const int* d_idx, int m, double2* out);
 
 void launch_split_theta_gather(afqmc_handle* h, const int* d_idx, int m) {
-  k_split_theta_gather<<<m * 2 * h->nce, 128, 0, h->stream>>>(h->theta, d_idx, m, h->nce, h->N, h->ke_pad, h->thetaE);
+  k_split_theta_gather<<<m * 2 * h->nce, 128, 0, h->stream>>>(h->theta32, d_idx, m, h->nce, h->N, h->ke_pad, h->thetaE);
   h->launches++;
 }
 }
@@ -160,9 +161,12 @@ int afqmc_cv_features(afqmc_handle* h, float* out) {
   if (!h->cv_x) return AFQMC_ERR_STATE;
   if (h->precision == AFQMC_PREC_MIXED) launch_force_bias_mixed(h);
   else launch_force_bias(h);
-  k_cv_features<<<h->nwalk, 128, 0, h->stream>>>(h->precision == AFQMC_PREC_MIXED ? h->fb32 : nullptr, h->fb,
-                                                 h->theta, h->h1phi, h->ovlp, h->N, h->nce, h->G, h->mult, nullptr,
-                                                 nullptr, h->cv_x);
+  if (h->precision == AFQMC_PREC_MIXED)
+    k_cv_features<float><<<h->nwalk, 128, 0, h->stream>>>(h->fb32, h->fb, h->theta32, h->h1phi, h->ovlp, h->N, h->nce,
+                                                          h->G, h->mult, nullptr, nullptr, h->cv_x);
+  else
+    k_cv_features<double><<<h->nwalk, 128, 0, h->stream>>>(nullptr, h->fb, h->theta, h->h1phi, h->ovlp, h->N, h->nce,
+                                                           h->G, h->mult, nullptr, nullptr, h->cv_x);
   h->launches++;
   if (cudaMemcpyAsync(out, h->cv_x, (size_t)h->nwalk * CV_NF * 4, cudaMemcpyDeviceToHost, h->stream) != cudaSuccess ||
       cudaStreamSynchronize(h->stream) != cudaSuccess) {
@@ -224,7 +228,7 @@ int afqmc_cv_measure(afqmc_handle* h, uint64_t tag, int slot) {
   cudaSetDevice(h->device);
   const int W = h->nwalk, den = h->cv_den, m = (W + den - 1) / den;
   launch_force_bias_mixed(h);
-  k_cv_features<<<W, 128, 0, h->stream>>>(h->fb32, nullptr, h->theta, h->h1phi, h->ovlp, h->N, h->nce, h->G, h->mult,
+  k_cv_features<float><<<W, 128, 0, h->stream>>>(h->fb32, nullptr, h->theta32, h->h1phi, h->ovlp, h->N, h->nce, h->G, h->mult,
                                           h->cv_ms, h->cv_ms + CV_NF, h->cv_x);
   mlp_forward_on(h->cv_mlp, h->cv_x, W, h->cv_f, h->stream);
   k_cv_select<<<(m + 127) / 128, 128, 0, h->stream>>>(h->cv_idx, W, den, h->seed, tag, h->d_step);

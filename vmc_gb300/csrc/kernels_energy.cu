@@ -182,17 +182,17 @@ __global__ void __launch_bounds__(128, 1)
 }
 
 // E = ecore + mult sum theta.h1phi + 1/2 sum_g [(mult sum_s c_sg)^2 - mult sum_s X_sg]
-__global__ void k_energy_assemble(const double* __restrict__ theta, const double* __restrict__ h1phi,
+__global__ void k_energy_assemble(const float* __restrict__ theta, const double* __restrict__ h1phi,
                                   const double2* __restrict__ xc, double2* __restrict__ eloc, int N, int nce, int Gene,
                                   int nchan, int mult, double ecore, const int* __restrict__ idx) {
   const int w = blockIdx.x;  // local index (row of xc); theta of walker idx[w] (or w)
   const int ws = idx ? idx[w] : w;
-  const double* tre = theta + (size_t)(2 * ws) * nce * N;
-  const double* tim = tre + (size_t)nce * N;
-  double re = 0.0, im = 0.0;
+  const float* tre = theta + (size_t)(2 * ws) * nce * N;
+  const float* tim = tre + (size_t)nce * N;
+  double re = 0.0, im = 0.0;  // the one-body term accumulates in FP64
   for (int k = threadIdx.x; k < nce * N; k += blockDim.x) {
-    re += tre[k] * h1phi[k];
-    im += tim[k] * h1phi[k];
+    re += (double)tre[k] * h1phi[k];
+    im += (double)tim[k] * h1phi[k];
   }
   double er = 0.0, ei = 0.0;
   for (int g = threadIdx.x; g < Gene; g += blockDim.x) {
@@ -221,7 +221,7 @@ void launch_split_theta_gather(afqmc_handle* h, const int* d_idx, int m);
 void launch_local_energy_mixed_subset(afqmc_handle* h, const int* d_idx, int m, double2* out) {
   const int Kn = h->N;
   if (d_idx) launch_split_theta_gather(h, d_idx, m);
-  else split_rows(h, h->theta, Kn, 2 * m * h->nce, Kn, h->ke_pad, 1, h->thetaE);
+  else split_rows(h, h->theta32, Kn, 2 * m * h->nce, Kn, h->ke_pad, 1, h->thetaE);
   static bool attr = false;
   if (!attr) {
     cudaFuncSetAttribute(k_tc_exchange, cudaFuncAttributeMaxDynamicSharedMemorySize, EX_SMEM);
@@ -249,7 +249,7 @@ void launch_local_energy_mixed_subset(afqmc_handle* h, const int* d_idx, int m, 
                                                     h->nchan, h->xc, h->d_err);
     h->launches++;
   }
-  k_energy_assemble<<<m, 256, 0, h->stream>>>(h->theta, h->h1phi, h->xc, out, h->N, h->nce, h->nchol_ene, h->nchan,
+  k_energy_assemble<<<m, 256, 0, h->stream>>>(h->theta32, h->h1phi, h->xc, out, h->N, h->nce, h->nchol_ene, h->nchan,
                                               h->mult, h->ecore, d_idx);
   h->launches++;
 }

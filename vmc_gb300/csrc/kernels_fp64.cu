@@ -21,7 +21,7 @@ namespace afqmc {
 // first row of largest |M_ik| as Eigen's PartialPivLU.  One CTA per (walker, channel).
 // ---------------------------------------------------------------------------
 __global__ void k_overlap_theta(const double2* __restrict__ psi, const double* __restrict__ phi,
-                                double* __restrict__ theta, double2* __restrict__ det,
+                                double* __restrict__ theta, float* __restrict__ theta32, double2* __restrict__ det,
                                 const double* __restrict__ weights, int N, int ncw, int nce,
                                 Channel c0, Channel c1, int only_live, int theta_fp32) {
   const int w = blockIdx.x;
@@ -92,10 +92,10 @@ __global__ void k_overlap_theta(const double2* __restrict__ psi, const double* _
   }
   if (threadIdx.x == 0) det[2 * w + blockIdx.y] = detv;
   // theta[p][j] = sum_i psi[p][i] Minv[i][j]
-  double* tre = theta + (size_t)(2 * w) * nce * N + (size_t)ch.col_off * N;
-  double* tim = tre + (size_t)nce * N;
   if (theta_fp32) {
     // mixed form: theta feeds split-BF16 contractions, FP32 arithmetic suffices
+    float* tre = theta32 + (size_t)(2 * w) * nce * N + (size_t)ch.col_off * N;
+    float* tim = tre + (size_t)nce * N;
     for (int e = threadIdx.x; e < N * n; e += blockDim.x) {
       const int j = e / N, p = e % N;
       float re = 0.f, im = 0.f;
@@ -111,6 +111,8 @@ __global__ void k_overlap_theta(const double2* __restrict__ psi, const double* _
     }
     return;
   }
+  double* tre = theta + (size_t)(2 * w) * nce * N + (size_t)ch.col_off * N;
+  double* tim = tre + (size_t)nce * N;
   for (int e = threadIdx.x; e < N * n; e += blockDim.x) {
     const int j = e / N, p = e % N;
     double re = 0.0, im = 0.0;
@@ -144,9 +146,9 @@ constexpr int OW_WARPS = 4;
 template <bool F32, int NM, bool MB>
 __global__ void __launch_bounds__(OW_WARPS * 32)
     k_overlap_lu(const double2* __restrict__ psi, const float2* __restrict__ psi32, const double* __restrict__ phi,
-                 double* __restrict__ theta, double2* __restrict__ det, const double* __restrict__ weights, int W,
-                 int N, int ncw, int nce, Channel c0, Channel c1, int only_live, int nmax,
-                 const double2* __restrict__ mbuf) {
+                 double* __restrict__ theta, float* __restrict__ theta32, double2* __restrict__ det,
+                 const double* __restrict__ weights, int W, int N, int ncw, int nce, Channel c0, Channel c1,
+                 int only_live, int nmax, const double2* __restrict__ mbuf) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int s = blockIdx.y;
   const Channel ch = s == 0 ? c0 : c1;
@@ -265,9 +267,9 @@ __global__ void __launch_bounds__(OW_WARPS * 32)
     for (int e = lane; e < n * n; e += 32) af[e] = make_float2((float)a[e].x, (float)a[e].y);
   __syncwarp();
   // theta[p][:] = psi[p][:] M^-1 ; with P M = L U: w U = psi[p], z L = w, theta[perm[k]] = z[k]
-  double* tre = theta + (size_t)(2 * w) * nce * N + (size_t)ch.col_off * N;
-  double* tim = tre + (size_t)nce * N;
   if (F32) {
+    float* tre = theta32 + (size_t)(2 * w) * nce * N + (size_t)ch.col_off * N;
+    float* tim = tre + (size_t)nce * N;
     // FP32: lane j < n forms row j of G = U^-1 L^-1 (the same two solves with
     // psi[p] = e_j), stored with its columns in theta order, G[j][perm[k]] =
     // z[k], over the FP64 factors (no longer needed); then every orbital row
@@ -339,6 +341,8 @@ __global__ void __launch_bounds__(OW_WARPS * 32)
     }
     return;
   }
+  double* tre = theta + (size_t)(2 * w) * nce * N + (size_t)ch.col_off * N;
+  double* tim = tre + (size_t)nce * N;
   for (int p = lane; p < N; p += 32) {
     {
       double2 r[NM];
@@ -411,7 +415,8 @@ void launch_overlap_theta(afqmc_handle* h, bool only_live) {
       attr = true;                                                                                           \
     }                                                                                                        \
     k_overlap_lu<F, NMV, MBV><<<grid, OW_WARPS * 32, smem, h->stream>>>(                                     \
-        h->psi, h->psi32, h->phi, h->theta, h->det, h->weights, h->nwalk, h->N, h->ncw, h->nce, h->chan[0],  \
+        h->psi, h->psi32, h->phi, h->theta, h->theta32, h->det, h->weights, h->nwalk, h->N, h->ncw, h->nce,  \
+        h->chan[0],                                                                                          \
         h->chan[1], only_live ? 1 : 0, nmax, h->ovl_M);                                                       \
   }
 #define OW_NM(F, MBV)                          \
@@ -444,7 +449,7 @@ void launch_overlap_theta(afqmc_handle* h, bool only_live) {
     attr_set = true;
   }
   dim3 grid(h->nwalk, h->nchan);
-  k_overlap_theta<<<grid, 256, smem, h->stream>>>(h->psi, h->phi, h->theta, h->det, h->weights, h->N,
+  k_overlap_theta<<<grid, 256, smem, h->stream>>>(h->psi, h->phi, h->theta, h->theta32, h->det, h->weights, h->N,
                                                   h->ncw, h->nce, h->chan[0], h->chan[1],
                                                   only_live ? 1 : 0, h->precision == AFQMC_PREC_MIXED ? 1 : 0);
   h->launches++;

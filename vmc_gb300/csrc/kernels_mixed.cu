@@ -77,15 +77,21 @@ __device__ __forceinline__ void split_bf16(double x, __nv_bfloat16& hi, __nv_bfl
   hi = __float2bfloat16_rn(xf);
   lo = __float2bfloat16_rn((float)(x - (double)__bfloat162float(hi)));
 }
+// FP32 source: the remainder is exact in FP32, and no FP64 work is done
+__device__ __forceinline__ void split_bf16(float x, __nv_bfloat16& hi, __nv_bfloat16& lo) {
+  hi = __float2bfloat16_rn(x);
+  lo = __float2bfloat16_rn(x - __bfloat162float(hi));
+}
 
 // dst[r][0:3K] = pattern of src[r][0:K] (FP64, row stride lds); pattern 0:
 // [hi | hi | lo] (the static side), 1: [hi | lo | hi] (the per-step side).
 // Columns 3K .. kpad-1 are zero.  Grid (column blocks, rows); each thread
 // splits one source element and writes its three copies.
-__global__ void k_split_rows(const double* __restrict__ src, long lds, int rows, int K, int kpad, int pattern,
+template <class T>
+__global__ void k_split_rows(const T* __restrict__ src, long lds, int rows, int K, int kpad, int pattern,
                              __nv_bfloat16* __restrict__ dst) {
   const int r = blockIdx.y;
-  const double* s = src + (long)r * lds;
+  const T* s = src + (long)r * lds;
   __nv_bfloat16* d = dst + (long)r * kpad;
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < K; k += gridDim.x * blockDim.x) {
     __nv_bfloat16 hi, lo;
@@ -98,15 +104,24 @@ __global__ void k_split_rows(const double* __restrict__ src, long lds, int rows,
   for (int c = 3 * K + blockIdx.x * blockDim.x + threadIdx.x; c < kpad; c += gridDim.x * blockDim.x) d[c] = z;
 }
 
-void split_rows(afqmc_handle* h, const double* src, long lds, int rows, int K, int kpad, int pattern,
-                __nv_bfloat16* dst) {
+template <class T>
+static void split_rows_t(afqmc_handle* h, const T* src, long lds, int rows, int K, int kpad, int pattern,
+                         __nv_bfloat16* dst) {
   const int cb = std::max(1, std::min(8, (K + 255) / 256));
   for (int r0 = 0; r0 < rows; r0 += 65535) {
     dim3 grid(cb, std::min(65535, rows - r0));
-    k_split_rows<<<grid, 256, 0, h->stream>>>(src + (long)r0 * lds, lds, rows - r0, K, kpad, pattern,
-                                              dst + (long)r0 * kpad);
+    k_split_rows<T><<<grid, 256, 0, h->stream>>>(src + (long)r0 * lds, lds, rows - r0, K, kpad, pattern,
+                                                 dst + (long)r0 * kpad);
     h->launches++;
   }
+}
+void split_rows(afqmc_handle* h, const double* src, long lds, int rows, int K, int kpad, int pattern,
+                __nv_bfloat16* dst) {
+  split_rows_t(h, src, lds, rows, K, kpad, pattern, dst);
+}
+void split_rows(afqmc_handle* h, const float* src, long lds, int rows, int K, int kpad, int pattern,
+                __nv_bfloat16* dst) {
+  split_rows_t(h, src, lds, rows, K, kpad, pattern, dst);
 }
 
 // ---------------------------------------------------------------------------
@@ -163,7 +178,7 @@ static void launch_tc(afqmc_handle* h, const CUtensorMap& ta, const CUtensorMap*
 // theta planes (FP64) -> split BF16 operand rows (w, plane)
 void launch_theta_split(afqmc_handle* h) {
   const int K = h->nce * h->N;
-  split_rows(h, h->theta, K, 2 * h->nwalk, K, h->kf_pad, 1, h->thetaB);
+  split_rows(h, h->theta32, K, 2 * h->nwalk, K, h->kf_pad, 1, h->thetaB);
 }
 
 void launch_force_bias_mixed(afqmc_handle* h) {
