@@ -223,10 +223,10 @@ __global__ void k_fields_mixed(const float* __restrict__ fb, const double2* __re
     ftr += xg * fsr - 0.5 * (fsr * fsr - fsi * fsi);
     fti += xg * fsi - 0.5 * (2.0 * fsr * fsi);
     if (!live) { xr = 0.0; xim = 0.0; }
-    __nv_bfloat16 hi, lo;
-    split_bf16(xr, hi, lo);
+    __nv_bfloat16 hi, lo;  // split of the FP32 value (the VHS contraction is split-BF16)
+    split_bf16((float)xr, hi, lo);
     xr_out[g] = hi; xr_out[G + g] = lo; xr_out[2 * G + g] = hi;
-    split_bf16(xim, hi, lo);
+    split_bf16((float)xim, hi, lo);
     xi_out[g] = hi; xi_out[G + g] = lo; xi_out[2 * G + g] = hi;
   }
   shr = block_sum(shr);
