@@ -209,32 +209,69 @@ __global__ void __launch_bounds__(OW_WARPS * 32)
       }
   }
   __syncwarp();
-  // LU with partial pivoting (FP64)
+  // LU with partial pivoting (FP64 factors).  The FP64 form follows Eigen's
+  // PartialPivLU exactly (FP64 pivot search, first row of the largest |M_ik|,
+  // FP64 reciprocal, running determinant).  The mixed form keeps the FP64
+  // factors and determinant but spends fewer FP64 instructions on the scalar
+  // work of each step, which on this GPU occupies the scarce FP64 pipe even
+  // when one lane is active: the pivot search compares |M_ik|^2 in FP32 (any
+  // near-largest pivot is as good), the reciprocal is an FP32 estimate with
+  // one FP64 Newton step (relative error ~1e-14), and the determinant is the
+  // product of U's diagonal formed at the end by a tree across lanes.
   double2 detv = make_double2(1.0, 0.0);
+  int nswap = 0;
   for (int k = 0; k < n; ++k) {
-    double best = -1.0;
     int bi = k;
-    for (int i = k + lane; i < n; i += 32) {
-      const double v = cabs2(a[i * n + k]);
-      if (v > best) { best = v; bi = i; }
-    }
-    for (int off = 16; off > 0; off >>= 1) {
-      const double ob = __shfl_xor_sync(0xffffffffu, best, off);
-      const int oi = __shfl_xor_sync(0xffffffffu, bi, off);
-      if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+    if (F32) {
+      float best = -1.f;
+      for (int i = k + lane; i < n; i += 32) {
+        const double2 z = a[i * n + k];
+        const float zx = (float)z.x, zy = (float)z.y;
+        const float v = zx * zx + zy * zy;
+        if (v > best) { best = v; bi = i; }
+      }
+      for (int off = 16; off > 0; off >>= 1) {
+        const float ob = __shfl_xor_sync(0xffffffffu, best, off);
+        const int oi = __shfl_xor_sync(0xffffffffu, bi, off);
+        if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+      }
+    } else {
+      double best = -1.0;
+      for (int i = k + lane; i < n; i += 32) {
+        const double v = cabs2(a[i * n + k]);
+        if (v > best) { best = v; bi = i; }
+      }
+      for (int off = 16; off > 0; off >>= 1) {
+        const double ob = __shfl_xor_sync(0xffffffffu, best, off);
+        const int oi = __shfl_xor_sync(0xffffffffu, bi, off);
+        if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+      }
     }
     if (lane == 0) perm[k] = bi;
-    if (bi != k)
+    if (bi != k) {
+      ++nswap;
       for (int j = lane; j < n; j += 32) {
         const double2 t = a[k * n + j];
         a[k * n + j] = a[bi * n + j];
         a[bi * n + j] = t;
       }
+    }
     __syncwarp();
-    // the pivot's reciprocal and the determinant on lane 0 only (FP64 is this
-    // GPU's scarce pipe), the reciprocal broadcast to the lanes that scale
     double2 inv = make_double2(0.0, 0.0);
-    if (lane == 0) {
+    if (F32) {
+      if (lane == 0) {
+        const double2 pv = a[k * n + k];
+        // 1 / pv = conj(pv) / |pv|^2, with 1 / |pv|^2 from FP32 and one Newton step
+        const double d = pv.x * pv.x + pv.y * pv.y;
+        if (d > 1e-30 && d < 1e30) {
+          double r = (double)(1.f / (float)d);
+          r = r * (2.0 - d * r);
+          inv = make_double2(pv.x * r, -pv.y * r);
+        } else {
+          inv = crecip(pv);  // outside FP32's comfortable range
+        }
+      }
+    } else if (lane == 0) {
       const double2 pv = a[k * n + k];
       detv = cmul(detv, pv);
       if (bi != k) detv = make_double2(-detv.x, -detv.y);
@@ -250,6 +287,19 @@ __global__ void __launch_bounds__(OW_WARPS * 32)
       a[i * n + j] = csub(a[i * n + j], cmul(a[i * n + k], a[k * n + j]));
     }
     __syncwarp();
+  }
+  if (F32) {
+    // det = (-1)^swaps prod_k U_kk by a tree product across lanes
+    double2 dv = lane < n ? a[lane * n + lane] : make_double2(1.0, 0.0);
+    for (int k2 = lane + 32; k2 < n; k2 += 32) dv = cmul(dv, a[k2 * n + k2]);
+    for (int off = 16; off > 0; off >>= 1) {
+      double2 o;
+      o.x = __shfl_xor_sync(0xffffffffu, dv.x, off);
+      o.y = __shfl_xor_sync(0xffffffffu, dv.y, off);
+      dv = cmul(dv, o);
+    }
+    if (nswap & 1) dv = make_double2(-dv.x, -dv.y);
+    detv = dv;
   }
   if (lane == 0) det[2 * w + s] = detv;
   // perm[k]: row swapped with k at step k -> final row order of P M
