@@ -26,10 +26,10 @@
 // the groups run their five V products independently and the tensor core works
 // on one group's MMAs while the other group's threads write or read.  Thread
 // (g, h, p) owns 20 B rows (10 columns, half h of group g) of orbital row p =
-// TMEM lane p: it reads them from each product with tcgen05.ld, keeps them of
-// the Taylor sum in TMEM (columns 128.., its own lane; the additions are its
-// own, in FP32 round-to-nearest) and writes them back as K column p (and
-// 128 + p) of its group's next B operand.  Seven products per walker: B, five
+// TMEM lane p: it reads them from each product with tcgen05.ld (one batched
+// read per product), keeps its part of the Taylor sum in registers (the
+// additions are its own, in FP32 round-to-nearest) and writes them back as K
+// column p (and 128 + p) of its group's next B operand.  Seven products per walker: B, five
 // Taylor terms, B.
 #include <cuda.h>
 #include <cuda_bf16.h>
@@ -134,8 +134,7 @@ __device__ __forceinline__ bool pt_gand(int g, bool v) {
   return r != 0;
 }
 
-constexpr int PT_ACC = 128;        // TMEM column of the Taylor sum (the product tile is at 0)
-constexpr int PT_TMEM_COLS = 256;
+constexpr int PT_TMEM_COLS = 128;  // the two groups' product tiles at columns 0 and 64
 
 // One group's product: TMEM[128 x nc] at tcol0 = A . B_g^T over the first ns
 // K-steps of 16, three split passes, issued by the group's first thread.
@@ -254,22 +253,6 @@ __device__ __forceinline__ void pt_tmem_ld(uint32_t taddr, float* v) {
   for (int i = 0; i < PT_CW; ++i) v[i] = __uint_as_float(u[i]);
 }
 
-// PT_CW = 20 columns to this thread's TMEM lane at taddr, one wait
-__device__ __forceinline__ void pt_tmem_st(uint32_t taddr, const float* v) {
-  asm volatile(
-      "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17};\n"
-      "tcgen05.st.sync.aligned.32x32b.x4.b32 [%1], {%18,%19,%20,%21};\n"
-      "tcgen05.wait::st.sync.aligned;\n" ::"r"(taddr),
-      "r"(taddr + 16), "r"(__float_as_uint(v[0])), "r"(__float_as_uint(v[1])), "r"(__float_as_uint(v[2])),
-      "r"(__float_as_uint(v[3])), "r"(__float_as_uint(v[4])), "r"(__float_as_uint(v[5])), "r"(__float_as_uint(v[6])),
-      "r"(__float_as_uint(v[7])), "r"(__float_as_uint(v[8])), "r"(__float_as_uint(v[9])),
-      "r"(__float_as_uint(v[10])), "r"(__float_as_uint(v[11])), "r"(__float_as_uint(v[12])),
-      "r"(__float_as_uint(v[13])), "r"(__float_as_uint(v[14])), "r"(__float_as_uint(v[15])),
-      "r"(__float_as_uint(v[16])), "r"(__float_as_uint(v[17])), "r"(__float_as_uint(v[18])),
-      "r"(__float_as_uint(v[19]))
-      : "memory");
-}
-
 static_assert(PT_CW == 20 && PT_NP * 2 * PT_CW == PT_NCMAX, "the TMEM row helpers move 20 columns (x16 + x4)");
 
 // Additions are made by the threads (round to nearest): the tensor core's
@@ -283,14 +266,6 @@ __device__ __forceinline__ void pt_add_row(uint32_t taddr, float* y) {
   for (int i = 0; i < PT_CW; ++i) y[i] += t[i];
 }
 
-// the 20 columns at taddr += x
-__device__ __forceinline__ void pt_acc_add(uint32_t taddr, const float* x) {
-  float t[PT_CW];
-  pt_tmem_ld(taddr, t);
-#pragma unroll
-  for (int i = 0; i < PT_CW; ++i) t[i] += x[i];
-  pt_tmem_st(taddr, t);
-}
 
 __global__ void __launch_bounds__(PT_THREADS, 1)
     k_prop_tc(double2* __restrict__ psi, float2* __restrict__ psi32, const float* __restrict__ Vp,
@@ -332,7 +307,6 @@ __global__ void __launch_bounds__(PT_THREADS, 1)
   const uint32_t trow = tmem + ((uint32_t)((warp & 3) * 32) << 16);
   const uint32_t tD = tmem + (uint32_t)(64 * g);                       // the group's product tile
   const uint32_t tcol = trow + (uint32_t)(64 * g + h * PT_CW);        // this thread's product columns
-  const uint32_t tacc = trow + (uint32_t)(PT_ACC + 64 * g + h * PT_CW);  // this thread's Taylor-sum columns
 
   const int T = N * (N + 1) / 2;
   const float* vre = Vp + ((size_t)(w * nspV + sp) * 2) * T;
@@ -350,7 +324,7 @@ __global__ void __launch_bounds__(PT_THREADS, 1)
     const int nc = ((2 * ncg + 15) / 16) * 16;                              // its B rows (MMA N)
     const int cg0 = c0 + g * (PT_GROWS / 2) + h * (PT_CW / 2);              // this thread's first column
     const int nmine = max(0, min(PT_CW / 2, ncg - h * (PT_CW / 2)));
-    float x[PT_CW];
+    float x[PT_CW], acc[PT_CW];
     __syncthreads();
     pt_issue_image(sA, im, bar_ld);
 #pragma unroll
@@ -371,7 +345,8 @@ __global__ void __launch_bounds__(PT_THREADS, 1)
       gok = pt_product(sA, sB, nc, nsB, tD, &bar_mma[g], ph_mma, err, g);
       if (gok) {
         pt_add_row(tcol, x);
-        pt_tmem_st(tacc, x);  // the Taylor sum starts from B psi
+#pragma unroll
+        for (int c = 0; c < PT_CW; ++c) acc[c] = x[c];  // the Taylor sum starts from B psi
       }
     }
     // the shared A operand changes: both groups are done with B
@@ -387,13 +362,16 @@ __global__ void __launch_bounds__(PT_THREADS, 1)
       pt_tmem_ld(tcol, x);
       const float inv = 1.f / (float)k;
 #pragma unroll
-      for (int c = 0; c < PT_CW; ++c) x[c] *= inv;
-      pt_acc_add(tacc, x);
+      for (int c = 0; c < PT_CW; ++c) {
+        x[c] *= inv;
+        acc[c] += x[c];
+      }
     }
     if (!(ok = __syncthreads_and(gok ? 1 : 0) != 0)) break;
     // B (sum) = sum + (B - I) sum
     pt_issue_image(sA, im, bar_ld);
-    if (nc > 0) pt_tmem_ld(tacc, x);
+#pragma unroll
+    for (int c = 0; c < PT_CW; ++c) x[c] = acc[c];
     if (p < N) pt_store_X(sB, x, nc, p, !realB, h);
     if (!(ok = pt_wait(bar_ld, ph_ld, err, 22))) break;
     if (nc > 0) {
