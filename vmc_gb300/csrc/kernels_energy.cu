@@ -114,10 +114,10 @@ __global__ void __launch_bounds__(128, 1)
       }
       tc::tc_fence_after();
       const uint32_t sa = tc::smem_u32(smem + s * EX_STAGE);
-      const uint64_t ad = tc::sdesc_sw128(sa), bd = tc::sdesc_sw128(sa + EX_A_BYTES);
 #pragma unroll
       for (int k = 0; k < BK / 16; ++k)
-        tc::mma_bf16(tmem, ad + (uint64_t)(2 * k), bd + (uint64_t)(2 * k), idesc, (kb > 0 || k > 0) ? 1u : 0u);
+        tc::mma_bf16(tmem, tc::sdesc_sw128(sa + 32 * k), tc::sdesc_sw128(sa + EX_A_BYTES + 32 * k), idesc,
+                     (kb > 0 || k > 0) ? 1u : 0u);
       tc::mma_commit(&empty[s]);
     }
     tc::mma_commit(accum);
@@ -154,18 +154,13 @@ __global__ void __launch_bounds__(128, 1)
       const float* rowbase = tile + (gl * n) * EX_LD;
       const int cre = (2 * wl) * n, cim = (2 * wl + 1) * n;
       float xr = 0.f, xi = 0.f, cr = 0.f, ci = 0.f;
-      // lanes over j, a loop over i (no division by the runtime n); f[i][j]
-      // reads along a row, f[j][i] down a column (row pitch EX_LD = 257: no
-      // bank conflicts)
-      for (int i = 0; i < n; ++i) {
-        const float* ri = rowbase + i * EX_LD;
-        for (int j = lane; j < n; j += 32) {
-          const float a_r = ri[cre + j], a_i = ri[cim + j];
-          const float b_r = rowbase[j * EX_LD + cre + i], b_i = rowbase[j * EX_LD + cim + i];
-          xr = fmaf(a_r, b_r, fmaf(-a_i, b_i, xr));
-          xi = fmaf(a_r, b_i, fmaf(a_i, b_r, xi));
-          if (i == j) { cr += a_r; ci += a_i; }
-        }
+      for (int e = lane; e < n * n; e += 32) {
+        const int i = e / n, j = e % n;
+        const float a_r = rowbase[i * EX_LD + cre + j], a_i = rowbase[i * EX_LD + cim + j];
+        const float b_r = rowbase[j * EX_LD + cre + i], b_i = rowbase[j * EX_LD + cim + i];
+        xr = fmaf(a_r, b_r, fmaf(-a_i, b_i, xr));
+        xi = fmaf(a_r, b_i, fmaf(a_i, b_r, xi));
+        if (i == j) { cr += a_r; ci += a_i; }
       }
       xr = warp_sumf(xr);
       xi = warp_sumf(xi);

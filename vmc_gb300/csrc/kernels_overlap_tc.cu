@@ -261,14 +261,14 @@ __global__ void __launch_bounds__(128, 1)
       if (s_abort) { ok = false; break; }
       tc::tc_fence_after();
       const int sl = kb / npanel, kk = kb % npanel;
-      const uint64_t ad = tc::sdesc_sw128(tc::smem_u32(ring + s * OZ_TILE));
+      const uint32_t aa = tc::smem_u32(ring + s * OZ_TILE);
       for (int L = sl; L < OZ_S; ++L) {
         const int t = L - sl;
-        const uint64_t bd = tc::sdesc_sw128(tc::smem_u32(sB + (size_t)(t * npanel + kk) * g.BNP * 128));
+        const uint32_t ba = tc::smem_u32(sB) + (uint32_t)((t * npanel + kk) * g.BNP * 128);
 #pragma unroll
         for (int k = 0; k < 4; ++k)  // +32 bytes per K=16 step inside the swizzle row
-          tc::mma_bf16(tmem + (uint32_t)(L * g.BNP), ad + (uint64_t)(2 * k), bd + (uint64_t)(2 * k), idesc,
-                       (sl > 0 || kk > 0 || k > 0) ? 1u : 0u);
+          tc::mma_bf16(tmem + (uint32_t)(L * g.BNP), tc::sdesc_sw128(aa + 32 * k), tc::sdesc_sw128(ba + 32 * k),
+                       idesc, (sl > 0 || kk > 0 || k > 0) ? 1u : 0u);
       }
       tc::mma_commit(&empty[s]);
     }

@@ -119,10 +119,16 @@ __host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
 // Shared-memory matrix descriptor, K-major operand with 128-byte swizzle:
 // start address >> 4 (bits 0-13), leading byte offset 16 B (unused for this
 // layout), stride byte offset 1024 B between 8-row groups (bits 32-45),
-// descriptor version 1 (bit 46), swizzle mode 2 = 128 B (bits 61-63).
+// descriptor version 1 (bit 46), swizzle mode 2 = 128 B (bits 61-63).  Built
+// from two 32-bit words and packed with one move: 64-bit integer arithmetic
+// runs on this GPU's small FP64 pipe, and the MMA issue loops build one
+// descriptor pair per instruction.
 __device__ __forceinline__ uint64_t sdesc_sw128(uint32_t saddr) {
-  return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((uint64_t)1 << 16) | ((uint64_t)(1024 >> 4) << 32) |
-         ((uint64_t)1 << 46) | ((uint64_t)2 << 61);
+  const uint32_t lo = ((saddr & 0x3FFFFu) >> 4) | (1u << 16);
+  const uint32_t hi = (uint32_t)(1024 >> 4) | (1u << 14) | (2u << 29);
+  uint64_t d;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(d) : "r"(lo), "r"(hi));
+  return d;
 }
 
 // 32 lanes x 32 bit, 16 consecutive columns per thread
@@ -216,10 +222,9 @@ __global__ void __launch_bounds__(128, 1)
       tc_fence_after();
       const uint32_t a = smem_u32(smem + s * L::STAGE_BYTES);
       const uint32_t b = a + L::A_BYTES;
-      const uint64_t ad = sdesc_sw128(a), bd = sdesc_sw128(b);
 #pragma unroll
       for (int k = 0; k < BK / 16; ++k)  // +32 bytes per K=16 step inside the swizzle row
-        mma_bf16(tmem, ad + (uint64_t)(2 * k), bd + (uint64_t)(2 * k), idesc, (kb > 0 || k > 0) ? 1u : 0u);
+        mma_bf16(tmem, sdesc_sw128(a + 32 * k), sdesc_sw128(b + 32 * k), idesc, (kb > 0 || k > 0) ? 1u : 0u);
       mma_commit(&empty[s]);
     }
     mma_commit(accum);
