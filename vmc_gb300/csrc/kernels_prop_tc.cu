@@ -20,17 +20,14 @@
 // B - I is built once per handle in global memory and copied in with
 // cp.async.bulk.
 // V comes from the packed lower triangle written by the VHS GEMM and is
-// scattered into A by the CTA.  The walker's columns form two pipeline groups
-// (warps 0-7 and 8-15) with their own B operand, TMEM tiles, MMA issuer,
-// mbarrier and named barrier: the Taylor recursion is column by column, so
-// the groups run their five V products independently and the tensor core works
-// on one group's MMAs while the other group's threads write or read.  Thread
-// (g, h, p) owns 20 B rows (10 columns, half h of group g) of orbital row p =
-// TMEM lane p: it reads them from each product with tcgen05.ld (one batched
-// read per product), keeps its part of the Taylor sum in registers (the
+// scattered into A by the CTA.  Thread (p, g) owns 20 columns (group g of 4)
+// of orbital row p = TMEM lane p: it reads them from each product with one
+// batched tcgen05.ld, keeps its part of the Taylor sum in registers (the
 // additions are its own, in FP32 round-to-nearest) and writes them back as K
-// column p (and 128 + p) of its group's next B operand.  Seven products per walker: B, five
-// Taylor terms, B.
+// column p (and 128 + p) of the next B operand.  Four warps share
+// each TMEM lane quadrant, so one 214 KB CTA per SM still keeps four warps per
+// scheduler to hide the load and barrier latencies.  Seven products per walker:
+// B, five Taylor terms, B.
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -45,15 +42,11 @@ namespace afqmc {
 constexpr int PT_K = 256;                          // K: real block [0, 128), imaginary block [128, 256)
 constexpr int PT_A_BYTES = 128 * PT_K * 2;         // one BF16 half of A
 constexpr int PT_NCMAX = 80;                       // max B rows (2 x 40 columns) per pass
-constexpr int PT_NP = 2;                           // pipeline groups (independent column halves)
-constexpr int PT_GROWS = PT_NCMAX / PT_NP;         // B rows of one group (20 columns)
-constexpr int PT_GPAD = 48;                        // rows of a group's B buffer (MMA N: multiple of 16)
-constexpr int PT_CW = 20;                          // B rows (product columns) per thread
-constexpr int PT_THREADS = 512;                    // group = warp / 8; column half = (warp / 4) % 2
-constexpr int PT_GTHREADS = PT_THREADS / PT_NP;
-constexpr int PT_B_BYTES = PT_GPAD * PT_K * 2;     // one BF16 half of one group's B operand
-constexpr int PT_SMEM = 2 * PT_A_BYTES + PT_NP * 2 * PT_B_BYTES + 128 + 1024;
-static_assert(PT_SMEM <= 232448, "shared memory per CTA");
+constexpr int PT_NG = 4;                           // column groups: 4 warps per TMEM lane quadrant
+constexpr int PT_CW = PT_NCMAX / PT_NG;            // B rows (product columns) per thread
+constexpr int PT_THREADS = 128 * PT_NG;
+constexpr int PT_B_BYTES = PT_NCMAX * PT_K * 2;    // one BF16 half of B
+constexpr int PT_SMEM = 2 * PT_A_BYTES + 2 * PT_B_BYTES + 64 + 1024;
 constexpr int PT_IMG = 128 * PT_K;                 // BF16 elements of one half of the B image
 constexpr int PT_COPY = 16384;                     // bytes per bulk copy
 
@@ -119,31 +112,15 @@ __device__ __forceinline__ bool pt_wait(uint64_t* bar, uint32_t& phase, int* err
   return __syncthreads_and(ok ? 1 : 0) != 0;
 }
 
-// Barrier of one pipeline group (named barrier 1 + g, PT_GTHREADS threads),
-// plain and with an AND of a predicate.
-__device__ __forceinline__ void pt_gsync(int g) {
-  asm volatile("bar.sync %0, %1;" ::"r"(1 + g), "r"(PT_GTHREADS) : "memory");
-}
-__device__ __forceinline__ bool pt_gand(int g, bool v) {
-  uint32_t r;
-  asm volatile(
-      "{\n .reg .pred p, q;\n setp.ne.u32 p, %1, 0;\n bar.red.and.pred q, %2, %3, p;\n selp.u32 %0, 1, 0, q;\n}\n"
-      : "=r"(r)
-      : "r"(v ? 1u : 0u), "r"(1 + g), "r"(PT_GTHREADS)
-      : "memory");
-  return r != 0;
-}
+constexpr int PT_TMEM_COLS = 128;  // the 128 x 80 product tile
 
-constexpr int PT_TMEM_COLS = 128;  // the two groups' product tiles at columns 0 and 64
-
-// One group's product: TMEM[128 x nc] at tcol0 = A . B_g^T over the first ns
-// K-steps of 16, three split passes, issued by the group's first thread.
-__device__ __forceinline__ bool pt_product(uint8_t* sA, uint8_t* sB, int nc, int ns, uint32_t tcol0, uint64_t* bar,
-                                           uint32_t& phase, int* err, int g) {
+// TMEM[128 x nc] = A . B^T over the first ns K-steps of 16, three split passes.
+__device__ __forceinline__ bool pt_product(uint8_t* sA, uint8_t* sB, int nc, int ns, uint32_t tmem, uint64_t* bar,
+                                           uint32_t& phase, int* err) {
   pt_fence_proxy();  // this thread's generic writes to A / B -> visible to the tensor core
   tc::tc_fence_before();
-  pt_gsync(g);
-  if (threadIdx.x == g * PT_GTHREADS) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
     tc::tc_fence_after();
     const uint32_t idesc = tc::idesc_bf16(128, nc);
     const uint32_t a_hi = tc::smem_u32(sA), a_lo = a_hi + PT_A_BYTES;
@@ -156,28 +133,25 @@ __device__ __forceinline__ bool pt_product(uint8_t* sA, uint8_t* sB, int nc, int
       for (int s = 0; s < ns; ++s) {
         const uint32_t ao = (uint32_t)((s >> 2) * 128 * 128 + (s & 3) * 32);
         const uint32_t bo = (uint32_t)((s >> 2) * nc * 128 + (s & 3) * 32);
-        tc::mma_bf16(tcol0, tc::sdesc_sw128(a0 + ao), tc::sdesc_sw128(b0 + bo), idesc,
+        tc::mma_bf16(tmem, tc::sdesc_sw128(a0 + ao), tc::sdesc_sw128(b0 + bo), idesc,
                      (pass > 0 || s > 0) ? 1u : 0u);
       }
     }
     tc::mma_commit(bar);
   }
-  const bool ok = tc::mbar_wait(bar, phase, err, 21);
-  phase ^= 1u;
-  const bool all = pt_gand(g, ok);
+  const bool ok = pt_wait(bar, phase, err, 21);
   tc::tc_fence_after();
-  return all;
+  return ok;
 }
 
 // This thread's part of row p of X (x[2jj] = Re X(p, j), x[2jj+1] = Im X(p, j)
-// for its columns j, B rows 20 h .. 20 h + 19 of its group's buffer of nc rows)
-// into K column p (and 128 + p when `both`) of the rows (j, re) and (j, im),
-// split in BF16.
-__device__ __forceinline__ void pt_store_X(uint8_t* sB, const float* x, int nc, int p, bool both, int h) {
+// for the columns j of group g) into K column p (and 128 + p when `both`) of
+// the B operand rows (j, re) and (j, im), split in BF16.
+__device__ __forceinline__ void pt_store_X(uint8_t* sB, const float* x, int nc, int p, bool both, int g) {
   uint8_t* sBl = sB + PT_B_BYTES;
 #pragma unroll
   for (int jj = 0; jj < PT_CW; jj += 2) {
-    const int j2 = h * PT_CW + jj;
+    const int j2 = g * PT_CW + jj;
     if (j2 < nc) {
       __nv_bfloat16 rh, rl, ih, il;
       pt_split(x[jj], rh, rl);
@@ -253,7 +227,7 @@ __device__ __forceinline__ void pt_tmem_ld(uint32_t taddr, float* v) {
   for (int i = 0; i < PT_CW; ++i) v[i] = __uint_as_float(u[i]);
 }
 
-static_assert(PT_CW == 20 && PT_NP * 2 * PT_CW == PT_NCMAX, "the TMEM row helpers move 20 columns (x16 + x4)");
+static_assert(PT_CW == 20 && PT_NG * PT_CW == PT_NCMAX, "the TMEM row helpers move 20 columns (x16 + x4)");
 
 // Additions are made by the threads (round to nearest): the tensor core's
 // accumulation of small products onto a stored O(1) value was measured to
@@ -277,20 +251,19 @@ __global__ void __launch_bounds__(PT_THREADS, 1)
   extern __shared__ uint8_t pt_raw[];
   uint8_t* smem = (uint8_t*)(((uintptr_t)pt_raw + 1023) & ~(uintptr_t)1023);
   uint8_t* sA = smem;                    // hi at 0, lo at PT_A_BYTES
-  uint8_t* sBase = smem + 2 * PT_A_BYTES;  // group g: hi at g 2 PT_B_BYTES, lo PT_B_BYTES later
-  uint64_t* bar_ld = (uint64_t*)(sBase + PT_NP * 2 * PT_B_BYTES);
-  uint64_t* bar_mma = bar_ld + 1;        // one per group
-  uint32_t* tmem_holder = (uint32_t*)(bar_mma + PT_NP);
+  uint8_t* sB = smem + 2 * PT_A_BYTES;   // hi at 0, lo at PT_B_BYTES
+  uint64_t* bar_ld = (uint64_t*)(sB + 2 * PT_B_BYTES);
+  uint64_t* bar_mma = bar_ld + 1;
+  uint32_t* tmem_holder = (uint32_t*)(bar_mma + 1);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (threadIdx.x == 0) {
     tc::mbar_init(bar_ld, 1);
-    for (int g = 0; g < PT_NP; ++g) tc::mbar_init(&bar_mma[g], 1);
+    tc::mbar_init(bar_mma, 1);
     tc::fence_mbar_init();
   }
   if (warp == 0) tc::tmem_alloc(tmem_holder, PT_TMEM_COLS);
-  // B operands: K positions no row of X is written to stay zero
-  for (int e = threadIdx.x; e < PT_NP * 2 * PT_B_BYTES / 16; e += blockDim.x)
-    ((uint4*)sBase)[e] = make_uint4(0, 0, 0, 0);
+  // B operand: K positions no row of X is written to stay zero
+  for (int e = threadIdx.x; e < 2 * PT_B_BYTES / 16; e += blockDim.x) ((uint4*)sB)[e] = make_uint4(0, 0, 0, 0);
   tc::tc_fence_before();
   __syncthreads();
   tc::tc_fence_after();
@@ -298,15 +271,12 @@ __global__ void __launch_bounds__(PT_THREADS, 1)
   uint32_t ph_ld = 0, ph_mma = 0;
   bool ok = true;
 
-  // thread = (pipeline group g, column half h, orbital row p = TMEM lane p):
-  // warp w reaches lanes 32 (w % 4) .. + 31; group g owns walker columns
-  // 20 g .. 20 g + 19 of the pass (B rows of its own buffer), half h ten of them
-  const int g = warp >> 3, h = (warp >> 2) & 1;
+  // thread = (orbital row p = TMEM lane, column group g): warp w reaches lanes
+  // 32 (w % 4) .. + 31, and the warps with the same w % 4 split the columns
   const int p = ((warp & 3) << 5) | lane;
-  uint8_t* sB = sBase + (size_t)g * 2 * PT_B_BYTES;
+  const int g = warp >> 2;
   const uint32_t trow = tmem + ((uint32_t)((warp & 3) * 32) << 16);
-  const uint32_t tD = tmem + (uint32_t)(64 * g);                       // the group's product tile
-  const uint32_t tcol = trow + (uint32_t)(64 * g + h * PT_CW);        // this thread's product columns
+  const uint32_t tcol = trow + (uint32_t)(g * PT_CW);            // product columns of this thread
 
   const int T = N * (N + 1) / 2;
   const float* vre = Vp + ((size_t)(w * nspV + sp) * 2) * T;
@@ -320,45 +290,33 @@ __global__ void __launch_bounds__(PT_THREADS, 1)
 
   for (int c0 = col_lo; c0 < col_hi && ok; c0 += PT_NCMAX / 2) {
     const int ncols = min(PT_NCMAX / 2, col_hi - c0);
-    const int ncg = max(0, min(PT_GROWS / 2, ncols - g * (PT_GROWS / 2)));  // this group's columns
-    const int nc = ((2 * ncg + 15) / 16) * 16;                              // its B rows (MMA N)
-    const int cg0 = c0 + g * (PT_GROWS / 2) + h * (PT_CW / 2);              // this thread's first column
-    const int nmine = max(0, min(PT_CW / 2, ncg - h * (PT_CW / 2)));
+    const int nc = ((2 * ncols + 15) / 16) * 16;
     float x[PT_CW], acc[PT_CW];
     __syncthreads();
     pt_issue_image(sA, im, bar_ld);
 #pragma unroll
     for (int jj = 0; jj < PT_CW / 2; ++jj) {
+      const int j = g * (PT_CW / 2) + jj;
       float2 v = make_float2(0.f, 0.f);
-      if (jj < nmine && p < N) {
-        const double2 d = pw[(size_t)(cg0 + jj) * N + p];
+      if (j < ncols && p < N) {
+        const double2 d = pw[(size_t)(c0 + j) * N + p];
         v = make_float2((float)d.x, (float)d.y);
       }
       x[2 * jj] = v.x;
       x[2 * jj + 1] = v.y;
     }
-    if (p < N) pt_store_X(sB, x, nc, p, !realB, h);
+    if (p < N) pt_store_X(sB, x, nc, p, !realB, g);
     if (!(ok = pt_wait(bar_ld, ph_ld, err, 22))) break;
     // B psi = psi + (B - I) psi
-    bool gok = true;
-    if (nc > 0) {
-      gok = pt_product(sA, sB, nc, nsB, tD, &bar_mma[g], ph_mma, err, g);
-      if (gok) {
-        pt_add_row(tcol, x);
+    if (!(ok = pt_product(sA, sB, nc, nsB, tmem, bar_mma, ph_mma, err))) break;
+    pt_add_row(tcol, x);
 #pragma unroll
-        for (int c = 0; c < PT_CW; ++c) acc[c] = x[c];  // the Taylor sum starts from B psi
-      }
-    }
-    // the shared A operand changes: both groups are done with B
-    if (!(ok = __syncthreads_and(gok ? 1 : 0) != 0)) break;
+    for (int c = 0; c < PT_CW; ++c) acc[c] = x[c];  // the Taylor sum starts from B psi
+    // Taylor terms with V: term_k = V term_{k-1} / k, added to the sum in TMEM
     pt_load_V(sA, vre, vim, tri, T);
-    pt_fence_proxy();
-    __syncthreads();
-    // Taylor terms with V, each group on its own: term_k = V term_{k-1} / k,
-    // added to the sum in TMEM; the groups' MMAs and thread work interleave
-    for (int k = 1; k <= 5 && gok && nc > 0; ++k) {
-      if (p < N) pt_store_X(sB, x, nc, p, true, h);
-      if (!(gok = pt_product(sA, sB, nc, 16, tD, &bar_mma[g], ph_mma, err, g))) break;
+    for (int k = 1; k <= 5 && ok; ++k) {
+      if (p < N) pt_store_X(sB, x, nc, p, true, g);
+      if (!(ok = pt_product(sA, sB, nc, 16, tmem, bar_mma, ph_mma, err))) break;
       pt_tmem_ld(tcol, x);
       const float inv = 1.f / (float)k;
 #pragma unroll
@@ -367,29 +325,26 @@ __global__ void __launch_bounds__(PT_THREADS, 1)
         acc[c] += x[c];
       }
     }
-    if (!(ok = __syncthreads_and(gok ? 1 : 0) != 0)) break;
+    if (!ok) break;
     // B (sum) = sum + (B - I) sum
     pt_issue_image(sA, im, bar_ld);
 #pragma unroll
     for (int c = 0; c < PT_CW; ++c) x[c] = acc[c];
-    if (p < N) pt_store_X(sB, x, nc, p, !realB, h);
+    if (p < N) pt_store_X(sB, x, nc, p, !realB, g);
     if (!(ok = pt_wait(bar_ld, ph_ld, err, 22))) break;
-    if (nc > 0) {
-      gok = pt_product(sA, sB, nc, nsB, tD, &bar_mma[g], ph_mma, err, g);
-      if (gok) {
-        pt_add_row(tcol, x);
-        if (p < N) {
+    if (!(ok = pt_product(sA, sB, nc, nsB, tmem, bar_mma, ph_mma, err))) break;
+    pt_add_row(tcol, x);
+    if (p < N) {
 #pragma unroll
-          for (int jj = 0; jj < PT_CW / 2; ++jj)
-            if (jj < nmine) {
-              const size_t o = (size_t)(cg0 + jj) * N + p;
-              pw[o] = make_double2((double)x[2 * jj], (double)x[2 * jj + 1]);
-              pw32[o] = make_float2(x[2 * jj], x[2 * jj + 1]);
-            }
+      for (int jj = 0; jj < PT_CW / 2; ++jj) {
+        const int j = g * (PT_CW / 2) + jj;
+        if (j < ncols) {
+          const size_t o = (size_t)(c0 + j) * N + p;
+          pw[o] = make_double2((double)x[2 * jj], (double)x[2 * jj + 1]);
+          pw32[o] = make_float2(x[2 * jj], x[2 * jj + 1]);
         }
       }
     }
-    ok = __syncthreads_and(gok ? 1 : 0) != 0;
   }
   tc::tc_fence_before();
   __syncthreads();

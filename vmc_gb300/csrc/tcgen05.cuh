@@ -54,13 +54,21 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
       : "memory");
   return ok != 0;
 }
+__device__ __forceinline__ uint32_t globaltimer_lo() {
+  uint32_t t;
+  asm volatile("mov.u32 %0, %%globaltimer_lo;" : "=r"(t));
+  return t;
+}
 // Wait for the phase with the given parity; false (and *err = code) after WAIT_NS.
+// The clock is the low word of the global timer (a wrapping 32-bit difference
+// covers WAIT_NS < 2^32 ns), so the spin loop does no 64-bit integer work,
+// which on this GPU would occupy the FP64 pipe.
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* err, int code) {
   if (mbar_try_wait(bar, parity)) return true;
-  const uint64_t t0 = globaltimer();
+  const uint32_t t0 = globaltimer_lo();
   while (true) {
     if (mbar_try_wait(bar, parity)) return true;
-    if (globaltimer() - t0 > WAIT_NS) {
+    if (globaltimer_lo() - t0 > (uint32_t)WAIT_NS) {
       atomicExch(err, code);
       return false;
     }
