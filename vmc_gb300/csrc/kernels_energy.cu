@@ -52,8 +52,11 @@ struct ExArgs {
   int s;          // channel index
 };
 
-// grid: (walker tiles, g tiles, channels); 128 threads
-__global__ void __launch_bounds__(128, 1)
+// grid: (walker tiles, g tiles, channels); EX_THREADS threads: warp 0 lane 0
+// loads, warp 1 lane 0 issues the MMAs, and all warps share the epilogue
+// (warp w reads TMEM lane quadrant w % 4, column half w / 4)
+constexpr int EX_THREADS = 256;
+__global__ void __launch_bounds__(EX_THREADS, 1)
     k_tc_exchange(const __grid_constant__ CUtensorMap tmA0, const __grid_constant__ CUtensorMap tmB0,
                   const __grid_constant__ CUtensorMap tmA1, const __grid_constant__ CUtensorMap tmB1, ExArgs a0,
                   ExArgs a1, int Gene, int W, int K, int nchan, double2* __restrict__ xc, int* err) {
@@ -133,11 +136,12 @@ __global__ void __launch_bounds__(128, 1)
   float* tile = (float*)smem;
   const int n = A.n, ncols = 2 * A.wbox * n;
   if (have && !s_abort) {
-    const int row = warp * 32 + lane;
+    const int q = warp & 3, half = warp >> 2;
+    const int row = q * 32 + lane;
 #pragma unroll 1
-    for (int c = 0; c < EX_BN; c += 16) {
+    for (int c = half * (EX_BN / 2); c < (half + 1) * (EX_BN / 2); c += 16) {
       float v[16];
-      tc::tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c, v);
+      tc::tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)c, v);
       if (c < ncols) {
 #pragma unroll
         for (int j = 0; j < 16; ++j) tile[row * EX_LD + c + j] = v[j];
@@ -147,7 +151,7 @@ __global__ void __launch_bounds__(128, 1)
   __syncthreads();
   if (have && !s_abort) {
     const int npairs = A.gbox * A.wbox;
-    for (int pr = warp; pr < npairs; pr += 4) {
+    for (int pr = warp; pr < npairs; pr += EX_THREADS / 32) {
       const int gl = pr / A.wbox, wl = pr % A.wbox;
       const int g = g0 + gl, w = w0 + wl;
       if (g >= Gene || w >= W) continue;
@@ -244,7 +248,7 @@ void launch_local_energy_mixed_subset(afqmc_handle* h, const int* d_idx, int m, 
   if (h->nchan == 1) a[1] = a[0];
   if (h->nchol_ene > 0) {
     dim3 grid(wt, gt, h->nchan);
-    k_tc_exchange<<<grid, 128, EX_SMEM, h->stream>>>(h->tm_rotE[0], h->tm_thE[0], h->tm_rotE[h->nchan - 1],
+    k_tc_exchange<<<grid, EX_THREADS, EX_SMEM, h->stream>>>(h->tm_rotE[0], h->tm_thE[0], h->tm_rotE[h->nchan - 1],
                                                     h->tm_thE[h->nchan - 1], a[0], a[1], h->nchol_ene, m, h->ke_pad,
                                                     h->nchan, h->xc, h->d_err);
     h->launches++;
