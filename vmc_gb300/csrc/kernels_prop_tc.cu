@@ -146,9 +146,16 @@ __device__ __forceinline__ bool pt_product(uint8_t* sA, uint8_t* sB, int nc, int
 
 // This thread's part of row p of X (x[2jj] = Re X(p, j), x[2jj+1] = Im X(p, j)
 // for the columns j of group g) into K column p (and 128 + p when `both`) of
-// the B operand rows (j, re) and (j, im), split in BF16.
+// the B operand rows (j, re) and (j, im), split in BF16.  The swizzled offset
+// pt_off(r, k, nc) of row r = 20 g + jj splits into a per-thread part (K
+// panel and byte of k = p, the row block 20 g) and (c ^ (r & 7)) << 4 with
+// c = (p & 63) >> 3; since 20 g = 4 (g & 1) mod 8, r & 7 = (jj & 7) ^ 4 (g & 1),
+// so each store needs an XOR with a constant, a shift and an add.
 __device__ __forceinline__ void pt_store_X(uint8_t* sB, const float* x, int nc, int p, bool both, int g) {
   uint8_t* sBl = sB + PT_B_BYTES;
+  const uint32_t base0 = (uint32_t)((p >> 6) * nc * 128 + (p & 7) * 2 + g * PT_CW * 128);
+  const uint32_t base1 = base0 + (uint32_t)(2 * nc * 128);  // k = 128 + p: two K panels further
+  const uint32_t cq = (uint32_t)(((p & 63) >> 3) ^ (4 * (g & 1)));
 #pragma unroll
   for (int jj = 0; jj < PT_CW; jj += 2) {
     const int j2 = g * PT_CW + jj;
@@ -156,13 +163,15 @@ __device__ __forceinline__ void pt_store_X(uint8_t* sB, const float* x, int nc, 
       __nv_bfloat16 rh, rl, ih, il;
       pt_split(x[jj], rh, rl);
       pt_split(x[jj + 1], ih, il);
-      const uint32_t o0 = pt_off(j2, p, nc), o1 = pt_off(j2 + 1, p, nc);
+      const uint32_t x0 = ((cq ^ (uint32_t)(jj & 7)) << 4) + (uint32_t)(jj * 128);
+      const uint32_t x1 = ((cq ^ (uint32_t)((jj + 1) & 7)) << 4) + (uint32_t)((jj + 1) * 128);
+      const uint32_t o0 = base0 + x0, o1 = base0 + x1;
       *(__nv_bfloat16*)(sB + o0) = rh;
       *(__nv_bfloat16*)(sBl + o0) = rl;
       *(__nv_bfloat16*)(sB + o1) = ih;
       *(__nv_bfloat16*)(sBl + o1) = il;
       if (both) {
-        const uint32_t q0 = pt_off(j2, 128 + p, nc), q1 = pt_off(j2 + 1, 128 + p, nc);
+        const uint32_t q0 = base1 + x0, q1 = base1 + x1;
         *(__nv_bfloat16*)(sB + q0) = __hneg(ih);
         *(__nv_bfloat16*)(sBl + q0) = __hneg(il);
         *(__nv_bfloat16*)(sB + q1) = rh;
