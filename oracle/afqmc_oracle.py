@@ -162,7 +162,7 @@ class Hamiltonian:
 
     @classmethod
     def from_fcidump(cls, d, int_type="r"):
-        """From ``oracle.hdf5_min.read_fcidump_chol`` output (integral.cpp:589-741)."""
+        """From ``vmc_gb300.hdf5.read_fcidump_chol`` output (integral.cpp:589-741)."""
         n = d["norb"]
         if int_type == "r":
             chol = d["chol"].transpose(0, 2, 1)  # column-major maps

@@ -2,7 +2,7 @@
 
 Reads, for each hot-path fixture directory of the reference checkout
 (tests/DQMC/{rhf_rhf,rhf_uhf,uhf_rhf,uhf_uhf,uhf_uhf_ui}), the integral file
-``FCIDUMP_chol`` (HDF5, via oracle/hdf5_min.py), the trial files ``rhf.txt`` /
+``FCIDUMP_chol`` (HDF5, via vmc_gb300/hdf5.py), the trial files ``rhf.txt`` /
 ``uhf.txt``, ``afqmc.json`` and the pinned series ``samples.ref`` (weight and
 energy of each 50-step block of a 4-rank run, checked by the reference's
 tests/testEnergy.py:108-121), and writes ``tests/golden/ref_<name>.npz``.
@@ -17,7 +17,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
-from oracle.hdf5_min import read_fcidump_chol  # noqa: E402
+from vmc_gb300.hdf5 import read_fcidump_chol  # noqa: E402
 
 FIXTURES = ["rhf_rhf", "rhf_uhf", "uhf_rhf", "uhf_uhf", "uhf_uhf_ui"]
 

@@ -59,7 +59,7 @@ def test_householder_convention():
 @pytest.mark.parametrize("name", refcases.FIXTURES)
 def test_fixture_npz_matches_reference(name):
     """The committed npz equals a fresh conversion of the reference's files."""
-    from oracle.hdf5_min import read_fcidump_chol
+    from vmc_gb300.hdf5 import read_fcidump_chol
     d = os.path.join(REF_ROOT, "tests", "DQMC", name)
     ints = read_fcidump_chol(os.path.join(d, "FCIDUMP_chol"))
     c = refcases.load(name)

@@ -1,13 +1,10 @@
 """Minimal read-only HDF5 reader for the reference's ``FCIDUMP_chol`` files.
 
-Test infrastructure (part of the oracle): only ``tests/`` and the oracle's own
-pin checks use it.
-
 The reference writes its Cholesky integral files with h5py
 (scripts/QMCUtils.py:1067-1097) and reads them with libhdf5 in
 utils/integral.cpp:589-741 (datasets ``header``, ``hcore``, ``hcore_mod``,
 ``chol``, ``energy_core``; the ``intType: "u"`` variant has ``*_up``/``*_dn``).
-Neither libhdf5 nor h5py exists in this environment, so this module restates the
+Neither libhdf5 nor h5py is a dependency here, so this module implements the
 small subset of the public HDF5 file-format specification that such files use:
 
 * superblock version 0 or 1 (symbol-table root group),
