@@ -71,6 +71,33 @@ def dist_env():
 FP64_NOMINAL_TFLOPS = 1.25  # GB300 FP64 (nominal; the FP64 pipe, not the tensor cores)
 
 
+def fp32_nominal_tflops(sm_mhz=2070.0):
+    """GB300 CUDA-core FP32: 152 SMs x 128 lanes x 2 FLOPs (FMA) per clock."""
+    return 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
+
+
+def mixed_stage_pipes(N, na, nb, G):
+    """Algorithmic FLOPs per walker of each stage of the mixed form, split by the
+    pipe that executes them (complex multiply-add = 8 FLOPs, real x complex = 4):
+      vhs      packed-triangle VHS on the tensor cores;
+      prop     B exp-Taylor B products on the tensor cores;
+      overlap  M = Phi^T psi on the tensor cores (exact BF16 slices), the LU, the
+               inverse rows and theta = psi M^-1 in FP32 on the CUDA cores;
+      ortho    Cholesky-QR: Hermitian Gram psi^H psi in FP32, Cholesky, R^-1 and
+               Q = psi R^-1 in FP64.
+    The force bias of the control-variate form runs inside its measurement."""
+    T = N * (N + 1) // 2
+    ns = [na, nb]
+    return {
+        "vhs": {"tensor": 4 * T * G},
+        "prop": {"tensor": sum(48 * N * N * n for n in ns)},
+        "overlap": {"tensor": sum(4 * n * n * N for n in ns),
+                    "fp32": sum(8 * n ** 3 / 3 + 8 * n ** 3 + 8 * N * n * n for n in ns)},
+        "ortho": {"fp32": sum(4 * N * n * n for n in ns),
+                  "fp64": sum(8 * n ** 3 / 3 + 8 * n ** 3 / 3 + 4 * N * n * n for n in ns)},
+    }
+
+
 def flops_model(N, na, nb, G, ortho_every=ORTHO_EVERY):
     """Algorithmic FLOPs per walker: force bias, VHS, propagator with
     a real exp(-dt/2 h1') (2 real x complex + 5 complex x complex products per
@@ -398,27 +425,31 @@ def main():
     launches_of = {s: args.steps for s in per_launch}
     launches_of["ortho"] = max(1, args.steps // ORTHO_EVERY)
     peak = pk["bf16_tflops_sustained"] if "bf16_tflops_sustained" in pk else pk["bf16_tflops"]
-    # every stage against the peak of the pipe that bounds it: tensor-core stages vs the
-    # measured bf16 peak, FP64 stages (overlap LU, QR) vs the nominal FP64 rate (no
-    # measured FP64 peak exists for this GPU pool)
-    fp64_stages = ("overlap", "ortho")
+    # every stage against the pipes that execute it: its bound is the sum over those
+    # pipes of (FLOPs on the pipe / the pipe's peak) -- tensor cores at the measured
+    # bf16 peak, FP32 and FP64 CUDA cores at their nominal rates (no measured FP32 or
+    # FP64 peak exists for this GPU pool) -- and frac = bound time / measured time
+    pipe_peak = {"tensor": peak, "fp32": fp32_nominal_tflops(), "fp64": FP64_NOMINAL_TFLOPS}
+    pipes = mixed_stage_pipes(N, na, nb, G)
     stage_roof = {}
-    for s in per_launch:
-        # the control-variate form forms the force bias inside its measurement (kept for the
-        # next step), so the "fb" stage of the step holds no work of its own
-        if launches_of[s] == 0 or stage[s] <= 0 or s == "fb":
+    for s in pipes:
+        if launches_of[s] == 0 or stage[s] <= 0:
             continue
         t = stage[s] / launches_of[s]
-        a = per_launch[s] / (t / 1e3) / 1e12
-        pp = FP64_NOMINAL_TFLOPS if s in fp64_stages else peak
-        stage_roof[s] = {"ms_per_launch": t, "achieved_tflops": a, "pipe": "fp64" if s in fp64_stages else "tensor",
-                         "peak_tflops": pp, "frac": a / pp}
+        fl_p = {p: f * W for p, f in pipes[s].items()}
+        bound_ms = sum(f / (pipe_peak[p] * 1e12) for p, f in fl_p.items()) * 1e3
+        stage_roof[s] = {"ms_per_launch": t, "gflop_per_launch": {p: f / 1e9 for p, f in fl_p.items()},
+                         "achieved_tflops": sum(fl_p.values()) / (t / 1e3) / 1e12,
+                         "bound_ms": bound_ms, "frac": bound_ms / t,
+                         "peaks_tflops": {p: pipe_peak[p] for p in fl_p}}
+    fp64_stages = ("overlap", "ortho")
     dom = max((s for s in stage_roof if s not in fp64_stages), key=lambda s: stage[s])
-    achieved = stage_roof[dom]["achieved_tflops"]
+    achieved = per_launch[dom] / (stage_roof[dom]["ms_per_launch"] / 1e3) / 1e12
     roof = {"bound": "tensor", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
             "frac": achieved / peak, "traffic": None,
             "peak_source": "%s bf16 sustained (MEASURED_PEAKS.json); algorithmic FLOPs of the stage per launch "
-                           "/ its CUDA-event time; the largest tensor-core stage (FP64 stages in stage_roofline)"
+                           "/ its CUDA-event time; the largest tensor-core stage (every stage against its pipes in "
+                           "stage_roofline; FP32 and FP64 peaks nominal)"
                            % src,
             "stage_roofline": stage_roof}
     out = {"metric": METRIC, "value": value, "unit": "walker-steps/s", "n_gpus": world, "steps": args.steps,

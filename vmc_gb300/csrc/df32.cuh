@@ -1,0 +1,115 @@
+// Double-FP32 ("double-float") arithmetic: a value is the unevaluated sum
+// h + l of two FP32 numbers with |l| <= ulp(h) / 2, about 48 significant bits,
+// computed on the FP32 pipe (this GPU's FP64 pipe runs a warp instruction in
+// ~64 cycles, its FP32 pipe in one).  The error-free transformations are the
+// published ones: Knuth's TwoSum (TAOCP vol. 2, 4.2.2), Dekker's Fast2Sum and
+// the FMA form of the exact product (Dekker, "A floating-point technique for
+// extending the available precision", Numer. Math. 18, 1971; Ogita, Rump,
+// Oishi, "Accurate sum and dot product", SIAM J. Sci. Comput. 26, 2005).
+// Every rounded product and sum that feeds an error term is written with the
+// _rn intrinsics, which the compiler never contracts into an FMA.
+#pragma once
+#include <cuda_runtime.h>
+
+namespace afqmc {
+
+struct df32 {
+  float h, l;
+};
+struct df32c {  // complex
+  df32 r, i;
+};
+
+// s + e == a + b exactly (any a, b)
+__device__ __forceinline__ void df_two_sum(float a, float b, float& s, float& e) {
+  s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+// s + e == a + b exactly when |a| >= |b| (or a == 0)
+__device__ __forceinline__ df32 df_fast(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  return {s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+__device__ __forceinline__ df32 df_neg(df32 a) { return {-a.h, -a.l}; }
+__device__ __forceinline__ df32 df_scale(df32 a, float p2) { return {a.h * p2, a.l * p2}; }  // p2 a power of two
+__device__ __forceinline__ df32 df_from_double(double x) {
+  const float h = (float)x;
+  return {h, (float)(x - (double)h)};
+}
+__device__ __forceinline__ double df_to_double(df32 a) { return (double)a.h + (double)a.l; }
+
+// a + b
+__device__ __forceinline__ df32 df_add(df32 a, df32 b) {
+  float s, e;
+  df_two_sum(a.h, b.h, s, e);
+  e = __fadd_rn(e, __fadd_rn(a.l, b.l));
+  return df_fast(s, e);
+}
+// a + f (f an FP32 number)
+__device__ __forceinline__ df32 df_add_f(df32 a, float f) {
+  float s, e;
+  df_two_sum(a.h, f, s, e);
+  return df_fast(s, __fadd_rn(e, a.l));
+}
+// a b
+__device__ __forceinline__ df32 df_mul(df32 a, df32 b) {
+  const float p = __fmul_rn(a.h, b.h);
+  float e = fmaf(a.h, b.h, -p);
+  e = fmaf(a.h, b.l, e);
+  e = fmaf(a.l, b.h, e);
+  return df_fast(p, e);
+}
+// x + a b + c d
+__device__ __forceinline__ df32 df_fma2(df32 x, df32 a, df32 b, df32 c, df32 d) {
+  const float p1 = __fmul_rn(a.h, b.h), e1 = fmaf(a.h, b.h, -p1);
+  const float p2 = __fmul_rn(c.h, d.h), e2 = fmaf(c.h, d.h, -p2);
+  float s1, t1, s2, t2;
+  df_two_sum(x.h, p1, s1, t1);
+  df_two_sum(s1, p2, s2, t2);
+  float lo = __fadd_rn(__fadd_rn(x.l, t1), __fadd_rn(t2, __fadd_rn(e1, e2)));
+  lo = fmaf(a.h, b.l, lo);
+  lo = fmaf(a.l, b.h, lo);
+  lo = fmaf(c.h, d.l, lo);
+  lo = fmaf(c.l, d.h, lo);
+  return df_fast(s2, lo);
+}
+// 1 / d (d > 0, normal): the rounded FP32 reciprocal q and one Newton
+// correction q (1 - d q), whose residual 1 - d.h q the FMA gives exactly
+__device__ __forceinline__ df32 df_recip(df32 d) {
+  const float q = __frcp_rn(d.h);
+  float e = fmaf(-d.h, q, 1.0f);
+  e = fmaf(-d.l, q, e);
+  return df_fast(q, __fmul_rn(q, e));
+}
+
+// complex x + a b
+__device__ __forceinline__ df32c dfc_fma(df32c x, df32c a, df32c b) {
+  return {df_fma2(x.r, a.r, b.r, df_neg(a.i), b.i), df_fma2(x.i, a.r, b.i, a.i, b.r)};
+}
+// complex x - a b
+__device__ __forceinline__ df32c dfc_fms(df32c x, df32c a, df32c b) {
+  return {df_fma2(x.r, df_neg(a.r), b.r, a.i, b.i), df_fma2(x.i, df_neg(a.r), b.i, df_neg(a.i), b.r)};
+}
+// complex a b
+__device__ __forceinline__ df32c dfc_mul(df32c a, df32c b) {
+  const df32 z = {0.f, 0.f};
+  return dfc_fma({z, z}, a, b);
+}
+// 2^k as an FP32 number, |k| <= 126
+__device__ __forceinline__ float df_pow2(int k) { return __int_as_float((127 + k) << 23); }
+// 1 / p: p scaled by a power of two so that max(|Re p|, |Im p|) is in [1, 2),
+// then conj(p') / |p'|^2 scaled back.  p == 0 gives a non-finite result, as a
+// division by zero does.
+__device__ __forceinline__ df32c dfc_recip(df32c p) {
+  const float m = fmaxf(fabsf(p.r.h), fabsf(p.i.h));
+  int k = ((__float_as_int(m) >> 23) & 255) - 127;
+  k = max(-126, min(126, k));
+  const float down = df_pow2(-k);
+  const df32c q = {df_scale(p.r, down), df_scale(p.i, down)};
+  const df32 z = {0.f, 0.f};
+  const df32 r = df_recip(df_fma2(z, q.r, q.r, q.i, q.i));
+  return {df_scale(df_mul(q.r, r), down), df_scale(df_neg(df_mul(q.i, r)), down)};
+}
+
+}  // namespace afqmc

@@ -12,6 +12,7 @@
 
 #include "afqmc_internal.h"
 #include "device_common.cuh"
+#include "df32.cuh"
 
 namespace afqmc {
 
@@ -129,8 +130,8 @@ __global__ void k_overlap_theta(const double2* __restrict__ psi, const double* _
 
 // Same results with one warp per (walker, channel), for n <= 32, and an LU
 // instead of Gauss-Jordan: M = Phi^T psi (FP64, register-tiled: lane
-// (li, lj) owns rows li + 4a and columns lj + 8b), partial-pivot LU of M in FP64
-// (pivot = first row of largest |M_ik|, det = sign * prod U_kk), then every
+// (li, lj) owns rows li + 4a and columns lj + 8b), partial-pivot LU of M (FP64
+// in the FP64 form, double-FP32 in the mixed form; det = sign * prod U_kk), then every
 // row p of theta from psi[p] . M^-1 with the LU factors (P M = L U => theta =
 // psi U^-1 L^-1 P): in the FP64 form by two triangular solves per row; in the
 // mixed form (FP32 from the FP32 copy of the walkers) by forming the n rows of
@@ -139,16 +140,104 @@ __global__ void k_overlap_theta(const double2* __restrict__ psi, const double* _
 // formed beforehand).
 constexpr int OW_WARPS = 4;
 
+__device__ __forceinline__ df32c ld_dfc(const float2* ah, const float2* al, int e) {
+  const float2 x = ah[e], y = al[e];
+  return {{x.x, y.x}, {x.y, y.y}};
+}
+__device__ __forceinline__ void st_dfc(float2* ah, float2* al, int e, df32c v) {
+  ah[e] = make_float2(v.r.h, v.i.h);
+  al[e] = make_float2(v.r.l, v.i.l);
+}
+
+// Partial-pivot LU, in place, of the n x n matrix (n <= 32) held in double-FP32
+// as high parts ah and low parts al ([n][n] row-major), by one warp: P M = L U
+// with unit-diagonal L below and U on and above the diagonal.  The pivot is the
+// first row of the largest |M_ik|^2 of the FP32 high parts (any near-largest
+// pivot is as good); perm[k] is the row swapped with k at step k.  Returns
+// det M = (-1)^swaps prod_k U_kk, the product formed in FP64 by a tree across
+// lanes, on every lane.  Each lane forms the pivot's reciprocal itself (no
+// broadcast), and the trailing update walks the (n-k-1)^2 block row-major in
+// steps of 32 entries without a division per entry.
+__device__ double2 lu_df32(float2* ah, float2* al, int* perm, int n, int lane) {
+  int nswap = 0;
+  for (int k = 0; k < n; ++k) {
+    int bi = k;
+    float best = -1.f;
+    for (int i = k + lane; i < n; i += 32) {
+      const float2 z = ah[i * n + k];
+      const float v = z.x * z.x + z.y * z.y;
+      if (v > best) { best = v; bi = i; }
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+      const float ob = __shfl_xor_sync(0xffffffffu, best, off);
+      const int oi = __shfl_xor_sync(0xffffffffu, bi, off);
+      if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+    }
+    if (lane == 0) perm[k] = bi;
+    if (bi != k) {
+      ++nswap;
+      for (int j = lane; j < n; j += 32) {
+        const float2 th = ah[k * n + j], tl = al[k * n + j];
+        ah[k * n + j] = ah[bi * n + j];
+        al[k * n + j] = al[bi * n + j];
+        ah[bi * n + j] = th;
+        al[bi * n + j] = tl;
+      }
+    }
+    __syncwarp();
+    const df32c inv = dfc_recip(ld_dfc(ah, al, k * n + k));
+    for (int i = k + 1 + lane; i < n; i += 32) st_dfc(ah, al, i * n + k, dfc_mul(ld_dfc(ah, al, i * n + k), inv));
+    __syncwarp();
+    const int rem = n - k - 1;
+    if (rem > 0) {
+      const int dq = 32 / rem, dr = 32 - dq * rem;  // 32 entries = dq rows + dr columns
+      int i = k + 1 + lane / rem, j = k + 1 + lane % rem;
+      for (int e = lane; e < rem * rem; e += 32) {
+        st_dfc(ah, al, i * n + j, dfc_fms(ld_dfc(ah, al, i * n + j), ld_dfc(ah, al, i * n + k), ld_dfc(ah, al, k * n + j)));
+        i += dq;
+        j += dr;
+        if (j >= n) {
+          j -= rem;
+          ++i;
+        }
+      }
+    }
+    __syncwarp();
+  }
+  double2 dv = make_double2(1.0, 0.0);
+  if (lane < n) {
+    const df32c u = ld_dfc(ah, al, lane * n + lane);
+    dv = make_double2(df_to_double(u.r), df_to_double(u.i));
+  }
+  for (int off = 16; off > 0; off >>= 1) {
+    double2 o;
+    o.x = __shfl_xor_sync(0xffffffffu, dv.x, off);
+    o.y = __shfl_xor_sync(0xffffffffu, dv.y, off);
+    dv = cmul(dv, o);
+  }
+  if (nswap & 1) dv = make_double2(-dv.x, -dv.y);
+  return dv;
+}
+
 // NM: n rounded up to a multiple of 4 (<= 32); lane (li, lj) of the M product
 // owns rows li + 4a (a < NM/4) and columns lj + 8b (b < ceil(NM/8)).
-// MB: M was formed beforehand (tensor-core overlap, mbuf[w][channel][i][j],
-// row stride n) and is read instead of computed here.
+// MB: M was formed beforehand (tensor-core overlap, mbuf[w][channel][i][j] as
+// double-FP32 (re hi, re lo, im hi, im lo), row stride n) and is read instead
+// of computed here (mixed form only).
+//
+// F32 (mixed form): the LU runs in double-FP32 arithmetic (lu_df32: ~48-bit
+// significands, error-free FP32 products and sums), which puts the O(n^3)
+// elimination on the FP32 pipe with a determinant accurate to ~1e-13; theta
+// then comes from the FP32 high parts of the factors.  The FP64 form follows
+// Eigen's PartialPivLU exactly (FP64 pivot search, first row of the largest
+// |M_ik|, FP64 reciprocal, running determinant).
 template <bool F32, int NM, bool MB>
 __global__ void __launch_bounds__(OW_WARPS * 32)
     k_overlap_lu(const double2* __restrict__ psi, const float2* __restrict__ psi32, const double* __restrict__ phi,
                  double* __restrict__ theta, float* __restrict__ theta32, double2* __restrict__ det,
                  const double* __restrict__ weights, int W, int N, int ncw, int nce, Channel c0, Channel c1,
-                 int only_live, int nmax, const double2* __restrict__ mbuf) {
+                 int only_live, int nmax, const float4* __restrict__ mbuf) {
+  static_assert(F32 || !MB, "M formed beforehand only in the mixed form");
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int s = blockIdx.y;
   const Channel ch = s == 0 ? c0 : c1;
@@ -158,8 +247,9 @@ __global__ void __launch_bounds__(OW_WARPS * 32)
   const size_t per_warp = ((size_t)nmax * nmax * (sizeof(double2) + sizeof(float2)) + nmax * sizeof(int) + 15) & ~(size_t)15;
   const size_t phs_bytes = MB ? 0 : (((size_t)nmax * N * sizeof(double) + 15) & ~(size_t)15);
   unsigned char* wbase = ow_raw + phs_bytes + warp * per_warp;
-  double2* a = (double2*)wbase;                                     // [n][n] LU, row-major
-  float2* af = (float2*)(wbase + (size_t)nmax * nmax * sizeof(double2));  // FP32 copy of the factors
+  double2* a = (double2*)wbase;  // FP64 form: [n][n] LU, row-major
+  float2* ah = (float2*)wbase;   // mixed form: [n][n] high parts, then [n][n] low parts
+  float2* al = ah + (size_t)nmax * nmax;
   int* perm = (int*)(wbase + (size_t)nmax * nmax * (sizeof(double2) + sizeof(float2)));
   if (!MB) {
     const double* ph = phi + (size_t)ch.col_off * N;
@@ -170,11 +260,14 @@ __global__ void __launch_bounds__(OW_WARPS * 32)
   if (w >= W) return;
   if (only_live && !(weights[w] > 1.0e-8)) return;
   const double2* ps = psi + (size_t)w * ncw * N + (size_t)ch.psi_off * N;
-  if (MB) {
-    const double2* mb = mbuf + ((size_t)w * 2 + s) * nmax * nmax;
-    for (int e = lane; e < n * n; e += 32) a[e] = mb[e];
+  if constexpr (MB) {
+    const float4* mb = mbuf + ((size_t)w * 2 + s) * nmax * nmax;
+    for (int e = lane; e < n * n; e += 32) {
+      const float4 v = mb[e];
+      ah[e] = make_float2(v.x, v.z);
+      al[e] = make_float2(v.y, v.w);
+    }
   } else {  // M = Phi^T psi
-
     constexpr int OW_RI = NM / 4, OW_RJ = (NM + 7) / 8;
     const int li = lane >> 3, lj = lane & 7;
     double2 acc[OW_RI][OW_RJ];
@@ -205,37 +298,23 @@ __global__ void __launch_bounds__(OW_WARPS * 32)
 #pragma unroll
       for (int y = 0; y < OW_RJ; ++y) {
         const int i = li + 4 * x, j = lj + 8 * y;
-        if (i < n && j < n) a[i * n + j] = acc[x][y];
+        if (i < n && j < n) {
+          if constexpr (F32) {
+            st_dfc(ah, al, i * n + j, {df_from_double(acc[x][y].x), df_from_double(acc[x][y].y)});
+          } else {
+            a[i * n + j] = acc[x][y];
+          }
+        }
       }
   }
   __syncwarp();
-  // LU with partial pivoting (FP64 factors).  The FP64 form follows Eigen's
-  // PartialPivLU exactly (FP64 pivot search, first row of the largest |M_ik|,
-  // FP64 reciprocal, running determinant).  The mixed form keeps the FP64
-  // factors and determinant but spends fewer FP64 instructions on the scalar
-  // work of each step, which on this GPU occupies the scarce FP64 pipe even
-  // when one lane is active: the pivot search compares |M_ik|^2 in FP32 (any
-  // near-largest pivot is as good), the reciprocal is an FP32 estimate with
-  // one FP64 Newton step (relative error ~1e-14), and the determinant is the
-  // product of U's diagonal formed at the end by a tree across lanes.
   double2 detv = make_double2(1.0, 0.0);
-  int nswap = 0;
-  for (int k = 0; k < n; ++k) {
-    int bi = k;
-    if (F32) {
-      float best = -1.f;
-      for (int i = k + lane; i < n; i += 32) {
-        const double2 z = a[i * n + k];
-        const float zx = (float)z.x, zy = (float)z.y;
-        const float v = zx * zx + zy * zy;
-        if (v > best) { best = v; bi = i; }
-      }
-      for (int off = 16; off > 0; off >>= 1) {
-        const float ob = __shfl_xor_sync(0xffffffffu, best, off);
-        const int oi = __shfl_xor_sync(0xffffffffu, bi, off);
-        if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
-      }
-    } else {
+  if constexpr (F32) {
+    detv = lu_df32(ah, al, perm, n, lane);
+  } else {
+    // LU with partial pivoting in FP64, as Eigen's PartialPivLU
+    for (int k = 0; k < n; ++k) {
+      int bi = k;
       double best = -1.0;
       for (int i = k + lane; i < n; i += 32) {
         const double v = cabs2(a[i * n + k]);
@@ -246,60 +325,33 @@ __global__ void __launch_bounds__(OW_WARPS * 32)
         const int oi = __shfl_xor_sync(0xffffffffu, bi, off);
         if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
       }
-    }
-    if (lane == 0) perm[k] = bi;
-    if (bi != k) {
-      ++nswap;
-      for (int j = lane; j < n; j += 32) {
-        const double2 t = a[k * n + j];
-        a[k * n + j] = a[bi * n + j];
-        a[bi * n + j] = t;
-      }
-    }
-    __syncwarp();
-    double2 inv = make_double2(0.0, 0.0);
-    if (F32) {
-      if (lane == 0) {
-        const double2 pv = a[k * n + k];
-        // 1 / pv = conj(pv) / |pv|^2, with 1 / |pv|^2 from FP32 and one Newton step
-        const double d = pv.x * pv.x + pv.y * pv.y;
-        if (d > 1e-30 && d < 1e30) {
-          double r = (double)(1.f / (float)d);
-          r = r * (2.0 - d * r);
-          inv = make_double2(pv.x * r, -pv.y * r);
-        } else {
-          inv = crecip(pv);  // outside FP32's comfortable range
+      if (lane == 0) perm[k] = bi;
+      if (bi != k) {
+        for (int j = lane; j < n; j += 32) {
+          const double2 t = a[k * n + j];
+          a[k * n + j] = a[bi * n + j];
+          a[bi * n + j] = t;
         }
       }
-    } else if (lane == 0) {
-      const double2 pv = a[k * n + k];
-      detv = cmul(detv, pv);
-      if (bi != k) detv = make_double2(-detv.x, -detv.y);
-      inv = crecip(pv);
+      __syncwarp();
+      double2 inv = make_double2(0.0, 0.0);
+      if (lane == 0) {
+        const double2 pv = a[k * n + k];
+        detv = cmul(detv, pv);
+        if (bi != k) detv = make_double2(-detv.x, -detv.y);
+        inv = crecip(pv);
+      }
+      inv.x = __shfl_sync(0xffffffffu, inv.x, 0);
+      inv.y = __shfl_sync(0xffffffffu, inv.y, 0);
+      for (int i = k + 1 + lane; i < n; i += 32) a[i * n + k] = cmul(a[i * n + k], inv);
+      __syncwarp();
+      const int rem = n - k - 1;
+      for (int e = lane; e < rem * rem; e += 32) {
+        const int i = k + 1 + e / rem, j = k + 1 + e % rem;
+        a[i * n + j] = csub(a[i * n + j], cmul(a[i * n + k], a[k * n + j]));
+      }
+      __syncwarp();
     }
-    inv.x = __shfl_sync(0xffffffffu, inv.x, 0);
-    inv.y = __shfl_sync(0xffffffffu, inv.y, 0);
-    for (int i = k + 1 + lane; i < n; i += 32) a[i * n + k] = cmul(a[i * n + k], inv);
-    __syncwarp();
-    const int rem = n - k - 1;
-    for (int e = lane; e < rem * rem; e += 32) {
-      const int i = k + 1 + e / rem, j = k + 1 + e % rem;
-      a[i * n + j] = csub(a[i * n + j], cmul(a[i * n + k], a[k * n + j]));
-    }
-    __syncwarp();
-  }
-  if (F32) {
-    // det = (-1)^swaps prod_k U_kk by a tree product across lanes
-    double2 dv = lane < n ? a[lane * n + lane] : make_double2(1.0, 0.0);
-    for (int k2 = lane + 32; k2 < n; k2 += 32) dv = cmul(dv, a[k2 * n + k2]);
-    for (int off = 16; off > 0; off >>= 1) {
-      double2 o;
-      o.x = __shfl_xor_sync(0xffffffffu, dv.x, off);
-      o.y = __shfl_xor_sync(0xffffffffu, dv.y, off);
-      dv = cmul(dv, o);
-    }
-    if (nswap & 1) dv = make_double2(-dv.x, -dv.y);
-    detv = dv;
   }
   if (lane == 0) det[2 * w + s] = detv;
   // perm[k]: row swapped with k at step k -> final row order of P M
@@ -313,8 +365,6 @@ __global__ void __launch_bounds__(OW_WARPS * 32)
     }
     for (int k = 0; k < n; ++k) perm[k] = order[k];
   }
-  if (F32)
-    for (int e = lane; e < n * n; e += 32) af[e] = make_float2((float)a[e].x, (float)a[e].y);
   __syncwarp();
   // theta[p][:] = psi[p][:] M^-1 ; with P M = L U: w U = psi[p], z L = w, theta[perm[k]] = z[k]
   if (F32) {
@@ -322,10 +372,10 @@ __global__ void __launch_bounds__(OW_WARPS * 32)
     float* tim = tre + (size_t)nce * N;
     // FP32: lane j < n forms row j of G = U^-1 L^-1 (the same two solves with
     // psi[p] = e_j), stored with its columns in theta order, G[j][perm[k]] =
-    // z[k], over the FP64 factors (no longer needed); then every orbital row
+    // z[k]; then every orbital row
     // of theta is psi32[p][:] G.  n solves instead of N, and the row products
-    // read G by broadcast.
-    float2* G = reinterpret_cast<float2*>(a);  // [n][n]
+    // read G by broadcast.  The solves use the FP32 high parts of the factors.
+    float2* G = al;  // [n][n], over the low parts (no longer needed)
     if (lane < n) {
       float2 r[NM];
 #pragma unroll
@@ -337,11 +387,11 @@ __global__ void __launch_bounds__(OW_WARPS * 32)
 #pragma unroll
           for (int i = 0; i < NM; ++i)
             if (i < j) {
-              const float2 u = af[i * n + j];
+              const float2 u = ah[i * n + j];
               t.x -= r[i].x * u.x - r[i].y * u.y;
               t.y -= r[i].x * u.y + r[i].y * u.x;
             }
-          const float2 d = af[j * n + j];
+          const float2 d = ah[j * n + j];
           const float den = d.x * d.x + d.y * d.y;
           r[j] = make_float2((t.x * d.x + t.y * d.y) / den, (t.y * d.x - t.x * d.y) / den);
         }
@@ -353,7 +403,7 @@ __global__ void __launch_bounds__(OW_WARPS * 32)
 #pragma unroll
           for (int i = 0; i < NM; ++i)
             if (i > jj && i < n) {
-              const float2 l = af[i * n + jj];
+              const float2 l = ah[i * n + jj];
               t.x -= r[i].x * l.x - r[i].y * l.y;
               t.y -= r[i].x * l.y + r[i].y * l.x;
             }

@@ -9,14 +9,18 @@
 // a_s b_t is an integer of at most 2^14, and the sum of the products of one
 // level L = s + t (at most 7 slice pairs x 128 orbitals) stays below 2^24
 // (7 x 128 x 2^14), so the FP32 TMEM accumulator of each level holds it
-// exactly.  The seven levels L < 7 are combined in FP64:
+// exactly.  The seven levels L < 7 are combined as
 //
 //   M_ij = sigma_j tau_i 2^-14 sum_L 2^-8L D_L[j][i]
 //
 // which drops only the slice pairs with s + t >= 7, ~2^-56 of a product (the
-// FP64 overlap this replaces carries ~2^-53 N).  The LU, determinant and theta
-// solves then run as before (DQMC/RHF.cpp:52-64, DQMC/UHF.cpp:57-68 for the
-// overlap; the force-bias theta of :71-91), reading M.
+// FP64 overlap this replaces carries ~2^-53 N).  The sum is formed in
+// double-FP32 (Horner over the exact integer levels with error-free sums) and
+// scaled by the powers of two exactly, so M leaves as a double-FP32 pair
+// (~48 bits) without an FP64 instruction: the LU that follows runs in the
+// same arithmetic.  The LU, determinant and theta solves then run as before
+// (DQMC/RHF.cpp:52-64, DQMC/UHF.cpp:57-68 for the overlap; the force-bias theta
+// of :71-91), reading M.
 //
 // The slices are cut with 32-bit integer arithmetic from the bits of each
 // double: the FP64 pipe of this GPU is its scarce unit (64-bit integer work
@@ -41,6 +45,7 @@
 
 #include "afqmc_internal.h"
 #include "device_common.cuh"
+#include "df32.cuh"
 #include "tcgen05.cuh"
 
 namespace afqmc {
@@ -100,6 +105,8 @@ __device__ __forceinline__ void oz_slices_bits(double x, int e, float* a) {
 
 // biased FP64 exponent of x (0 for zero and subnormals)
 __device__ __forceinline__ int oz_biased(double x) { return (__double2hiint(x) >> 20) & 0x7FF; }
+// the FP32 number equal to x = 2^k (a power of two, |k| <= 126), from its bits
+__device__ __forceinline__ float oz_pow2f(double x) { return __int_as_float((oz_biased(x) - 1023 + 127) << 23); }
 // row scale sigma = 2^e, e = 1 + the largest unbiased exponent of the row (0 if all zero)
 __device__ __forceinline__ int oz_row_e(int max_biased) { return max_biased > 0 ? max_biased - 1022 : 0; }
 
@@ -185,7 +192,7 @@ struct OzArgs {
   int bimg_bytes;
   const double* sig;    // row scales, channel blocks of rpad rows
   const double* tau;    // [channel][BNP] orbital scales
-  double2* M;           // [W][2][nmax][nmax]
+  float4* M;            // [W][2][nmax][nmax] double-FP32 (re hi, re lo, im hi, im lo)
   int rpad;             // rows per channel block (multiple of 128)
   int nw;               // walkers
   int nmax, KP, BNP, tmem_cols;
@@ -284,8 +291,9 @@ __global__ void __launch_bounds__(128, 1)
     const int nn = max(n_c, 1);
     const int w = q / nn, j = q % nn;
     const bool valid = n_c > 0 && q < g.nw * n_c;
-    const double sg = valid ? g.sig[rg] * (1.0 / 16384.0) : 0.0;
-    double* Md = (double*)g.M;
+    // sigma 2^-14 and tau are powers of two: their FP32 images by exponent
+    const float sg = valid ? oz_pow2f(g.sig[rg]) * (1.0f / 16384.0f) : 0.f;
+    float* Mf = (float*)g.M;
     const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
 #pragma unroll 1
     for (int cb = 0; cb < g.BNP; cb += 16) {
@@ -297,11 +305,12 @@ __global__ void __launch_bounds__(128, 1)
         for (int qq = 0; qq < 16; ++qq) {
           const int i = cb + qq;
           if (i >= n_c) continue;
-          double v = (double)d[OZ_S - 1][qq];
+          df32 v = {d[OZ_S - 1][qq], 0.f};
 #pragma unroll
-          for (int L = OZ_S - 2; L >= 0; --L) v = v * (1.0 / 256.0) + (double)d[L][qq];
-          v *= sg * g.tau[chn * g.BNP + i];
-          Md[2 * (((size_t)w * 2 + chn) * g.nmax * g.nmax + (size_t)i * n_c + j) + part] = v;
+          for (int L = OZ_S - 2; L >= 0; --L) v = df_add_f(df_scale(v, 1.0f / 256.0f), d[L][qq]);
+          v = df_scale(v, sg * oz_pow2f(g.tau[chn * g.BNP + i]));
+          *(float2*)(Mf + 4 * (((size_t)w * 2 + chn) * g.nmax * g.nmax + (size_t)i * n_c + j) + 2 * part) =
+              make_float2(v.h, v.l);
         }
       }
     }
