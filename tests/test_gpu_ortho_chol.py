@@ -2,10 +2,10 @@
 with the reference's (Eigen's) column convention.
 
 The two factorisations give the same Q up to the sign of each column: the
-Cholesky-QR's Gram matrix is formed in FP32, so its Q is orthonormal to ~1e-7
-and is checked against Householder's to 1e-6.  What keeps the walk exact is
-that the stored overlap is the overlap of the returned Q: checked against the
-FP64 oracle's overlap of those dets to 1e-10.  Every physical quantity is
+Cholesky-QR's Gram matrix, Cholesky factor and R^-1 are FP32, so its Q is
+orthonormal to ~1e-6 and is checked against Householder's to 5e-6.  What keeps
+the walk exact is that the stored overlap is the overlap of the returned Q:
+checked against the FP64 oracle's overlap of those dets to 1e-10.  Every physical quantity is
 unchanged: the local energies after either QR are within 2e-5 Eh of the FP64
 oracle's energies of the walkers before it (the mixed form's local-energy
 tolerance), and one further step with identical fields gives the same weights
@@ -62,15 +62,18 @@ def test_cholesky_qr_equals_householder_up_to_column_signs(A, kind):
     dh, oh_, elh, w1h = out["householder"]
     dc, oc, elc, w1c = out["cholesky"]
     qh, qc = dh, dc  # (W, N, columns): alpha columns, then beta for the unrestricted walker
+    dq, dg = 0.0, 0.0
     for w in range(W):
         sgn = np.sign(np.einsum("pj,pj->j", qh[w].conj(), qc[w]).real)
         assert np.all(np.abs(sgn) == 1)
-        assert np.abs(qc[w] - qh[w] * sgn[None]).max() < 1e-6
+        dq = max(dq, np.abs(qc[w] - qh[w] * sgn[None]).max())
         # orthonormal columns per spin block
         blocks = [(0, na)] if rw else [(0, na), (na, na + nb)]
         for a, b in blocks:
             g = qc[w][:, a:b].conj().T @ qc[w][:, a:b]
-            assert np.abs(g - np.eye(b - a)).max() < 1e-6
+            dg = max(dg, np.abs(g - np.eye(b - a)).max())
+    print("cholesky-qr: |Q - Q_householder| %.2e, |Q^H Q - I| %.2e" % (dq, dg))
+    assert dq < 5e-6 and dg < 5e-6
     ref_o = O.overlap(ot, O.Walkers(oh, rw, dc))
     assert np.abs(oc / ref_o - 1).max() < 1e-10
     ref_h = O.overlap(ot, O.Walkers(oh, rw, dh))

@@ -10,6 +10,7 @@
 // _rn intrinsics, which the compiler never contracts into an FMA.
 #pragma once
 #include <cuda_runtime.h>
+#include <stdint.h>
 
 namespace afqmc {
 
@@ -82,6 +83,37 @@ __device__ __forceinline__ df32 df_recip(df32 d) {
   e = fmaf(-d.l, q, e);
   return df_fast(q, __fmul_rn(q, e));
 }
+
+// x split exactly into a double-FP32 pair with 32-bit integer operations (no
+// FP64 instruction): h = x rounded to nearest FP32 (ties to even), l = x - h
+// rounded to FP32 (x - h is at most 29 significant bits).  Values below 2^-74
+// in magnitude, where l would leave the FP32 normal range, give l = 0 (h too
+// below 2^-126); magnitudes of 2^128 and more, infinities and NaN give h = (float)x.
+__device__ __forceinline__ df32 df_split_bits(double x) {
+  const uint32_t whi = (uint32_t)__double2hiint(x), wlo = (uint32_t)__double2loint(x);
+  const int E = (int)((whi >> 20) & 0x7FFu) - 1023;
+  if (E > 127) return {(float)x, 0.f};  // beyond FP32 range, infinities, NaN
+  if (E < -126) return {0.f, 0.f};
+  const uint32_t sign = whi & 0x80000000u;
+  const uint32_t m23 = ((whi & 0xFFFFFu) << 3) | (wlo >> 29);
+  const uint32_t low29 = wlo & 0x1FFFFFFFu;
+  const bool up = low29 > 0x10000000u || (low29 == 0x10000000u && (m23 & 1u));
+  const float h = __uint_as_float((sign | ((uint32_t)(E + 127) << 23) | m23) + (up ? 1u : 0u));
+  if (E < -74) return {h, 0.f};
+  const int li = up ? (int)low29 - 0x20000000 : (int)low29;  // (|x| - |h|) / 2^(E - 52)
+  const float l = (float)li * __int_as_float((E - 52 + 127) << 23);
+  return {h, sign ? -l : l};
+}
+// FP32 -> FP64 by the bits (exact; subnormal FP32 inputs give a signed zero)
+__device__ __forceinline__ double df_f2d_bits(float f) {
+  const uint32_t b = __float_as_uint(f);
+  const uint32_t e8 = (b >> 23) & 255u;
+  const uint32_t ex = e8 == 0u ? 0u : (e8 == 255u ? 0x7FFu : e8 + 896u);
+  const uint32_t m = e8 == 0u ? 0u : (b & 0x7FFFFFu);
+  return __hiloint2double((int)((b & 0x80000000u) | (ex << 20) | (m >> 3)), (int)((m & 7u) << 29));
+}
+// the double nearest h + l: two exact conversions and one FP64 addition
+__device__ __forceinline__ double df_to_double_bits(df32 a) { return df_f2d_bits(a.h) + df_f2d_bits(a.l); }
 
 // complex x + a b
 __device__ __forceinline__ df32c dfc_fma(df32c x, df32c a, df32c b) {

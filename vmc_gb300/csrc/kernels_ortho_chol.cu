@@ -1,6 +1,6 @@
 // Cholesky-QR orthonormalisation of the walkers (mixed form):
 //     G = psi_s^H psi_s,   G = R^H R (R upper triangular, positive real diagonal),
-//     psi_s <- psi_s R^-1,  overlap /= prod_s prod_k R_kk  (squared for the restricted walker)
+//     X = R^-1,  psi_s <- psi_s X,  overlap *= prod_s prod_k X_kk  (squared for the restricted walker)
 // per spin block s.  This is the reference's orthogonalize
 // (DQMC/DQMCWalker.cpp:295-326) with a different factorisation: Householder QR
 // (Eigen) gives R_kk = beta_k of either sign, Cholesky-QR gives |beta_k|, so
@@ -14,38 +14,60 @@
 // no overlap or theta recompute follows; the per-channel determinants are
 // recomputed by the next step before they are used.
 //
-// Precision: R only has to make Q well conditioned -- whatever R is used, the
-// walker stays the same as long as psi R^-1 and overlap / det R are formed
-// with that same R.  So the Gram matrix is formed in FP32 from the FP32 copy of
-// psi (Q orthonormal to ~1e-7), while the Cholesky factor, R^-1, Q = psi R^-1
-// and det R are FP64: the stored overlap stays det(Phi^T Q) to FP64 accuracy.
+// Precision: the walker is the column span of psi_s together with the stored
+// overlap, and psi_s -> psi_s X for ANY invertible upper-triangular X is the
+// same walker once the overlap is multiplied by det X = prod_k X_kk.  X only
+// has to make Q = psi_s X well conditioned, so the Gram matrix, its Cholesky
+// factor R and X = R^-1 are FP32 (Q orthonormal to ~1e-6; the next
+// orthonormalisation starts from there).  What must be exact is that Q and the
+// overlap factor belong to the same X: Q = psi_s X is a compensated
+// double-FP32 dot product (psi_s split exactly into FP32 pairs, X's entries
+// FP32 numbers, products error-free and their sum carried in a pair: ~1e-14),
+// and prod_k X_kk is formed in FP64.  psi_s leaves as the FP64 nearest to the
+// pair, psi32 as its high part.  None of it runs on the FP64 pipe but the one
+// addition per stored number and the n multiplications of the determinant.
 //
-// One CTA (256 threads) per walker, both spin blocks in turn; the block, the
-// Gram/R matrix and R^-1 live in shared memory.  Dead walkers (weight <= 1e-8)
-// are skipped: they are never propagated again, and the comb only copies live
-// walkers over them.  A block whose Gram matrix is not numerically positive
-// definite is left unchanged (the overlap stays consistent with it).
+// One CTA (256 threads) per walker, both spin blocks in turn; the block (as
+// high and low parts), the Gram/R matrix and X live in shared memory.  Dead
+// walkers (weight <= 1e-8) are skipped: they are never propagated again, and
+// the comb only copies live walkers over them.  A block whose Gram matrix is
+// not numerically positive definite is left unchanged (the overlap stays
+// consistent with it).
 #include <cuda_runtime.h>
 
 #include <algorithm>
 
 #include "afqmc_internal.h"
 #include "device_common.cuh"
+#include "df32.cuh"
 
 namespace afqmc {
 
 constexpr int OC_THREADS = 256;
+
+// x + a b for a double-FP32 a and an FP32 b, accumulated as Ogita-Rump-Oishi's
+// Dot2: s carries the rounded sum of the high products, c the sum of every
+// rounding error (TwoSum of s, TwoProduct of a.h b) and of the low products.
+__device__ __forceinline__ void dot2_acc(float& s, float& c, float ah, float al, float b) {
+  const float p = __fmul_rn(ah, b);
+  const float pe = fmaf(ah, b, -p);
+  float t, e;
+  df_two_sum(s, p, t, e);
+  s = t;
+  c = __fadd_rn(c, __fadd_rn(e, pe));
+  c = fmaf(al, b, c);
+}
 
 __global__ void __launch_bounds__(OC_THREADS)
     k_ortho_chol(double2* __restrict__ psi, float2* __restrict__ psi32, double2* __restrict__ ovlp,
                  const double* __restrict__ weights, int N, int ncw, int na, int nb, int rhf_walker, int nmax) {
   const int w = blockIdx.x;
   if (!(weights[w] > 1.0e-8)) return;
-  extern __shared__ double2 oc_sm[];
-  double2* A = oc_sm;                          // [nmax][N]     spin block, column-major
-  double2* R = A + (size_t)nmax * N;           // [nmax][nmax]  Gram, then R in its upper triangle (R[i * n + j])
-  double2* Ri = R + (size_t)nmax * nmax;       // [nmax][nmax]  R^-1, upper (Ri[i * n + j])
-  float2* A32 = reinterpret_cast<float2*>(Ri + (size_t)nmax * nmax);  // [nmax][N] FP32 copy of the block
+  extern __shared__ float2 oc_sm[];
+  float2* Ah = oc_sm;                      // [nmax][N] spin block, high parts, column-major
+  float2* Al = Ah + (size_t)nmax * N;      // [nmax][N] low parts
+  float2* R = Al + (size_t)nmax * N;       // [nmax][nmax] Gram, then R in its upper triangle (R[i * n + j])
+  float2* X = R + (size_t)nmax * nmax;     // [nmax][nmax] X = R^-1, upper (X[i * n + j])
   __shared__ int s_bad;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   double fac = 1.0;  // thread 0
@@ -55,10 +77,12 @@ __global__ void __launch_bounds__(OC_THREADS)
     if (n == 0) continue;
     double2* Ag = psi + ((size_t)w * ncw + off) * N;
     float2* Ag32 = psi32 + ((size_t)w * ncw + off) * N;
-    __syncthreads();  // A, R, Ri free (previous block done)
+    __syncthreads();  // Ah, Al, R, X free (previous block done)
     for (int e = tid; e < n * N; e += OC_THREADS) {
-      A[e] = Ag[e];
-      A32[e] = Ag32[e];
+      const double2 v = Ag[e];
+      const df32 re = df_split_bits(v.x), im = df_split_bits(v.y);
+      Ah[e] = make_float2(re.h, im.h);
+      Al[e] = make_float2(re.l, im.l);
     }
     if (tid == 0) s_bad = 0;
     __syncthreads();
@@ -66,8 +90,8 @@ __global__ void __launch_bounds__(OC_THREADS)
     for (int e = tid; e < n * n; e += OC_THREADS) {
       const int i = e / n, j = e % n;
       if (i > j) continue;
-      const float2* ai = A32 + (size_t)i * N;
-      const float2* aj = A32 + (size_t)j * N;
+      const float2* ai = Ah + (size_t)i * N;
+      const float2* aj = Ah + (size_t)j * N;
       float sr = 0.f, si = 0.f, tr = 0.f, ti = 0.f;
       int p = 0;
       for (; p + 1 < N; p += 2) {
@@ -82,30 +106,37 @@ __global__ void __launch_bounds__(OC_THREADS)
         sr += x0.x * y0.x + x0.y * y0.y;
         si += x0.x * y0.y - x0.y * y0.x;
       }
-      R[i * n + j] = make_double2((double)(sr + tr), (double)(si + ti));
+      R[i * n + j] = make_float2(sr + tr, si + ti);
     }
     __syncthreads();
-    // Cholesky (warp 0): row k of R from G and rows m < k
+    // Cholesky (warp 0, FP32): row k of R from G and rows m < k
     if (warp == 0) {
       bool bad = false;
       for (int k = 0; k < n; ++k) {
-        double dkk = 0.0;
+        float dkk = 0.f;
         if (lane == 0) {
-          double d = R[k * n + k].x;
-          for (int m = 0; m < k; ++m) d -= cabs2(R[m * n + k]);
-          if (!(d > 0.0) || !isfinite(d)) {
-            bad = true;
-            d = 1.0;
+          float d = R[k * n + k].x;
+          for (int m = 0; m < k; ++m) {
+            const float2 r = R[m * n + k];
+            d -= r.x * r.x + r.y * r.y;
           }
-          dkk = sqrt(d);
-          R[k * n + k] = make_double2(dkk, 0.0);
+          if (!(d > 0.f) || !isfinite(d)) {
+            bad = true;
+            d = 1.f;
+          }
+          dkk = sqrtf(d);
+          R[k * n + k] = make_float2(dkk, 0.f);
         }
         dkk = __shfl_sync(0xffffffffu, dkk, 0);
-        const double inv = 1.0 / dkk;
+        const float inv = 1.f / dkk;
         for (int j = k + 1 + lane; j < n; j += 32) {
-          double2 g = R[k * n + j];
-          for (int m = 0; m < k; ++m) g = csub(g, cmul(cconj(R[m * n + k]), R[m * n + j]));
-          R[k * n + j] = make_double2(g.x * inv, g.y * inv);
+          float2 g = R[k * n + j];
+          for (int m = 0; m < k; ++m) {
+            const float2 a = R[m * n + k], c = R[m * n + j];  // g -= conj(a) c
+            g.x -= a.x * c.x + a.y * c.y;
+            g.y -= a.x * c.y - a.y * c.x;
+          }
+          R[k * n + j] = make_float2(g.x * inv, g.y * inv);
         }
         __syncwarp();
       }
@@ -113,38 +144,49 @@ __global__ void __launch_bounds__(OC_THREADS)
     }
     __syncthreads();
     if (s_bad) continue;  // leave this block as it is
-    // R^-1 by columns: thread j solves R x = e_j by back substitution
+    // X = R^-1 by columns (FP32): thread j solves R x = e_j by back substitution
     for (int j = tid; j < n; j += OC_THREADS) {
-      Ri[j * n + j] = make_double2(1.0 / R[j * n + j].x, 0.0);
+      X[j * n + j] = make_float2(1.f / R[j * n + j].x, 0.f);
       for (int i = j - 1; i >= 0; --i) {
-        double2 s = make_double2(0.0, 0.0);
-        for (int m = i + 1; m <= j; ++m) s = cfma(R[i * n + m], Ri[m * n + j], s);
-        const double inv = 1.0 / R[i * n + i].x;
-        Ri[i * n + j] = make_double2(-s.x * inv, -s.y * inv);
+        float2 t = make_float2(0.f, 0.f);
+        for (int m = i + 1; m <= j; ++m) {
+          const float2 r = R[i * n + m], x = X[m * n + j];
+          t.x += r.x * x.x - r.y * x.y;
+          t.y += r.x * x.y + r.y * x.x;
+        }
+        const float inv = 1.f / R[i * n + i].x;
+        X[i * n + j] = make_float2(-t.x * inv, -t.y * inv);
       }
     }
     __syncthreads();
-    // Q = A R^-1: Q[j][p] = sum_{i <= j} A[i][p] Ri[i][j]
+    // Q = A X: Q[j][p] = sum_{i <= j} A[i][p] X[i][j], compensated
     for (int e = tid; e < n * N; e += OC_THREADS) {
       const int j = e / N, p = e % N;
-      double2 q = make_double2(0.0, 0.0);
-      for (int i = 0; i <= j; ++i) q = cfma(A[(size_t)i * N + p], Ri[i * n + j], q);
-      Ag[e] = q;
-      Ag32[e] = make_float2((float)q.x, (float)q.y);
+      float sr = 0.f, cr = 0.f, si = 0.f, ci = 0.f;
+      for (int i = 0; i <= j; ++i) {
+        const float2 h = Ah[(size_t)i * N + p], l = Al[(size_t)i * N + p], x = X[i * n + j];
+        dot2_acc(sr, cr, h.x, l.x, x.x);
+        dot2_acc(sr, cr, -h.y, -l.y, x.y);
+        dot2_acc(si, ci, h.x, l.x, x.y);
+        dot2_acc(si, ci, h.y, l.y, x.x);
+      }
+      const df32 qr = df_fast(sr, cr), qi = df_fast(si, ci);
+      Ag[e] = make_double2(df_to_double_bits(qr), df_to_double_bits(qi));
+      Ag32[e] = make_float2(qr.h, qi.h);
     }
     if (tid == 0)
-      for (int k = 0; k < n; ++k) fac *= R[k * n + k].x;
+      for (int k = 0; k < n; ++k) fac *= (double)X[k * n + k].x;
   }
   if (tid == 0) {
     if (rhf_walker) fac *= fac;
     const double2 o = ovlp[w];
-    ovlp[w] = make_double2(o.x / fac, o.y / fac);
+    ovlp[w] = make_double2(o.x * fac, o.y * fac);
   }
 }
 
 size_t ortho_chol_smem(const afqmc_handle* h) {
   const size_t nmax = (size_t)std::max(h->na, h->rhf_walker ? 0 : h->nb);
-  return (nmax * h->N + 2 * nmax * nmax) * sizeof(double2) + nmax * h->N * sizeof(float2);
+  return (2 * nmax * h->N + 2 * nmax * nmax) * sizeof(float2);
 }
 
 bool ortho_chol_available(const afqmc_handle* h) {
