@@ -68,7 +68,6 @@ def dist_env():
             int(os.environ.get("LOCAL_RANK", "0")))
 
 
-FP64_NOMINAL_TFLOPS = 1.25  # GB300 FP64 (nominal; the FP64 pipe, not the tensor cores)
 
 
 def fp32_nominal_tflops(sm_mhz=2070.0):
@@ -76,41 +75,36 @@ def fp32_nominal_tflops(sm_mhz=2070.0):
     return 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
 
 
+# executed cost per algorithmic multiply-add of the mixed form's emulated arithmetic
+SPLIT_BF16_PASSES = 3   # hi*hi + lo*hi + hi*lo tensor-core products per FP32-accurate product
+OZAKI_PAIRS = 28        # slice pairs of levels 0..6 (7 slices per operand) per FP64-accurate product
+DF32_LU_OPS = 14        # FP32 instructions per double-FP32 complex-part multiply-add in the LU
+DF32_DOT_OPS = 11       # FP32 instructions per multiply-add of the compensated (Dot2) product Q = psi X
+
+
 def mixed_stage_pipes(N, na, nb, G):
-    """Algorithmic FLOPs per walker of each stage of the mixed form, split by the
-    pipe that executes them (complex multiply-add = 8 FLOPs, real x complex = 4):
-      vhs      packed-triangle VHS on the tensor cores;
-      prop     B exp-Taylor B products on the tensor cores;
-      overlap  M = Phi^T psi on the tensor cores (exact BF16 slices), the LU, the
-               inverse rows and theta = psi M^-1 in FP32 on the CUDA cores;
-      ortho    Cholesky-QR: Hermitian Gram psi^H psi in FP32, Cholesky, R^-1 and
-               Q = psi R^-1 in FP64.
+    """Work per walker of each stage of the mixed form: for each part, its
+    algorithmic FLOPs (complex multiply-add = 8, real x complex = 4), the pipe
+    that executes it and the executed instructions per algorithmic multiply-add
+    (the bound of the part is FLOPs x cost / the pipe's peak):
+      vhs      packed-triangle VHS: split-BF16 tensor-core products;
+      prop     B exp-Taylor B products: split-BF16 tensor-core products;
+      overlap  M = Phi^T psi by exact BF16 slices on the tensor cores, the LU in
+               double-FP32, the inverse rows and theta = psi M^-1 in FP32;
+      ortho    Cholesky-QR: Gram, Cholesky and R^-1 in FP32, Q = psi R^-1 as a
+               compensated double-FP32 product.
     The force bias of the control-variate form runs inside its measurement."""
     T = N * (N + 1) // 2
     ns = [na, nb]
     return {
-        "vhs": {"tensor": 4 * T * G},
-        "prop": {"tensor": sum(48 * N * N * n for n in ns)},
-        "overlap": {"tensor": sum(4 * n * n * N for n in ns),
-                    "fp32": sum(8 * n ** 3 / 3 + 8 * n ** 3 + 8 * N * n * n for n in ns)},
-        "ortho": {"fp32": sum(4 * N * n * n for n in ns),
-                  "fp64": sum(8 * n ** 3 / 3 + 8 * n ** 3 / 3 + 4 * N * n * n for n in ns)},
+        "vhs": [("bf16x3", 4 * T * G, "tensor", SPLIT_BF16_PASSES)],
+        "prop": [("bf16x3", sum(48 * N * N * n for n in ns), "tensor", SPLIT_BF16_PASSES)],
+        "overlap": [("ozaki bf16 slices", sum(4 * n * n * N for n in ns), "tensor", OZAKI_PAIRS),
+                    ("double-fp32 LU", sum(8 * n ** 3 / 3 for n in ns), "fp32", DF32_LU_OPS),
+                    ("fp32 inverse rows + theta", sum(8 * n ** 3 + 8 * N * n * n for n in ns), "fp32", 1)],
+        "ortho": [("fp32 Gram + Cholesky + R^-1", sum(4 * N * n * n + 8 * n ** 3 / 3 for n in ns), "fp32", 1),
+                  ("double-fp32 Q = psi R^-1", sum(4 * N * n * n for n in ns), "fp32", DF32_DOT_OPS)],
     }
-
-
-def flops_model(N, na, nb, G, ortho_every=ORTHO_EVERY):
-    """Algorithmic FLOPs per walker: force bias, VHS, propagator with
-    a real exp(-dt/2 h1') (2 real x complex + 5 complex x complex products per
-    spin), overlap, QR amortised, and one exact local energy."""
-    T = N * (N + 1) // 2
-    ns = [na, nb]
-    fb = sum(4 * n * n * N + 16 * n ** 3 + 8 * N * n * n + 4 * n * N * G for n in ns)
-    vhs = 4 * T * G
-    prop = sum(48 * N * N * n for n in ns)
-    ovl = sum(4 * n * n * N + 5.3 * n ** 3 for n in ns)
-    qr = sum(32 * N * n * n for n in ns) / ortho_every
-    el = sum(4 * G * n * n * N + 8 * G * n * n + 4 * n * N for n in ns)
-    return dict(fb=fb, vhs=vhs, prop=prop, overlap=ovl, ortho=qr, energy=el, step=fb + vhs + prop + ovl + qr)
 
 
 class Clocks:
@@ -425,31 +419,30 @@ def main():
     launches_of = {s: args.steps for s in per_launch}
     launches_of["ortho"] = max(1, args.steps // ORTHO_EVERY)
     peak = pk["bf16_tflops_sustained"] if "bf16_tflops_sustained" in pk else pk["bf16_tflops"]
-    # every stage against the pipes that execute it: its bound is the sum over those
-    # pipes of (FLOPs on the pipe / the pipe's peak) -- tensor cores at the measured
-    # bf16 peak, FP32 and FP64 CUDA cores at their nominal rates (no measured FP32 or
-    # FP64 peak exists for this GPU pool) -- and frac = bound time / measured time
-    pipe_peak = {"tensor": peak, "fp32": fp32_nominal_tflops(), "fp64": FP64_NOMINAL_TFLOPS}
+    # every stage against the pipes that execute it: its bound is the sum over its
+    # parts of (algorithmic FLOPs x executed instructions per multiply-add / the
+    # pipe's peak) -- tensor cores at the measured bf16 peak, the FP32 CUDA cores
+    # at their nominal rate (no measured FP32 peak exists for this GPU pool) --
+    # and frac = bound time / measured time
+    pipe_peak = {"tensor": peak, "fp32": fp32_nominal_tflops()}
     pipes = mixed_stage_pipes(N, na, nb, G)
     stage_roof = {}
     for s in pipes:
         if launches_of[s] == 0 or stage[s] <= 0:
             continue
         t = stage[s] / launches_of[s]
-        fl_p = {p: f * W for p, f in pipes[s].items()}
-        bound_ms = sum(f / (pipe_peak[p] * 1e12) for p, f in fl_p.items()) * 1e3
-        stage_roof[s] = {"ms_per_launch": t, "gflop_per_launch": {p: f / 1e9 for p, f in fl_p.items()},
-                         "achieved_tflops": sum(fl_p.values()) / (t / 1e3) / 1e12,
-                         "bound_ms": bound_ms, "frac": bound_ms / t,
-                         "peaks_tflops": {p: pipe_peak[p] for p in fl_p}}
-    fp64_stages = ("overlap", "ortho")
-    dom = max((s for s in stage_roof if s not in fp64_stages), key=lambda s: stage[s])
+        parts = {name: {"gflop": f * W / 1e9, "pipe": pp, "cost": c} for name, f, pp, c in pipes[s]}
+        bound_ms = sum(f * W * c / (pipe_peak[pp] * 1e12) for _, f, pp, c in pipes[s]) * 1e3
+        stage_roof[s] = {"ms_per_launch": t, "parts": parts,
+                         "achieved_tflops": sum(f * W for _, f, _, _ in pipes[s]) / (t / 1e3) / 1e12,
+                         "bound_ms": bound_ms, "frac": bound_ms / t}
+    dom = max(("vhs", "prop"), key=lambda s: stage[s])
     achieved = per_launch[dom] / (stage_roof[dom]["ms_per_launch"] / 1e3) / 1e12
     roof = {"bound": "tensor", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
             "frac": achieved / peak, "traffic": None,
             "peak_source": "%s bf16 sustained (MEASURED_PEAKS.json); algorithmic FLOPs of the stage per launch "
-                           "/ its CUDA-event time; the largest tensor-core stage (every stage against its pipes in "
-                           "stage_roofline; FP32 and FP64 peaks nominal)"
+                           "/ its CUDA-event time; the largest tensor-core stage (every stage against the executed "
+                           "cost of its parts in stage_roofline; FP32 peak nominal)"
                            % src,
             "stage_roofline": stage_roof}
     out = {"metric": METRIC, "value": value, "unit": "walker-steps/s", "n_gpus": world, "steps": args.steps,
