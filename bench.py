@@ -107,6 +107,21 @@ def mixed_stage_pipes(N, na, nb, G):
     }
 
 
+def flops_model(N, na, nb, G, ortho_every=ORTHO_EVERY):
+    """Algorithmic FLOPs per walker: force bias, VHS, propagator with
+    a real exp(-dt/2 h1') (2 real x complex + 5 complex x complex products per
+    spin), overlap, QR amortised, and one exact local energy."""
+    T = N * (N + 1) // 2
+    ns = [na, nb]
+    fb = sum(4 * n * n * N + 16 * n ** 3 + 8 * N * n * n + 4 * n * N * G for n in ns)
+    vhs = 4 * T * G
+    prop = sum(48 * N * N * n for n in ns)
+    ovl = sum(4 * n * n * N + 5.3 * n ** 3 for n in ns)
+    qr = sum(32 * N * n * n for n in ns) / ortho_every
+    el = sum(4 * G * n * n * N + 8 * G * n * n + 4 * n * N for n in ns)
+    return dict(fb=fb, vhs=vhs, prop=prop, overlap=ovl, ortho=qr, energy=el, step=fb + vhs + prop + ovl + qr)
+
+
 class Clocks:
     """nvidia-smi samples during the timed region."""
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
