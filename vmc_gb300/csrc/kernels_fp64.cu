@@ -139,6 +139,11 @@ __global__ void k_overlap_theta(const double2* __restrict__ psi, const double* _
 // of one channel and stages that channel's Phi in shared memory (unless M is
 // formed beforehand).
 constexpr int OW_WARPS = 4;
+// shared memory of one warp: the n x n matrix (FP64 complex, or the mixed
+// form's high and low FP32 planes: 16 bytes an entry either way) and the pivots
+__host__ __device__ inline size_t ow_per_warp(int nmax) {
+  return ((size_t)nmax * nmax * sizeof(double2) + nmax * sizeof(int) + 15) & ~(size_t)15;
+}
 
 __device__ __forceinline__ df32c ld_dfc(const float2* ah, const float2* al, int e) {
   const float2 x = ah[e], y = al[e];
@@ -244,13 +249,13 @@ __global__ void __launch_bounds__(OW_WARPS * 32)
   const int n = ch.n;
   extern __shared__ __align__(16) unsigned char ow_raw[];
   double* phs = (double*)ow_raw;  // [n][N] channel orbitals (column i at i N)
-  const size_t per_warp = ((size_t)nmax * nmax * (sizeof(double2) + sizeof(float2)) + nmax * sizeof(int) + 15) & ~(size_t)15;
+  const size_t per_warp = ow_per_warp(nmax);
   const size_t phs_bytes = MB ? 0 : (((size_t)nmax * N * sizeof(double) + 15) & ~(size_t)15);
   unsigned char* wbase = ow_raw + phs_bytes + warp * per_warp;
   double2* a = (double2*)wbase;  // FP64 form: [n][n] LU, row-major
   float2* ah = (float2*)wbase;   // mixed form: [n][n] high parts, then [n][n] low parts
   float2* al = ah + (size_t)nmax * nmax;
-  int* perm = (int*)(wbase + (size_t)nmax * nmax * (sizeof(double2) + sizeof(float2)));
+  int* perm = (int*)(wbase + (size_t)nmax * nmax * sizeof(double2));
   if (!MB) {
     const double* ph = phi + (size_t)ch.col_off * N;
     for (int e = threadIdx.x; e < n * N; e += blockDim.x) phs[e] = ph[e];
@@ -497,8 +502,7 @@ void launch_psi_to_f32(afqmc_handle* h) {
 void launch_overlap_theta(afqmc_handle* h, bool only_live) {
   h->fb_current = false;  // theta changes
   int nmax = std::max(h->chan[0].n, h->nchan > 1 ? h->chan[1].n : 0);
-  const size_t per_warp =
-      ((size_t)nmax * nmax * (sizeof(double2) + sizeof(float2)) + nmax * sizeof(int) + 15) & ~(size_t)15;
+  const size_t per_warp = ow_per_warp(nmax);
   const size_t smem_lu = (((size_t)nmax * h->N * sizeof(double) + 15) & ~(size_t)15) + OW_WARPS * per_warp;
   const bool mtc = h->tune_ovl == 3 && ovl_tc_available(h);  // M on the tensor cores
   if (nmax <= 32 && h->tune_ovl != 2 && (mtc || smem_lu <= 160 * 1024)) {

@@ -64,9 +64,12 @@ __global__ void __launch_bounds__(OC_THREADS)
   const int w = blockIdx.x;
   if (!(weights[w] > 1.0e-8)) return;
   extern __shared__ float2 oc_sm[];
-  float2* Ah = oc_sm;                      // [nmax][N] spin block, high parts, column-major
-  float2* Al = Ah + (size_t)nmax * N;      // [nmax][N] low parts
-  float2* R = Al + (size_t)nmax * N;       // [nmax][nmax] Gram, then R in its upper triangle (R[i * n + j])
+  // spin block columns at an odd stride (in 8-byte words), so that the Gram
+  // loop's reads of up to 16 different columns at one row hit 16 different banks
+  const int ld = N | 1;
+  float2* Ah = oc_sm;                      // [nmax][ld] spin block, high parts, column-major
+  float2* Al = Ah + (size_t)nmax * ld;     // [nmax][ld] low parts
+  float2* R = Al + (size_t)nmax * ld;      // [nmax][nmax] Gram, then R in its upper triangle (R[i * n + j])
   float2* X = R + (size_t)nmax * nmax;     // [nmax][nmax] X = R^-1, upper (X[i * n + j])
   __shared__ int s_bad;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -81,8 +84,9 @@ __global__ void __launch_bounds__(OC_THREADS)
     for (int e = tid; e < n * N; e += OC_THREADS) {
       const double2 v = Ag[e];
       const df32 re = df_split_bits(v.x), im = df_split_bits(v.y);
-      Ah[e] = make_float2(re.h, im.h);
-      Al[e] = make_float2(re.l, im.l);
+      const int o = (e / N) * ld + e % N;
+      Ah[o] = make_float2(re.h, im.h);
+      Al[o] = make_float2(re.l, im.l);
     }
     if (tid == 0) s_bad = 0;
     __syncthreads();
@@ -90,8 +94,8 @@ __global__ void __launch_bounds__(OC_THREADS)
     for (int e = tid; e < n * n; e += OC_THREADS) {
       const int i = e / n, j = e % n;
       if (i > j) continue;
-      const float2* ai = Ah + (size_t)i * N;
-      const float2* aj = Ah + (size_t)j * N;
+      const float2* ai = Ah + (size_t)i * ld;
+      const float2* aj = Ah + (size_t)j * ld;
       float sr = 0.f, si = 0.f, tr = 0.f, ti = 0.f;
       int p = 0;
       for (; p + 1 < N; p += 2) {
@@ -164,7 +168,7 @@ __global__ void __launch_bounds__(OC_THREADS)
       const int j = e / N, p = e % N;
       float sr = 0.f, cr = 0.f, si = 0.f, ci = 0.f;
       for (int i = 0; i <= j; ++i) {
-        const float2 h = Ah[(size_t)i * N + p], l = Al[(size_t)i * N + p], x = X[i * n + j];
+        const float2 h = Ah[(size_t)i * ld + p], l = Al[(size_t)i * ld + p], x = X[i * n + j];
         dot2_acc(sr, cr, h.x, l.x, x.x);
         dot2_acc(sr, cr, -h.y, -l.y, x.y);
         dot2_acc(si, ci, h.x, l.x, x.y);
@@ -186,7 +190,7 @@ __global__ void __launch_bounds__(OC_THREADS)
 
 size_t ortho_chol_smem(const afqmc_handle* h) {
   const size_t nmax = (size_t)std::max(h->na, h->rhf_walker ? 0 : h->nb);
-  return (2 * nmax * h->N + 2 * nmax * nmax) * sizeof(float2);
+  return (2 * nmax * (size_t)(h->N | 1) + 2 * nmax * nmax) * sizeof(float2);
 }
 
 bool ortho_chol_available(const afqmc_handle* h) {
