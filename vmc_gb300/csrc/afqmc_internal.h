@@ -158,7 +158,8 @@ struct afqmc_handle {
   double* ovl_sig = nullptr;
   double* ovl_tau = nullptr;
   uint8_t* ovl_bimg = nullptr;
-  float4* ovl_M = nullptr;                // [W][2][nmax][nmax] M in double-FP32 (re hi, re lo, im hi, im lo)
+  float4* ovl_M = nullptr;
+  float4* mf32 = nullptr;                 // [G] mean field as double-FP32 (re hi, re lo, im hi, im lo)                // [W][2][nmax][nmax] M in double-FP32 (re hi, re lo, im hi, im lo)
   CUtensorMap tm_ovlA;       // [nsp][hi, lo][128 x 256] swizzled A image of B (tensor-core propagator, N <= 128)
   // control variate
   float* cv_x = nullptr;             // [W][67] features

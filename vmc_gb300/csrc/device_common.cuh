@@ -97,7 +97,7 @@ __device__ __forceinline__ U4 philox4x32_10(U4 c, uint32_t k0, uint32_t k1) {
 // Standard normal for (step, walker, field): one Philox block gives the
 // Box-Muller pair of fields (2m, 2m+1).  The transform runs in FP32 (24-bit
 // uniforms; the FP64 pipe of this GPU is ~60x slower than its FP32 pipe).
-__device__ __forceinline__ double philox_normal(uint64_t seed, uint64_t step, uint32_t w, uint32_t g) {
+__device__ __forceinline__ float philox_normal_f(uint64_t seed, uint64_t step, uint32_t w, uint32_t g) {
   const U4 r = philox4x32_10(U4{g >> 1, w, (uint32_t)step, (uint32_t)(step >> 32)}, (uint32_t)seed,
                              (uint32_t)(seed >> 32));
   const float two24 = 1.0f / 16777216.0f;
@@ -106,7 +106,10 @@ __device__ __forceinline__ double philox_normal(uint64_t seed, uint64_t step, ui
   const float rad = sqrtf(-2.0f * logf(u1));
   float s, c;
   sincospif(2.0f * u2, &s, &c);
-  return (double)((g & 1u) ? rad * s : rad * c);
+  return (g & 1u) ? rad * s : rad * c;
+}
+__device__ __forceinline__ double philox_normal(uint64_t seed, uint64_t step, uint32_t w, uint32_t g) {
+  return (double)philox_normal_f(seed, step, w, g);
 }
 
 }  // namespace afqmc

@@ -115,6 +115,20 @@ __device__ __forceinline__ double df_f2d_bits(float f) {
 // the double nearest h + l: two exact conversions and one FP64 addition
 __device__ __forceinline__ double df_to_double_bits(df32 a) { return df_f2d_bits(a.h) + df_f2d_bits(a.l); }
 
+// s + c += a b for a double-FP32 a and an FP32 b, accumulated as Ogita-Rump-
+// Oishi's Dot2: s carries the rounded sum of the high products, c the sum of
+// every rounding error (TwoSum of s, the exact product's error of a.h b) and of
+// the low products; the sum is s + c (accurate as if formed in ~48-bit arithmetic).
+__device__ __forceinline__ void dot2_acc(float& s, float& c, float ah, float al, float b) {
+  const float p = __fmul_rn(ah, b);
+  const float pe = fmaf(ah, b, -p);
+  float t, e;
+  df_two_sum(s, p, t, e);
+  s = t;
+  c = __fadd_rn(c, __fadd_rn(e, pe));
+  c = fmaf(al, b, c);
+}
+
 // complex x + a b
 __device__ __forceinline__ df32c dfc_fma(df32c x, df32c a, df32c b) {
   return {df_fma2(x.r, a.r, b.r, df_neg(a.i), b.i), df_fma2(x.i, a.r, b.i, a.i, b.r)};

@@ -15,6 +15,7 @@
 
 #include "afqmc_internal.h"
 #include "device_common.cuh"
+#include "df32.cuh"
 #include "tcgen05.cuh"
 
 namespace afqmc {
@@ -197,51 +198,77 @@ void launch_vhs_mixed(afqmc_handle* h) {
 }
 
 // ---------------------------------------------------------------------------
-// shifted fields from the FP32 force bias; x written as split BF16 rows
+// shifted fields from the FP32 force bias; x written as split BF16 rows.
+// Per field (DQMCWalker.cpp:451-457): fs = -sqrt(dt) (i fb - mf), x = xi - fs,
+// shift += x mf, fbTerm += xi fs - fs^2 / 2.  The inputs are FP32 numbers (the
+// force bias of the split-BF16 contraction, the FP32 Box-Muller fields; host
+// fields enter as exact FP32 pairs), so each term is formed in FP32 and the
+// four per-walker sums are compensated (Dot2) with the mean field as a
+// double-FP32 pair: FP64-grade sums without an FP64 instruction per field.
 // ---------------------------------------------------------------------------
-__global__ void k_fields_mixed(const float* __restrict__ fb, const double2* __restrict__ mf,
+__global__ void k_split_mf(const double2* __restrict__ mf, float4* __restrict__ mf32, int G) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= G) return;
+  const df32 re = df_split_bits(mf[g].x), im = df_split_bits(mf[g].y);
+  mf32[g] = make_float4(re.h, re.l, im.h, im.l);
+}
+
+__global__ void k_fields_mixed(const float* __restrict__ fb, const float4* __restrict__ mf32,
                                const double* __restrict__ xi, __nv_bfloat16* __restrict__ xB, int kv_pad,
                                double2* __restrict__ shift, double2* __restrict__ fbterm,
-                               const double* __restrict__ weights, int G, double sdt, int use_rng, uint64_t seed,
+                               const double* __restrict__ weights, int G, float sdt, int use_rng, uint64_t seed,
                                const unsigned long long* __restrict__ stepp) {
   const int w = blockIdx.x;
   const uint64_t step = *stepp;
   const bool live = weights[w] > 1.0e-8;
-  double shr = 0.0, shi = 0.0, ftr = 0.0, fti = 0.0;
+  float shr = 0.f, cshr = 0.f, shi = 0.f, cshi = 0.f, ftr = 0.f, cftr = 0.f, fti = 0.f, cfti = 0.f;
   const float* fbr = fb + (size_t)(2 * w) * G;
   const float* fbi = fbr + G;
   __nv_bfloat16* xr_out = xB + (size_t)(2 * w) * kv_pad;
   __nv_bfloat16* xi_out = xr_out + kv_pad;
   for (int g = threadIdx.x; g < G; g += blockDim.x) {
-    const double xg = use_rng ? philox_normal(seed, step, (uint32_t)w, (uint32_t)g) : xi[(size_t)w * G + g];
-    const double2 m = mf[g];
-    const double fsr = -sdt * (-(double)fbi[g] - m.x);
-    const double fsi = -sdt * ((double)fbr[g] - m.y);
-    double xr = xg - fsr, xim = -fsi;
-    shr += xr * m.x - xim * m.y;
-    shi += xr * m.y + xim * m.x;
-    ftr += xg * fsr - 0.5 * (fsr * fsr - fsi * fsi);
-    fti += xg * fsi - 0.5 * (2.0 * fsr * fsi);
-    if (!live) { xr = 0.0; xim = 0.0; }
+    df32 xg;
+    if (use_rng) xg = {philox_normal_f(seed, step, (uint32_t)w, (uint32_t)g), 0.f};
+    else xg = df_split_bits(xi[(size_t)w * G + g]);
+    const float4 m = mf32[g];  // (re hi, re lo, im hi, im lo)
+    const float fsr = sdt * (fbi[g] + m.x);
+    const float fsi = -sdt * (fbr[g] - m.z);
+    // x = xg - fs; shift += x mf
+    dot2_acc(shr, cshr, m.x, m.y, xg.h);
+    dot2_acc(shr, cshr, m.x, m.y, xg.l);
+    dot2_acc(shr, cshr, m.x, m.y, -fsr);
+    dot2_acc(shr, cshr, m.z, m.w, fsi);   // - Im x Im mf, Im x = -fsi
+    dot2_acc(shi, cshi, m.z, m.w, xg.h);
+    dot2_acc(shi, cshi, m.z, m.w, xg.l);
+    dot2_acc(shi, cshi, m.z, m.w, -fsr);
+    dot2_acc(shi, cshi, m.x, m.y, -fsi);  // Im x Re mf
+    // fbTerm += xg fs - fs^2 / 2
+    dot2_acc(ftr, cftr, xg.h, xg.l, fsr);
+    dot2_acc(ftr, cftr, -0.5f * fsr, 0.f, fsr);
+    dot2_acc(ftr, cftr, 0.5f * fsi, 0.f, fsi);
+    dot2_acc(fti, cfti, xg.h, xg.l, fsi);
+    dot2_acc(fti, cfti, -fsr, 0.f, fsi);
+    float xr = (xg.h - fsr) + xg.l, xim = -fsi;
+    if (!live) { xr = 0.f; xim = 0.f; }
     __nv_bfloat16 hi, lo;  // split of the FP32 value (the VHS contraction is split-BF16)
-    split_bf16((float)xr, hi, lo);
+    split_bf16(xr, hi, lo);
     xr_out[g] = hi; xr_out[G + g] = lo; xr_out[2 * G + g] = hi;
-    split_bf16((float)xim, hi, lo);
+    split_bf16(xim, hi, lo);
     xi_out[g] = hi; xi_out[G + g] = lo; xi_out[2 * G + g] = hi;
   }
-  shr = block_sum(shr);
-  shi = block_sum(shi);
-  ftr = block_sum(ftr);
-  fti = block_sum(fti);
+  const double sr = block_sum((double)shr + (double)cshr);
+  const double si = block_sum((double)shi + (double)cshi);
+  const double tr = block_sum((double)ftr + (double)cftr);
+  const double ti = block_sum((double)fti + (double)cfti);
   if (threadIdx.x == 0) {
-    shift[w] = make_double2(shr, shi);
-    fbterm[w] = make_double2(ftr, fti);
+    shift[w] = make_double2(sr, si);
+    fbterm[w] = make_double2(tr, ti);
   }
 }
 
 void launch_fields_mixed(afqmc_handle* h, bool device_rng) {
-  k_fields_mixed<<<h->nwalk, 256, 0, h->stream>>>(h->fb32, h->mf, h->xi, h->xB, h->kv_pad, h->shift, h->fbterm,
-                                                  h->weights, h->G, sqrt(h->dt), device_rng ? 1 : 0, h->seed,
+  k_fields_mixed<<<h->nwalk, 256, 0, h->stream>>>(h->fb32, h->mf32, h->xi, h->xB, h->kv_pad, h->shift, h->fbterm,
+                                                  h->weights, h->G, (float)sqrt(h->dt), device_rng ? 1 : 0, h->seed,
                                                   h->d_step);
   h->launches++;
 }
@@ -526,6 +553,7 @@ bool setup_mixed(afqmc_handle* h) {
   for (int s = 0; s < h->nsp; ++s)
     split_rows(h, h->LT + (size_t)s * h->T * h->G, h->G, h->T, h->G, h->kv_pad, 0,
                h->LTA + (size_t)s * h->T * h->kv_pad);
+  k_split_mf<<<(h->G + 127) / 128, 128, 0, h->stream>>>(h->mf, h->mf32, h->G);
   bool ok = setup_prop_tc(h) && setup_ovl_tc(h) && make_tmap_bf16(&h->tm_rot, h->rotA, h->G, h->kf_pad, tc::BM);
   const int bns[3] = {64, 128, 256};
   for (int i = 0; i < 3 && ok; ++i)

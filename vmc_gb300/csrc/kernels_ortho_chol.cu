@@ -45,19 +45,6 @@ namespace afqmc {
 
 constexpr int OC_THREADS = 256;
 
-// x + a b for a double-FP32 a and an FP32 b, accumulated as Ogita-Rump-Oishi's
-// Dot2: s carries the rounded sum of the high products, c the sum of every
-// rounding error (TwoSum of s, TwoProduct of a.h b) and of the low products.
-__device__ __forceinline__ void dot2_acc(float& s, float& c, float ah, float al, float b) {
-  const float p = __fmul_rn(ah, b);
-  const float pe = fmaf(ah, b, -p);
-  float t, e;
-  df_two_sum(s, p, t, e);
-  s = t;
-  c = __fadd_rn(c, __fadd_rn(e, pe));
-  c = fmaf(al, b, c);
-}
-
 __global__ void __launch_bounds__(OC_THREADS)
     k_ortho_chol(double2* __restrict__ psi, float2* __restrict__ psi32, double2* __restrict__ ovlp,
                  const double* __restrict__ weights, int N, int ncw, int na, int nb, int rhf_walker, int nmax) {
