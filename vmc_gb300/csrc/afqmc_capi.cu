@@ -178,7 +178,7 @@ void release(afqmc_handle* h) {
                   h->thetaB, h->xB, h->fb32, h->V32, h->expm32, h->d_chunks32, h->rotE, h->thetaE,
                   h->xc, h->cv_x, h->cv_idx, h->cv_esub, h->cv_f, h->cv_ms, h->cv_out, h->d_step, h->psi32,
                   h->pt_img, h->comb_cum, h->comb_idx, h->comb_ovl, h->blk, h->blk_zeta, h->wpart,
-                  h->ovl_A, h->ovl_sig, h->ovl_tau, h->ovl_bimg, h->ovl_M, h->theta32, h->mf32};
+                  h->ovl_tau, h->ovl_bimg, h->ovl_M, h->theta32, h->mf32};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (h->host_pinned) cudaFreeHost(h->host_pinned);
@@ -469,8 +469,6 @@ int afqmc_create(const afqmc_ham* ham, const afqmc_trial* trial, const afqmc_opt
     if (N <= 128) ALLOC(pt_img, (size_t)nsp * 2 * 128 * 256);
     if (afqmc::ovl_tc_wanted(h)) {
       const size_t nm = std::max(h->chan[0].n, h->nchan > 1 ? h->chan[1].n : 0);
-      ALLOC(ovl_A, afqmc::ovl_a_elems(h));
-      ALLOC(ovl_sig, afqmc::ovl_rows(h));
       ALLOC(ovl_tau, (size_t)h->nchan * afqmc::ovl_bnp(h));
       ALLOC(ovl_bimg, (size_t)h->nchan * afqmc::ovl_bimg_bytes(h));
       ALLOC(ovl_M, W * 2 * nm * nm);

@@ -151,16 +151,12 @@ struct afqmc_handle {
   double* blk = nullptr;        // [BLK_MAX][2] total weight, block energy
   double* blk_zeta = nullptr;   // [BLK_MAX]
   __nv_bfloat16* pt_img = nullptr;
-  // tensor-core overlap matrices (exact BF16 slices): psi slices (one block of rows per
-  // channel) [rows][7 KP], row scales, trial-orbital scales [channel][BNP], the swizzled
-  // trial-slice images [channel][bytes], and M [W][2][nmax][nmax]
-  __nv_bfloat16* ovl_A = nullptr;
-  double* ovl_sig = nullptr;
+  // tensor-core overlap matrices (exact BF16 slices): trial-orbital scales
+  // [channel][BNP], the swizzled trial-slice images [channel][bytes], and M
   double* ovl_tau = nullptr;
   uint8_t* ovl_bimg = nullptr;
-  float4* ovl_M = nullptr;
-  float4* mf32 = nullptr;                 // [G] mean field as double-FP32 (re hi, re lo, im hi, im lo)                // [W][2][nmax][nmax] M in double-FP32 (re hi, re lo, im hi, im lo)
-  CUtensorMap tm_ovlA;       // [nsp][hi, lo][128 x 256] swizzled A image of B (tensor-core propagator, N <= 128)
+  float4* ovl_M = nullptr;  // [W][2][nmax][nmax] double-FP32 (re hi, re lo, im hi, im lo)
+  float4* mf32 = nullptr;   // [G] mean field as double-FP32 (re hi, re lo, im hi, im lo)
   // control variate
   float* cv_x = nullptr;             // [W][67] features
   float* cv_f = nullptr;             // [W]     predicted local energies
@@ -195,8 +191,6 @@ bool ovl_tc_available(const afqmc_handle* h);
 int ovl_kp(const afqmc_handle* h);
 int ovl_bnp(const afqmc_handle* h);
 size_t ovl_bimg_bytes(const afqmc_handle* h);
-size_t ovl_a_elems(const afqmc_handle* h);
-size_t ovl_rows(const afqmc_handle* h);
 bool setup_ovl_tc(afqmc_handle* h);
 void launch_overlap_m_tc(afqmc_handle* h);
 bool prop_tc_available(const afqmc_handle* h);

@@ -27,15 +27,16 @@
 // runs there too), and cutting seven slices with FP64 rint / multiply costs
 // more than the FP64 product it replaces.
 //
-// k_ovl_slice writes the slices of psi as a BF16 operand [rows][7 x KP], one
-// block of rows per channel (row = (walker, channel column, re / im), each
-// block padded to a multiple of 128 rows; KP = N padded to 64).  k_ovl_tc
-// streams one channel's 128-row tiles with TMA (64-wide K boxes, 128-byte
-// swizzle) against the slices of that channel's trial orbitals, resident in
-// shared memory (copied once per CTA from a swizzled image built at set-up),
-// issuing for the K block of slice s the MMAs of every level L >= s into that
-// level's TMEM accumulator; the epilogue combines the levels per (row,
-// orbital) and writes M.
+// k_ovl_tc takes one channel's 128-row tile (64 walker columns, real and
+// imaginary rows) per CTA and cuts the slices of psi itself, straight into
+// shared memory: a pre-pass over each column gives its two row scales, then
+// for every 64-wide K panel the 16 warps write the seven 128 x 64 BF16 slice
+// tiles (128-byte swizzle, K-major), one thread issues for slice s the MMAs of
+// every level L >= s into that level's TMEM accumulator against the trial
+// slices (resident in shared memory, copied once per CTA from a swizzled image
+// built at set-up), and the next panel is cut once those MMAs have read the
+// tiles.  The epilogue combines the levels per (row, orbital) and writes M.
+// Nothing but psi is read and nothing but M is written.
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -51,8 +52,7 @@
 namespace afqmc {
 
 constexpr int OZ_S = 7;        // slices per operand (levels 0..6 kept)
-constexpr int OZ_STAGES = 3;   // A-tile ring
-constexpr int OZ_TILE = 128 * 64 * 2;  // one 128 x 64 BF16 A tile
+constexpr int OZ_TILE = 128 * 64 * 2;  // one 128 x 64 BF16 slice tile of psi
 
 // Slices of x for the row scale sigma = 2^e (|x| < sigma), from the bits of x
 // with 32-bit integer arithmetic only (on this GPU 64-bit integer and FP64
@@ -140,46 +140,6 @@ __global__ void k_ovl_bimage(const double* __restrict__ phi, int N, int n, int K
   }
 }
 
-// Slices of psi: one warp per (walker, channel column) q = w n + j; rows 2 q and
-// 2 q + 1 of the channel's block (real and imaginary parts), K = s KP + p.
-__global__ void k_ovl_slice(const double2* __restrict__ psi, int W, int ncw, int N, int KP, int n, int psi_off,
-                            __nv_bfloat16* __restrict__ A, double* __restrict__ sig) {
-  const int q = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  const int lane = threadIdx.x & 31;
-  if (q >= W * n) return;
-  const int w = q / n, j = q % n;
-  const double2* src = psi + ((size_t)w * ncw + psi_off + j) * N;
-  int br = 0, bi = 0;
-  for (int p = lane; p < N; p += 32) {
-    const double2 v = src[p];
-    br = max(br, oz_biased(v.x));
-    bi = max(bi, oz_biased(v.y));
-  }
-  for (int o = 16; o > 0; o >>= 1) {
-    br = max(br, __shfl_xor_sync(0xffffffffu, br, o));
-    bi = max(bi, __shfl_xor_sync(0xffffffffu, bi, o));
-  }
-  const int er = oz_row_e(br), ei = oz_row_e(bi);
-  if (lane == 0) {
-    sig[2 * q] = ldexp(1.0, er);
-    sig[2 * q + 1] = ldexp(1.0, ei);
-  }
-  const size_t K = (size_t)OZ_S * KP;
-  __nv_bfloat16* rr = A + (size_t)(2 * q) * K;
-  __nv_bfloat16* ri = rr + K;
-  for (int p = lane; p < KP; p += 32) {
-    const double2 v = p < N ? src[p] : make_double2(0.0, 0.0);
-    float a[OZ_S], b[OZ_S];
-    oz_slices_bits(v.x, er, a);
-    oz_slices_bits(v.y, ei, b);
-#pragma unroll
-    for (int s = 0; s < OZ_S; ++s) {
-      rr[(size_t)s * KP + p] = __float2bfloat16_rn(a[s]);
-      ri[(size_t)s * KP + p] = __float2bfloat16_rn(b[s]);
-    }
-  }
-}
-
 __device__ __forceinline__ void oz_bulk(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
   asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
                    tc::smem_u32(dst)),
@@ -187,116 +147,156 @@ __device__ __forceinline__ void oz_bulk(void* dst, const void* src, uint32_t byt
                : "memory");
 }
 
+constexpr int OZ_THREADS = 512;      // 16 warps: 4 walker columns each per tile
+constexpr int OZ_COLS = 64;          // walker columns per 128-row tile
+
 struct OzArgs {
+  const double2* psi;   // walker dets [W][ncw][N]
   const uint8_t* bimg;  // [channel][bimg_bytes] swizzled trial-orbital slices
   int bimg_bytes;
-  const double* sig;    // row scales, channel blocks of rpad rows
   const double* tau;    // [channel][BNP] orbital scales
   float4* M;            // [W][2][nmax][nmax] double-FP32 (re hi, re lo, im hi, im lo)
   int rpad;             // rows per channel block (multiple of 128)
-  int nw;               // walkers
+  int nw, ncw, N;       // walkers, walker columns, orbitals
   int nmax, KP, BNP, tmem_cols;
   int n0, n1;           // orbitals of channels 0 and 1
+  int off0, off1;       // first walker column of channels 0 and 1
 };
 
-__global__ void __launch_bounds__(128, 1)
-    k_ovl_tc(const __grid_constant__ CUtensorMap tmA, OzArgs g, int* err) {
+__global__ void __launch_bounds__(OZ_THREADS, 1) k_ovl_tc(OzArgs g, int* err) {
   extern __shared__ uint8_t oz_raw[];
   uint8_t* smem = (uint8_t*)(((uintptr_t)oz_raw + 1023) & ~(uintptr_t)1023);
   uint8_t* sB = smem;                                              // bimg_bytes (multiple of 1024)
-  uint8_t* ring = smem + ((g.bimg_bytes + 1023) & ~1023);           // OZ_STAGES x OZ_TILE
-  uint64_t* full = (uint64_t*)(ring + OZ_STAGES * OZ_TILE);
-  uint64_t* empty = full + OZ_STAGES;
-  uint64_t* accum = empty + OZ_STAGES;
-  uint64_t* bload = accum + 1;
-  uint32_t* tmem_holder = (uint32_t*)(bload + 1);
+  uint8_t* sA = smem + ((g.bimg_bytes + 1023) & ~1023);            // OZ_S slice tiles of one K panel
+  int* s_e = (int*)(sA + OZ_S * OZ_TILE);                          // [128] row scale exponents
+  uint64_t* bload = (uint64_t*)(s_e + 128);
+  uint64_t* mdone = bload + 1;
+  uint32_t* tmem_holder = (uint32_t*)(mdone + 1);
   __shared__ int s_abort;
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int m0 = blockIdx.x * 128;          // row of the whole operand
   const int chn = m0 / g.rpad;              // this tile's channel
   const int n_c = chn == 0 ? g.n0 : g.n1;
+  const int off_c = chn == 0 ? g.off0 : g.off1;
+  const int q0 = (m0 - chn * g.rpad) >> 1;  // first (walker, column) pair of the tile
   const int npanel = g.KP / 64;
-  const int nk = OZ_S * npanel;  // K blocks of 64: slice kb / npanel, panel kb % npanel
 
   if (threadIdx.x == 0) {
     s_abort = 0;
-    for (int s = 0; s < OZ_STAGES; ++s) {
-      tc::mbar_init(&full[s], 1);
-      tc::mbar_init(&empty[s], 1);
-    }
-    tc::mbar_init(accum, 1);
     tc::mbar_init(bload, 1);
+    tc::mbar_init(mdone, 1);
     tc::fence_mbar_init();
-    tc::prefetch_tmap(&tmA);
   }
   if (warp == 0) tc::tmem_alloc(tmem_holder, g.tmem_cols);
   tc::tc_fence_before();
   __syncthreads();
   tc::tc_fence_after();
   const uint32_t tmem = *tmem_holder;
-
-  int issued = 0;
-  if (warp == 0 && lane == 0) {
+  if (threadIdx.x == 0) {
     tc::mbar_expect_tx(bload, (uint32_t)g.bimg_bytes);
     for (int o = 0; o < g.bimg_bytes; o += 16384) {
       const int b = min(16384, g.bimg_bytes - o);
       oz_bulk(sB + o, g.bimg + (size_t)chn * g.bimg_bytes + o, (uint32_t)b, bload);
     }
-    for (int kb = 0; kb < nk; ++kb) {
-      const int s = kb % OZ_STAGES;
-      if (kb >= OZ_STAGES && !tc::mbar_wait(&empty[s], ((kb / OZ_STAGES) - 1) & 1, err, 31)) {
-        s_abort = 1;
-        break;
-      }
-      if (s_abort) break;
-      tc::mbar_expect_tx(&full[s], OZ_TILE);
-      tc::tma_load_2d(ring + s * OZ_TILE, &tmA, &full[s], kb * 64, m0);
-      issued = kb + 1;
-    }
-  } else if (warp == 1 && lane == 0) {
-    const uint32_t idesc = tc::idesc_bf16(128, g.BNP);
-    bool ok = tc::mbar_wait(bload, 0, err, 32);
-    if (!ok) s_abort = 1;
-    for (int kb = 0; kb < nk && ok; ++kb) {
-      const int s = kb % OZ_STAGES;
-      if (!tc::mbar_wait(&full[s], (kb / OZ_STAGES) & 1, err, 33)) {
-        s_abort = 1;
-        ok = false;
-        break;
-      }
-      if (s_abort) { ok = false; break; }
-      tc::tc_fence_after();
-      const int sl = kb / npanel, kk = kb % npanel;
-      const uint32_t aa = tc::smem_u32(ring + s * OZ_TILE);
-      for (int L = sl; L < OZ_S; ++L) {
-        const int t = L - sl;
-        const uint32_t ba = tc::smem_u32(sB) + (uint32_t)((t * npanel + kk) * g.BNP * 128);
-#pragma unroll
-        for (int k = 0; k < 4; ++k)  // +32 bytes per K=16 step inside the swizzle row
-          tc::mma_bf16(tmem + (uint32_t)(L * g.BNP), tc::sdesc_sw128(aa + 32 * k), tc::sdesc_sw128(ba + 32 * k),
-                       idesc, (sl > 0 || kk > 0 || k > 0) ? 1u : 0u);
-      }
-      tc::mma_commit(&empty[s]);
-    }
-    tc::mma_commit(accum);
   }
-  __syncwarp();
-  const bool have = tc::mbar_wait(accum, 0, err, 34);
-  tc::tc_fence_after();
-  if (have && !s_abort) {
-    const int rg = m0 + warp * 32 + lane;    // row of the whole operand
-    const int r = rg - chn * g.rpad;         // row within the channel block
-    const int q = r >> 1, part = r & 1;
+
+  // this warp's columns qq = warp + 16 c: source and row scales (pre-pass over the whole row)
+  const double2* src[OZ_COLS / 16];
+  int er[OZ_COLS / 16], ei[OZ_COLS / 16];
+#pragma unroll
+  for (int c = 0; c < OZ_COLS / 16; ++c) {
+    const int q = q0 + warp + 16 * c;
+    const bool valid = n_c > 0 && q < g.nw * n_c;
+    src[c] = nullptr;
+    int br = 0, bi = 0;
+    if (valid) {
+      const int w = q / n_c, j = q % n_c;
+      src[c] = g.psi + ((size_t)w * g.ncw + off_c + j) * g.N;
+      for (int p = lane; p < g.N; p += 32) {
+        const double2 v = src[c][p];
+        br = max(br, oz_biased(v.x));
+        bi = max(bi, oz_biased(v.y));
+      }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      br = max(br, __shfl_xor_sync(0xffffffffu, br, o));
+      bi = max(bi, __shfl_xor_sync(0xffffffffu, bi, o));
+    }
+    er[c] = oz_row_e(br);
+    ei[c] = oz_row_e(bi);
+    if (lane == 0) {
+      s_e[2 * (warp + 16 * c)] = er[c];
+      s_e[2 * (warp + 16 * c) + 1] = ei[c];
+    }
+  }
+
+  const uint32_t idesc = tc::idesc_bf16(128, g.BNP);
+  bool ok = true;
+  for (int kk = 0; kk < npanel; ++kk) {
+    // the seven slice tiles of K panel kk: row r = 2 qq + part, k = p - 64 kk
+#pragma unroll
+    for (int c = 0; c < OZ_COLS / 16; ++c) {
+      const int qq = warp + 16 * c;
+      const int r0 = 2 * qq, r1 = r0 + 1;
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int k = lane + 32 * h, p = 64 * kk + k;
+        const double2 v = (src[c] != nullptr && p < g.N) ? src[c][p] : make_double2(0.0, 0.0);
+        float a[OZ_S], b[OZ_S];
+        oz_slices_bits(v.x, er[c], a);
+        oz_slices_bits(v.y, ei[c], b);
+        const uint32_t o0 = (uint32_t)(r0 * 128 + ((((k >> 3) ^ (r0 & 7))) << 4) + (k & 7) * 2);
+        const uint32_t o1 = (uint32_t)(r1 * 128 + ((((k >> 3) ^ (r1 & 7))) << 4) + (k & 7) * 2);
+#pragma unroll
+        for (int t = 0; t < OZ_S; ++t) {
+          *(__nv_bfloat16*)(sA + t * OZ_TILE + o0) = __float2bfloat16_rn(a[t]);
+          *(__nv_bfloat16*)(sA + t * OZ_TILE + o1) = __float2bfloat16_rn(b[t]);
+        }
+      }
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // generic writes -> tensor core
+    tc::tc_fence_before();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      tc::tc_fence_after();
+      if (kk == 0 && !tc::mbar_wait(bload, 0, err, 32)) s_abort = 1;
+      if (!s_abort) {
+        for (int sl = 0; sl < OZ_S; ++sl) {
+          const uint32_t aa = tc::smem_u32(sA + sl * OZ_TILE);
+          for (int L = sl; L < OZ_S; ++L) {
+            const int t = L - sl;
+            const uint32_t ba = tc::smem_u32(sB) + (uint32_t)((t * npanel + kk) * g.BNP * 128);
+#pragma unroll
+            for (int k = 0; k < 4; ++k)  // +32 bytes per K=16 step inside the swizzle row
+              tc::mma_bf16(tmem + (uint32_t)(L * g.BNP), tc::sdesc_sw128(aa + 32 * k),
+                           tc::sdesc_sw128(ba + 32 * k), idesc, (sl > 0 || kk > 0 || k > 0) ? 1u : 0u);
+          }
+        }
+      }
+      tc::mma_commit(mdone);  // also when nothing was issued: the waiters are released
+    }
+    // the tiles may be rewritten (and, after the last panel, TMEM read) once the MMAs are done
+    ok = tc::mbar_wait(mdone, (uint32_t)(kk & 1), err, 34);
+    ok = __syncthreads_and(ok ? 1 : 0) != 0 && !s_abort;
+    tc::tc_fence_after();
+    if (!ok) break;
+  }
+
+  // epilogue: warp (quadrant warp & 3, column group warp >> 2) combines the levels
+  if (ok) {
+    const int r = (warp & 3) * 32 + lane;      // tile row = TMEM lane
+    const int rg = m0 + r;                     // row of the whole operand
+    const int ri = rg - chn * g.rpad;          // row within the channel block
+    const int q = ri >> 1, part = ri & 1;
     const int nn = max(n_c, 1);
     const int w = q / nn, j = q % nn;
     const bool valid = n_c > 0 && q < g.nw * n_c;
-    // sigma 2^-14 and tau are powers of two: their FP32 images by exponent
-    const float sg = valid ? oz_pow2f(g.sig[rg]) * (1.0f / 16384.0f) : 0.f;
+    const float sg = df_pow2(max(-126, min(126, s_e[r] - 14)));  // sigma 2^-14
     float* Mf = (float*)g.M;
-    const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
+    const uint32_t lane_base = (uint32_t)((warp & 3) * 32) << 16;
 #pragma unroll 1
-    for (int cb = 0; cb < g.BNP; cb += 16) {
+    for (int cb = (warp >> 2) * 16; cb < g.BNP; cb += 64) {
       float d[OZ_S][16];
 #pragma unroll
       for (int L = 0; L < OZ_S; ++L) tc::tmem_ld16(tmem + lane_base + (uint32_t)(L * g.BNP + cb), d[L]);
@@ -315,11 +315,7 @@ __global__ void __launch_bounds__(128, 1)
       }
     }
   }
-  if (s_abort && warp == 0 && lane == 0) {
-    for (int kb = (issued > OZ_STAGES ? issued - OZ_STAGES : 0); kb < issued; ++kb)
-      tc::mbar_wait(&full[kb % OZ_STAGES], (kb / OZ_STAGES) & 1, err, 35);
-    tc::mbar_wait(bload, 0, err, 36);
-  }
+  if (s_abort && threadIdx.x == 0) tc::mbar_wait(bload, 0, err, 36);  // the image copy has landed
   tc::tc_fence_before();
   __syncthreads();
   if (warp == 0) {
@@ -339,68 +335,56 @@ bool ovl_tc_wanted(const afqmc_handle* h) {
   return h->precision == AFQMC_PREC_MIXED && h->N <= 128 && ovl_nmax(h) <= 32;
 }
 
-bool ovl_tc_available(const afqmc_handle* h) { return ovl_tc_wanted(h) && h->ovl_A != nullptr; }
+bool ovl_tc_available(const afqmc_handle* h) { return ovl_tc_wanted(h) && h->ovl_M != nullptr; }
 
 // bytes of one channel's trial-slice image
 size_t ovl_bimg_bytes(const afqmc_handle* h) { return (size_t)OZ_S * (ovl_kp(h) / 64) * ovl_bnp(h) * 128; }
-size_t ovl_a_elems(const afqmc_handle* h) { return (size_t)h->nchan * ovl_rpad(h) * OZ_S * ovl_kp(h); }
-size_t ovl_rows(const afqmc_handle* h) { return (size_t)h->nchan * ovl_rpad(h); }
 
 static size_t ovl_smem(const afqmc_handle* h) {
-  return ((ovl_bimg_bytes(h) + 1023) & ~(size_t)1023) + OZ_STAGES * OZ_TILE + (2 * OZ_STAGES + 2) * 8 + 16 + 1024;
+  return ((ovl_bimg_bytes(h) + 1023) & ~(size_t)1023) + OZ_S * OZ_TILE + 128 * sizeof(int) + 2 * 8 + 16 + 1024;
 }
-
-bool make_tmap_bf16(CUtensorMap* tm, const void* base, int rows, int kpad, int box_rows);
 
 bool setup_ovl_tc(afqmc_handle* h) {
   if (!ovl_tc_available(h)) return true;
   const int KP = ovl_kp(h), BNP = ovl_bnp(h);
   const size_t bytes = ovl_bimg_bytes(h);
   cudaMemsetAsync(h->ovl_bimg, 0, h->nchan * bytes, h->stream);
-  // padding rows of the slice operand stay zero
-  cudaMemsetAsync(h->ovl_A, 0, ovl_a_elems(h) * sizeof(__nv_bfloat16), h->stream);
-  cudaMemsetAsync(h->ovl_sig, 0, ovl_rows(h) * sizeof(double), h->stream);
   for (int c = 0; c < h->nchan; ++c)
     k_ovl_bimage<<<(BNP + 7) / 8, 256, 0, h->stream>>>(h->phi + (size_t)h->chan[c].col_off * h->N, h->N,
                                                        h->chan[c].n, KP, BNP,
                                                        (__nv_bfloat16*)(h->ovl_bimg + c * bytes),
                                                        h->ovl_tau + (size_t)c * BNP);
-  return cudaGetLastError() == cudaSuccess &&
-         make_tmap_bf16(&h->tm_ovlA, h->ovl_A, (int)ovl_rows(h), OZ_S * KP, 128);
+  return cudaGetLastError() == cudaSuccess;
 }
 
 void launch_overlap_m_tc(afqmc_handle* h) {
-  const int KP = ovl_kp(h), BNP = ovl_bnp(h), rpad = ovl_rpad(h);
-  const size_t K = (size_t)OZ_S * KP;
-  for (int c = 0; c < h->nchan; ++c) {
-    const int q = h->nwalk * h->chan[c].n;
-    k_ovl_slice<<<(q + 7) / 8, 256, 0, h->stream>>>(h->psi, h->nwalk, h->ncw, h->N, KP, h->chan[c].n,
-                                                    h->chan[c].psi_off, h->ovl_A + (size_t)c * rpad * K,
-                                                    h->ovl_sig + (size_t)c * rpad);
-  }
   static bool attr = false;
   if (!attr) {
     cudaFuncSetAttribute(k_ovl_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
     attr = true;
   }
   OzArgs g;
+  g.psi = h->psi;
   g.bimg = h->ovl_bimg;
   g.bimg_bytes = (int)ovl_bimg_bytes(h);
-  g.sig = h->ovl_sig;
   g.tau = h->ovl_tau;
   g.M = h->ovl_M;
-  g.rpad = rpad;
+  g.rpad = ovl_rpad(h);
   g.nw = h->nwalk;
+  g.ncw = h->ncw;
+  g.N = h->N;
   g.nmax = ovl_nmax(h);
-  g.KP = KP;
-  g.BNP = BNP;
+  g.KP = ovl_kp(h);
+  g.BNP = ovl_bnp(h);
   int tc = 32;
-  while (tc < OZ_S * BNP) tc *= 2;
+  while (tc < OZ_S * g.BNP) tc *= 2;
   g.tmem_cols = tc;
   g.n0 = h->chan[0].n;
   g.n1 = h->nchan > 1 ? h->chan[1].n : 0;
-  k_ovl_tc<<<(unsigned)(ovl_rows(h) / 128), 128, ovl_smem(h), h->stream>>>(h->tm_ovlA, g, h->d_err);
-  h->launches += h->nchan + 1;
+  g.off0 = h->chan[0].psi_off;
+  g.off1 = h->nchan > 1 ? h->chan[1].psi_off : 0;
+  k_ovl_tc<<<(unsigned)(h->nchan * g.rpad / 128), OZ_THREADS, ovl_smem(h), h->stream>>>(g, h->d_err);
+  h->launches++;
 }
 
 }  // namespace afqmc
