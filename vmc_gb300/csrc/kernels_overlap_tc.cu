@@ -201,23 +201,30 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_ovl_tc(OzArgs g, int* err) {
     }
   }
 
-  // this warp's columns qq = warp + 16 c: source and row scales (pre-pass over the whole row)
-  const double2* src[OZ_COLS / 16];
+  // this warp's columns qq = warp + 16 c: all of their values are loaded at
+  // once (lane p + 32 it, it < 4, N <= 128), then the row scales and both K
+  // panels' slices come from registers -- one load latency per tile
+  double2 v[OZ_COLS / 16][4];
   int er[OZ_COLS / 16], ei[OZ_COLS / 16];
 #pragma unroll
   for (int c = 0; c < OZ_COLS / 16; ++c) {
     const int q = q0 + warp + 16 * c;
     const bool valid = n_c > 0 && q < g.nw * n_c;
-    src[c] = nullptr;
+    const int qs = valid ? q : 0;
+    const double2* src = g.psi + ((size_t)(qs / max(n_c, 1)) * g.ncw + off_c + qs % max(n_c, 1)) * g.N;
+#pragma unroll
+    for (int it = 0; it < 4; ++it) {
+      const int p = lane + 32 * it;
+      v[c][it] = (valid && p < g.N) ? src[p] : make_double2(0.0, 0.0);
+    }
+  }
+#pragma unroll
+  for (int c = 0; c < OZ_COLS / 16; ++c) {
     int br = 0, bi = 0;
-    if (valid) {
-      const int w = q / n_c, j = q % n_c;
-      src[c] = g.psi + ((size_t)w * g.ncw + off_c + j) * g.N;
-      for (int p = lane; p < g.N; p += 32) {
-        const double2 v = src[c][p];
-        br = max(br, oz_biased(v.x));
-        bi = max(bi, oz_biased(v.y));
-      }
+#pragma unroll
+    for (int it = 0; it < 4; ++it) {
+      br = max(br, oz_biased(v[c][it].x));
+      bi = max(bi, oz_biased(v[c][it].y));
     }
     for (int o = 16; o > 0; o >>= 1) {
       br = max(br, __shfl_xor_sync(0xffffffffu, br, o));
@@ -233,7 +240,9 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_ovl_tc(OzArgs g, int* err) {
 
   const uint32_t idesc = tc::idesc_bf16(128, g.BNP);
   bool ok = true;
-  for (int kk = 0; kk < npanel; ++kk) {
+#pragma unroll
+  for (int kk = 0; kk < 2; ++kk) {
+    if (kk >= npanel) break;
     // the seven slice tiles of K panel kk: row r = 2 qq + part, k = p - 64 kk
 #pragma unroll
     for (int c = 0; c < OZ_COLS / 16; ++c) {
@@ -241,11 +250,11 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_ovl_tc(OzArgs g, int* err) {
       const int r0 = 2 * qq, r1 = r0 + 1;
 #pragma unroll
       for (int h = 0; h < 2; ++h) {
-        const int k = lane + 32 * h, p = 64 * kk + k;
-        const double2 v = (src[c] != nullptr && p < g.N) ? src[c][p] : make_double2(0.0, 0.0);
+        const int k = lane + 32 * h;
+        const double2 x = v[c][2 * kk + h];
         float a[OZ_S], b[OZ_S];
-        oz_slices_bits(v.x, er[c], a);
-        oz_slices_bits(v.y, ei[c], b);
+        oz_slices_bits(x.x, er[c], a);
+        oz_slices_bits(x.y, ei[c], b);
         const uint32_t o0 = (uint32_t)(r0 * 128 + ((((k >> 3) ^ (r0 & 7))) << 4) + (k & 7) * 2);
         const uint32_t o1 = (uint32_t)(r1 * 128 + ((((k >> 3) ^ (r1 & 7))) << 4) + (k & 7) * 2);
 #pragma unroll
