@@ -3,7 +3,9 @@ the FP64 overlap and the FP64 oracle.
 
 * Overlaps of perturbed walkers (det of M = Phi^T psi per channel) within
   1e-11 relative of the oracle and of the FP64-M kernel, for the RHF and UHF
-  walkers, N <= 64 (one 64-wide K panel per slice), N = 100 and N = 128.
+  walkers, N <= 64 (one 64-wide K panel per slice), N = 100 and N = 128: FP64
+  walkers (integer slicing of the bits) and, after one step, walkers of FP32
+  numbers (FP32 slicing).
 * One step with identical fields: weights within 1e-9 relative of the FP64-M
   kernel (the same FP32 propagation either way).
 * 100 steps with the mixed form's fastest kernels (tensor-core propagator,
@@ -70,7 +72,11 @@ def test_overlap_tc_matches_fp64(A, name):
         _, o, _ = wk.get_det()
         fb = wk.force_bias()
         wk.propagate_phaseless(xi, e0)
-        _, _, w1 = wk.get_det()
+        d1, o1_, w1 = wk.get_det()
+        if ovl == 3:
+            # after a step the walkers hold FP32 numbers: the FP32 slicing path
+            ref1 = O.overlap(ot, O.Walkers(oh, rw, d1))
+            assert np.abs(o1_ / ref1 - 1).max() < 1e-11, np.abs(o1_ / ref1 - 1).max()
         out[ovl] = (o, fb, w1)
     ref = O.overlap(ot, O.Walkers(oh, rw, dets))
     o3, fb3, w3 = out[3]

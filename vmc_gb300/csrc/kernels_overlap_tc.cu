@@ -109,9 +109,36 @@ __device__ __forceinline__ int oz_biased(double x) { return (__double2hiint(x) >
 __device__ __forceinline__ float oz_pow2f(double x) { return __int_as_float((oz_biased(x) - 1023 + 127) << 23); }
 // row scale sigma = 2^e, e = 1 + the largest unbiased exponent of the row (0 if all zero)
 __device__ __forceinline__ int oz_row_e(int max_biased) { return max_biased > 0 ? max_biased - 1022 : 0; }
+// x as an FP32 number h, when it is one (zero, or a normal FP32 value: the low
+// 29 fraction bits are zero), from the bits
+__device__ __forceinline__ bool oz_as_f32(double x, float& h) {
+  const uint32_t whi = (uint32_t)__double2hiint(x), wlo = (uint32_t)__double2loint(x);
+  const int E = (int)((whi >> 20) & 0x7FFu) - 1023;
+  if ((whi & 0x7FFFFFFFu) == 0u && wlo == 0u) {
+    h = 0.f;
+    return true;
+  }
+  h = __uint_as_float((whi & 0x80000000u) | ((uint32_t)(E + 127) << 23) | ((whi & 0xFFFFFu) << 3) | (wlo >> 29));
+  return (wlo & 0x1FFFFFFFu) == 0u && E >= -126 && E <= 127;
+}
+// Slices of an FP32 number h for the row scale 2^e (|h| < 2^e) in FP32
+// arithmetic: y = h 2^(7 - e), a_s = rint(y), y <- (y - a_s) 256.  Every step is
+// exact (|y| <= 128, y - rint(y) is exact, the scalings are by powers of two),
+// |a_s| <= 128, and h = 2^e 2^-7 sum_s a_s 2^-8s up to the dropped remainder
+// (below 2^(e - 56)), as with the integer digits.
+__device__ __forceinline__ void oz_slices_f32(float h, int e, float* a) {
+  float y = __fmul_rn(h, __int_as_float((127 + 7 - e) << 23));
+#pragma unroll
+  for (int t = 0; t < OZ_S; ++t) {
+    const float d = rintf(y);
+    a[t] = d;
+    y = __fmul_rn(__fsub_rn(y, d), 256.f);
+  }
+}
 
 // Swizzled (128-byte, K-major) image of one channel's trial-orbital slices:
-// img[t][kk][BNP rows][64] for slice t and K panel kk; tau[i] per orbital.
+// img[kk][t][BNP rows][64] for K panel kk and slice t (the seven slices of a
+// panel are one operand of 7 BNP rows); tau[i] per orbital.
 // One warp per orbital i < BNP (rows i >= n are zero).  phi: the channel's
 // orbitals, column i at i N.
 __global__ void k_ovl_bimage(const double* __restrict__ phi, int N, int n, int KP, int BNP,
@@ -125,7 +152,6 @@ __global__ void k_ovl_bimage(const double* __restrict__ phi, int N, int n, int K
   for (int o = 16; o > 0; o >>= 1) mb = max(mb, __shfl_xor_sync(0xffffffffu, mb, o));
   const int e = oz_row_e(mb);
   if (lane == 0) tau[i] = i < n ? ldexp(1.0, e) : 0.0;
-  const int npanel = KP / 64;
   for (int p = lane; p < KP; p += 32) {
     float a[OZ_S];
     const double v = (i < n && p < N) ? phi[(size_t)i * N + p] : 0.0;
@@ -134,7 +160,7 @@ __global__ void k_ovl_bimage(const double* __restrict__ phi, int N, int n, int K
     const uint32_t off = (uint32_t)(i * 128 + (((k >> 3) ^ (i & 7)) * 16) + (k & 7) * 2);
 #pragma unroll
     for (int t = 0; t < OZ_S; ++t) {
-      uint8_t* panel = (uint8_t*)img + (size_t)(t * npanel + kk) * BNP * 128;
+      uint8_t* panel = (uint8_t*)img + (size_t)(kk * OZ_S + t) * BNP * 128;
       *(__nv_bfloat16*)(panel + off) = __float2bfloat16_rn(a[t]);
     }
   }
@@ -202,10 +228,12 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_ovl_tc(OzArgs g, int* err) {
   }
 
   // this warp's columns qq = warp + 16 c: all of their values are loaded at
-  // once (lane p + 32 it, it < 4, N <= 128), then the row scales and both K
-  // panels' slices come from registers -- one load latency per tile
+  // once (lane: positions 2 lane and 2 lane + 1 of both K panels, N <= 128),
+  // then the row scales and both panels' slices come from registers -- one
+  // load latency per tile
   double2 v[OZ_COLS / 16][4];
   int er[OZ_COLS / 16], ei[OZ_COLS / 16];
+  bool f32r[OZ_COLS / 16], f32i[OZ_COLS / 16];  // the column part holds FP32 numbers only
 #pragma unroll
   for (int c = 0; c < OZ_COLS / 16; ++c) {
     const int q = q0 + warp + 16 * c;
@@ -214,7 +242,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_ovl_tc(OzArgs g, int* err) {
     const double2* src = g.psi + ((size_t)(qs / max(n_c, 1)) * g.ncw + off_c + qs % max(n_c, 1)) * g.N;
 #pragma unroll
     for (int it = 0; it < 4; ++it) {
-      const int p = lane + 32 * it;
+      const int p = 64 * (it >> 1) + 2 * lane + (it & 1);  // lane: K positions 2 lane, 2 lane + 1 of each panel
       v[c][it] = (valid && p < g.N) ? src[p] : make_double2(0.0, 0.0);
     }
   }
@@ -232,35 +260,55 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_ovl_tc(OzArgs g, int* err) {
     }
     er[c] = oz_row_e(br);
     ei[c] = oz_row_e(bi);
+    bool fr = true, fi = true;
+#pragma unroll
+    for (int it = 0; it < 4; ++it) {
+      float t;
+      fr = fr && oz_as_f32(v[c][it].x, t);
+      fi = fi && oz_as_f32(v[c][it].y, t);
+    }
+    f32r[c] = __all_sync(0xffffffffu, fr);
+    f32i[c] = __all_sync(0xffffffffu, fi);
     if (lane == 0) {
       s_e[2 * (warp + 16 * c)] = er[c];
       s_e[2 * (warp + 16 * c) + 1] = ei[c];
     }
   }
 
-  const uint32_t idesc = tc::idesc_bf16(128, g.BNP);
   bool ok = true;
 #pragma unroll
   for (int kk = 0; kk < 2; ++kk) {
     if (kk >= npanel) break;
-    // the seven slice tiles of K panel kk: row r = 2 qq + part, k = p - 64 kk
+    // the seven slice tiles of K panel kk: row r = 2 qq + part, k = 2 lane (and
+    // 2 lane + 1, packed in one 32-bit store); FP32 arithmetic for a column
+    // part of FP32 numbers (the walkers of the mixed form between steps), the
+    // integer digits of the FP64 bits otherwise
 #pragma unroll
     for (int c = 0; c < OZ_COLS / 16; ++c) {
       const int qq = warp + 16 * c;
-      const int r0 = 2 * qq, r1 = r0 + 1;
+      const int k = 2 * lane;
 #pragma unroll
-      for (int h = 0; h < 2; ++h) {
-        const int k = lane + 32 * h;
-        const double2 x = v[c][2 * kk + h];
-        float a[OZ_S], b[OZ_S];
-        oz_slices_bits(x.x, er[c], a);
-        oz_slices_bits(x.y, ei[c], b);
-        const uint32_t o0 = (uint32_t)(r0 * 128 + ((((k >> 3) ^ (r0 & 7))) << 4) + (k & 7) * 2);
-        const uint32_t o1 = (uint32_t)(r1 * 128 + ((((k >> 3) ^ (r1 & 7))) << 4) + (k & 7) * 2);
+      for (int part = 0; part < 2; ++part) {
+        const int r = 2 * qq + part;
+        const double x0 = part ? v[c][2 * kk].y : v[c][2 * kk].x;
+        const double x1 = part ? v[c][2 * kk + 1].y : v[c][2 * kk + 1].x;
+        const int e = part ? ei[c] : er[c];
+        float a0[OZ_S], a1[OZ_S];
+        if (part ? f32i[c] : f32r[c]) {
+          float h0, h1;
+          oz_as_f32(x0, h0);
+          oz_as_f32(x1, h1);
+          oz_slices_f32(h0, e, a0);
+          oz_slices_f32(h1, e, a1);
+        } else {
+          oz_slices_bits(x0, e, a0);
+          oz_slices_bits(x1, e, a1);
+        }
+        const uint32_t o = (uint32_t)(r * 128 + ((((k >> 3) ^ (r & 7))) << 4) + (k & 7) * 2);
 #pragma unroll
         for (int t = 0; t < OZ_S; ++t) {
-          *(__nv_bfloat16*)(sA + t * OZ_TILE + o0) = __float2bfloat16_rn(a[t]);
-          *(__nv_bfloat16*)(sA + t * OZ_TILE + o1) = __float2bfloat16_rn(b[t]);
+          const __nv_bfloat162 pr = __floats2bfloat162_rn(a0[t], a1[t]);  // k in the low half
+          *(uint32_t*)(sA + t * OZ_TILE + o) = *(const uint32_t*)&pr;
         }
       }
     }
@@ -271,16 +319,16 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_ovl_tc(OzArgs g, int* err) {
       tc::tc_fence_after();
       if (kk == 0 && !tc::mbar_wait(bload, 0, err, 32)) s_abort = 1;
       if (!s_abort) {
+        // slice sl against the panel's trial slices t = 0 .. 6 - sl (stacked rows)
+        // accumulates levels L = sl + t into TMEM columns L BNP: one MMA per K step
+        const uint32_t ba = tc::smem_u32(sB) + (uint32_t)(kk * OZ_S * g.BNP * 128);
         for (int sl = 0; sl < OZ_S; ++sl) {
           const uint32_t aa = tc::smem_u32(sA + sl * OZ_TILE);
-          for (int L = sl; L < OZ_S; ++L) {
-            const int t = L - sl;
-            const uint32_t ba = tc::smem_u32(sB) + (uint32_t)((t * npanel + kk) * g.BNP * 128);
+          const uint32_t idesc = tc::idesc_bf16(128, (OZ_S - sl) * g.BNP);
 #pragma unroll
-            for (int k = 0; k < 4; ++k)  // +32 bytes per K=16 step inside the swizzle row
-              tc::mma_bf16(tmem + (uint32_t)(L * g.BNP), tc::sdesc_sw128(aa + 32 * k),
-                           tc::sdesc_sw128(ba + 32 * k), idesc, (sl > 0 || kk > 0 || k > 0) ? 1u : 0u);
-          }
+          for (int k = 0; k < 4; ++k)  // +32 bytes per K=16 step inside the swizzle row
+            tc::mma_bf16(tmem + (uint32_t)(sl * g.BNP), tc::sdesc_sw128(aa + 32 * k),
+                         tc::sdesc_sw128(ba + 32 * k), idesc, (sl > 0 || kk > 0 || k > 0) ? 1u : 0u);
         }
       }
       tc::mma_commit(mdone);  // also when nothing was issued: the waiters are released
