@@ -35,14 +35,21 @@ __device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* tm, ui
 }
 
 constexpr int EX_BN = 256;  // TMEM columns / max B rows per tile
-constexpr int EX_STAGES = 3;
+constexpr int EX_STAGES = 2;  // two stages keep a CTA under half the SM's shared memory: 2 CTAs per SM
 constexpr int EX_A_BYTES = BM * BK * 2;       // 16 KB
 constexpr int EX_B_BYTES = EX_BN * BK * 2;    // 32 KB
 constexpr int EX_STAGE = EX_A_BYTES + EX_B_BYTES;
-constexpr int EX_BAR_OFF = EX_STAGES * EX_STAGE;
-constexpr int EX_SMEM = EX_BAR_OFF + (2 * EX_STAGES + 1) * 8 + 16 + 1024;
-constexpr int EX_LD = EX_BN + 1;  // fp32 row pitch of the staged tile
-static_assert(BM * EX_LD * 4 <= EX_BAR_OFF, "staged tile must fit in the pipeline buffers");
+constexpr int EX_HEAD = 1024;  // barriers and the TMEM address, ahead of the (1024-aligned) stages
+constexpr int EX_PIPE = EX_STAGES * EX_STAGE;
+static_assert((2 * EX_STAGES + 1) * 8 + 16 <= EX_HEAD, "barrier block");
+
+// fp32 row pitch of one walker's staged columns [2 wl n, 2 (wl + 1) n) widened
+// to 16-column bounds (at most 2n rounded up, plus 16, and at most the tile)
+static int ex_pitch(int n) { return std::min(EX_BN, (2 * n + 15) / 16 * 16 + 16) + 1; }
+// dynamic shared memory: the stages, which the staged columns reuse
+static size_t ex_smem(int n) {
+  return 1024 + EX_HEAD + std::max((size_t)EX_PIPE, (size_t)BM * ex_pitch(n) * 4);
+}
 
 struct ExArgs {
   int n;          // occupied orbitals of this channel
@@ -50,19 +57,23 @@ struct ExArgs {
   int a_bytes, b_bytes;
   int col_off;    // channel column offset in the [nce] axis
   int s;          // channel index
+  int ld;         // fp32 pitch of the staged walker columns (ex_pitch(n))
 };
 
 // grid: (walker tiles, g tiles, channels); EX_THREADS threads: warp 0 lane 0
-// loads, warp 1 lane 0 issues the MMAs, and all warps share the epilogue
-// (warp w reads TMEM lane quadrant w % 4, column half w / 4)
+// loads, warp 1 lane 0 issues the MMAs, and all warps share the epilogue,
+// one walker of the tile at a time: its 2n columns are copied from TMEM to
+// shared memory (warp w reads lane quadrant w % 4, 16-column pieces w / 4,
+// w / 4 + 2, ...) and warp w then reduces the (g, walker) blocks gl = w, w + 8, ...
 constexpr int EX_THREADS = 256;
-__global__ void __launch_bounds__(EX_THREADS, 1)
+__global__ void __launch_bounds__(EX_THREADS, 2)
     k_tc_exchange(const __grid_constant__ CUtensorMap tmA0, const __grid_constant__ CUtensorMap tmB0,
                   const __grid_constant__ CUtensorMap tmA1, const __grid_constant__ CUtensorMap tmB1, ExArgs a0,
                   ExArgs a1, int Gene, int W, int K, int nchan, double2* __restrict__ xc, int* err) {
   extern __shared__ uint8_t smem_raw[];
-  uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-  uint64_t* full = (uint64_t*)(smem + EX_BAR_OFF);
+  uint8_t* head = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  uint8_t* smem = head + EX_HEAD;  // stages (1024-aligned for the 128-byte swizzle)
+  uint64_t* full = (uint64_t*)head;
   uint64_t* empty = full + EX_STAGES;
   uint64_t* accum = empty + EX_STAGES;
   uint32_t* tmem_holder = (uint32_t*)(accum + 1);
@@ -132,50 +143,61 @@ __global__ void __launch_bounds__(EX_THREADS, 1)
     for (int kb = (issued > EX_STAGES ? issued - EX_STAGES : 0); kb < issued; ++kb)
       tc::mbar_wait(&full[kb % EX_STAGES], (kb / EX_STAGES) & 1, err, 14);
   }
-  __syncthreads();  // all loads consumed: the pipeline buffers become the staging tile
+  __syncthreads();  // all loads consumed: the pipeline buffers become the staging buffer
   float* tile = (float*)smem;
-  const int n = A.n, ncols = 2 * A.wbox * n;
-  if (have && !s_abort) {
-    const int q = warp & 3, half = warp >> 2;
-    const int row = q * 32 + lane;
+  const int n = A.n, ld = A.ld;
+  const bool run = have && !s_abort;
+  const int q = warp & 3;
+  const int row = q * 32 + lane;
+  // walk of the n x n block: lane's first (i, j) and the step of 32 entries
+  const int dq = 32 / n, dr = 32 - dq * n;
 #pragma unroll 1
-    for (int c = half * (EX_BN / 2); c < (half + 1) * (EX_BN / 2); c += 16) {
-      float v[16];
-      tc::tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)c, v);
-      if (c < ncols) {
+  for (int wl = 0; wl < A.wbox; ++wl) {
+    const int w = w0 + wl;
+    const int c_lo = (2 * wl * n) & ~15, c_hi = (2 * (wl + 1) * n + 15) & ~15;
+    if (run && w < W) {
+#pragma unroll 1
+      for (int c = c_lo + (warp >> 2) * 16; c < c_hi; c += 32) {
+        float v[16];
+        tc::tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)c, v);
 #pragma unroll
-        for (int j = 0; j < 16; ++j) tile[row * EX_LD + c + j] = v[j];
+        for (int j = 0; j < 16; ++j) tile[row * ld + (c - c_lo) + j] = v[j];
       }
     }
-  }
-  __syncthreads();
-  if (have && !s_abort) {
-    const int npairs = A.gbox * A.wbox;
-    for (int pr = warp; pr < npairs; pr += EX_THREADS / 32) {
-      const int gl = pr / A.wbox, wl = pr % A.wbox;
-      const int g = g0 + gl, w = w0 + wl;
-      if (g >= Gene || w >= W) continue;
-      const float* rowbase = tile + (gl * n) * EX_LD;
-      const int cre = (2 * wl) * n, cim = (2 * wl + 1) * n;
-      float xr = 0.f, xi = 0.f, cr = 0.f, ci = 0.f;
-      for (int e = lane; e < n * n; e += 32) {
-        const int i = e / n, j = e % n;
-        const float a_r = rowbase[i * EX_LD + cre + j], a_i = rowbase[i * EX_LD + cim + j];
-        const float b_r = rowbase[j * EX_LD + cre + i], b_i = rowbase[j * EX_LD + cim + i];
-        xr = fmaf(a_r, b_r, fmaf(-a_i, b_i, xr));
-        xi = fmaf(a_r, b_i, fmaf(a_i, b_r, xi));
-        if (i == j) { cr += a_r; ci += a_i; }
-      }
-      xr = warp_sumf(xr);
-      xi = warp_sumf(xi);
-      cr = warp_sumf(cr);
-      ci = warp_sumf(ci);
-      if (lane == 0) {
-        double2* o = xc + (((size_t)w * 2 + A.s) * Gene + g) * 2;
-        o[0] = make_double2(xr, xi);
-        o[1] = make_double2(cr, ci);
+    __syncthreads();
+    if (run && w < W) {
+      const int cre = 2 * wl * n - c_lo, cim = cre + n;
+      for (int gl = warp; gl < A.gbox; gl += EX_THREADS / 32) {
+        const int g = g0 + gl;
+        if (g >= Gene) continue;
+        const float* rowbase = tile + (gl * n) * ld;
+        float xr = 0.f, xi = 0.f, cr = 0.f, ci = 0.f;
+        int i = lane / n, j = lane % n;
+        for (int e = lane; e < n * n; e += 32) {
+          const float a_r = rowbase[i * ld + cre + j], a_i = rowbase[i * ld + cim + j];
+          const float b_r = rowbase[j * ld + cre + i], b_i = rowbase[j * ld + cim + i];
+          xr = fmaf(a_r, b_r, fmaf(-a_i, b_i, xr));
+          xi = fmaf(a_r, b_i, fmaf(a_i, b_r, xi));
+          if (i == j) { cr += a_r; ci += a_i; }
+          i += dq;
+          j += dr;
+          if (j >= n) {
+            j -= n;
+            ++i;
+          }
+        }
+        xr = warp_sumf(xr);
+        xi = warp_sumf(xi);
+        cr = warp_sumf(cr);
+        ci = warp_sumf(ci);
+        if (lane == 0) {
+          double2* o = xc + (((size_t)w * 2 + A.s) * Gene + g) * 2;
+          o[0] = make_double2(xr, xi);
+          o[1] = make_double2(cr, ci);
+        }
       }
     }
+    __syncthreads();  // the chunk is consumed before the next one is staged
   }
   tc::tc_fence_before();
   __syncthreads();
@@ -228,10 +250,11 @@ void launch_local_energy_mixed_subset(afqmc_handle* h, const int* d_idx, int m, 
   else split_rows(h, h->theta32, Kn, 2 * m * h->nce, Kn, h->ke_pad, 1, h->thetaE);
   static bool attr = false;
   if (!attr) {
-    cudaFuncSetAttribute(k_tc_exchange, cudaFuncAttributeMaxDynamicSharedMemorySize, EX_SMEM);
+    cudaFuncSetAttribute(k_tc_exchange, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ex_smem(128));
     attr = true;
   }
   ExArgs a[2];
+  size_t smem = 0;
   int gt = 1, wt = 1;
   for (int s = 0; s < h->nchan; ++s) {
     const int n = h->chan[s].n;
@@ -242,13 +265,15 @@ void launch_local_energy_mixed_subset(afqmc_handle* h, const int* d_idx, int m, 
     a[s].b_bytes = BK * 2 * n * 2 * a[s].wbox;
     a[s].col_off = h->chan[s].col_off;
     a[s].s = s;
+    a[s].ld = ex_pitch(n);
+    smem = std::max(smem, ex_smem(n));
     gt = std::max(gt, (h->nchol_ene + a[s].gbox - 1) / a[s].gbox);
     wt = std::max(wt, (m + a[s].wbox - 1) / a[s].wbox);
   }
   if (h->nchan == 1) a[1] = a[0];
   if (h->nchol_ene > 0) {
     dim3 grid(wt, gt, h->nchan);
-    k_tc_exchange<<<grid, EX_THREADS, EX_SMEM, h->stream>>>(h->tm_rotE[0], h->tm_thE[0], h->tm_rotE[h->nchan - 1],
+    k_tc_exchange<<<grid, EX_THREADS, smem, h->stream>>>(h->tm_rotE[0], h->tm_thE[0], h->tm_rotE[h->nchan - 1],
                                                     h->tm_thE[h->nchan - 1], a[0], a[1], h->nchol_ene, m, h->ke_pad,
                                                     h->nchan, h->xc, h->d_err);
     h->launches++;
