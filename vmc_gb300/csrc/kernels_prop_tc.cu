@@ -95,13 +95,22 @@ __global__ void k_pt_image(const float* __restrict__ expm32, __nv_bfloat16* __re
   img[(size_t)(2 * s + 1) * PT_IMG + o] = lo;
 }
 
-// Start the copy of one spin block's B - I image (hi and lo, 128 KB) into A.
-__device__ __forceinline__ void pt_issue_image(uint8_t* sA, const __nv_bfloat16* img, uint64_t* bar) {
+// Start the copy of one spin block's B - I image into A: hi and lo, 64 KB each,
+// or, when B is real, only the two K panels of its real block (32 KB each) --
+// the products with a real B read no further, and the imaginary panels keep
+// zeros or V's imaginary part, never read by them.  The copies of this image
+// (the same one for every walker) are the largest cost of the kernel after
+// the products themselves, so a real B halves them.
+__device__ __forceinline__ void pt_issue_image(uint8_t* sA, const __nv_bfloat16* img, uint64_t* bar, bool realB) {
   if (threadIdx.x == 0) {
-    tc::mbar_expect_tx(bar, 2 * PT_A_BYTES);
+    const int bytes = realB ? PT_A_BYTES / 2 : PT_A_BYTES;  // per half
+    tc::mbar_expect_tx(bar, 2 * bytes);
     const uint8_t* src = (const uint8_t*)img;
 #pragma unroll 1
-    for (int o = 0; o < 2 * PT_A_BYTES; o += PT_COPY) pt_bulk(sA + o, src + o, PT_COPY, bar);
+    for (int h = 0; h < 2; ++h)
+#pragma unroll 1
+      for (int o = 0; o < bytes; o += PT_COPY)
+        pt_bulk(sA + h * PT_A_BYTES + o, src + h * PT_A_BYTES + o, PT_COPY, bar);
   }
 }
 
@@ -271,8 +280,15 @@ __global__ void __launch_bounds__(PT_THREADS, 1)
     tc::fence_mbar_init();
   }
   if (warp == 0) tc::tmem_alloc(tmem_holder, PT_TMEM_COLS);
-  // B operand: K positions no row of X is written to stay zero
+  // B operand: K positions no row of X is written to stay zero; with a real B
+  // the imaginary K panels of A are never copied from the image, so their
+  // padding (rows >= N, K >= 128 + N) is zeroed here and V's scatter leaves it
   for (int e = threadIdx.x; e < 2 * PT_B_BYTES / 16; e += blockDim.x) ((uint4*)sB)[e] = make_uint4(0, 0, 0, 0);
+  if (realB)
+    for (int e = threadIdx.x; e < PT_A_BYTES / 16; e += blockDim.x) {
+      const int h = e / (PT_A_BYTES / 32), o = e % (PT_A_BYTES / 32);  // half, 16-byte word of its panels 2-3
+      ((uint4*)(sA + h * PT_A_BYTES + PT_A_BYTES / 2))[o] = make_uint4(0, 0, 0, 0);
+    }
   tc::tc_fence_before();
   __syncthreads();
   tc::tc_fence_after();
@@ -302,7 +318,7 @@ __global__ void __launch_bounds__(PT_THREADS, 1)
     const int nc = ((2 * ncols + 15) / 16) * 16;
     float x[PT_CW], acc[PT_CW];
     __syncthreads();
-    pt_issue_image(sA, im, bar_ld);
+    pt_issue_image(sA, im, bar_ld, realB != 0);
 #pragma unroll
     for (int jj = 0; jj < PT_CW / 2; ++jj) {
       const int j = g * (PT_CW / 2) + jj;
@@ -336,7 +352,7 @@ __global__ void __launch_bounds__(PT_THREADS, 1)
     }
     if (!ok) break;
     // B (sum) = sum + (B - I) sum
-    pt_issue_image(sA, im, bar_ld);
+    pt_issue_image(sA, im, bar_ld, realB != 0);
 #pragma unroll
     for (int c = 0; c < PT_CW; ++c) x[c] = acc[c];
     if (p < N) pt_store_X(sB, x, nc, p, !realB, g);
