@@ -121,9 +121,18 @@ __device__ __forceinline__ bool pt_wait(uint64_t* bar, uint32_t& phase, int* err
   return __syncthreads_and(ok ? 1 : 0) != 0;
 }
 
-constexpr int PT_TMEM_COLS = 128;  // the 128 x 80 product tile
+// Independent accumulators: every MMA of a product into one TMEM tile would
+// make each wait for the previous one's result, and at N = 80 that latency,
+// not the tensor core's rate, set the pace (~6x the MMA's own time, measured).
+// Pass p (hi.hi, lo.hi, hi.lo) of K step s accumulates into tile 2 p + (s & 1),
+// so consecutive MMAs are independent; the threads add the six tiles in FP32
+// (round to nearest) when they read the product.
+constexpr int PT_NACC = 6;
+constexpr int PT_TMEM_COLS = 512;  // six 128 x 80 tiles (one CTA per SM)
+static_assert(PT_NACC * PT_NCMAX <= PT_TMEM_COLS, "accumulator tiles fit the allocation");
 
-// TMEM[128 x nc] = A . B^T over the first ns K-steps of 16, three split passes.
+// TMEM tiles a = 0..5 [128 x nc] summing to A . B^T over the first ns K-steps
+// of 16 (ns even), three split passes.
 __device__ __forceinline__ bool pt_product(uint8_t* sA, uint8_t* sB, int nc, int ns, uint32_t tmem, uint64_t* bar,
                                            uint32_t& phase, int* err) {
   pt_fence_proxy();  // this thread's generic writes to A / B -> visible to the tensor core
@@ -135,15 +144,15 @@ __device__ __forceinline__ bool pt_product(uint8_t* sA, uint8_t* sB, int nc, int
     const uint32_t a_hi = tc::smem_u32(sA), a_lo = a_hi + PT_A_BYTES;
     const uint32_t b_hi = tc::smem_u32(sB), b_lo = b_hi + PT_B_BYTES;
 #pragma unroll 1
-    for (int pass = 0; pass < 3; ++pass) {
-      const uint32_t a0 = pass == 1 ? a_lo : a_hi;
-      const uint32_t b0 = pass == 2 ? b_lo : b_hi;
-#pragma unroll 1
-      for (int s = 0; s < ns; ++s) {
-        const uint32_t ao = (uint32_t)((s >> 2) * 128 * 128 + (s & 3) * 32);
-        const uint32_t bo = (uint32_t)((s >> 2) * nc * 128 + (s & 3) * 32);
-        tc::mma_bf16(tmem, tc::sdesc_sw128(a0 + ao), tc::sdesc_sw128(b0 + bo), idesc,
-                     (pass > 0 || s > 0) ? 1u : 0u);
+    for (int s = 0; s < ns; ++s) {
+      const uint32_t ao = (uint32_t)((s >> 2) * 128 * 128 + (s & 3) * 32);
+      const uint32_t bo = (uint32_t)((s >> 2) * nc * 128 + (s & 3) * 32);
+#pragma unroll
+      for (int pass = 0; pass < 3; ++pass) {
+        const uint32_t a0 = pass == 1 ? a_lo : a_hi;
+        const uint32_t b0 = pass == 2 ? b_lo : b_hi;
+        const uint32_t acc = (uint32_t)((2 * pass + (s & 1)) * PT_NCMAX);
+        tc::mma_bf16(tmem + acc, tc::sdesc_sw128(a0 + ao), tc::sdesc_sw128(b0 + bo), idesc, s >= 2 ? 1u : 0u);
       }
     }
     tc::mma_commit(bar);
@@ -231,21 +240,36 @@ __device__ __forceinline__ void pt_load_V(uint8_t* sA, const float* __restrict__
   }
 }
 
-// PT_CW = 20 columns of this thread's TMEM lane from taddr (x16 + x4), one wait
-__device__ __forceinline__ void pt_tmem_ld(uint32_t taddr, float* v) {
-  uint32_t u[PT_CW];
+// PT_CW = 20 columns of this thread's TMEM lane at taddr and at taddr2 (x16 + x4 each), one wait
+__device__ __forceinline__ void pt_tmem_ld2(uint32_t taddr, uint32_t taddr2, uint32_t* u, uint32_t* w) {
   asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%20];\n"
-      "tcgen05.ld.sync.aligned.32x32b.x4.b32 {%16,%17,%18,%19}, [%21];\n"
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%40];\n"
+      "tcgen05.ld.sync.aligned.32x32b.x4.b32 {%16,%17,%18,%19}, [%41];\n"
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31,%32,%33,%34,%35}, [%42];\n"
+      "tcgen05.ld.sync.aligned.32x32b.x4.b32 {%36,%37,%38,%39}, [%43];\n"
       "tcgen05.wait::ld.sync.aligned;\n"
-      : "=r"(u[0]), "=r"(u[1]), "=r"(u[2]), "=r"(u[3]), "=r"(u[4]), "=r"(u[5]), "=r"(u[6]), "=r"(u[7]), "=r"(u[8]), "=r"(u[9]), "=r"(u[10]), "=r"(u[11]), "=r"(u[12]), "=r"(u[13]), "=r"(u[14]), "=r"(u[15]), "=r"(u[16]), "=r"(u[17]), "=r"(u[18]), "=r"(u[19])
-      : "r"(taddr), "r"(taddr + 16)
+      : "=r"(u[0]), "=r"(u[1]), "=r"(u[2]), "=r"(u[3]), "=r"(u[4]), "=r"(u[5]), "=r"(u[6]), "=r"(u[7]), "=r"(u[8]), "=r"(u[9]), "=r"(u[10]), "=r"(u[11]), "=r"(u[12]), "=r"(u[13]), "=r"(u[14]), "=r"(u[15]), "=r"(u[16]), "=r"(u[17]), "=r"(u[18]), "=r"(u[19]),
+        "=r"(w[0]), "=r"(w[1]), "=r"(w[2]), "=r"(w[3]), "=r"(w[4]), "=r"(w[5]), "=r"(w[6]), "=r"(w[7]), "=r"(w[8]), "=r"(w[9]), "=r"(w[10]), "=r"(w[11]), "=r"(w[12]), "=r"(w[13]), "=r"(w[14]), "=r"(w[15]), "=r"(w[16]), "=r"(w[17]), "=r"(w[18]), "=r"(w[19])
+      : "r"(taddr), "r"(taddr + 16), "r"(taddr2), "r"(taddr2 + 16)
       : "memory");
-#pragma unroll
-  for (int i = 0; i < PT_CW; ++i) v[i] = __uint_as_float(u[i]);
 }
 
-static_assert(PT_CW == 20 && PT_NG * PT_CW == PT_NCMAX, "the TMEM row helpers move 20 columns (x16 + x4)");
+// v = this thread's PT_CW product columns: the sum of the PT_NACC tiles at taddr
+__device__ __forceinline__ void pt_tmem_ld(uint32_t taddr, float* v) {
+#pragma unroll
+  for (int a = 0; a < PT_NACC; a += 2) {
+    uint32_t u[PT_CW], w[PT_CW];
+    pt_tmem_ld2(taddr + (uint32_t)(a * PT_NCMAX), taddr + (uint32_t)((a + 1) * PT_NCMAX), u, w);
+#pragma unroll
+    for (int i = 0; i < PT_CW; ++i) {
+      const float t = __uint_as_float(u[i]) + __uint_as_float(w[i]);
+      v[i] = a == 0 ? t : v[i] + t;
+    }
+  }
+}
+
+static_assert(PT_CW == 20 && PT_NG * PT_CW == PT_NCMAX && PT_NACC % 2 == 0,
+              "the TMEM row helpers move 20 columns (x16 + x4) of two tiles at a time");
 
 // Additions are made by the threads (round to nearest): the tensor core's
 // accumulation of small products onto a stored O(1) value was measured to
