@@ -131,8 +131,32 @@ constexpr int PT_NACC = 6;
 constexpr int PT_TMEM_COLS = 512;  // six 128 x 80 tiles (one CTA per SM)
 static_assert(PT_NACC * PT_NCMAX <= PT_TMEM_COLS, "accumulator tiles fit the allocation");
 
+// The MMAs of one product, fully unrolled over the NS K-steps of 16: the
+// descriptors' low words are formed once and each instruction adds constant
+// offsets (one thread issues them all, and at N <= 80 the issue path, not the
+// tensor core, bounded a rolled loop that rebuilt both descriptors per MMA).
+template <int NS>
+__device__ __forceinline__ void pt_issue(uint32_t tmem, uint8_t* sA, uint8_t* sB, int nc) {
+  const uint32_t idesc = tc::idesc_bf16(128, nc);
+  const uint32_t dah = tc::sdesc_lo(tc::smem_u32(sA)), dal = dah + (PT_A_BYTES >> 4);
+  const uint32_t dbh = tc::sdesc_lo(tc::smem_u32(sB)), dbl = dbh + (PT_B_BYTES >> 4);
+  const uint32_t bpanel = (uint32_t)(nc * 128) >> 4;  // B K-panel stride, 16-byte units
+#pragma unroll
+  for (int s = 0; s < NS; ++s) {
+    const uint32_t ao = (uint32_t)((s >> 2) * 128 * 128 + (s & 3) * 32) >> 4;
+    const uint32_t bo = (uint32_t)(s >> 2) * bpanel + (uint32_t)((s & 3) * 2);
+#pragma unroll
+    for (int pass = 0; pass < 3; ++pass) {
+      const uint32_t a = (pass == 1 ? dal : dah) + ao;
+      const uint32_t b = (pass == 2 ? dbl : dbh) + bo;
+      tc::mma_bf16(tmem + (uint32_t)((2 * pass + (s & 1)) * PT_NCMAX), tc::sdesc_from_lo(a), tc::sdesc_from_lo(b),
+                   idesc, s >= 2 ? 1u : 0u);
+    }
+  }
+}
+
 // TMEM tiles a = 0..5 [128 x nc] summing to A . B^T over the first ns K-steps
-// of 16 (ns even), three split passes.
+// of 16 (ns = 8 or 16), three split passes.
 __device__ __forceinline__ bool pt_product(uint8_t* sA, uint8_t* sB, int nc, int ns, uint32_t tmem, uint64_t* bar,
                                            uint32_t& phase, int* err) {
   pt_fence_proxy();  // this thread's generic writes to A / B -> visible to the tensor core
@@ -140,21 +164,8 @@ __device__ __forceinline__ bool pt_product(uint8_t* sA, uint8_t* sB, int nc, int
   __syncthreads();
   if (threadIdx.x == 0) {
     tc::tc_fence_after();
-    const uint32_t idesc = tc::idesc_bf16(128, nc);
-    const uint32_t a_hi = tc::smem_u32(sA), a_lo = a_hi + PT_A_BYTES;
-    const uint32_t b_hi = tc::smem_u32(sB), b_lo = b_hi + PT_B_BYTES;
-#pragma unroll 1
-    for (int s = 0; s < ns; ++s) {
-      const uint32_t ao = (uint32_t)((s >> 2) * 128 * 128 + (s & 3) * 32);
-      const uint32_t bo = (uint32_t)((s >> 2) * nc * 128 + (s & 3) * 32);
-#pragma unroll
-      for (int pass = 0; pass < 3; ++pass) {
-        const uint32_t a0 = pass == 1 ? a_lo : a_hi;
-        const uint32_t b0 = pass == 2 ? b_lo : b_hi;
-        const uint32_t acc = (uint32_t)((2 * pass + (s & 1)) * PT_NCMAX);
-        tc::mma_bf16(tmem + acc, tc::sdesc_sw128(a0 + ao), tc::sdesc_sw128(b0 + bo), idesc, s >= 2 ? 1u : 0u);
-      }
-    }
+    if (ns == 8) pt_issue<8>(tmem, sA, sB, nc);
+    else pt_issue<16>(tmem, sA, sB, nc);
     tc::mma_commit(bar);
   }
   const bool ok = pt_wait(bar, phase, err, 21);

@@ -139,6 +139,17 @@ __device__ __forceinline__ uint64_t sdesc_sw128(uint32_t saddr) {
   return d;
 }
 
+// The same descriptor from its low word (sdesc_lo(saddr) + offset >> 4 for an
+// operand offset inside the first 256 KB of shared memory): issue loops form
+// the low words once and add constant offsets per instruction.
+__device__ __forceinline__ uint32_t sdesc_lo(uint32_t saddr) { return ((saddr & 0x3FFFFu) >> 4) | (1u << 16); }
+__device__ __forceinline__ uint64_t sdesc_from_lo(uint32_t lo) {
+  const uint32_t hi = (uint32_t)(1024 >> 4) | (1u << 14) | (2u << 29);
+  uint64_t d;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(d) : "r"(lo), "r"(hi));
+  return d;
+}
+
 // 32 lanes x 32 bit, 16 consecutive columns per thread
 __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
   uint32_t r[16];
