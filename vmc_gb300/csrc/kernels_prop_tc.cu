@@ -1,18 +1,20 @@
 // Tensor-core (tcgen05) propagator of the mixed form:
 //     psi <- B (sum_{k=0}^{5} V^k / k!) B psi          (DQMCWalker.cpp:424-431, :482-491)
 // for N <= 128.  One CTA (16 warps) per walker and V block.  Every complex
-// product M X is one real GEMM
-//     [Re MX | Im MX] = [Mr | Mi] . [[Xr, Xi], [-Xi, Xr]]
-// with K = 256: K columns [0, N) carry the real part of M, [128, 128 + N) the
-// imaginary part, the rest are zero.  A = M is 128 x 256 (rows >= N zero), the
-// B operand holds NC = 2 x (columns of X) rows: row (j, re) = [Xr(:, j) | -Xi(:, j)],
-// row (j, im) = [Xi(:, j) | Xr(:, j)].  Both operands are split into BF16
-// high and low parts (x = hi + lo) and the product is accumulated in FP32 in
+// product M X is formed from two real GEMMs with one B operand,
+//     C1 = Mr . [Xr, Xi],   C2 = Mi . [Xr, Xi],
+//     Re MX = C1 re - C2 im,   Im MX = C1 im + C2 re,
+// combined by the threads as they read the product.  A = M is 128 x 256 (rows
+// >= N zero): K columns [0, N) carry the real part of M, [128, 128 + N) the
+// imaginary part; the B operand holds NC = 2 x (columns of X) rows, row (j, re)
+// = Xr(:, j) and row (j, im) = Xi(:, j), K = 128.  A real M (B - I for a
+// real one-body propagator) needs C1 only.  Both operands are split into BF16
+// high and low parts (x = hi + lo) and the products are accumulated in FP32 in
 // TMEM from three MMA passes hi.hi + lo.hi + hi.lo (the dropped lo.lo term is
 // 2^-16 of the product), which keeps the propagator close to FP32 accuracy.
 //
-// Shared memory: A (hi, lo; 64 KB each) and B (hi, lo; up to 80 rows, 40 KB
-// each), K-major with the 128-byte swizzle (4 panels of 64 BF16 per row).
+// Shared memory: A (hi, lo; 64 KB each, 4 K panels of 64 BF16 per row) and B
+// (hi, lo; up to 80 rows, 2 K panels), K-major with the 128-byte swizzle.
 // B = exp(-dt/2 h1') is the same for every walker, so an error in its split
 // would bias every walker's overlap the same way; the tensor core therefore
 // multiplies by B - I (entries of order dt, whose split error is ~1e-8 of B)
@@ -24,7 +26,7 @@
 // of orbital row p = TMEM lane p: it reads them from each product with one
 // batched tcgen05.ld, keeps its part of the Taylor sum in registers (the
 // additions are its own, in FP32 round-to-nearest) and writes them back as K
-// column p (and 128 + p) of the next B operand.  Four warps share
+// column p of the next B operand.  Four warps share
 // each TMEM lane quadrant, so one 214 KB CTA per SM still keeps four warps per
 // scheduler to hide the load and barrier latencies.  Seven products per walker:
 // B, five Taylor terms, B.
@@ -45,7 +47,7 @@ constexpr int PT_NCMAX = 80;                       // max B rows (2 x 40 columns
 constexpr int PT_NG = 4;                           // column groups: 4 warps per TMEM lane quadrant
 constexpr int PT_CW = PT_NCMAX / PT_NG;            // B rows (product columns) per thread
 constexpr int PT_THREADS = 128 * PT_NG;
-constexpr int PT_B_BYTES = PT_NCMAX * PT_K * 2;    // one BF16 half of B
+constexpr int PT_B_BYTES = PT_NCMAX * 128 * 2;     // one BF16 half of B (K = 128: two panels)
 constexpr int PT_SMEM = 2 * PT_A_BYTES + 2 * PT_B_BYTES + 64 + 1024;
 constexpr int PT_IMG = 128 * PT_K;                 // BF16 elements of one half of the B image
 constexpr int PT_COPY = 16384;                     // bytes per bulk copy
@@ -121,51 +123,52 @@ __device__ __forceinline__ bool pt_wait(uint64_t* bar, uint32_t& phase, int* err
   return __syncthreads_and(ok ? 1 : 0) != 0;
 }
 
-// Independent accumulators: every MMA of a product into one TMEM tile would
-// make each wait for the previous one's result, and at N = 80 that latency,
-// not the tensor core's rate, set the pace (~6x the MMA's own time, measured).
-// Pass p (hi.hi, lo.hi, hi.lo) of K step s accumulates into tile 2 p + (s & 1),
-// so consecutive MMAs are independent; the threads add the six tiles in FP32
-// (round to nearest) when they read the product.
+// Independent accumulators: pass p (hi.hi, lo.hi, hi.lo) accumulates C1 in
+// TMEM tile p and C2 in tile 3 + p, so consecutive MMAs never wait for each
+// other's results, and the threads add the tiles in FP32 (round to nearest)
+// when they read the product.
 constexpr int PT_NACC = 6;
 constexpr int PT_TMEM_COLS = 512;  // six 128 x 80 tiles (one CTA per SM)
 static_assert(PT_NACC * PT_NCMAX <= PT_TMEM_COLS, "accumulator tiles fit the allocation");
 
-// The MMAs of one product, fully unrolled over the NS K-steps of 16: the
-// descriptors' low words are formed once and each instruction adds constant
-// offsets (one thread issues them all, and at N <= 80 the issue path, not the
-// tensor core, bounded a rolled loop that rebuilt both descriptors per MMA).
-template <int NS>
+// The MMAs of one product, fully unrolled over the 8 K-steps of 16 of the B
+// operand: the descriptors' low words are formed once and each instruction
+// adds constant offsets (one thread issues them all, and at N <= 80 the issue
+// path of a rolled loop that rebuilt both descriptors per MMA was measured to
+// bound the products).  CPLX: M has an imaginary block (A's K panels 2-3).
+template <bool CPLX>
 __device__ __forceinline__ void pt_issue(uint32_t tmem, uint8_t* sA, uint8_t* sB, int nc) {
   const uint32_t idesc = tc::idesc_bf16(128, nc);
   const uint32_t dah = tc::sdesc_lo(tc::smem_u32(sA)), dal = dah + (PT_A_BYTES >> 4);
   const uint32_t dbh = tc::sdesc_lo(tc::smem_u32(sB)), dbl = dbh + (PT_B_BYTES >> 4);
   const uint32_t bpanel = (uint32_t)(nc * 128) >> 4;  // B K-panel stride, 16-byte units
 #pragma unroll
-  for (int s = 0; s < NS; ++s) {
+  for (int s = 0; s < 8; ++s) {
     const uint32_t ao = (uint32_t)((s >> 2) * 128 * 128 + (s & 3) * 32) >> 4;
+    const uint32_t ai = ao + (uint32_t)((2 * 128 * 128) >> 4);  // the imaginary block: K panels 2-3
     const uint32_t bo = (uint32_t)(s >> 2) * bpanel + (uint32_t)((s & 3) * 2);
 #pragma unroll
     for (int pass = 0; pass < 3; ++pass) {
-      const uint32_t a = (pass == 1 ? dal : dah) + ao;
-      const uint32_t b = (pass == 2 ? dbl : dbh) + bo;
-      tc::mma_bf16(tmem + (uint32_t)((2 * pass + (s & 1)) * PT_NCMAX), tc::sdesc_from_lo(a), tc::sdesc_from_lo(b),
-                   idesc, s >= 2 ? 1u : 0u);
+      const uint32_t a = pass == 1 ? dal : dah;
+      const uint64_t b = tc::sdesc_from_lo((pass == 2 ? dbl : dbh) + bo);
+      tc::mma_bf16(tmem + (uint32_t)(pass * PT_NCMAX), tc::sdesc_from_lo(a + ao), b, idesc, s > 0 ? 1u : 0u);
+      if (CPLX)
+        tc::mma_bf16(tmem + (uint32_t)((3 + pass) * PT_NCMAX), tc::sdesc_from_lo(a + ai), b, idesc,
+                     s > 0 ? 1u : 0u);
     }
   }
 }
 
-// TMEM tiles a = 0..5 [128 x nc] summing to A . B^T over the first ns K-steps
-// of 16 (ns = 8 or 16), three split passes.
-__device__ __forceinline__ bool pt_product(uint8_t* sA, uint8_t* sB, int nc, int ns, uint32_t tmem, uint64_t* bar,
+// TMEM tiles 0..2 (C1) and, for a complex M, 3..5 (C2) [128 x nc] of M X.
+__device__ __forceinline__ bool pt_product(uint8_t* sA, uint8_t* sB, int nc, bool cplx, uint32_t tmem, uint64_t* bar,
                                            uint32_t& phase, int* err) {
   pt_fence_proxy();  // this thread's generic writes to A / B -> visible to the tensor core
   tc::tc_fence_before();
   __syncthreads();
   if (threadIdx.x == 0) {
     tc::tc_fence_after();
-    if (ns == 8) pt_issue<8>(tmem, sA, sB, nc);
-    else pt_issue<16>(tmem, sA, sB, nc);
+    if (cplx) pt_issue<true>(tmem, sA, sB, nc);
+    else pt_issue<false>(tmem, sA, sB, nc);
     tc::mma_commit(bar);
   }
   const bool ok = pt_wait(bar, phase, err, 21);
@@ -174,38 +177,24 @@ __device__ __forceinline__ bool pt_product(uint8_t* sA, uint8_t* sB, int nc, int
 }
 
 // This thread's part of row p of X (x[2jj] = Re X(p, j), x[2jj+1] = Im X(p, j)
-// for the columns j of group g) into K column p (and 128 + p when `both`) of
-// the B operand rows (j, re) and (j, im), split in BF16.  The swizzled offset
-// pt_off(r, k, nc) of row r = 20 g + jj splits into a per-thread part (K
-// panel and byte of k = p, the row block 20 g) and (c ^ (r & 7)) << 4 with
-// c = (p & 63) >> 3; since 20 g = 4 (g & 1) mod 8, r & 7 = (jj & 7) ^ 4 (g & 1),
-// so each store needs an XOR with a constant, a shift and an add.
-__device__ __forceinline__ void pt_store_X(uint8_t* sB, const float* x, int nc, int p, bool both, int g) {
+// for the columns j of group g) into K column p of the B operand rows (j, re)
+// and (j, im), split in BF16.  The swizzled offset pt_off(r, p, nc) of row
+// r = 20 g + jj splits into a per-thread part (K panel and byte of k = p, the
+// row block 20 g) and (c ^ (r & 7)) << 4 with c = (p & 63) >> 3; since
+// 20 g = 4 (g & 1) mod 8, r & 7 = (jj & 7) ^ 4 (g & 1), so each store needs an
+// XOR with a constant, a shift and an add.
+__device__ __forceinline__ void pt_store_X(uint8_t* sB, const float* x, int nc, int p, int g) {
   uint8_t* sBl = sB + PT_B_BYTES;
   const uint32_t base0 = (uint32_t)((p >> 6) * nc * 128 + (p & 7) * 2 + g * PT_CW * 128);
-  const uint32_t base1 = base0 + (uint32_t)(2 * nc * 128);  // k = 128 + p: two K panels further
   const uint32_t cq = (uint32_t)(((p & 63) >> 3) ^ (4 * (g & 1)));
 #pragma unroll
-  for (int jj = 0; jj < PT_CW; jj += 2) {
-    const int j2 = g * PT_CW + jj;
-    if (j2 < nc) {
-      __nv_bfloat16 rh, rl, ih, il;
-      pt_split(x[jj], rh, rl);
-      pt_split(x[jj + 1], ih, il);
-      const uint32_t x0 = ((cq ^ (uint32_t)(jj & 7)) << 4) + (uint32_t)(jj * 128);
-      const uint32_t x1 = ((cq ^ (uint32_t)((jj + 1) & 7)) << 4) + (uint32_t)((jj + 1) * 128);
-      const uint32_t o0 = base0 + x0, o1 = base0 + x1;
-      *(__nv_bfloat16*)(sB + o0) = rh;
-      *(__nv_bfloat16*)(sBl + o0) = rl;
-      *(__nv_bfloat16*)(sB + o1) = ih;
-      *(__nv_bfloat16*)(sBl + o1) = il;
-      if (both) {
-        const uint32_t q0 = base1 + x0, q1 = base1 + x1;
-        *(__nv_bfloat16*)(sB + q0) = __hneg(ih);
-        *(__nv_bfloat16*)(sBl + q0) = __hneg(il);
-        *(__nv_bfloat16*)(sB + q1) = rh;
-        *(__nv_bfloat16*)(sBl + q1) = rl;
-      }
+  for (int jj = 0; jj < PT_CW; ++jj) {
+    if (g * PT_CW + jj < nc) {
+      __nv_bfloat16 h, l;
+      pt_split(x[jj], h, l);
+      const uint32_t o = base0 + ((cq ^ (uint32_t)(jj & 7)) << 4) + (uint32_t)(jj * 128);
+      *(__nv_bfloat16*)(sB + o) = h;
+      *(__nv_bfloat16*)(sBl + o) = l;
     }
   }
 }
@@ -265,16 +254,41 @@ __device__ __forceinline__ void pt_tmem_ld2(uint32_t taddr, uint32_t taddr2, uin
       : "memory");
 }
 
-// v = this thread's PT_CW product columns: the sum of the PT_NACC tiles at taddr
-__device__ __forceinline__ void pt_tmem_ld(uint32_t taddr, float* v) {
-#pragma unroll
-  for (int a = 0; a < PT_NACC; a += 2) {
+// PT_CW = 20 columns of this thread's TMEM lane at taddr (x16 + x4), one wait
+__device__ __forceinline__ void pt_tmem_ld1(uint32_t taddr, uint32_t* u) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%20];\n"
+      "tcgen05.ld.sync.aligned.32x32b.x4.b32 {%16,%17,%18,%19}, [%21];\n"
+      "tcgen05.wait::ld.sync.aligned;\n"
+      : "=r"(u[0]), "=r"(u[1]), "=r"(u[2]), "=r"(u[3]), "=r"(u[4]), "=r"(u[5]), "=r"(u[6]), "=r"(u[7]), "=r"(u[8]), "=r"(u[9]), "=r"(u[10]), "=r"(u[11]), "=r"(u[12]), "=r"(u[13]), "=r"(u[14]), "=r"(u[15]), "=r"(u[16]), "=r"(u[17]), "=r"(u[18]), "=r"(u[19])
+      : "r"(taddr), "r"(taddr + 16)
+      : "memory");
+}
+
+// v = this thread's PT_CW columns of M X at taddr: C1 (tiles 0..2) for a real
+// M; for a complex M, Re = C1 re - C2 im and Im = C1 im + C2 re, pass by pass
+// (tiles p and 3 + p)
+__device__ __forceinline__ void pt_tmem_ld(uint32_t taddr, float* v, bool cplx) {
+  if (!cplx) {
     uint32_t u[PT_CW], w[PT_CW];
-    pt_tmem_ld2(taddr + (uint32_t)(a * PT_NCMAX), taddr + (uint32_t)((a + 1) * PT_NCMAX), u, w);
+    pt_tmem_ld2(taddr, taddr + (uint32_t)PT_NCMAX, u, w);
 #pragma unroll
-    for (int i = 0; i < PT_CW; ++i) {
-      const float t = __uint_as_float(u[i]) + __uint_as_float(w[i]);
-      v[i] = a == 0 ? t : v[i] + t;
+    for (int i = 0; i < PT_CW; ++i) v[i] = __uint_as_float(u[i]) + __uint_as_float(w[i]);
+    pt_tmem_ld1(taddr + (uint32_t)(2 * PT_NCMAX), u);
+#pragma unroll
+    for (int i = 0; i < PT_CW; ++i) v[i] += __uint_as_float(u[i]);
+    return;
+  }
+#pragma unroll
+  for (int pass = 0; pass < 3; ++pass) {
+    uint32_t u[PT_CW], w[PT_CW];  // C1 and C2 of this pass
+    pt_tmem_ld2(taddr + (uint32_t)(pass * PT_NCMAX), taddr + (uint32_t)((3 + pass) * PT_NCMAX), u, w);
+#pragma unroll
+    for (int i = 0; i < PT_CW; i += 2) {
+      const float re = __uint_as_float(u[i]) - __uint_as_float(w[i + 1]);
+      const float im = __uint_as_float(u[i + 1]) + __uint_as_float(w[i]);
+      v[i] = pass == 0 ? re : v[i] + re;
+      v[i + 1] = pass == 0 ? im : v[i + 1] + im;
     }
   }
 }
@@ -286,9 +300,9 @@ static_assert(PT_CW == 20 && PT_NG * PT_CW == PT_NCMAX && PT_NACC % 2 == 0,
 // accumulation of small products onto a stored O(1) value was measured to
 // shrink it systematically, which biased every walker's overlap.
 // y += the 20 columns at taddr
-__device__ __forceinline__ void pt_add_row(uint32_t taddr, float* y) {
+__device__ __forceinline__ void pt_add_row(uint32_t taddr, float* y, bool cplx) {
   float t[PT_CW];
-  pt_tmem_ld(taddr, t);
+  pt_tmem_ld(taddr, t, cplx);
 #pragma unroll
   for (int i = 0; i < PT_CW; ++i) y[i] += t[i];
 }
@@ -344,7 +358,6 @@ __global__ void __launch_bounds__(PT_THREADS, 1)
   const __nv_bfloat16* im = img + (size_t)sp * 2 * PT_IMG;
   const int col_lo = nspV == 1 ? 0 : (sp == 0 ? 0 : na);
   const int col_hi = nspV == 1 ? ncw : (sp == 0 ? na : ncw);
-  const int nsB = realB ? 8 : 16;  // K-steps of a product with B (imaginary block all zero when real)
   double2* pw = psi + (size_t)w * ncw * N;
   float2* pw32 = psi32 + (size_t)w * ncw * N;
 
@@ -365,19 +378,19 @@ __global__ void __launch_bounds__(PT_THREADS, 1)
       x[2 * jj] = v.x;
       x[2 * jj + 1] = v.y;
     }
-    if (p < N) pt_store_X(sB, x, nc, p, !realB, g);
+    if (p < N) pt_store_X(sB, x, nc, p, g);
     if (!(ok = pt_wait(bar_ld, ph_ld, err, 22))) break;
     // B psi = psi + (B - I) psi
-    if (!(ok = pt_product(sA, sB, nc, nsB, tmem, bar_mma, ph_mma, err))) break;
-    pt_add_row(tcol, x);
+    if (!(ok = pt_product(sA, sB, nc, !realB, tmem, bar_mma, ph_mma, err))) break;
+    pt_add_row(tcol, x, !realB);
 #pragma unroll
     for (int c = 0; c < PT_CW; ++c) acc[c] = x[c];  // the Taylor sum starts from B psi
     // Taylor terms with V: term_k = V term_{k-1} / k, added to the sum in TMEM
     pt_load_V(sA, vre, vim, tri, T);
     for (int k = 1; k <= 5 && ok; ++k) {
-      if (p < N) pt_store_X(sB, x, nc, p, true, g);
-      if (!(ok = pt_product(sA, sB, nc, 16, tmem, bar_mma, ph_mma, err))) break;
-      pt_tmem_ld(tcol, x);
+      if (p < N) pt_store_X(sB, x, nc, p, g);
+      if (!(ok = pt_product(sA, sB, nc, true, tmem, bar_mma, ph_mma, err))) break;
+      pt_tmem_ld(tcol, x, true);
       const float inv = 1.f / (float)k;
 #pragma unroll
       for (int c = 0; c < PT_CW; ++c) {
@@ -390,10 +403,10 @@ __global__ void __launch_bounds__(PT_THREADS, 1)
     pt_issue_image(sA, im, bar_ld, realB != 0);
 #pragma unroll
     for (int c = 0; c < PT_CW; ++c) x[c] = acc[c];
-    if (p < N) pt_store_X(sB, x, nc, p, !realB, g);
+    if (p < N) pt_store_X(sB, x, nc, p, g);
     if (!(ok = pt_wait(bar_ld, ph_ld, err, 22))) break;
-    if (!(ok = pt_product(sA, sB, nc, nsB, tmem, bar_mma, ph_mma, err))) break;
-    pt_add_row(tcol, x);
+    if (!(ok = pt_product(sA, sB, nc, !realB, tmem, bar_mma, ph_mma, err))) break;
+    pt_add_row(tcol, x, !realB);
     if (p < N) {
 #pragma unroll
       for (int jj = 0; jj < PT_CW / 2; ++jj) {
