@@ -24,7 +24,7 @@
 // double-FP32 dot product (psi_s split exactly into FP32 pairs, X's entries
 // FP32 numbers, products error-free and their sum carried in a pair: ~1e-14),
 // and prod_k X_kk is formed in FP64.  psi_s leaves as the FP64 nearest to the
-// pair, psi32 as its high part.  None of it runs on the FP64 pipe but the one
+// pair, psi32 as that double rounded to FP32.  None of it runs on the FP64 pipe but the one
 // addition per stored number and the n multiplications of the determinant.
 //
 // One CTA (256 threads) per walker, both spin blocks in turn; the block (as
@@ -162,8 +162,11 @@ __global__ void __launch_bounds__(OC_THREADS)
         dot2_acc(si, ci, h.y, l.y, x.x);
       }
       const df32 qr = df_fast(sr, cr), qi = df_fast(si, ci);
-      Ag[e] = make_double2(df_to_double_bits(qr), df_to_double_bits(qi));
-      Ag32[e] = make_float2(qr.h, qi.h);
+      const double2 q = make_double2(df_to_double_bits(qr), df_to_double_bits(qi));
+      Ag[e] = q;
+      // the FP32 copy is the stored double rounded to nearest, as everywhere
+      // (the pair's high part can differ from it when the low part is a tie)
+      Ag32[e] = make_float2(df_split_bits(q.x).h, df_split_bits(q.y).h);
     }
     if (tid == 0)
       for (int k = 0; k < n; ++k) fac *= (double)X[k * n + k].x;

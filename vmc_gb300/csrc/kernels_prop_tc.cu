@@ -37,6 +37,7 @@
 
 #include "afqmc_internal.h"
 #include "device_common.cuh"
+#include "df32.cuh"
 #include "tcgen05.cuh"
 
 namespace afqmc {
@@ -371,10 +372,7 @@ __global__ void __launch_bounds__(PT_THREADS, 1)
     for (int jj = 0; jj < PT_CW / 2; ++jj) {
       const int j = g * (PT_CW / 2) + jj;
       float2 v = make_float2(0.f, 0.f);
-      if (j < ncols && p < N) {
-        const double2 d = pw[(size_t)(c0 + j) * N + p];
-        v = make_float2((float)d.x, (float)d.y);
-      }
+      if (j < ncols && p < N) v = pw32[(size_t)(c0 + j) * N + p];  // the walker rounded to FP32
       x[2 * jj] = v.x;
       x[2 * jj + 1] = v.y;
     }
@@ -413,7 +411,7 @@ __global__ void __launch_bounds__(PT_THREADS, 1)
         const int j = g * (PT_CW / 2) + jj;
         if (j < ncols) {
           const size_t o = (size_t)(c0 + j) * N + p;
-          pw[o] = make_double2((double)x[2 * jj], (double)x[2 * jj + 1]);
+          pw[o] = make_double2(df_f2d_bits(x[2 * jj]), df_f2d_bits(x[2 * jj + 1]));  // exact, no FP64 work
           pw32[o] = make_float2(x[2 * jj], x[2 * jj + 1]);
         }
       }
