@@ -86,6 +86,7 @@ struct afqmc_handle {
   double* phi = nullptr;      // [nce][N]             channel trial orbitals
   double* rot = nullptr;      // [G][nce*N]           rot[g][(col)*N + p] = (Phi^T L_g)[i, p]
   double* h1phi = nullptr;    // [nce][N]             (h1 Phi)[p, i]
+  float* h1phi32 = nullptr;   // [nce][N]             FP32 copy (mixed form: control-variate features)
   double* LT = nullptr;       // [nsp][T][G]          packed lower-triangle Cholesky, FP64
   float* LT32 = nullptr;      // [nsp][T][G]          FP32 copy (REF32)
   int2* tri = nullptr;        // [T]                  packed index -> (i, j), j <= i
@@ -142,6 +143,7 @@ struct afqmc_handle {
   CUtensorMap tm_rotE[2], tm_thE[2];
   unsigned long long* d_step = nullptr;  // device step counter of the Philox field stream
   bool fb_current = false;               // fb32 holds the force bias of the current theta
+  bool thetaB_from_lu = false;           // the overlap LU wrote thetaB (the split of the current theta)
   float2* psi32 = nullptr;               // [W][ncw][N] FP32 copy of psi (mixed form)
   // device-resident blocks: comb scratch, the block ring and host-given zetas
   double* wpart = nullptr;      // [WT_MAXPARTS][2] partial sums of the weight update

@@ -4,6 +4,7 @@
 // Reference algorithm: DQMC/DQMCWalker.cpp:441-554 (step), :295-326 (QR),
 // DQMC/RHF.cpp, DQMC/UHF.cpp (trial contractions), DQMC/MixedEstimator.cpp:461-475
 // (weights, cap, population control).
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdint.h>
@@ -237,11 +238,12 @@ __device__ double2 lu_df32(float2* ah, float2* al, int* perm, int n, int lane) {
 // Eigen's PartialPivLU exactly (FP64 pivot search, first row of the largest
 // |M_ik|, FP64 reciprocal, running determinant).
 template <bool F32, int NM, bool MB>
-__global__ void __launch_bounds__(OW_WARPS * 32)
+__global__ void __launch_bounds__(OW_WARPS * 32, (F32 && MB && NM <= 20) ? 7 : 1)  // 7 CTAs per SM where that does not spill
     k_overlap_lu(const double2* __restrict__ psi, const float2* __restrict__ psi32, const double* __restrict__ phi,
                  double* __restrict__ theta, float* __restrict__ theta32, double2* __restrict__ det,
                  const double* __restrict__ weights, int W, int N, int ncw, int nce, Channel c0, Channel c1,
-                 int only_live, int nmax, const float4* __restrict__ mbuf) {
+                 int only_live, int nmax, const float4* __restrict__ mbuf, __nv_bfloat16* __restrict__ thetaB,
+                 int kf_pad) {
   static_assert(F32 || !MB, "M formed beforehand only in the mixed form");
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int s = blockIdx.y;
@@ -443,6 +445,28 @@ __global__ void __launch_bounds__(OW_WARPS * 32)
           tre[(size_t)c * N + p] = acc[c].x;
           tim[(size_t)c * N + p] = acc[c].y;
         }
+      if (thetaB) {
+        // the force bias's operand: rows (w, re) and (w, im), [hi | lo | hi] along
+        // K = nce N (what k_split_rows would write from theta32)
+        const int Kf = nce * N;
+        __nv_bfloat16* br = thetaB + (size_t)(2 * w) * kf_pad + (size_t)ch.col_off * N + p;
+        __nv_bfloat16* bi = br + kf_pad;
+#pragma unroll
+        for (int c = 0; c < NM; ++c)
+          if (c < n) {
+            const __nv_bfloat16 rh = __float2bfloat16_rn(acc[c].x);
+            const __nv_bfloat16 rl = __float2bfloat16_rn(acc[c].x - __bfloat162float(rh));
+            const __nv_bfloat16 ih = __float2bfloat16_rn(acc[c].y);
+            const __nv_bfloat16 il = __float2bfloat16_rn(acc[c].y - __bfloat162float(ih));
+            const size_t o = (size_t)c * N;
+            br[o] = rh;
+            br[o + Kf] = rl;
+            br[o + 2 * Kf] = rh;
+            bi[o] = ih;
+            bi[o + Kf] = il;
+            bi[o + 2 * Kf] = ih;
+          }
+      }
     }
     return;
   }
@@ -501,6 +525,7 @@ void launch_psi_to_f32(afqmc_handle* h) {
 
 void launch_overlap_theta(afqmc_handle* h, bool only_live) {
   h->fb_current = false;  // theta changes
+  h->thetaB_from_lu = false;  // set below when the FP32 LU writes the force bias's operand too
   int nmax = std::max(h->chan[0].n, h->nchan > 1 ? h->chan[1].n : 0);
   const size_t per_warp = ow_per_warp(nmax);
   const size_t smem_lu = (((size_t)nmax * h->N * sizeof(double) + 15) & ~(size_t)15) + OW_WARPS * per_warp;
@@ -521,7 +546,7 @@ void launch_overlap_theta(afqmc_handle* h, bool only_live) {
     k_overlap_lu<F, NMV, MBV><<<grid, OW_WARPS * 32, smem, h->stream>>>(                                     \
         h->psi, h->psi32, h->phi, h->theta, h->theta32, h->det, h->weights, h->nwalk, h->N, h->ncw, h->nce,  \
         h->chan[0],                                                                                          \
-        h->chan[1], only_live ? 1 : 0, nmax, h->ovl_M);                                                       \
+        h->chan[1], only_live ? 1 : 0, nmax, h->ovl_M, F ? h->thetaB : nullptr, h->kf_pad);                   \
   }
 #define OW_NM(F, MBV)                          \
   switch (nm) {                                \
@@ -534,6 +559,7 @@ void launch_overlap_theta(afqmc_handle* h, bool only_live) {
     case 28: OW_LAUNCH(F, 28, MBV) break;      \
     default: OW_LAUNCH(F, 32, MBV) break;      \
   }
+    h->thetaB_from_lu = f32 && h->thetaB != nullptr;
     if (mtc) {
       OW_NM(true, true)
     } else if (f32) {

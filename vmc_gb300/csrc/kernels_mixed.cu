@@ -184,7 +184,7 @@ void launch_theta_split(afqmc_handle* h) {
 
 void launch_force_bias_mixed(afqmc_handle* h) {
   if (h->fb_current) return;  // already computed from this theta (control-variate features)
-  launch_theta_split(h);
+  if (!h->thetaB_from_lu) launch_theta_split(h);
   EpiFB epi{h->fb32, h->G, (float)h->mult};
   launch_tc(h, h->tm_rot, h->tm_theta_bn, h->tune_bn_fb, h->G, 2 * h->nwalk, h->kf_pad, epi);
   h->fb_current = true;
@@ -211,6 +211,11 @@ __global__ void k_split_mf(const double2* __restrict__ mf, float4* __restrict__ 
   if (g >= G) return;
   const df32 re = df_split_bits(mf[g].x), im = df_split_bits(mf[g].y);
   mf32[g] = make_float4(re.h, re.l, im.h, im.l);
+}
+
+__global__ void k_to_f32(const double* __restrict__ src, float* __restrict__ dst, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) dst[i] = (float)src[i];
 }
 
 __global__ void k_fields_mixed(const float* __restrict__ fb, const float4* __restrict__ mf32,
@@ -554,6 +559,9 @@ bool setup_mixed(afqmc_handle* h) {
     split_rows(h, h->LT + (size_t)s * h->T * h->G, h->G, h->T, h->G, h->kv_pad, 0,
                h->LTA + (size_t)s * h->T * h->kv_pad);
   k_split_mf<<<(h->G + 127) / 128, 128, 0, h->stream>>>(h->mf, h->mf32, h->G);
+  // the force bias's theta operand: its padding columns stay zero when the LU writes it
+  cudaMemsetAsync(h->thetaB, 0, (size_t)h->nwalk * 2 * h->kf_pad * sizeof(__nv_bfloat16), h->stream);
+  k_to_f32<<<(h->nce * h->N + 255) / 256, 256, 0, h->stream>>>(h->h1phi, h->h1phi32, h->nce * h->N);
   bool ok = setup_prop_tc(h) && setup_ovl_tc(h) && make_tmap_bf16(&h->tm_rot, h->rotA, h->G, h->kf_pad, tc::BM);
   const int bns[3] = {64, 128, 256};
   for (int i = 0; i < 3 && ok; ++i)
