@@ -453,8 +453,11 @@ def main():
                          "bound_ms": bound_ms, "frac": bound_ms / t}
     dom = max(("vhs", "prop"), key=lambda s: stage[s])
     achieved = per_launch[dom] / (stage_roof[dom]["ms_per_launch"] / 1e3) / 1e12
+    # DRAM bytes per launch of the dominant kernel from one ncu capture of this workload
+    # (dram__bytes_read.sum + dram__bytes_write.sum; profiles/k_prop_tc_cfg2.md)
+    traffic = {"prop": 198.0e6 + 179.0e6}.get(dom) if args.workload == "cfg2" else None
     roof = {"bound": "tensor", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-            "frac": achieved / peak, "traffic": None,
+            "frac": achieved / peak, "traffic": traffic, "traffic_unit": "bytes per launch (ncu capture)",
             "peak_source": "%s bf16 sustained (MEASURED_PEAKS.json); algorithmic FLOPs of the stage per launch "
                            "/ its CUDA-event time; the largest tensor-core stage (every stage against the executed "
                            "cost of its parts in stage_roofline; FP32 peak nominal)"
