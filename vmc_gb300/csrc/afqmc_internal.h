@@ -86,7 +86,7 @@ struct afqmc_handle {
   double* phi = nullptr;      // [nce][N]             channel trial orbitals
   double* rot = nullptr;      // [G][nce*N]           rot[g][(col)*N + p] = (Phi^T L_g)[i, p]
   double* h1phi = nullptr;    // [nce][N]             (h1 Phi)[p, i]
-  float* h1phi32 = nullptr;   // [nce][N]             FP32 copy (mixed form: control-variate features)
+  float2* h1phi32 = nullptr;  // [nce][N]             double-FP32 copy (mixed form: features, one-body energy)
   double* LT = nullptr;       // [nsp][T][G]          packed lower-triangle Cholesky, FP64
   float* LT32 = nullptr;      // [nsp][T][G]          FP32 copy (REF32)
   int2* tri = nullptr;        // [T]                  packed index -> (i, j), j <= i

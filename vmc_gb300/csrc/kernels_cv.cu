@@ -41,7 +41,7 @@ int mlp_n_in(const afqmc_mlp* m);
 // log|overlap| and arg(overlap) after scaling the overlap by a power of two.
 // One CTA of 128 threads per walker.
 __global__ void k_cv_features32(const float* __restrict__ fb32, const float* __restrict__ theta,
-                                const float* __restrict__ h1phi32, const double2* __restrict__ ovlp, int N, int nce,
+                                const float2* __restrict__ h1phi32, const double2* __restrict__ ovlp, int N, int nce,
                                 int G, int mult, const float* __restrict__ mean, const float* __restrict__ stdv,
                                 float* __restrict__ out) {
   __shared__ float s_part[4];
@@ -50,7 +50,7 @@ __global__ void k_cv_features32(const float* __restrict__ fb32, const float* __r
   for (int g = threadIdx.x; g < 64; g += blockDim.x) o[g] = g < G ? fb32[(size_t)(2 * w) * G + g] : 0.f;
   const float* tre = theta + (size_t)(2 * w) * nce * N;
   float e1 = 0.f;
-  for (int k = threadIdx.x; k < nce * N; k += blockDim.x) e1 = fmaf(tre[k], h1phi32[k], e1);
+  for (int k = threadIdx.x; k < nce * N; k += blockDim.x) e1 = fmaf(tre[k], h1phi32[k].x, e1);
   e1 = warp_sumf(e1);
   if ((threadIdx.x & 31) == 0) s_part[threadIdx.x >> 5] = e1;
   __syncthreads();
@@ -111,23 +111,27 @@ __global__ void k_cv_select(int* __restrict__ idx, int W, int den, uint64_t seed
   idx[b] = b * den + (int)(r.x % (uint32_t)size);
 }
 
-// dst rows (i, plane, c) = split of theta rows of walker idx[i] ([hi | lo | hi] along p)
+// dst rows (i, plane, c) = split of theta rows of walker idx[i] ([hi | lo | hi]
+// along p, zeros to kpad); one block per (i, plane) covering its nce rows
 __global__ void k_split_theta_gather(const float* __restrict__ theta, const int* __restrict__ idx, int m, int nce,
                                      int N, int kpad, __nv_bfloat16* __restrict__ dst) {
-  const int row = blockIdx.x;  // (i, plane, c)
-  const int i = row / (2 * nce), rem = row % (2 * nce);
-  const float* s = theta + ((size_t)idx[i] * 2 * nce + rem) * N;
-  __nv_bfloat16* d = dst + (size_t)row * kpad;
-  for (int k = threadIdx.x; k < kpad; k += blockDim.x) {
-    __nv_bfloat16 v = __float2bfloat16_rn(0.f);
-    if (k < 3 * N) {
-      const int part = k / N, p = k % N;
-      const float x = s[p];
+  const int ip = blockIdx.x;  // (i, plane)
+  const int i = ip >> 1, plane = ip & 1;
+  const float* s = theta + ((size_t)idx[i] * 2 + plane) * nce * N;
+  __nv_bfloat16* d = dst + (size_t)ip * nce * kpad;
+  const __nv_bfloat16 z = __float2bfloat16_rn(0.f);
+  for (int c = 0; c < nce; ++c) {
+    const float* sr = s + (size_t)c * N;
+    __nv_bfloat16* dr = d + (size_t)c * kpad;
+    for (int p = threadIdx.x; p < N; p += blockDim.x) {
+      const float x = sr[p];
       const __nv_bfloat16 hi = __float2bfloat16_rn(x);
       const __nv_bfloat16 lo = __float2bfloat16_rn(x - __bfloat162float(hi));
-      v = part == 1 ? lo : hi;
+      dr[p] = hi;
+      dr[N + p] = lo;
+      dr[2 * N + p] = hi;
     }
-    d[k] = v;
+    for (int k = 3 * N + threadIdx.x; k < kpad; k += blockDim.x) dr[k] = z;
   }
 }
 
@@ -139,39 +143,49 @@ __global__ void k_cv_scale(float* __restrict__ f, int W, float ymean, float ystd
 __global__ void k_cv_estimate(const double* __restrict__ weights, const float* __restrict__ f,
                               const int* __restrict__ idx, const double2* __restrict__ esub, int W, int m, int den,
                               double* __restrict__ out) {
-  double sw = 0.0, swf = 0.0;
+  constexpr int NV = 7;  // sw, swf, corr, ht, nrw, nrwe, nrwf: one reduction for all seven
+  __shared__ double s_part[32][NV];
+  double v[NV] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
   for (int w = threadIdx.x; w < W; w += blockDim.x) {
-    sw += weights[w];
-    swf += weights[w] * (double)f[w];
+    v[0] += weights[w];
+    v[1] += weights[w] * (double)f[w];
   }
-  double corr = 0.0, ht = 0.0, nrw = 0.0, nrwe = 0.0, nrwf = 0.0;
   for (int i = threadIdx.x; i < m; i += blockDim.x) {
     const int w = idx[i];
     const double inv = (double)min(den, W - i * den);
     const double wt = weights[w];
     const double e = esub[i].x;
     if (wt != 0.0) {
-      corr += inv * wt * (e - (double)f[w]);
-      ht += inv * wt * e;
-      nrw += wt;
-      nrwe += wt * e;
-      nrwf += wt * (double)f[w];
+      v[2] += inv * wt * (e - (double)f[w]);
+      v[3] += inv * wt * e;
+      v[4] += wt;
+      v[5] += wt * e;
+      v[6] += wt * (double)f[w];
     }
   }
-  sw = block_sum(sw);
-  swf = block_sum(swf);
-  corr = block_sum(corr);
-  ht = block_sum(ht);
-  nrw = block_sum(nrw);
-  nrwe = block_sum(nrwe);
-  nrwf = block_sum(nrwf);
-  if (threadIdx.x == 0) {
-    out[0] = swf / sw + (nrwe - nrwf) / nrw;
-    out[1] = (swf + corr) / sw;
-    out[2] = ht / sw;
-    out[3] = nrwe / nrw;
-    out[4] = sw;
-    out[5] = nrw;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int j = 0; j < NV; ++j) {
+    for (int o = 16; o > 0; o >>= 1) v[j] += __shfl_down_sync(0xffffffffu, v[j], o);
+    if (lane == 0) s_part[warp][j] = v[j];
+  }
+  __syncthreads();
+  if (warp == 0) {
+    const int nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+    for (int j = 0; j < NV; ++j) {
+      v[j] = lane < nw ? s_part[lane][j] : 0.0;
+      for (int o = 16; o > 0; o >>= 1) v[j] += __shfl_down_sync(0xffffffffu, v[j], o);
+    }
+    if (lane == 0) {
+      const double sw = v[0], swf = v[1], corr = v[2], ht = v[3], nrw = v[4], nrwe = v[5], nrwf = v[6];
+      out[0] = swf / sw + (nrwe - nrwf) / nrw;
+      out[1] = (swf + corr) / sw;
+      out[2] = ht / sw;
+      out[3] = nrwe / nrw;
+      out[4] = sw;
+      out[5] = nrw;
+    }
   }
 }
 
@@ -183,7 +197,7 @@ namespace afqmc {
 void launch_local_energy_mixed_subset(afqmc_handle* h, const int* d_idx, int m, double2* out);
 
 void launch_split_theta_gather(afqmc_handle* h, const int* d_idx, int m) {
-  k_split_theta_gather<<<m * 2 * h->nce, 128, 0, h->stream>>>(h->theta32, d_idx, m, h->nce, h->N, h->ke_pad, h->thetaE);
+  k_split_theta_gather<<<m * 2, 128, 0, h->stream>>>(h->theta32, d_idx, m, h->nce, h->N, h->ke_pad, h->thetaE);
   h->launches++;
 }
 }
@@ -269,7 +283,7 @@ int afqmc_cv_measure(afqmc_handle* h, uint64_t tag, int slot) {
   k_cv_select<<<(m + 127) / 128, 128, 0, h->stream>>>(h->cv_idx, W, den, h->seed, tag, h->d_step);
   launch_local_energy_mixed_subset(h, h->cv_idx, m, h->cv_esub);
   k_cv_scale<<<(W + 255) / 256, 256, 0, h->stream>>>(h->cv_f, W, h->cv_ymean, h->cv_ystd);
-  k_cv_estimate<<<1, 1024, 0, h->stream>>>(h->weights, h->cv_f, h->cv_idx, h->cv_esub, W, m, den,
+  k_cv_estimate<<<1, 256, 0, h->stream>>>(h->weights, h->cv_f, h->cv_idx, h->cv_esub, W, m, den,
                                            h->cv_out + 6 * (size_t)slot);
   h->launches += 8;
   cudaError_t e = cudaGetLastError();

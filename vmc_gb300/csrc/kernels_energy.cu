@@ -19,6 +19,7 @@
 
 #include "afqmc_internal.h"
 #include "device_common.cuh"
+#include "df32.cuh"
 #include "tcgen05.cuh"
 
 namespace afqmc {
@@ -208,19 +209,24 @@ __global__ void __launch_bounds__(EX_THREADS, 2)
 }
 
 // E = ecore + mult sum theta.h1phi + 1/2 sum_g [(mult sum_s c_sg)^2 - mult sum_s X_sg]
-__global__ void k_energy_assemble(const float* __restrict__ theta, const double* __restrict__ h1phi,
+// The one-body term is a compensated FP32 dot product (Dot2) of the FP32 theta
+// with h1 Phi as double-FP32 pairs: an FP64-grade sum without FP64 work per
+// element.  The four per-walker sums share one block reduction.
+__global__ void k_energy_assemble(const float* __restrict__ theta, const float2* __restrict__ h1phi,
                                   const double2* __restrict__ xc, double2* __restrict__ eloc, int N, int nce, int Gene,
                                   int nchan, int mult, double ecore, const int* __restrict__ idx) {
+  __shared__ double s_part[32][4];
   const int w = blockIdx.x;  // local index (row of xc); theta of walker idx[w] (or w)
   const int ws = idx ? idx[w] : w;
   const float* tre = theta + (size_t)(2 * ws) * nce * N;
   const float* tim = tre + (size_t)nce * N;
-  double re = 0.0, im = 0.0;  // the one-body term accumulates in FP64
+  float sr = 0.f, cr = 0.f, si = 0.f, ci = 0.f;
   for (int k = threadIdx.x; k < nce * N; k += blockDim.x) {
-    re += (double)tre[k] * h1phi[k];
-    im += (double)tim[k] * h1phi[k];
+    const float2 hp = h1phi[k];
+    dot2_acc(sr, cr, hp.x, hp.y, tre[k]);
+    dot2_acc(si, ci, hp.x, hp.y, tim[k]);
   }
-  double er = 0.0, ei = 0.0;
+  double v[4] = {(double)sr + (double)cr, (double)si + (double)ci, 0.0, 0.0};
   for (int g = threadIdx.x; g < Gene; g += blockDim.x) {
     double2 c = make_double2(0.0, 0.0), x = make_double2(0.0, 0.0);
     for (int s = 0; s < nchan; ++s) {
@@ -230,14 +236,25 @@ __global__ void k_energy_assemble(const float* __restrict__ theta, const double*
     }
     c = make_double2(mult * c.x, mult * c.y);
     const double2 c2 = cmul(c, c);
-    er += 0.5 * (c2.x - mult * x.x);
-    ei += 0.5 * (c2.y - mult * x.y);
+    v[2] += 0.5 * (c2.x - mult * x.x);
+    v[3] += 0.5 * (c2.y - mult * x.y);
   }
-  re = block_sum(re);
-  im = block_sum(im);
-  er = block_sum(er);
-  ei = block_sum(ei);
-  if (threadIdx.x == 0) eloc[w] = make_double2(ecore + mult * re + er, mult * im + ei);
+  const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    for (int o = 16; o > 0; o >>= 1) v[j] += __shfl_down_sync(0xffffffffu, v[j], o);
+    if (lane == 0) s_part[wp][j] = v[j];
+  }
+  __syncthreads();
+  if (wp == 0) {
+    const int nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      v[j] = lane < nw ? s_part[lane][j] : 0.0;
+      for (int o = 16; o > 0; o >>= 1) v[j] += __shfl_down_sync(0xffffffffu, v[j], o);
+    }
+    if (lane == 0) eloc[w] = make_double2(ecore + mult * v[0] + v[2], mult * v[1] + v[3]);
+  }
 }
 
 void launch_split_theta_gather(afqmc_handle* h, const int* d_idx, int m);
@@ -278,7 +295,7 @@ void launch_local_energy_mixed_subset(afqmc_handle* h, const int* d_idx, int m, 
                                                     h->nchan, h->xc, h->d_err);
     h->launches++;
   }
-  k_energy_assemble<<<m, 256, 0, h->stream>>>(h->theta32, h->h1phi, h->xc, out, h->N, h->nce, h->nchol_ene, h->nchan,
+  k_energy_assemble<<<m, 256, 0, h->stream>>>(h->theta32, h->h1phi32, h->xc, out, h->N, h->nce, h->nchol_ene, h->nchan,
                                               h->mult, h->ecore, d_idx);
   h->launches++;
 }

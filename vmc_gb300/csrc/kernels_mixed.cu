@@ -213,9 +213,12 @@ __global__ void k_split_mf(const double2* __restrict__ mf, float4* __restrict__ 
   mf32[g] = make_float4(re.h, re.l, im.h, im.l);
 }
 
-__global__ void k_to_f32(const double* __restrict__ src, float* __restrict__ dst, int n) {
+__global__ void k_to_df32(const double* __restrict__ src, float2* __restrict__ dst, int n) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) dst[i] = (float)src[i];
+  if (i < n) {
+    const df32 v = df_split_bits(src[i]);
+    dst[i] = make_float2(v.h, v.l);
+  }
 }
 
 __global__ void k_fields_mixed(const float* __restrict__ fb, const float4* __restrict__ mf32,
@@ -561,7 +564,7 @@ bool setup_mixed(afqmc_handle* h) {
   k_split_mf<<<(h->G + 127) / 128, 128, 0, h->stream>>>(h->mf, h->mf32, h->G);
   // the force bias's theta operand: its padding columns stay zero when the LU writes it
   cudaMemsetAsync(h->thetaB, 0, (size_t)h->nwalk * 2 * h->kf_pad * sizeof(__nv_bfloat16), h->stream);
-  k_to_f32<<<(h->nce * h->N + 255) / 256, 256, 0, h->stream>>>(h->h1phi, h->h1phi32, h->nce * h->N);
+  k_to_df32<<<(h->nce * h->N + 255) / 256, 256, 0, h->stream>>>(h->h1phi, h->h1phi32, h->nce * h->N);
   bool ok = setup_prop_tc(h) && setup_ovl_tc(h) && make_tmap_bf16(&h->tm_rot, h->rotA, h->G, h->kf_pad, tc::BM);
   const int bns[3] = {64, 128, 256};
   for (int i = 0; i < 3 && ok; ++i)
