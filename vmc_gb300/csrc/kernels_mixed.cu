@@ -155,14 +155,18 @@ template <int BN, class Epi>
 static void launch_tc_bn(afqmc_handle* h, const CUtensorMap& ta, const CUtensorMap& tb, int M, int N, int K,
                          const Epi& epi) {
   constexpr int ST = 4;
-  const int smem = tc::GemmSmem<BN, ST>::TOTAL;
+  const int smem = tc::GemmPSmem<BN, ST>::TOTAL;
   static bool attr = false;
+  static int nsm = 0;
   if (!attr) {
-    cudaFuncSetAttribute(tc::k_tc_gemm<BN, ST, Epi>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    cudaFuncSetAttribute(tc::k_tc_gemm_p<BN, ST, Epi>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, h->device);
     attr = true;
   }
-  dim3 grid((N + BN - 1) / BN, (M + tc::BM - 1) / tc::BM);
-  tc::k_tc_gemm<BN, ST, Epi><<<grid, 128, smem, h->stream>>>(ta, tb, M, N, K, epi, h->d_err);
+  // persistent: one CTA per SM (or per tile when there are fewer tiles)
+  const int tiles = ((N + BN - 1) / BN) * ((M + tc::BM - 1) / tc::BM);
+  const int grid = std::max(1, std::min(tiles, nsm > 0 ? nsm : tiles));
+  tc::k_tc_gemm_p<BN, ST, Epi><<<grid, tc::GP_THREADS, smem, h->stream>>>(ta, tb, M, N, K, epi, h->d_err);
   h->launches++;
 }
 

@@ -41,6 +41,9 @@ __device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
 __device__ __forceinline__ void fence_mbar_init() {
   asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
 }
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
 __device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
                : "memory");
@@ -277,6 +280,154 @@ __global__ void __launch_bounds__(128, 1)
   if (warp == 0) {
     tc_fence_after();
     tmem_dealloc(tmem, BN);
+  }
+}
+
+
+// Persistent, warp-specialised form of k_tc_gemm: one CTA per SM strides over
+// the output tiles (m-tiles fastest, so the CTAs running together share the
+// per-step B tile in L2).  Warp 0 lane 0 streams the K blocks of every tile
+// through the STAGES ring by TMA, warp 1 lane 0 issues the MMAs into one of two
+// TMEM accumulators (2 BN columns), and warps 2-5 (one TMEM lane quadrant
+// each) run the epilogue of tile i while the MMAs of tile i + 1 proceed; the
+// accumulators are handed over by acc_full (MMA commit) and acc_empty (the 128
+// epilogue threads).  Every wait is bounded; on a timeout the roles leave
+// their loops, issued loads land, and TMEM is freed.
+template <int BN, int STAGES>
+struct GemmPSmem {
+  static constexpr int A_BYTES = BM * BK * 2;
+  static constexpr int B_BYTES = BN * BK * 2;
+  static constexpr int STAGE_BYTES = A_BYTES + B_BYTES;
+  static constexpr int BAR_OFF = STAGES * STAGE_BYTES;
+  static constexpr int TOTAL = BAR_OFF + (2 * STAGES + 4) * 8 + 16 + 1024;  // + alignment slack
+};
+constexpr int GP_THREADS = 192;
+
+template <int BN, int STAGES, class Epi>
+__global__ void __launch_bounds__(GP_THREADS, 1)
+    k_tc_gemm_p(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, int M, int N,
+                int K, Epi epi, int* err) {
+  using L = GemmPSmem<BN, STAGES>;
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  uint64_t* full = (uint64_t*)(smem + L::BAR_OFF);
+  uint64_t* empty = full + STAGES;
+  uint64_t* acc_full = empty + STAGES;  // [2]
+  uint64_t* acc_empty = acc_full + 2;   // [2]
+  uint32_t* tmem_holder = (uint32_t*)(acc_empty + 2);
+  __shared__ int s_abort;
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int ntm = (M + BM - 1) / BM, ntn = (N + BN - 1) / BN, ntiles = ntm * ntn;
+  const int nk = K / BK;
+
+  if (threadIdx.x == 0) {
+    s_abort = 0;
+    for (int s = 0; s < STAGES; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&acc_full[b], 1);
+      mbar_init(&acc_empty[b], 128);
+    }
+    fence_mbar_init();
+    prefetch_tmap(&tmA);
+    prefetch_tmap(&tmB);
+  }
+  if (warp == 0) tmem_alloc(tmem_holder, 2 * BN);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_holder;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      int kt = 0;  // K blocks issued over all tiles: the ring position
+      for (int t = blockIdx.x; t < ntiles && !s_abort; t += gridDim.x) {
+        const int m0 = (t % ntm) * BM, n0 = (t / ntm) * BN;
+        for (int kb = 0; kb < nk; ++kb, ++kt) {
+          const int s = kt % STAGES;
+          if (kt >= STAGES && !mbar_wait(&empty[s], ((kt / STAGES) - 1) & 1, err, 41)) {
+            s_abort = 1;
+            break;
+          }
+          uint8_t* a = smem + s * L::STAGE_BYTES;
+          mbar_expect_tx(&full[s], L::STAGE_BYTES);
+          tma_load_2d(a, &tmA, &full[s], kb * BK, m0);
+          tma_load_2d(a + L::A_BYTES, &tmB, &full[s], kb * BK, n0);
+        }
+      }
+      // the loads already issued land before the CTA releases its shared memory
+      for (int k = kt > STAGES ? kt - STAGES : 0; k < kt; ++k)
+        mbar_wait(&full[k % STAGES], (k / STAGES) & 1, err, 42);
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      constexpr uint32_t idesc = idesc_bf16(BM, BN);
+      int kt = 0, tl = 0, last = -1;  // last: local index of the last tile committed
+      for (int t = blockIdx.x; t < ntiles && !s_abort; t += gridDim.x, ++tl) {
+        const int b = tl & 1, u = tl >> 1;
+        if (u > 0 && !mbar_wait(&acc_empty[b], (u - 1) & 1, err, 43)) {
+          s_abort = 1;
+          break;
+        }
+        tc_fence_after();
+        const uint32_t d = tmem + (uint32_t)(b * BN);
+        bool ok = true;
+        for (int kb = 0; kb < nk; ++kb, ++kt) {
+          const int s = kt % STAGES;
+          if (!mbar_wait(&full[s], (kt / STAGES) & 1, err, 44)) {
+            s_abort = 1;
+            ok = false;
+            break;
+          }
+          tc_fence_after();
+          const uint32_t a = smem_u32(smem + s * L::STAGE_BYTES);
+          const uint32_t bb = a + L::A_BYTES;
+#pragma unroll
+          for (int k = 0; k < BK / 16; ++k)
+            mma_bf16(d, sdesc_sw128(a + 32 * k), sdesc_sw128(bb + 32 * k), idesc, (kb > 0 || k > 0) ? 1u : 0u);
+          mma_commit(&empty[s]);
+        }
+        mma_commit(&acc_full[b]);  // also after a break: the epilogue is released
+        last = tl;
+        if (!ok) break;
+      }
+      // no MMA of this thread is in flight when TMEM is freed
+      if (last >= 0) mbar_wait(&acc_full[last & 1], (last >> 1) & 1, err, 46);
+    }
+  } else {
+    const int q = warp & 3;  // TMEM lane quadrant of this warp
+    int tl = 0;
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x, ++tl) {
+      const int b = tl & 1, u = tl >> 1;
+      const bool have = mbar_wait(&acc_full[b], u & 1, err, 45);
+      tc_fence_after();
+      if (!have || s_abort) break;
+      const int m0 = (t % ntm) * BM, n0 = (t / ntm) * BN;
+      const int row = m0 + q * 32 + lane;
+#pragma unroll 1
+      for (int c = 0; c < BN; c += 16) {
+        float v[16];
+        tmem_ld16(tmem + (uint32_t)(b * BN) + ((uint32_t)(q * 32) << 16) + (uint32_t)c, v);
+        if (row < M) {
+#pragma unroll
+          for (int j = 0; j < 16; ++j) {
+            const int n = n0 + c + j;
+            if (n < N) epi(row, n, v[j]);
+          }
+        }
+      }
+      tc_fence_before();
+      mbar_arrive(&acc_empty[b]);
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    tc_fence_after();
+    tmem_dealloc(tmem, 2 * BN);
   }
 }
 
