@@ -182,6 +182,8 @@ void release(afqmc_handle* h) {
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (h->host_pinned) cudaFreeHost(h->host_pinned);
+  for (auto& e : h->stage_ev)
+    if (e) cudaEventDestroy(e);
   if (h->timer[0]) { cudaEventDestroy(h->timer[0]); cudaEventDestroy(h->timer[1]); }
   for (int s = 0; s < afqmc::ST_N; ++s)
     for (auto& e : h->ev[s]) { cudaEventDestroy(e.first); cudaEventDestroy(e.second); }
@@ -489,7 +491,9 @@ int afqmc_create(const afqmc_ham* ham, const afqmc_trial* trial, const afqmc_opt
   ALLOC(blk, 2 * (size_t)afqmc::BLK_MAX);
   ALLOC(blk_zeta, (size_t)afqmc::BLK_MAX);
 #undef ALLOC
-  ce = cudaMallocHost((void**)&h->host_pinned, W * G * sizeof(double));
+  ce = cudaMallocHost((void**)&h->host_pinned, 2 * W * G * sizeof(double));
+  for (auto& e : h->stage_ev)
+    if (ce == cudaSuccess) ce = cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
   if (ce != cudaSuccess) { g_create_err = cudaGetErrorString(ce); release(h); delete h; return AFQMC_ERR_CUDA; }
   h->host_pinned_bytes = W * G * sizeof(double);
 
@@ -700,11 +704,17 @@ int afqmc_step(afqmc_handle* h, const double* xi, const double* eshift) {
     h->launches++;
   }
   if (xi) {
-    // the previous step's copy out of the staging buffer must be done
-    CK(cudaStreamSynchronize(h->stream));
-    memcpy(h->host_pinned, xi, (size_t)h->nwalk * h->G * sizeof(double));
-    CK(cudaMemcpyAsync(h->xi, h->host_pinned, (size_t)h->nwalk * h->G * sizeof(double), cudaMemcpyHostToDevice,
-                       h->stream));
+    // two pinned staging buffers in turn: this step's fields are copied into the
+    // buffer whose last transfer has finished (its event), so the host's copy
+    // overlaps the device's previous step; the transfer itself is stream-ordered
+    // after that step, which still reads the device copy
+    const int b = h->stage_next;
+    h->stage_next ^= 1;
+    CK(cudaEventSynchronize(h->stage_ev[b]));
+    double* stage = h->host_pinned + (size_t)b * h->nwalk * h->G;
+    memcpy(stage, xi, h->host_pinned_bytes);
+    CK(cudaMemcpyAsync(h->xi, stage, h->host_pinned_bytes, cudaMemcpyHostToDevice, h->stream));
+    CK(cudaEventRecord(h->stage_ev[b], h->stream));
   }
   cudaEvent_t e0;
   stage_begin(h, afqmc::ST_FB, &e0);

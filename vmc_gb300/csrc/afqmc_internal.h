@@ -108,8 +108,10 @@ struct afqmc_handle {
   double2* epart = nullptr;   // [W][nechunk]         local-energy partial sums
   double2* eloc = nullptr;    // [W]
   double* scal = nullptr;     // [S_NSLOTS]
-  double* host_pinned = nullptr;  // pinned staging for xi
-  size_t host_pinned_bytes = 0;
+  double* host_pinned = nullptr;  // pinned staging for xi: two buffers of W G doubles, used in turn
+  size_t host_pinned_bytes = 0;   // bytes of one buffer
+  cudaEvent_t stage_ev[2] = {nullptr, nullptr};  // recorded after each buffer's copy to the device
+  int stage_next = 0;
   int nechunk = 0;
   afqmc::PropChunk* d_chunks = nullptr;
   int nchunks = 0;
