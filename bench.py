@@ -385,7 +385,12 @@ def main():
     # end to end through the public API with host buffers: fields H2D, weights and the
     # step's energy estimate D2H every step
     rng = np.random.default_rng(1)
-    xis = [np.ascontiguousarray(rng.standard_normal((W, G))) for _ in range(2)]
+    import torch
+    xis = []
+    for _ in range(2):  # the step's fields in page-locked host memory
+        t = torch.empty((W, G), dtype=torch.float64, pin_memory=True)
+        t.numpy()[:] = rng.standard_normal((W, G))
+        xis.append(t.numpy())
     wbuf = np.zeros(W)
     ebuf = np.zeros(4)
     wk.sync()
@@ -400,7 +405,7 @@ def main():
     wk.sync()
     e2e_s = time.perf_counter() - t0
     e2e = {"value": W * args.steps * world / e2e_s, "unit": "walker-steps/s",
-           "h2d_bytes_per_step": W * G * 8, "d2h_bytes_per_step": W * 8 + 32}
+           "h2d_bytes_per_step": W * G * 8, "d2h_bytes_per_step": W * 8 + 32, "host_fields": "page-locked"}
 
     forms = {}
     if not args.quick:

@@ -9,6 +9,7 @@ measurement on the device, and whole blocks as graph replays.
   samples.dat columns within 1e-10 relative, the same count of clamped energies.
 * One block as a graph replay equals the same launches made one by one, bit
   for bit.
+* Host fields from page-locked and from pageable memory give the same steps.
 """
 import numpy as np
 import pytest
@@ -98,3 +99,25 @@ def test_block_graph_equals_calls(A):
     # after the comb every weight is the mean weight
     assert np.allclose(wa, wa[0])
     g.close()
+
+
+def test_host_fields_pinned_and_pageable_give_the_same_step(A):
+    """afqmc_step takes a page-locked field buffer by direct transfer and a
+    pageable one through its two staging buffers: the same fields give the
+    same walkers bit for bit, over several steps (the staging buffers are
+    reused in turn)."""
+    torch = pytest.importorskip("torch")
+    s = S.make_system(40, 7, 150, 77, "uhf")
+    W, G = 64, s["nchol"]
+    rng = np.random.default_rng(11)
+    fields = [rng.standard_normal((W, G)) for _ in range(3)]
+    a = make(A, s, W)
+    b = make(A, s, W)
+    pinned = torch.empty((W, G), dtype=torch.float64, pin_memory=True)
+    for f in fields:
+        a.propagate_phaseless(np.array(f))
+        pinned.numpy()[:] = f
+        b.propagate_phaseless(pinned.numpy())
+    da, oa, wa = a.get_det()
+    db, ob, wb = b.get_det()
+    assert np.array_equal(da, db) and np.array_equal(oa, ob) and np.array_equal(wa, wb)

@@ -703,7 +703,15 @@ int afqmc_step(afqmc_handle* h, const double* xi, const double* eshift) {
     k_set_scalar<<<1, 1, 0, h->stream>>>(h->scal, afqmc::S_ESHIFT, *eshift);
     h->launches++;
   }
-  if (xi) {
+  cudaPointerAttributes xa;
+  if (xi && cudaPointerGetAttributes(&xa, xi) == cudaSuccess && xa.type == cudaMemoryTypeHost) {
+    // a page-locked (or registered) caller buffer is transferred directly; the
+    // call returns once the transfer is done, so the caller may reuse it
+    CK(cudaMemcpyAsync(h->xi, xi, h->host_pinned_bytes, cudaMemcpyHostToDevice, h->stream));
+    CK(cudaEventRecord(h->stage_ev[h->stage_next], h->stream));
+    CK(cudaEventSynchronize(h->stage_ev[h->stage_next]));
+  } else if (xi) {
+    cudaGetLastError();  // a pageable pointer is not an error
     // two pinned staging buffers in turn: this step's fields are copied into the
     // buffer whose last transfer has finished (its event), so the host's copy
     // overlaps the device's previous step; the transfer itself is stream-ordered
