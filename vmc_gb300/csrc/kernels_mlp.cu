@@ -186,9 +186,116 @@ __global__ void k_to_bf16(const float* __restrict__ P, __nv_bfloat16* __restrict
 
 static dim3 g2(int M, int N) { return dim3((N + 63) / 64, (M + 63) / 64); }
 
-// forward of a device batch X [B][nin] -> Y [B] on stream st (activations kept for backward)
-void mlp_forward_on(afqmc_mlp* m, const float* X, int B, float* Y, cudaStream_t st) {
+// The whole forward pass for MF_RB walkers per CTA, one hidden unit per thread
+// (H <= MF_THREADS): the same FP32 multiply-add chains over k in the same order,
+// bias, SiLU and output reduction as the layer kernels above, so the results
+// are bit-identical, in one launch.  Each weight matrix passes through shared
+// memory in chunks of MF_KC input columns, transposed so thread o reads its
+// column without conflicts; activations are kept as [unit][walker] so one
+// 128-bit broadcast load feeds four walkers.  Z1, H1, Z2, H2 (for backward)
+// are written when non-null.
+constexpr int MF_RB = 16, MF_KC = 32, MF_THREADS = 256;
+static size_t mf_smem(int nin, int H) { return ((size_t)MF_RB * (nin + 2 * H) + (size_t)MF_KC * H) * sizeof(float); }
+
+__device__ __forceinline__ void mf_layer(const float* __restrict__ inT, int K, int H, const __nv_bfloat16* __restrict__ W,
+                                         float* Ws, float* acc) {
+  const int o = threadIdx.x;
+#pragma unroll
+  for (int b = 0; b < MF_RB; ++b) acc[b] = 0.f;
+  for (int k0 = 0; k0 < K; k0 += MF_KC) {
+    const int kc = min(MF_KC, K - k0);
+    __syncthreads();  // the previous chunk is consumed
+    for (int e = threadIdx.x; e < kc * H; e += blockDim.x) {
+      const int oo = e / kc, kk = e - oo * kc;
+      Ws[kk * H + oo] = __bfloat162float(W[(size_t)oo * K + k0 + kk]);
+    }
+    __syncthreads();
+    if (o < H)
+      for (int kk = 0; kk < kc; ++kk) {
+        const float w = Ws[kk * H + o];
+        const float4* x = reinterpret_cast<const float4*>(inT + (size_t)(k0 + kk) * MF_RB);
+#pragma unroll
+        for (int q = 0; q < MF_RB / 4; ++q) {
+          const float4 v = x[q];
+          acc[4 * q] = fmaf(v.x, w, acc[4 * q]);
+          acc[4 * q + 1] = fmaf(v.y, w, acc[4 * q + 1]);
+          acc[4 * q + 2] = fmaf(v.z, w, acc[4 * q + 2]);
+          acc[4 * q + 3] = fmaf(v.w, w, acc[4 * q + 3]);
+        }
+      }
+  }
+}
+
+__global__ void __launch_bounds__(MF_THREADS)
+    k_mlp_fwd(const float* __restrict__ X, int B, int nin, int H, const __nv_bfloat16* __restrict__ W1,
+              const float* __restrict__ b1, const __nv_bfloat16* __restrict__ W2, const float* __restrict__ b2,
+              const __nv_bfloat16* __restrict__ w3, const float* __restrict__ b3, float* __restrict__ Y,
+              float* __restrict__ Z1, float* __restrict__ H1, float* __restrict__ Z2, float* __restrict__ H2) {
+  extern __shared__ __align__(16) float mf_sm[];
+  float* XT = mf_sm;                 // [nin][MF_RB]
+  float* H1T = XT + MF_RB * nin;     // [H][MF_RB]
+  float* H2T = H1T + MF_RB * H;      // [H][MF_RB]
+  float* Ws = H2T + MF_RB * H;       // [MF_KC][H]
+  const int b0 = blockIdx.x * MF_RB, nb = min(MF_RB, B - b0), o = threadIdx.x;
+  for (int e = threadIdx.x; e < MF_RB * nin; e += blockDim.x) {
+    const int b = e / nin, k = e - b * nin;
+    XT[k * MF_RB + b] = b < nb ? X[(size_t)(b0 + b) * nin + k] : 0.f;
+  }
+  float acc[MF_RB];
+  mf_layer(XT, nin, H, W1, Ws, acc);
+  if (o < H) {
+#pragma unroll
+    for (int b = 0; b < MF_RB; ++b) {
+      const float z = acc[b] + b1[o];
+      const float h = silu_f(z);
+      H1T[o * MF_RB + b] = h;
+      if (Z1 && b < nb) {
+        Z1[(size_t)(b0 + b) * H + o] = z;
+        H1[(size_t)(b0 + b) * H + o] = h;
+      }
+    }
+  }
+  mf_layer(H1T, H, H, W2, Ws, acc);  // begins with a barrier: H1T is complete
+  if (o < H) {
+#pragma unroll
+    for (int b = 0; b < MF_RB; ++b) {
+      const float z = acc[b] + b2[o];
+      const float h = silu_f(z);
+      H2T[o * MF_RB + b] = h;
+      if (Z2 && b < nb) {
+        Z2[(size_t)(b0 + b) * H + o] = z;
+        H2[(size_t)(b0 + b) * H + o] = h;
+      }
+    }
+  }
+  __syncthreads();
+  // y[b] = h2[b] . w3 + b3, lane-strided partial sums and a butterfly (as k_mlp_out)
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int b = warp; b < nb; b += MF_THREADS / 32) {
+    float sum = 0.f;
+    for (int oo = lane; oo < H; oo += 32) sum = fmaf(H2T[oo * MF_RB + b], __bfloat162float(w3[oo]), sum);
+    sum = warp_sumf(sum);
+    if (lane == 0) Y[b0 + b] = sum + b3[0];
+  }
+}
+
+// forward of a device batch X [B][nin] -> Y [B] on stream st; keep: the
+// activations are stored for a backward pass
+void mlp_forward_on(afqmc_mlp* m, const float* X, int B, float* Y, cudaStream_t st, bool keep) {
   const int H = m->H, nin = m->nin;
+  if (H <= MF_THREADS && mf_smem(nin, H) <= 200 * 1024) {
+    static size_t attr = 0;
+    const size_t smem = mf_smem(nin, H);
+    if (smem > attr) {
+      cudaFuncSetAttribute(k_mlp_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      attr = smem;
+    }
+    k_mlp_fwd<<<(B + MF_RB - 1) / MF_RB, MF_THREADS, smem, st>>>(
+        X, B, nin, H, m->Pb, m->P + m->o_b1(), m->Pb + m->o_W2(), m->P + m->o_b2(), m->Pb + m->o_w3(),
+        m->P + m->o_b3(), Y, keep ? m->Z1 : nullptr, keep ? m->H1 : nullptr, keep ? m->Z2 : nullptr,
+        keep ? m->H2 : nullptr);
+    return;
+  }
   k_mlp_gemm<__nv_bfloat16, EpiDense><<<g2(B, H), 256, 0, st>>>(
       B, H, nin, X, nin, 1, m->Pb, nin, 1, EpiDense{m->P + m->o_b1(), m->Z1, m->H1, H});
   k_mlp_gemm<__nv_bfloat16, EpiDense><<<g2(B, H), 256, 0, st>>>(
@@ -196,14 +303,16 @@ void mlp_forward_on(afqmc_mlp* m, const float* X, int B, float* Y, cudaStream_t 
   k_mlp_out<<<(B + 7) / 8, 256, 0, st>>>(m->H2, m->Pb + m->o_w3(), m->P + m->o_b3(), Y, B, H);
 }
 
-void mlp_forward(afqmc_mlp* m, const float* X, int B, float* Y) { mlp_forward_on(m, X, B, Y, m->stream); }
+void mlp_forward(afqmc_mlp* m, const float* X, int B, float* Y, bool keep) {
+  mlp_forward_on(m, X, B, Y, m->stream, keep);
+}
 int mlp_max_batch(const afqmc_mlp* m) { return m->maxb; }
 int mlp_n_in(const afqmc_mlp* m) { return m->nin; }
 
 // loss and gradients (into m->Gr) for the device batch (X, T)
 void mlp_backward(afqmc_mlp* m, const float* X, const float* T, int B) {
   const int H = m->H, nin = m->nin;
-  mlp_forward(m, X, B, m->Y);
+  mlp_forward(m, X, B, m->Y, true);
   k_mlp_out_back<<<1, 1024, 0, m->stream>>>(m->Y, T, m->H2, m->Z2, m->Pb + m->o_w3(), m->D2, m->Gr + m->o_w3(),
                                             m->Gr + m->o_b3(), m->loss, B, H);
   // gW2[o][i] = sum_b dz2[b][o] h1[b][i]
@@ -331,7 +440,7 @@ int afqmc_mlp_predict(afqmc_mlp* m, const float* x, int B, float* y) {
   if (!m || !x || !y || B <= 0 || B > m->maxb) return AFQMC_ERR_ARG;
   cudaSetDevice(m->device);
   MCK(cudaMemcpyAsync(m->X, x, (size_t)B * m->nin * 4, cudaMemcpyHostToDevice, m->stream));
-  mlp_forward(m, m->X, B, m->Y);
+  mlp_forward(m, m->X, B, m->Y, false);
   MCK(cudaGetLastError());
   MCK(cudaMemcpyAsync(y, m->Y, (size_t)B * 4, cudaMemcpyDeviceToHost, m->stream));
   MCK(cudaStreamSynchronize(m->stream));
