@@ -189,40 +189,32 @@ static dim3 g2(int M, int N) { return dim3((N + 63) / 64, (M + 63) / 64); }
 // The whole forward pass for MF_RB walkers per CTA, one hidden unit per thread
 // (H <= MF_THREADS): the same FP32 multiply-add chains over k in the same order,
 // bias, SiLU and output reduction as the layer kernels above, so the results
-// are bit-identical, in one launch.  Each weight matrix passes through shared
-// memory in chunks of MF_KC input columns, transposed so thread o reads its
-// column without conflicts; activations are kept as [unit][walker] so one
-// 128-bit broadcast load feeds four walkers.  Z1, H1, Z2, H2 (for backward)
-// are written when non-null.
-constexpr int MF_RB = 16, MF_KC = 32, MF_THREADS = 256;
-static size_t mf_smem(int nin, int H) { return ((size_t)MF_RB * (nin + 2 * H) + (size_t)MF_KC * H) * sizeof(float); }
+// are bit-identical, in one launch.  Both BF16 weight matrices are copied into
+// shared memory once, transposed ([k][o]: thread o loads its own row and
+// stores along o, conflict-free, and reads its column the same way);
+// activations are kept as [unit][walker] so one 128-bit broadcast load feeds
+// four walkers.  Z1, H1, Z2, H2 (for backward) are written when non-null.
+constexpr int MF_RB = 16, MF_THREADS = 256;
+static size_t mf_smem(int nin, int H) {
+  return (size_t)(nin + H) * H * sizeof(__nv_bfloat16) + (size_t)MF_RB * (nin + 2 * H) * sizeof(float) + 16;
+}
 
-__device__ __forceinline__ void mf_layer(const float* __restrict__ inT, int K, int H, const __nv_bfloat16* __restrict__ W,
-                                         float* Ws, float* acc) {
+__device__ __forceinline__ void mf_layer(const float* __restrict__ inT, int K, int H, const __nv_bfloat16* WT,
+                                         float* acc) {
   const int o = threadIdx.x;
 #pragma unroll
   for (int b = 0; b < MF_RB; ++b) acc[b] = 0.f;
-  for (int k0 = 0; k0 < K; k0 += MF_KC) {
-    const int kc = min(MF_KC, K - k0);
-    __syncthreads();  // the previous chunk is consumed
-    for (int e = threadIdx.x; e < kc * H; e += blockDim.x) {
-      const int oo = e / kc, kk = e - oo * kc;
-      Ws[kk * H + oo] = __bfloat162float(W[(size_t)oo * K + k0 + kk]);
-    }
-    __syncthreads();
-    if (o < H)
-      for (int kk = 0; kk < kc; ++kk) {
-        const float w = Ws[kk * H + o];
-        const float4* x = reinterpret_cast<const float4*>(inT + (size_t)(k0 + kk) * MF_RB);
+  for (int k = 0; k < K; ++k) {
+    const float w = __bfloat162float(WT[k * H + o]);
+    const float4* x = reinterpret_cast<const float4*>(inT + (size_t)k * MF_RB);
 #pragma unroll
-        for (int q = 0; q < MF_RB / 4; ++q) {
-          const float4 v = x[q];
-          acc[4 * q] = fmaf(v.x, w, acc[4 * q]);
-          acc[4 * q + 1] = fmaf(v.y, w, acc[4 * q + 1]);
-          acc[4 * q + 2] = fmaf(v.z, w, acc[4 * q + 2]);
-          acc[4 * q + 3] = fmaf(v.w, w, acc[4 * q + 3]);
-        }
-      }
+    for (int q = 0; q < MF_RB / 4; ++q) {
+      const float4 v = x[q];
+      acc[4 * q] = fmaf(v.x, w, acc[4 * q]);
+      acc[4 * q + 1] = fmaf(v.y, w, acc[4 * q + 1]);
+      acc[4 * q + 2] = fmaf(v.z, w, acc[4 * q + 2]);
+      acc[4 * q + 3] = fmaf(v.w, w, acc[4 * q + 3]);
+    }
   }
 }
 
@@ -235,15 +227,32 @@ __global__ void __launch_bounds__(MF_THREADS)
   float* XT = mf_sm;                 // [nin][MF_RB]
   float* H1T = XT + MF_RB * nin;     // [H][MF_RB]
   float* H2T = H1T + MF_RB * H;      // [H][MF_RB]
-  float* Ws = H2T + MF_RB * H;       // [MF_KC][H]
+  __nv_bfloat16* W1T = reinterpret_cast<__nv_bfloat16*>(H2T + MF_RB * H);  // [nin][H]
+  __nv_bfloat16* W2T = W1T + (size_t)nin * H;                                // [H][H]
   const int b0 = blockIdx.x * MF_RB, nb = min(MF_RB, B - b0), o = threadIdx.x;
   for (int e = threadIdx.x; e < MF_RB * nin; e += blockDim.x) {
     const int b = e / nin, k = e - b * nin;
     XT[k * MF_RB + b] = b < nb ? X[(size_t)(b0 + b) * nin + k] : 0.f;
   }
-  float acc[MF_RB];
-  mf_layer(XT, nin, H, W1, Ws, acc);
   if (o < H) {
+    const __nv_bfloat16* r1 = W1 + (size_t)o * nin;
+    for (int k = 0; k < nin; ++k) W1T[k * H + o] = r1[k];
+    const __nv_bfloat16* r2 = W2 + (size_t)o * H;
+    if ((H & 7) == 0) {
+      for (int k8 = 0; k8 < H; k8 += 8) {
+        const uint4 v = *reinterpret_cast<const uint4*>(r2 + k8);
+        const __nv_bfloat16* e = reinterpret_cast<const __nv_bfloat16*>(&v);
+#pragma unroll
+        for (int i = 0; i < 8; ++i) W2T[(k8 + i) * H + o] = e[i];
+      }
+    } else {
+      for (int k = 0; k < H; ++k) W2T[k * H + o] = r2[k];
+    }
+  }
+  __syncthreads();
+  float acc[MF_RB];
+  if (o < H) {
+    mf_layer(XT, nin, H, W1T, acc);
 #pragma unroll
     for (int b = 0; b < MF_RB; ++b) {
       const float z = acc[b] + b1[o];
@@ -255,8 +264,9 @@ __global__ void __launch_bounds__(MF_THREADS)
       }
     }
   }
-  mf_layer(H1T, H, H, W2, Ws, acc);  // begins with a barrier: H1T is complete
+  __syncthreads();
   if (o < H) {
+    mf_layer(H1T, H, H, W2T, acc);
 #pragma unroll
     for (int b = 0; b < MF_RB; ++b) {
       const float z = acc[b] + b2[o];
@@ -283,7 +293,7 @@ __global__ void __launch_bounds__(MF_THREADS)
 // activations are stored for a backward pass
 void mlp_forward_on(afqmc_mlp* m, const float* X, int B, float* Y, cudaStream_t st, bool keep) {
   const int H = m->H, nin = m->nin;
-  if (H <= MF_THREADS && mf_smem(nin, H) <= 200 * 1024) {
+  if (H <= MF_THREADS && mf_smem(nin, H) <= 220 * 1024) {
     static size_t attr = 0;
     const size_t smem = mf_smem(nin, H);
     if (smem > attr) {
