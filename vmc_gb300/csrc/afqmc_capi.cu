@@ -178,7 +178,7 @@ void release(afqmc_handle* h) {
                   h->thetaB, h->xB, h->fb32, h->V32, h->expm32, h->d_chunks32, h->rotE, h->thetaE,
                   h->xc, h->cv_x, h->cv_idx, h->cv_esub, h->cv_f, h->cv_ms, h->cv_out, h->d_step, h->psi32,
                   h->pt_img, h->comb_cum, h->comb_idx, h->comb_ovl, h->blk, h->blk_zeta, h->wpart,
-                  h->ovl_tau, h->ovl_bimg, h->ovl_M, h->theta32, h->mf32, h->h1phi32};
+                  h->ovl_tau, h->ovl_bimg, h->ovl_M, h->theta32, h->mf32, h->h1phi32, h->pt_voff};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (h->host_pinned) cudaFreeHost(h->host_pinned);
@@ -469,7 +469,10 @@ int afqmc_create(const afqmc_ham* ham, const afqmc_trial* trial, const afqmc_opt
     ALLOC(d_chunks32, h->chunks32.size());
     ALLOC(rotE, (size_t)G * h->nce * h->ke_pad);
     ALLOC(psi32, W * h->ncw * N);
-    if (N <= 128) ALLOC(pt_img, (size_t)nsp * 2 * 128 * 256);
+    if (N <= 128) {
+      ALLOC(pt_img, (size_t)nsp * 2 * 128 * 256);
+      ALLOC(pt_voff, (size_t)T);
+    }
     if (afqmc::ovl_tc_wanted(h)) {
       const size_t nm = std::max(h->chan[0].n, h->nchan > 1 ? h->chan[1].n : 0);
       ALLOC(ovl_tau, (size_t)h->nchan * afqmc::ovl_bnp(h));

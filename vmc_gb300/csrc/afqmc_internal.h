@@ -155,6 +155,7 @@ struct afqmc_handle {
   double* blk = nullptr;        // [BLK_MAX][2] total weight, block energy
   double* blk_zeta = nullptr;   // [BLK_MAX]
   __nv_bfloat16* pt_img = nullptr;
+  uint2* pt_voff = nullptr;  // [T] swizzled scatter offsets of the packed triangle (tensor-core propagator)
   // tensor-core overlap matrices (exact BF16 slices): trial-orbital scales
   // [channel][BNP], the swizzled trial-slice images [channel][bytes], and M
   double* ovl_tau = nullptr;

@@ -203,18 +203,21 @@ __device__ __forceinline__ void pt_store_X(uint8_t* sB, const float* x, int nc, 
 // Scatter the walker's V (packed lower triangle, V(i, j) = V(j, i)) into A,
 // split in BF16: row i gets Re V(i, j) at K = j and Im V(i, j) at K = 128 + j.
 // Positions outside [0, N) x ([0, N) U [128, 128 + N)) keep the image's zeros.
+// voff[t] holds entry t's four swizzled byte offsets in one half of A
+// (pt_off of (i, j), (i, 128 + j), (j, i), (j, 128 + i); 16 bits each),
+// built once per handle, so the scatter computes no offsets.
 __device__ __forceinline__ void pt_load_V(uint8_t* sA, const float* __restrict__ vre, const float* __restrict__ vim,
-                                          const int2* __restrict__ tri, int T) {
+                                          const uint2* __restrict__ voff, int T) {
   uint8_t* sAl = sA + PT_A_BYTES;
   constexpr int VB = 8;  // loads of VB entries in flight per thread before their stores
   for (int t0 = threadIdx.x; t0 < T; t0 += VB * blockDim.x) {
-    int2 ij[VB];
+    uint2 off[VB];
     float re[VB], im[VB];
 #pragma unroll
     for (int u = 0; u < VB; ++u) {
       const int t = t0 + u * blockDim.x;
       if (t < T) {
-        ij[u] = __ldg(tri + t);
+        off[u] = __ldg(voff + t);
         re[u] = __ldg(vre + t);
         im[u] = __ldg(vim + t);
       }
@@ -225,20 +228,26 @@ __device__ __forceinline__ void pt_load_V(uint8_t* sA, const float* __restrict__
       __nv_bfloat16 rh, rl, ih, il;
       pt_split(re[u], rh, rl);
       pt_split(im[u], ih, il);
-      uint32_t o = pt_off(ij[u].x, ij[u].y, 128);
-      *(__nv_bfloat16*)(sA + o) = rh;
-      *(__nv_bfloat16*)(sAl + o) = rl;
-      o = pt_off(ij[u].x, 128 + ij[u].y, 128);
-      *(__nv_bfloat16*)(sA + o) = ih;
-      *(__nv_bfloat16*)(sAl + o) = il;
-      o = pt_off(ij[u].y, ij[u].x, 128);
-      *(__nv_bfloat16*)(sA + o) = rh;
-      *(__nv_bfloat16*)(sAl + o) = rl;
-      o = pt_off(ij[u].y, 128 + ij[u].x, 128);
-      *(__nv_bfloat16*)(sA + o) = ih;
-      *(__nv_bfloat16*)(sAl + o) = il;
+      const uint32_t o0 = off[u].x & 0xFFFFu, o1 = off[u].x >> 16, o2 = off[u].y & 0xFFFFu, o3 = off[u].y >> 16;
+      *(__nv_bfloat16*)(sA + o0) = rh;
+      *(__nv_bfloat16*)(sAl + o0) = rl;
+      *(__nv_bfloat16*)(sA + o1) = ih;
+      *(__nv_bfloat16*)(sAl + o1) = il;
+      *(__nv_bfloat16*)(sA + o2) = rh;
+      *(__nv_bfloat16*)(sAl + o2) = rl;
+      *(__nv_bfloat16*)(sA + o3) = ih;
+      *(__nv_bfloat16*)(sAl + o3) = il;
     }
   }
+}
+
+// the scatter offsets of every packed-triangle entry (see pt_load_V)
+__global__ void k_pt_voff(const int2* __restrict__ tri, uint2* __restrict__ voff, int T) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= T) return;
+  const int i = tri[t].x, j = tri[t].y;
+  voff[t] = make_uint2(pt_off(i, j, 128) | (pt_off(i, 128 + j, 128) << 16),
+                       pt_off(j, i, 128) | (pt_off(j, 128 + i, 128) << 16));
 }
 
 // PT_CW = 20 columns of this thread's TMEM lane at taddr and at taddr2 (x16 + x4 each), one wait
@@ -311,7 +320,7 @@ __device__ __forceinline__ void pt_add_row(uint32_t taddr, float* y, bool cplx) 
 
 __global__ void __launch_bounds__(PT_THREADS, 1)
     k_prop_tc(double2* __restrict__ psi, float2* __restrict__ psi32, const float* __restrict__ Vp,
-              const __nv_bfloat16* __restrict__ img, const int2* __restrict__ tri,
+              const __nv_bfloat16* __restrict__ img, const uint2* __restrict__ voff,
               const double* __restrict__ weights, int N, int ncw, int na, int nspV, int realB, int* err) {
   const int w = blockIdx.x;
   if (!(weights[w] > 1.0e-8)) return;
@@ -384,7 +393,7 @@ __global__ void __launch_bounds__(PT_THREADS, 1)
 #pragma unroll
     for (int c = 0; c < PT_CW; ++c) acc[c] = x[c];  // the Taylor sum starts from B psi
     // Taylor terms with V: term_k = V term_{k-1} / k, added to the sum in TMEM
-    pt_load_V(sA, vre, vim, tri, T);
+    pt_load_V(sA, vre, vim, voff, T);
     for (int k = 1; k <= 5 && ok; ++k) {
       if (p < N) pt_store_X(sB, x, nc, p, g);
       if (!(ok = pt_product(sA, sB, nc, true, tmem, bar_mma, ph_mma, err))) break;
@@ -429,6 +438,7 @@ bool setup_prop_tc(afqmc_handle* h) {
   if (h->N > 128 || !h->pt_img) return true;
   dim3 grid(128 * PT_K / 256, h->nsp);
   k_pt_image<<<grid, 256, 0, h->stream>>>(h->expm32, h->pt_img, h->N);
+  k_pt_voff<<<(h->T + 255) / 256, 256, 0, h->stream>>>(h->tri, h->pt_voff, h->T);
   return cudaGetLastError() == cudaSuccess;
 }
 
@@ -441,7 +451,7 @@ void launch_propagate_tc(afqmc_handle* h) {
     attr = true;
   }
   dim3 grid(h->nwalk, h->nspV);
-  k_prop_tc<<<grid, PT_THREADS, PT_SMEM, h->stream>>>(h->psi, h->psi32, h->V32, h->pt_img, h->tri, h->weights, h->N,
+  k_prop_tc<<<grid, PT_THREADS, PT_SMEM, h->stream>>>(h->psi, h->psi32, h->V32, h->pt_img, h->pt_voff, h->weights, h->N,
                                                h->ncw, h->na, h->nspV, h->real_expm ? 1 : 0, h->d_err);
   h->launches++;
 }
