@@ -27,9 +27,8 @@
 // pair, psi32 as that double rounded to FP32.  None of it runs on the FP64 pipe but the one
 // addition per stored number and the n multiplications of the determinant.
 //
-// One CTA (256 threads) per walker, the two spin blocks at once in its two
-// halves; each block (as high and low parts), its Gram/R matrix and X live in
-// shared memory.  Dead
+// One CTA (256 threads) per walker, both spin blocks in turn; the block (as
+// high and low parts), the Gram/R matrix and X live in shared memory.  Dead
 // walkers (weight <= 1e-8) are skipped: they are never propagated again, and
 // the comb only copies live walkers over them.  A block whose Gram matrix is
 // not numerically positive definite is left unchanged (the overlap stays
@@ -46,48 +45,40 @@ namespace afqmc {
 
 constexpr int OC_THREADS = 256;
 
-// the half of the CTA working on spin block h: 128 threads, named barrier 1 + h
-__device__ __forceinline__ void oc_bar(int h) { asm volatile("bar.sync %0, 128;" ::"r"(1 + h) : "memory"); }
-
 __global__ void __launch_bounds__(OC_THREADS)
     k_ortho_chol(double2* __restrict__ psi, float2* __restrict__ psi32, double2* __restrict__ ovlp,
                  const double* __restrict__ weights, int N, int ncw, int na, int nb, int rhf_walker, int nmax) {
   const int w = blockIdx.x;
   if (!(weights[w] > 1.0e-8)) return;
   extern __shared__ float2 oc_sm[];
-  __shared__ int s_bad[2];
-  __shared__ double s_fac[2];
-  // the two spin blocks are orthonormalised at once, one per half of the CTA
-  // (128 threads each, own shared memory), so that the serial Cholesky and
-  // R^-1 of one overlap those of the other
-  const int h = threadIdx.x >> 7, tid = threadIdx.x & 127, lane = tid & 31, warp = tid >> 5;
   // spin block columns at an odd stride (in 8-byte words), so that the Gram
   // loop's reads of up to 16 different columns at one row hit 16 different banks
   const int ld = N | 1;
-  const size_t region = (size_t)2 * nmax * ld + 2 * (size_t)nmax * nmax;
-  float2* Ah = oc_sm + h * region;         // [nmax][ld] spin block, high parts, column-major
+  float2* Ah = oc_sm;                      // [nmax][ld] spin block, high parts, column-major
   float2* Al = Ah + (size_t)nmax * ld;     // [nmax][ld] low parts
   float2* R = Al + (size_t)nmax * ld;      // [nmax][nmax] Gram, then R in its upper triangle (R[i * n + j])
   float2* X = R + (size_t)nmax * nmax;     // [nmax][nmax] X = R^-1, upper (X[i * n + j])
-  const int off = h == 0 ? 0 : na, n = h == 0 ? na : nb;
-  const bool active = n > 0 && (h == 0 || !rhf_walker);
-  if (tid == 0) {
-    s_bad[h] = 0;
-    s_fac[h] = 1.0;
-  }
-  if (active) {
+  __shared__ int s_bad;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  double fac = 1.0;  // thread 0
+  const int nblk = rhf_walker ? 1 : 2;
+  for (int b = 0; b < nblk; ++b) {
+    const int off = b == 0 ? 0 : na, n = b == 0 ? na : nb;
+    if (n == 0) continue;
     double2* Ag = psi + ((size_t)w * ncw + off) * N;
     float2* Ag32 = psi32 + ((size_t)w * ncw + off) * N;
-    for (int e = tid; e < n * N; e += 128) {
+    __syncthreads();  // Ah, Al, R, X free (previous block done)
+    for (int e = tid; e < n * N; e += OC_THREADS) {
       const double2 v = Ag[e];
       const df32 re = df_split_bits(v.x), im = df_split_bits(v.y);
       const int o = (e / N) * ld + e % N;
       Ah[o] = make_float2(re.h, im.h);
       Al[o] = make_float2(re.l, im.l);
     }
-    oc_bar(h);
+    if (tid == 0) s_bad = 0;
+    __syncthreads();
     // Gram matrix (FP32), upper triangle: R[i][j] = sum_p conj(A_i[p]) A_j[p], i <= j
-    for (int e = tid; e < n * n; e += 128) {
+    for (int e = tid; e < n * n; e += OC_THREADS) {
       const int i = e / n, j = e % n;
       if (i > j) continue;
       const float2* ai = Ah + (size_t)i * ld;
@@ -108,8 +99,8 @@ __global__ void __launch_bounds__(OC_THREADS)
       }
       R[i * n + j] = make_float2(sr + tr, si + ti);
     }
-    oc_bar(h);
-    // Cholesky (the half's first warp, FP32): row k of R from G and rows m < k
+    __syncthreads();
+    // Cholesky (warp 0, FP32): row k of R from G and rows m < k
     if (warp == 0) {
       bool bad = false;
       for (int k = 0; k < n; ++k) {
@@ -140,13 +131,12 @@ __global__ void __launch_bounds__(OC_THREADS)
         }
         __syncwarp();
       }
-      if (lane == 0 && bad) s_bad[h] = 1;
+      if (lane == 0 && bad) s_bad = 1;
     }
-    oc_bar(h);
-  }
-  if (active && !s_bad[h]) {  // a block that is not numerically positive definite is left as it is
+    __syncthreads();
+    if (s_bad) continue;  // leave this block as it is
     // X = R^-1 by columns (FP32): thread j solves R x = e_j by back substitution
-    for (int j = tid; j < n; j += 128) {
+    for (int j = tid; j < n; j += OC_THREADS) {
       X[j * n + j] = make_float2(1.f / R[j * n + j].x, 0.f);
       for (int i = j - 1; i >= 0; --i) {
         float2 t = make_float2(0.f, 0.f);
@@ -159,19 +149,17 @@ __global__ void __launch_bounds__(OC_THREADS)
         X[i * n + j] = make_float2(-t.x * inv, -t.y * inv);
       }
     }
-    oc_bar(h);
-    double2* Ag = psi + ((size_t)w * ncw + off) * N;
-    float2* Ag32 = psi32 + ((size_t)w * ncw + off) * N;
+    __syncthreads();
     // Q = A X: Q[j][p] = sum_{i <= j} A[i][p] X[i][j], compensated
-    for (int e = tid; e < n * N; e += 128) {
+    for (int e = tid; e < n * N; e += OC_THREADS) {
       const int j = e / N, p = e % N;
       float sr = 0.f, cr = 0.f, si = 0.f, ci = 0.f;
       for (int i = 0; i <= j; ++i) {
-        const float2 hh = Ah[(size_t)i * ld + p], l = Al[(size_t)i * ld + p], x = X[i * n + j];
-        dot2_acc(sr, cr, hh.x, l.x, x.x);
-        dot2_acc(sr, cr, -hh.y, -l.y, x.y);
-        dot2_acc(si, ci, hh.x, l.x, x.y);
-        dot2_acc(si, ci, hh.y, l.y, x.x);
+        const float2 h = Ah[(size_t)i * ld + p], l = Al[(size_t)i * ld + p], x = X[i * n + j];
+        dot2_acc(sr, cr, h.x, l.x, x.x);
+        dot2_acc(sr, cr, -h.y, -l.y, x.y);
+        dot2_acc(si, ci, h.x, l.x, x.y);
+        dot2_acc(si, ci, h.y, l.y, x.x);
       }
       const df32 qr = df_fast(sr, cr), qi = df_fast(si, ci);
       const double2 q = make_double2(df_to_double_bits(qr), df_to_double_bits(qi));
@@ -180,15 +168,10 @@ __global__ void __launch_bounds__(OC_THREADS)
       // (the pair's high part can differ from it when the low part is a tie)
       Ag32[e] = make_float2(df_split_bits(q.x).h, df_split_bits(q.y).h);
     }
-    if (tid == 0) {
-      double f = 1.0;
-      for (int k = 0; k < n; ++k) f *= (double)X[k * n + k].x;
-      s_fac[h] = f;
-    }
+    if (tid == 0)
+      for (int k = 0; k < n; ++k) fac *= (double)X[k * n + k].x;
   }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double fac = s_fac[0] * s_fac[1];
+  if (tid == 0) {
     if (rhf_walker) fac *= fac;
     const double2 o = ovlp[w];
     ovlp[w] = make_double2(o.x * fac, o.y * fac);
@@ -197,7 +180,7 @@ __global__ void __launch_bounds__(OC_THREADS)
 
 size_t ortho_chol_smem(const afqmc_handle* h) {
   const size_t nmax = (size_t)std::max(h->na, h->rhf_walker ? 0 : h->nb);
-  return 2 * (2 * nmax * (size_t)(h->N | 1) + 2 * nmax * nmax) * sizeof(float2);  // one region per spin block
+  return (2 * nmax * (size_t)(h->N | 1) + 2 * nmax * nmax) * sizeof(float2);
 }
 
 bool ortho_chol_available(const afqmc_handle* h) {
