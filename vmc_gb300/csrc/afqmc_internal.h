@@ -161,7 +161,6 @@ struct afqmc_handle {
   double* ovl_tau = nullptr;
   uint8_t* ovl_bimg = nullptr;
   float4* ovl_M = nullptr;  // [W][2][nmax][nmax] double-FP32 (re hi, re lo, im hi, im lo)
-  float* fb_ws = nullptr;   // [3][2W][G] K-split partial force biases (tensor-core GEMM with few tiles)
   float4* mf32 = nullptr;   // [G] mean field as double-FP32 (re hi, re lo, im hi, im lo)
   // control variate
   float* cv_x = nullptr;             // [W][67] features

@@ -133,23 +133,8 @@ struct EpiFB {
   float* fb;
   int G;
   float mult;
-  float* ws;  // split > 1: partial products [split][N][G], summed by k_fb_reduce
   __device__ __forceinline__ void operator()(int m, int n, float v) const { fb[(size_t)n * G + m] = mult * v; }
-  __device__ __forceinline__ void operator()(int m, int n, float v, int sp) const {
-    if (ws) ws[((size_t)sp * gridN + n) * G + m] = v;
-    else fb[(size_t)n * G + m] = mult * v;
-  }
-  int gridN;  // N of the GEMM (2 W)
 };
-
-// fb = mult (sum of the K-split partial products, in a fixed order)
-__global__ void k_fb_reduce(const float* __restrict__ ws, float* __restrict__ fb, size_t n, int split, float mult) {
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-    float s = ws[i];
-    for (int k = 1; k < split; ++k) s += ws[(size_t)k * n + i];
-    fb[i] = mult * s;
-  }
-}
 
 // VHS: rows t (packed index), columns (walker, plane) with plane 0 = L.Re(x),
 // plane 1 = L.Im(x); V = sqrt(dt)(i L.Re(x) - L.Im(x)) kept packed (lower
@@ -164,12 +149,11 @@ struct EpiV32 {
     const float val = plane == 0 ? sdt * v : -(sdt * v);
     V[((size_t)(w * nspV + s) * 2 + (plane == 0 ? 1 : 0)) * T + m] = val;
   }
-  __device__ __forceinline__ void operator()(int m, int n, float v, int) const { (*this)(m, n, v); }
 };
 
 template <int BN, class Epi>
 static void launch_tc_bn(afqmc_handle* h, const CUtensorMap& ta, const CUtensorMap& tb, int M, int N, int K,
-                         const Epi& epi, int split = 1) {
+                         const Epi& epi) {
   constexpr int ST = 4;
   const int smem = tc::GemmPSmem<BN, ST>::TOTAL;
   static bool attr = false;
@@ -179,11 +163,10 @@ static void launch_tc_bn(afqmc_handle* h, const CUtensorMap& ta, const CUtensorM
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, h->device);
     attr = true;
   }
-  // persistent: one CTA per SM (or per work unit when there are fewer)
+  // persistent: one CTA per SM (or per tile when there are fewer tiles)
   const int tiles = ((N + BN - 1) / BN) * ((M + tc::BM - 1) / tc::BM);
-  const int units = tiles * split;
-  const int grid = std::max(1, std::min(units, nsm > 0 ? nsm : units));
-  tc::k_tc_gemm_p<BN, ST, Epi><<<grid, tc::GP_THREADS, smem, h->stream>>>(ta, tb, M, N, K, split, epi, h->d_err);
+  const int grid = std::max(1, std::min(tiles, nsm > 0 ? nsm : tiles));
+  tc::k_tc_gemm_p<BN, ST, Epi><<<grid, tc::GP_THREADS, smem, h->stream>>>(ta, tb, M, N, K, epi, h->d_err);
   h->launches++;
 }
 
@@ -191,30 +174,10 @@ static void launch_tc_bn(afqmc_handle* h, const CUtensorMap& ta, const CUtensorM
 // tbs holds the B-operand tensor maps of the three box heights.
 template <class Epi>
 static void launch_tc(afqmc_handle* h, const CUtensorMap& ta, const CUtensorMap* tbs, int bn, int M, int N, int K,
-                      const Epi& epi, int split = 1) {
-  if (bn == 64) launch_tc_bn<64>(h, ta, tbs[0], M, N, K, epi, split);
-  else if (bn == 256) launch_tc_bn<256>(h, ta, tbs[2], M, N, K, epi, split);
-  else launch_tc_bn<128>(h, ta, tbs[1], M, N, K, epi, split);
-}
-
-// The force bias has few output tiles (G / 128 x 2W / BN) for a long K: when
-// they fill less than two thirds of the SMs, three K-split units per tile
-// keep more SMs busy; their partials meet in fixed order in k_fb_reduce.
-static int fb_split(afqmc_handle* h, int bn) {
-  static int nsm = 0;
-  if (!nsm) cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, h->device);
-  const int tiles = ((2 * h->nwalk + bn - 1) / bn) * ((h->G + tc::BM - 1) / tc::BM);
-  return (h->fb_ws && 3 * tiles < 2 * nsm && h->kf_pad / tc::BK >= 3) ? 3 : 1;
-}
-
-static void launch_fb(afqmc_handle* h, int bn) {
-  const int split = fb_split(h, bn);
-  EpiFB epi{h->fb32, h->G, (float)h->mult, split > 1 ? h->fb_ws : nullptr, 2 * h->nwalk};
-  launch_tc(h, h->tm_rot, h->tm_theta_bn, bn, h->G, 2 * h->nwalk, h->kf_pad, epi, split);
-  if (split > 1) {
-    k_fb_reduce<<<1024, 256, 0, h->stream>>>(h->fb_ws, h->fb32, (size_t)2 * h->nwalk * h->G, split, (float)h->mult);
-    h->launches++;
-  }
+                      const Epi& epi) {
+  if (bn == 64) launch_tc_bn<64>(h, ta, tbs[0], M, N, K, epi);
+  else if (bn == 256) launch_tc_bn<256>(h, ta, tbs[2], M, N, K, epi);
+  else launch_tc_bn<128>(h, ta, tbs[1], M, N, K, epi);
 }
 
 // theta planes (FP64) -> split BF16 operand rows (w, plane)
@@ -226,7 +189,8 @@ void launch_theta_split(afqmc_handle* h) {
 void launch_force_bias_mixed(afqmc_handle* h) {
   if (h->fb_current) return;  // already computed from this theta (control-variate features)
   if (!h->thetaB_from_lu) launch_theta_split(h);
-  launch_fb(h, h->tune_bn_fb);
+  EpiFB epi{h->fb32, h->G, (float)h->mult};
+  launch_tc(h, h->tm_rot, h->tm_theta_bn, h->tune_bn_fb, h->G, 2 * h->nwalk, h->kf_pad, epi);
   h->fb_current = true;
 }
 
@@ -629,7 +593,8 @@ bool setup_mixed(afqmc_handle* h) {
 namespace afqmc {
 // single GEMMs for the autotuner (operands must be current)
 void launch_fb_gemm(afqmc_handle* h, int bn) {
-  launch_fb(h, bn);
+  EpiFB epi{h->fb32, h->G, (float)h->mult};
+  launch_tc(h, h->tm_rot, h->tm_theta_bn, bn, h->G, 2 * h->nwalk, h->kf_pad, epi);
 }
 void launch_vhs_gemm(afqmc_handle* h, int bn) {
   for (int s = 0; s < h->nspV; ++s) {

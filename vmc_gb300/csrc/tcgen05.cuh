@@ -303,13 +303,10 @@ struct GemmPSmem {
 };
 constexpr int GP_THREADS = 192;
 
-// split > 1: each output tile is split into `split` work units over ranges of
-// the K blocks, and the epilogue receives the unit's index in the split (epi(m,
-// n, v, sp)) to store a partial result; a functor that does not split ignores it.
 template <int BN, int STAGES, class Epi>
 __global__ void __launch_bounds__(GP_THREADS, 1)
     k_tc_gemm_p(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, int M, int N,
-                int K, int split, Epi epi, int* err) {
+                int K, Epi epi, int* err) {
   using L = GemmPSmem<BN, STAGES>;
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
@@ -321,7 +318,7 @@ __global__ void __launch_bounds__(GP_THREADS, 1)
   __shared__ int s_abort;
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int ntm = (M + BM - 1) / BM, ntn = (N + BN - 1) / BN, ntiles = ntm * ntn * split;
+  const int ntm = (M + BM - 1) / BM, ntn = (N + BN - 1) / BN, ntiles = ntm * ntn;
   const int nk = K / BK;
 
   if (threadIdx.x == 0) {
@@ -347,10 +344,9 @@ __global__ void __launch_bounds__(GP_THREADS, 1)
   if (warp == 0) {
     if (lane == 0) {
       int kt = 0;  // K blocks issued over all tiles: the ring position
-      for (int u = blockIdx.x; u < ntiles && !s_abort; u += gridDim.x) {
-        const int t = u / split, sp = u - t * split;
+      for (int t = blockIdx.x; t < ntiles && !s_abort; t += gridDim.x) {
         const int m0 = (t % ntm) * BM, n0 = (t / ntm) * BN;
-        for (int kb = sp * nk / split; kb < (sp + 1) * nk / split; ++kb, ++kt) {
+        for (int kb = 0; kb < nk; ++kb, ++kt) {
           const int s = kt % STAGES;
           if (kt >= STAGES && !mbar_wait(&empty[s], ((kt / STAGES) - 1) & 1, err, 41)) {
             s_abort = 1;
@@ -370,7 +366,7 @@ __global__ void __launch_bounds__(GP_THREADS, 1)
     if (lane == 0) {
       constexpr uint32_t idesc = idesc_bf16(BM, BN);
       int kt = 0, tl = 0, last = -1;  // last: local index of the last tile committed
-      for (int w = blockIdx.x; w < ntiles && !s_abort; w += gridDim.x, ++tl) {
+      for (int t = blockIdx.x; t < ntiles && !s_abort; t += gridDim.x, ++tl) {
         const int b = tl & 1, u = tl >> 1;
         if (u > 0 && !mbar_wait(&acc_empty[b], (u - 1) & 1, err, 43)) {
           s_abort = 1;
@@ -379,8 +375,7 @@ __global__ void __launch_bounds__(GP_THREADS, 1)
         tc_fence_after();
         const uint32_t d = tmem + (uint32_t)(b * BN);
         bool ok = true;
-        const int sp = w % split, kb0 = sp * nk / split;
-        for (int kb = kb0; kb < (sp + 1) * nk / split; ++kb, ++kt) {
+        for (int kb = 0; kb < nk; ++kb, ++kt) {
           const int s = kt % STAGES;
           if (!mbar_wait(&full[s], (kt / STAGES) & 1, err, 44)) {
             s_abort = 1;
@@ -392,7 +387,7 @@ __global__ void __launch_bounds__(GP_THREADS, 1)
           const uint32_t bb = a + L::A_BYTES;
 #pragma unroll
           for (int k = 0; k < BK / 16; ++k)
-            mma_bf16(d, sdesc_sw128(a + 32 * k), sdesc_sw128(bb + 32 * k), idesc, (kb > kb0 || k > 0) ? 1u : 0u);
+            mma_bf16(d, sdesc_sw128(a + 32 * k), sdesc_sw128(bb + 32 * k), idesc, (kb > 0 || k > 0) ? 1u : 0u);
           mma_commit(&empty[s]);
         }
         mma_commit(&acc_full[b]);  // also after a break: the epilogue is released
@@ -405,12 +400,11 @@ __global__ void __launch_bounds__(GP_THREADS, 1)
   } else {
     const int q = warp & 3;  // TMEM lane quadrant of this warp
     int tl = 0;
-    for (int w = blockIdx.x; w < ntiles; w += gridDim.x, ++tl) {
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x, ++tl) {
       const int b = tl & 1, u = tl >> 1;
       const bool have = mbar_wait(&acc_full[b], u & 1, err, 45);
       tc_fence_after();
       if (!have || s_abort) break;
-      const int t = w / split, sp = w - t * split;
       const int m0 = (t % ntm) * BM, n0 = (t / ntm) * BN;
       const int row = m0 + q * 32 + lane;
 #pragma unroll 1
@@ -421,7 +415,7 @@ __global__ void __launch_bounds__(GP_THREADS, 1)
 #pragma unroll
           for (int j = 0; j < 16; ++j) {
             const int n = n0 + c + j;
-            if (n < N) epi(row, n, v[j], sp);
+            if (n < N) epi(row, n, v[j]);
           }
         }
       }
