@@ -32,7 +32,7 @@ struct afqmc_mlp;
 namespace afqmc {
 
 constexpr int CV_NF = 67;
-void mlp_forward_on(afqmc_mlp* m, const float* X, int B, float* Y, cudaStream_t st, bool keep);
+int mlp_forward_on(afqmc_mlp* m, const float* X, int B, float* Y, cudaStream_t st, bool keep);
 int mlp_max_batch(const afqmc_mlp* m);
 int mlp_n_in(const afqmc_mlp* m);
 
@@ -279,13 +279,13 @@ int afqmc_cv_measure(afqmc_handle* h, uint64_t tag, int slot) {
   launch_force_bias_mixed(h);
   k_cv_features32<<<W, 128, 0, h->stream>>>(h->fb32, h->theta32, h->h1phi32, h->ovlp, h->N, h->nce, h->G, h->mult,
                                             h->cv_ms, h->cv_ms + CV_NF, h->cv_x);
-  mlp_forward_on(h->cv_mlp, h->cv_x, W, h->cv_f, h->stream, false);
+  const int mlp_launches = mlp_forward_on(h->cv_mlp, h->cv_x, W, h->cv_f, h->stream, false);
   k_cv_select<<<(m + 127) / 128, 128, 0, h->stream>>>(h->cv_idx, W, den, h->seed, tag, h->d_step);
   launch_local_energy_mixed_subset(h, h->cv_idx, m, h->cv_esub);
   k_cv_scale<<<(W + 255) / 256, 256, 0, h->stream>>>(h->cv_f, W, h->cv_ymean, h->cv_ystd);
   k_cv_estimate<<<1, 256, 0, h->stream>>>(h->weights, h->cv_f, h->cv_idx, h->cv_esub, W, m, den,
                                            h->cv_out + 6 * (size_t)slot);
-  h->launches += 8;
+  h->launches += 4 + mlp_launches;  // features, select, scale, estimate and the MLP (the rest count themselves)
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) {
     h->err = std::string("cv_measure: ") + cudaGetErrorString(e);

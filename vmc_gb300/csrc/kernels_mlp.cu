@@ -290,8 +290,8 @@ __global__ void __launch_bounds__(MF_THREADS)
 }
 
 // forward of a device batch X [B][nin] -> Y [B] on stream st; keep: the
-// activations are stored for a backward pass
-void mlp_forward_on(afqmc_mlp* m, const float* X, int B, float* Y, cudaStream_t st, bool keep) {
+// activations are stored for a backward pass.  Returns the kernels launched.
+int mlp_forward_on(afqmc_mlp* m, const float* X, int B, float* Y, cudaStream_t st, bool keep) {
   const int H = m->H, nin = m->nin;
   if (H <= MF_THREADS && mf_smem(nin, H) <= 220 * 1024) {
     static size_t attr = 0;
@@ -304,13 +304,14 @@ void mlp_forward_on(afqmc_mlp* m, const float* X, int B, float* Y, cudaStream_t 
         X, B, nin, H, m->Pb, m->P + m->o_b1(), m->Pb + m->o_W2(), m->P + m->o_b2(), m->Pb + m->o_w3(),
         m->P + m->o_b3(), Y, keep ? m->Z1 : nullptr, keep ? m->H1 : nullptr, keep ? m->Z2 : nullptr,
         keep ? m->H2 : nullptr);
-    return;
+    return 1;
   }
   k_mlp_gemm<__nv_bfloat16, EpiDense><<<g2(B, H), 256, 0, st>>>(
       B, H, nin, X, nin, 1, m->Pb, nin, 1, EpiDense{m->P + m->o_b1(), m->Z1, m->H1, H});
   k_mlp_gemm<__nv_bfloat16, EpiDense><<<g2(B, H), 256, 0, st>>>(
       B, H, H, m->H1, H, 1, m->Pb + m->o_W2(), H, 1, EpiDense{m->P + m->o_b2(), m->Z2, m->H2, H});
   k_mlp_out<<<(B + 7) / 8, 256, 0, st>>>(m->H2, m->Pb + m->o_w3(), m->P + m->o_b3(), Y, B, H);
+  return 3;
 }
 
 void mlp_forward(afqmc_mlp* m, const float* X, int B, float* Y, bool keep) {
