@@ -164,7 +164,7 @@ struct afqmc_handle {
   float4* mf32 = nullptr;   // [G] mean field as double-FP32 (re hi, re lo, im hi, im lo)
   // control variate
   float* cv_x = nullptr;             // [W][67] features
-  float* cv_f = nullptr;             // [W]     predicted local energies
+  float* cv_f = nullptr;             // [W]     network outputs (standard units) of the local energies
   int* cv_idx = nullptr;             // [W]     subsample
   double2* cv_esub = nullptr;        // [W]     exact energies of the subsample
   float* cv_ms = nullptr;            // [2][67] feature mean / std

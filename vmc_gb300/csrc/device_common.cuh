@@ -108,6 +108,17 @@ __device__ __forceinline__ float philox_normal_f(uint64_t seed, uint64_t step, u
   sincospif(2.0f * u2, &s, &c);
   return (g & 1u) ? rad * s : rad * c;
 }
+// both normals of Philox block q: fields (2q, 2q + 1), equal to philox_normal_f of each
+__device__ __forceinline__ float2 philox_normal_pair_f(uint64_t seed, uint64_t step, uint32_t w, uint32_t q) {
+  const U4 r = philox4x32_10(U4{q, w, (uint32_t)step, (uint32_t)(step >> 32)}, (uint32_t)seed, (uint32_t)(seed >> 32));
+  const float two24 = 1.0f / 16777216.0f;
+  const float u1 = ((float)(r.x >> 8) + 0.5f) * two24;
+  const float u2 = ((float)(r.z >> 8) + 0.5f) * two24;
+  const float rad = sqrtf(-2.0f * logf(u1));
+  float s, c;
+  sincospif(2.0f * u2, &s, &c);
+  return make_float2(rad * c, rad * s);
+}
 __device__ __forceinline__ double philox_normal(uint64_t seed, uint64_t step, uint32_t w, uint32_t g) {
   return (double)philox_normal_f(seed, step, w, g);
 }

@@ -135,20 +135,18 @@ __global__ void k_split_theta_gather(const float* __restrict__ theta, const int*
   }
 }
 
-__global__ void k_cv_scale(float* __restrict__ f, int W, float ymean, float ystd) {
-  const int w = blockIdx.x * blockDim.x + threadIdx.x;
-  if (w < W) f[w] = ymean + ystd * f[w];
-}
-
-__global__ void k_cv_estimate(const double* __restrict__ weights, const float* __restrict__ f,
-                              const int* __restrict__ idx, const double2* __restrict__ esub, int W, int m, int den,
-                              double* __restrict__ out) {
+// f: the network's outputs in standard units; the prediction is ymean + ystd f
+// (FP32, as the energies were scaled for training)
+__global__ void k_cv_estimate(const double* __restrict__ weights, const float* __restrict__ fraw, float ymean,
+                              float ystd, const int* __restrict__ idx, const double2* __restrict__ esub, int W, int m,
+                              int den, double* __restrict__ out) {
+  const auto f = [&](int w) { return ymean + ystd * fraw[w]; };
   constexpr int NV = 7;  // sw, swf, corr, ht, nrw, nrwe, nrwf: one reduction for all seven
   __shared__ double s_part[32][NV];
   double v[NV] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
   for (int w = threadIdx.x; w < W; w += blockDim.x) {
     v[0] += weights[w];
-    v[1] += weights[w] * (double)f[w];
+    v[1] += weights[w] * (double)f(w);
   }
   for (int i = threadIdx.x; i < m; i += blockDim.x) {
     const int w = idx[i];
@@ -156,11 +154,11 @@ __global__ void k_cv_estimate(const double* __restrict__ weights, const float* _
     const double wt = weights[w];
     const double e = esub[i].x;
     if (wt != 0.0) {
-      v[2] += inv * wt * (e - (double)f[w]);
+      v[2] += inv * wt * (e - (double)f(w));
       v[3] += inv * wt * e;
       v[4] += wt;
       v[5] += wt * e;
-      v[6] += wt * (double)f[w];
+      v[6] += wt * (double)f(w);
     }
   }
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -282,10 +280,9 @@ int afqmc_cv_measure(afqmc_handle* h, uint64_t tag, int slot) {
   const int mlp_launches = mlp_forward_on(h->cv_mlp, h->cv_x, W, h->cv_f, h->stream, false);
   k_cv_select<<<(m + 127) / 128, 128, 0, h->stream>>>(h->cv_idx, W, den, h->seed, tag, h->d_step);
   launch_local_energy_mixed_subset(h, h->cv_idx, m, h->cv_esub);
-  k_cv_scale<<<(W + 255) / 256, 256, 0, h->stream>>>(h->cv_f, W, h->cv_ymean, h->cv_ystd);
-  k_cv_estimate<<<1, 256, 0, h->stream>>>(h->weights, h->cv_f, h->cv_idx, h->cv_esub, W, m, den,
+  k_cv_estimate<<<1, 256, 0, h->stream>>>(h->weights, h->cv_f, h->cv_ymean, h->cv_ystd, h->cv_idx, h->cv_esub, W, m, den,
                                            h->cv_out + 6 * (size_t)slot);
-  h->launches += 4 + mlp_launches;  // features, select, scale, estimate and the MLP (the rest count themselves)
+  h->launches += 3 + mlp_launches;  // features, select, estimate and the MLP (the rest count themselves)
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) {
     h->err = std::string("cv_measure: ") + cudaGetErrorString(e);

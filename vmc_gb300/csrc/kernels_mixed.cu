@@ -238,35 +238,64 @@ __global__ void k_fields_mixed(const float* __restrict__ fb, const float4* __res
   const float* fbi = fbr + G;
   __nv_bfloat16* xr_out = xB + (size_t)(2 * w) * kv_pad;
   __nv_bfloat16* xi_out = xr_out + kv_pad;
-  for (int g = threadIdx.x; g < G; g += blockDim.x) {
-    df32 xg;
-    if (use_rng) xg = {philox_normal_f(seed, step, (uint32_t)w, (uint32_t)g), 0.f};
-    else xg = df_split_bits(xi[(size_t)w * G + g]);
-    const float4 m = mf32[g];  // (re hi, re lo, im hi, im lo)
-    const float fsr = sdt * (fbi[g] + m.x);
-    const float fsi = -sdt * (fbr[g] - m.z);
-    // x = xg - fs; shift += x mf
-    dot2_acc(shr, cshr, m.x, m.y, xg.h);
-    dot2_acc(shr, cshr, m.x, m.y, xg.l);
-    dot2_acc(shr, cshr, m.x, m.y, -fsr);
-    dot2_acc(shr, cshr, m.z, m.w, fsi);   // - Im x Im mf, Im x = -fsi
-    dot2_acc(shi, cshi, m.z, m.w, xg.h);
-    dot2_acc(shi, cshi, m.z, m.w, xg.l);
-    dot2_acc(shi, cshi, m.z, m.w, -fsr);
-    dot2_acc(shi, cshi, m.x, m.y, -fsi);  // Im x Re mf
-    // fbTerm += xg fs - fs^2 / 2
-    dot2_acc(ftr, cftr, xg.h, xg.l, fsr);
-    dot2_acc(ftr, cftr, -0.5f * fsr, 0.f, fsr);
-    dot2_acc(ftr, cftr, 0.5f * fsi, 0.f, fsi);
-    dot2_acc(fti, cfti, xg.h, xg.l, fsi);
-    dot2_acc(fti, cfti, -fsr, 0.f, fsi);
-    float xr = (xg.h - fsr) + xg.l, xim = -fsi;
-    if (!live) { xr = 0.f; xim = 0.f; }
-    __nv_bfloat16 hi, lo;  // split of the FP32 value (the VHS contraction is split-BF16)
-    split_bf16(xr, hi, lo);
-    xr_out[g] = hi; xr_out[G + g] = lo; xr_out[2 * G + g] = hi;
-    split_bf16(xim, hi, lo);
-    xi_out[g] = hi; xi_out[G + g] = lo; xi_out[2 * G + g] = hi;
+  // each thread takes pairs of fields (2q, 2q + 1): one Philox block and one
+  // Box-Muller transform give both normals, and the BF16 pairs store as one word
+  for (int g0 = 2 * threadIdx.x; g0 < G; g0 += 2 * blockDim.x) {
+    df32 xs[2];
+    if (use_rng) {
+      const float2 z = philox_normal_pair_f(seed, step, (uint32_t)w, (uint32_t)(g0 >> 1));
+      xs[0] = {z.x, 0.f};
+      xs[1] = {z.y, 0.f};
+    } else {
+      xs[0] = df_split_bits(xi[(size_t)w * G + g0]);
+      xs[1] = g0 + 1 < G ? df_split_bits(xi[(size_t)w * G + g0 + 1]) : df32{0.f, 0.f};
+    }
+    __nv_bfloat16 rh[2], rl[2], ih[2], il[2];
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+      const int g = g0 + u;
+      if (g >= G) {
+        rh[u] = rl[u] = ih[u] = il[u] = __float2bfloat16_rn(0.f);
+        continue;
+      }
+      const df32 xg = xs[u];
+      const float4 m = mf32[g];  // (re hi, re lo, im hi, im lo)
+      const float fsr = sdt * (fbi[g] + m.x);
+      const float fsi = -sdt * (fbr[g] - m.z);
+      // x = xg - fs; shift += x mf
+      dot2_acc(shr, cshr, m.x, m.y, xg.h);
+      dot2_acc(shr, cshr, m.x, m.y, xg.l);
+      dot2_acc(shr, cshr, m.x, m.y, -fsr);
+      dot2_acc(shr, cshr, m.z, m.w, fsi);   // - Im x Im mf, Im x = -fsi
+      dot2_acc(shi, cshi, m.z, m.w, xg.h);
+      dot2_acc(shi, cshi, m.z, m.w, xg.l);
+      dot2_acc(shi, cshi, m.z, m.w, -fsr);
+      dot2_acc(shi, cshi, m.x, m.y, -fsi);  // Im x Re mf
+      // fbTerm += xg fs - fs^2 / 2
+      dot2_acc(ftr, cftr, xg.h, xg.l, fsr);
+      dot2_acc(ftr, cftr, -0.5f * fsr, 0.f, fsr);
+      dot2_acc(ftr, cftr, 0.5f * fsi, 0.f, fsi);
+      dot2_acc(fti, cfti, xg.h, xg.l, fsi);
+      dot2_acc(fti, cfti, -fsr, 0.f, fsi);
+      float xr = (xg.h - fsr) + xg.l, xim = -fsi;
+      if (!live) { xr = 0.f; xim = 0.f; }
+      split_bf16(xr, rh[u], rl[u]);  // split of the FP32 value (the VHS contraction is split-BF16)
+      split_bf16(xim, ih[u], il[u]);
+    }
+    if (g0 + 1 < G && ((G | kv_pad) & 1) == 0) {  // both fields: 32-bit stores (g0 even, rows even)
+      *(__nv_bfloat162*)(xr_out + g0) = __halves2bfloat162(rh[0], rh[1]);
+      *(__nv_bfloat162*)(xr_out + G + g0) = __halves2bfloat162(rl[0], rl[1]);
+      *(__nv_bfloat162*)(xr_out + 2 * G + g0) = __halves2bfloat162(rh[0], rh[1]);
+      *(__nv_bfloat162*)(xi_out + g0) = __halves2bfloat162(ih[0], ih[1]);
+      *(__nv_bfloat162*)(xi_out + G + g0) = __halves2bfloat162(il[0], il[1]);
+      *(__nv_bfloat162*)(xi_out + 2 * G + g0) = __halves2bfloat162(ih[0], ih[1]);
+    } else {
+      for (int u = 0; u < 2 && g0 + u < G; ++u) {
+        const int g = g0 + u;
+        xr_out[g] = rh[u]; xr_out[G + g] = rl[u]; xr_out[2 * G + g] = rh[u];
+        xi_out[g] = ih[u]; xi_out[G + g] = il[u]; xi_out[2 * G + g] = ih[u];
+      }
+    }
   }
   const double sr = block_sum((double)shr + (double)cshr);
   const double si = block_sum((double)shi + (double)cshi);
