@@ -167,126 +167,12 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
   for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 
-template <int BN, int STAGES>
-struct GemmSmem {
-  static constexpr int A_BYTES = BM * BK * 2;
-  static constexpr int B_BYTES = BN * BK * 2;
-  static constexpr int STAGE_BYTES = A_BYTES + B_BYTES;
-  static constexpr int BAR_OFF = STAGES * STAGE_BYTES;
-  static constexpr int TOTAL = BAR_OFF + (2 * STAGES + 1) * 8 + 16 + 1024;  // + alignment slack
-};
-
-// Generic tensor-core GEMM; grid (n tiles, m tiles), 128 threads, dynamic smem
-// GemmSmem<BN, STAGES>::TOTAL.  K must be a multiple of BK (operands are
-// zero-padded); rows beyond M / N read as zeros (TMA out-of-bounds fill) and
-// the epilogue is called only for m < M, n < N.
-template <int BN, int STAGES, class Epi>
-__global__ void __launch_bounds__(128, 1)
-    k_tc_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, int M, int N,
-              int K, Epi epi, int* err) {
-  using L = GemmSmem<BN, STAGES>;
-  extern __shared__ uint8_t smem_raw[];
-  uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-  uint64_t* full = (uint64_t*)(smem + L::BAR_OFF);
-  uint64_t* empty = full + STAGES;
-  uint64_t* accum = empty + STAGES;
-  uint32_t* tmem_holder = (uint32_t*)(accum + 1);
-  __shared__ int s_abort;
-
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int n0 = blockIdx.x * BN, m0 = blockIdx.y * BM;
-  const int nk = K / BK;
-
-  if (threadIdx.x == 0) {
-    s_abort = 0;
-    for (int s = 0; s < STAGES; ++s) {
-      mbar_init(&full[s], 1);
-      mbar_init(&empty[s], 1);
-    }
-    mbar_init(accum, 1);
-    fence_mbar_init();
-    prefetch_tmap(&tmA);
-    prefetch_tmap(&tmB);
-  }
-  if (warp == 0) tmem_alloc(tmem_holder, BN);
-  tc_fence_before();
-  __syncthreads();
-  tc_fence_after();
-  const uint32_t tmem = *tmem_holder;
-
-  int issued = 0;  // producer: stages loaded (for the bounded drain on abort)
-  if (warp == 0 && lane == 0) {
-    for (int kb = 0; kb < nk; ++kb) {
-      const int s = kb % STAGES;
-      if (kb >= STAGES && !mbar_wait(&empty[s], ((kb / STAGES) - 1) & 1, err, 1)) {
-        s_abort = 1;
-        break;
-      }
-      if (s_abort) break;
-      uint8_t* a = smem + s * L::STAGE_BYTES;
-      uint8_t* b = a + L::A_BYTES;
-      mbar_expect_tx(&full[s], L::STAGE_BYTES);
-      tma_load_2d(a, &tmA, &full[s], kb * BK, m0);
-      tma_load_2d(b, &tmB, &full[s], kb * BK, n0);
-      issued = kb + 1;
-    }
-  } else if (warp == 1 && lane == 0) {
-    constexpr uint32_t idesc = idesc_bf16(BM, BN);
-    bool ok = true;
-    for (int kb = 0; kb < nk && ok; ++kb) {
-      const int s = kb % STAGES;
-      if (!mbar_wait(&full[s], (kb / STAGES) & 1, err, 2)) {
-        s_abort = 1;
-        ok = false;
-        break;
-      }
-      if (s_abort) { ok = false; break; }
-      tc_fence_after();
-      const uint32_t a = smem_u32(smem + s * L::STAGE_BYTES);
-      const uint32_t b = a + L::A_BYTES;
-#pragma unroll
-      for (int k = 0; k < BK / 16; ++k)  // +32 bytes per K=16 step inside the swizzle row
-        mma_bf16(tmem, sdesc_sw128(a + 32 * k), sdesc_sw128(b + 32 * k), idesc, (kb > 0 || k > 0) ? 1u : 0u);
-      mma_commit(&empty[s]);
-    }
-    mma_commit(accum);
-  }
-  __syncwarp();
-  // epilogue: all four warps
-  const bool have = mbar_wait(accum, 0, err, 3);
-  tc_fence_after();
-  if (have && !s_abort) {
-    const int row = m0 + warp * 32 + lane;
-#pragma unroll 1
-    for (int c = 0; c < BN; c += 16) {
-      float v[16];
-      tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c, v);
-      if (row < M) {
-#pragma unroll
-        for (int j = 0; j < 16; ++j) {
-          const int n = n0 + c + j;
-          if (n < N) epi(row, n, v[j]);
-        }
-      }
-    }
-  }
-  // on abort: let the loads already issued land before the CTA releases its smem
-  if (s_abort && warp == 0 && lane == 0) {
-    for (int kb = (issued > STAGES ? issued - STAGES : 0); kb < issued; ++kb)
-      mbar_wait(&full[kb % STAGES], (kb / STAGES) & 1, err, 4);
-  }
-  tc_fence_before();
-  __syncthreads();
-  if (warp == 0) {
-    tc_fence_after();
-    tmem_dealloc(tmem, BN);
-  }
-}
-
-
-// Persistent, warp-specialised form of k_tc_gemm: one CTA per SM strides over
-// the output tiles (m-tiles fastest, so the CTAs running together share the
-// per-step B tile in L2).  Warp 0 lane 0 streams the K blocks of every tile
+// Tensor-core GEMM C[m][n] = sum_k A[m][k] B[n][k] (both operands K-major
+// BF16, K a multiple of BK, zero-padded; rows beyond M / N read as zeros by
+// the TMA bounds fill; the epilogue functor is called for m < M, n < N), in
+// persistent, warp-specialised form: one CTA per SM strides over the output
+// tiles (m-tiles fastest, so the CTAs running together share the per-step B
+// tile in L2).  Warp 0 lane 0 streams the K blocks of every tile
 // through the STAGES ring by TMA, warp 1 lane 0 issues the MMAs into one of two
 // TMEM accumulators (2 BN columns), and warps 2-5 (one TMEM lane quadrant
 // each) run the epilogue of tile i while the MMAs of tile i + 1 proceed; the
