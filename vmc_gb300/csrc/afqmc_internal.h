@@ -130,7 +130,6 @@ struct afqmc_handle {
   afqmc::PropChunk* d_chunks32 = nullptr;
   int nchunks32 = 0;
   CUtensorMap tm_rot, tm_LT[2];
-  CUtensorMap tm_rot_fb;  // rot's split operand as the B operand of the force bias (160-row boxes)
   CUtensorMap tm_theta_bn[3], tm_x_bn[3];  // B operands with box heights 64, 128, 256
   // autotuned choices (afqmc_autotune): GEMM N-tiles; propagator 0 auto / 1 SMEM / 2 chunked / 3 tcgen05;
   // overlap 0 auto / 1 warp per matrix / 2 block per matrix

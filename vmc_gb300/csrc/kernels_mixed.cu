@@ -128,17 +128,13 @@ void split_rows(afqmc_handle* h, const float* src, long lds, int rows, int K, in
 // ---------------------------------------------------------------------------
 // GEMM epilogues
 // ---------------------------------------------------------------------------
-
-// Force bias with the operands swapped: rows (walker, plane) (A = theta's split
-// operand), columns g (B = rot's): the walker rows give the GEMM many M tiles,
-// and an N tile of 160 covers G in few tiles, so more SMs share the long K.
-struct EpiFBT {
+// force bias: rows g, columns (walker, plane): fb32[(w, plane)][g] = mult * v
+struct EpiFB {
   float* fb;
   int G;
   float mult;
-  __device__ __forceinline__ void operator()(int m, int n, float v) const { fb[(size_t)m * G + n] = mult * v; }
+  __device__ __forceinline__ void operator()(int m, int n, float v) const { fb[(size_t)n * G + m] = mult * v; }
 };
-constexpr int FB_BN = 160;
 
 // VHS: rows t (packed index), columns (walker, plane) with plane 0 = L.Re(x),
 // plane 1 = L.Im(x); V = sqrt(dt)(i L.Re(x) - L.Im(x)) kept packed (lower
@@ -193,8 +189,8 @@ void launch_theta_split(afqmc_handle* h) {
 void launch_force_bias_mixed(afqmc_handle* h) {
   if (h->fb_current) return;  // already computed from this theta (control-variate features)
   if (!h->thetaB_from_lu) launch_theta_split(h);
-  launch_tc_bn<FB_BN>(h, h->tm_theta_bn[1], h->tm_rot_fb, 2 * h->nwalk, h->G, h->kf_pad,
-                      EpiFBT{h->fb32, h->G, (float)h->mult});
+  EpiFB epi{h->fb32, h->G, (float)h->mult};
+  launch_tc(h, h->tm_rot, h->tm_theta_bn, h->tune_bn_fb, h->G, 2 * h->nwalk, h->kf_pad, epi);
   h->fb_current = true;
 }
 
@@ -602,8 +598,7 @@ bool setup_mixed(afqmc_handle* h) {
   // the force bias's theta operand: its padding columns stay zero when the LU writes it
   cudaMemsetAsync(h->thetaB, 0, (size_t)h->nwalk * 2 * h->kf_pad * sizeof(__nv_bfloat16), h->stream);
   k_to_df32<<<(h->nce * h->N + 255) / 256, 256, 0, h->stream>>>(h->h1phi, h->h1phi32, h->nce * h->N);
-  bool ok = setup_prop_tc(h) && setup_ovl_tc(h) && make_tmap_bf16(&h->tm_rot, h->rotA, h->G, h->kf_pad, tc::BM) &&
-            make_tmap_bf16(&h->tm_rot_fb, h->rotA, h->G, h->kf_pad, FB_BN);
+  bool ok = setup_prop_tc(h) && setup_ovl_tc(h) && make_tmap_bf16(&h->tm_rot, h->rotA, h->G, h->kf_pad, tc::BM);
   const int bns[3] = {64, 128, 256};
   for (int i = 0; i < 3 && ok; ++i)
     ok = make_tmap_bf16(&h->tm_theta_bn[i], h->thetaB, 2 * h->nwalk, h->kf_pad, bns[i]) &&
@@ -627,9 +622,8 @@ bool setup_mixed(afqmc_handle* h) {
 namespace afqmc {
 // single GEMMs for the autotuner (operands must be current)
 void launch_fb_gemm(afqmc_handle* h, int bn) {
-  (void)bn;  // one shape since the operands were swapped (walker rows, N tile 160)
-  launch_tc_bn<FB_BN>(h, h->tm_theta_bn[1], h->tm_rot_fb, 2 * h->nwalk, h->G, h->kf_pad,
-                      EpiFBT{h->fb32, h->G, (float)h->mult});
+  EpiFB epi{h->fb32, h->G, (float)h->mult};
+  launch_tc(h, h->tm_rot, h->tm_theta_bn, bn, h->G, 2 * h->nwalk, h->kf_pad, epi);
 }
 void launch_vhs_gemm(afqmc_handle* h, int bn) {
   for (int s = 0; s < h->nspV; ++s) {

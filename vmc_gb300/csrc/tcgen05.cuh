@@ -188,12 +188,6 @@ struct GemmPSmem {
   static constexpr int TOTAL = BAR_OFF + (2 * STAGES + 4) * 8 + 16 + 1024;  // + alignment slack
 };
 constexpr int GP_THREADS = 192;
-// TMEM columns of the two accumulators: 2 BN rounded up to a power of two (>= 32)
-__host__ __device__ constexpr int gp_tmem_cols(int bn) {
-  int c = 32;
-  while (c < 2 * bn) c *= 2;
-  return c;
-}
 
 template <int BN, int STAGES, class Epi>
 __global__ void __launch_bounds__(GP_THREADS, 1)
@@ -227,7 +221,7 @@ __global__ void __launch_bounds__(GP_THREADS, 1)
     prefetch_tmap(&tmA);
     prefetch_tmap(&tmB);
   }
-  if (warp == 0) tmem_alloc(tmem_holder, gp_tmem_cols(BN));
+  if (warp == 0) tmem_alloc(tmem_holder, 2 * BN);
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
@@ -319,7 +313,7 @@ __global__ void __launch_bounds__(GP_THREADS, 1)
   __syncthreads();
   if (warp == 0) {
     tc_fence_after();
-    tmem_dealloc(tmem, gp_tmem_cols(BN));
+    tmem_dealloc(tmem, 2 * BN);
   }
 }
 
