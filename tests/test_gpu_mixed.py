@@ -4,7 +4,8 @@ propagator, FP64 overlap/QR/weights) against the FP64 oracle.
 Tolerances are stated per result: force bias 2e-5 relative (split BF16 keeps
 ~16 significant bits per product, FP32 accumulation), one-step walker dets
 2e-6, and the mixed-estimator energy after 100 steps with identical fields
-within 0.1 mEh of the FP64 oracle.
+within 0.1 mEh of the FP64 oracle; the same one-step and local-energy bounds
+for a system with more than 32 occupied orbitals per spin.
 """
 import numpy as np
 import pytest
@@ -131,3 +132,43 @@ def test_energy_error_vs_fp64_oracle(A):
     e_g = (w * el_g).sum() / w.sum()
     e_o = (ow.weights * el_o).sum() / ow.weights.sum()
     assert abs(e_g - e_o) < 1e-4, (e_g, e_o)
+
+
+def test_mixed_many_occupied_orbitals(A):
+    """More than 32 occupied orbitals per spin (N = 96, 40 alpha and 38 beta):
+    overlap and theta by the block Gauss-Jordan kernel, the tensor-core
+    propagator in two column passes per walker, the exchange with its wide
+    walker chunks, Cholesky-QR.  One step with identical fields against the
+    FP64 oracle, with bounds that follow the size: dets 4e-6 per element (N =
+    96 terms per product in FP32; 1.9e-6 measured); weights 5e-7 per occupied
+    orbital (a weight is a ratio of determinants over all 78 columns, each
+    carrying the ~1e-6 of the FP32 propagation: 2.0e-5 measured); every
+    walker's E_L within 2e-6 of |E_L| (|E_L| ~ 310 Eh here; 6.9e-7 measured).
+    After the QR the stored overlaps are the oracle's overlaps of the stored
+    dets to 1e-10 (8e-14 measured)."""
+    s = S.make_system(96, 40, 200, 4747, "uhf")
+    na, nb, rw = 40, 38, False
+    oh = O.Hamiltonian(96, na, nb, s["ecore"], s["h1"], s["h1mod"], s["chol"])
+    ot = O.Trial(oh, s["trial"], s["phi_a"][:, :na], s["phi_b"][:, :nb])
+    W = 24
+    wk = gpu(A, oh, ot, rw, W, "mixed")
+    A.set_tuning(wk, prop="tensor")
+    dets = start_dets(oh, ot, rw, W, 6)
+    wk.set_det(dets)
+    ow = O.Walkers(oh, rw, dets)
+    ow.overlaps = O.overlap(ot, ow)
+    prop = O.Propagator(oh, ot.phi, 0.005, mode="fp64")
+    xi = np.random.default_rng(7).standard_normal((W, oh.nchol))
+    e0 = O.hf_energy(ot, oh, ot.phi, rw).real
+    wk.propagate_phaseless(xi, e0)
+    O.step(ot, oh, prop, ow, xi, e0, 1e9)
+    d, o, w = wk.get_det()
+    el = wk.ham_and_overlap()
+    ref = O.local_energy(ot, O.Walkers(oh, rw, d), oh)
+    wk.orthogonalize()
+    dq, oq, _ = wk.get_det()
+    refq = O.overlap(ot, O.Walkers(oh, rw, dq))
+    assert rel(d, ow.dets) < 4e-6
+    assert rel(w, ow.weights) < 5e-7 * (na + nb)
+    assert np.abs(el - ref).max() < 2e-6 * np.abs(ref).max(), np.abs(el - ref).max()
+    assert np.abs(oq / refq - 1).max() < 1e-10
