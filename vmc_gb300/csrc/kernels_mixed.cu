@@ -297,13 +297,36 @@ __global__ void k_fields_mixed(const float* __restrict__ fb, const float4* __res
       }
     }
   }
-  const double sr = block_sum((double)shr + (double)cshr);
-  const double si = block_sum((double)shi + (double)cshi);
-  const double tr = block_sum((double)ftr + (double)cftr);
-  const double ti = block_sum((double)fti + (double)cfti);
-  if (threadIdx.x == 0) {
-    shift[w] = make_double2(sr, si);
-    fbterm[w] = make_double2(tr, ti);
+  // the four compensated sums, reduced over the block as double-FP32 pairs
+  // (FP32 pipe) and converted to FP64 once: an FP64 block reduction per walker
+  // kept this kernel's FP64 pipe 73% busy
+  __shared__ float2 s_part[32][4];
+  const auto pair = [](float a, float b) {  // a + b as a normalised pair, exactly (TwoSum)
+    df32 r;
+    df_two_sum(a, b, r.h, r.l);
+    return r;
+  };
+  df32 v[4] = {pair(shr, cshr), pair(shi, cshi), pair(ftr, cftr), pair(fti, cfti)};
+  const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    for (int o = 16; o > 0; o >>= 1)
+      v[j] = df_add(v[j], {__shfl_down_sync(0xffffffffu, v[j].h, o), __shfl_down_sync(0xffffffffu, v[j].l, o)});
+    if (lane == 0) s_part[wp][j] = make_float2(v[j].h, v[j].l);
+  }
+  __syncthreads();
+  if (wp == 0) {
+    const int nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      v[j] = lane < nw ? df32{s_part[lane][j].x, s_part[lane][j].y} : df32{0.f, 0.f};
+      for (int o = 16; o > 0; o >>= 1)
+        v[j] = df_add(v[j], {__shfl_down_sync(0xffffffffu, v[j].h, o), __shfl_down_sync(0xffffffffu, v[j].l, o)});
+    }
+    if (lane == 0) {
+      shift[w] = make_double2(df_to_double(v[0]), df_to_double(v[1]));
+      fbterm[w] = make_double2(df_to_double(v[2]), df_to_double(v[3]));
+    }
   }
 }
 
