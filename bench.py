@@ -108,7 +108,7 @@ def mixed_stage_pipes(N, na, nb, G):
 
 
 def flops_model(N, na, nb, G, ortho_every=ORTHO_EVERY):
-    """Algorithmic FLOPs per walker (SURVEY 8d): force bias, VHS, propagator with
+    """Algorithmic FLOPs per walker: force bias, VHS, propagator with
     a real exp(-dt/2 h1') (2 real x complex + 5 complex x complex products per
     spin), overlap, QR amortised, and one exact local energy."""
     T = N * (N + 1) // 2
