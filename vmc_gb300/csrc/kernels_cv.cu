@@ -39,24 +39,23 @@ int mlp_n_in(const afqmc_mlp* m);
 // Features of the mixed form, all in FP32 (they feed a BF16 network): the
 // force bias, the one-body term theta . h1Phi against an FP32 copy of h1Phi,
 // log|overlap| and arg(overlap) after scaling the overlap by a power of two.
-// One warp per walker (CV_FWALK walkers per CTA): the sums are warp sums, no
-// block barrier.
-constexpr int CV_FWALK = 4;
-__global__ void __launch_bounds__(32 * CV_FWALK)
-    k_cv_features32(const float* __restrict__ fb32, const float* __restrict__ theta,
-                    const float2* __restrict__ h1phi32, const double2* __restrict__ ovlp, int W, int N, int nce,
-                    int G, int mult, const float* __restrict__ mean, const float* __restrict__ stdv,
-                    float* __restrict__ out) {
-  const int lane = threadIdx.x & 31;
-  const int w = blockIdx.x * CV_FWALK + (threadIdx.x >> 5);
-  if (w >= W) return;
+// One CTA of 128 threads per walker.
+__global__ void k_cv_features32(const float* __restrict__ fb32, const float* __restrict__ theta,
+                                const float2* __restrict__ h1phi32, const double2* __restrict__ ovlp, int N, int nce,
+                                int G, int mult, const float* __restrict__ mean, const float* __restrict__ stdv,
+                                float* __restrict__ out) {
+  __shared__ float s_part[4];
+  const int w = blockIdx.x;
   float* o = out + (size_t)w * CV_NF;
-  for (int g = lane; g < 64; g += 32) o[g] = g < G ? fb32[(size_t)(2 * w) * G + g] : 0.f;
+  for (int g = threadIdx.x; g < 64; g += blockDim.x) o[g] = g < G ? fb32[(size_t)(2 * w) * G + g] : 0.f;
   const float* tre = theta + (size_t)(2 * w) * nce * N;
   float e1 = 0.f;
-  for (int k = lane; k < nce * N; k += 32) e1 = fmaf(tre[k], h1phi32[k].x, e1);
+  for (int k = threadIdx.x; k < nce * N; k += blockDim.x) e1 = fmaf(tre[k], h1phi32[k].x, e1);
   e1 = warp_sumf(e1);
-  if (lane == 0) {
+  if ((threadIdx.x & 31) == 0) s_part[threadIdx.x >> 5] = e1;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    e1 = (s_part[0] + s_part[1]) + (s_part[2] + s_part[3]);
     const double2 ov = ovlp[w];
     // |ov| = 2^k |ov 2^-k| with the larger part of ov 2^-k in [1, 2)
     const double m = fmax(fabs(ov.x), fabs(ov.y));
@@ -67,9 +66,9 @@ __global__ void __launch_bounds__(32 * CV_FWALK)
     o[65] = 0.5f * logf(x * x + y * y) + (float)k * 0.69314718f;
     o[66] = atan2f(y, x);
   }
-  __syncwarp();
+  __syncthreads();
   if (mean)
-    for (int f = lane; f < CV_NF; f += 32) o[f] = (o[f] - mean[f]) / stdv[f];
+    for (int f = threadIdx.x; f < CV_NF; f += blockDim.x) o[f] = (o[f] - mean[f]) / stdv[f];
 }
 
 template <class T>
@@ -210,8 +209,8 @@ int afqmc_cv_features(afqmc_handle* h, float* out) {
   if (h->precision == AFQMC_PREC_MIXED) launch_force_bias_mixed(h);
   else launch_force_bias(h);
   if (h->precision == AFQMC_PREC_MIXED)
-    k_cv_features32<<<(h->nwalk + CV_FWALK - 1) / CV_FWALK, 32 * CV_FWALK, 0, h->stream>>>(
-        h->fb32, h->theta32, h->h1phi32, h->ovlp, h->nwalk, h->N, h->nce, h->G, h->mult, nullptr, nullptr, h->cv_x);
+    k_cv_features32<<<h->nwalk, 128, 0, h->stream>>>(h->fb32, h->theta32, h->h1phi32, h->ovlp, h->N, h->nce, h->G,
+                                                     h->mult, nullptr, nullptr, h->cv_x);
   else
     k_cv_features<double><<<h->nwalk, 128, 0, h->stream>>>(nullptr, h->fb, h->theta, h->h1phi, h->ovlp, h->N, h->nce,
                                                            h->G, h->mult, nullptr, nullptr, h->cv_x);
@@ -276,8 +275,8 @@ int afqmc_cv_measure(afqmc_handle* h, uint64_t tag, int slot) {
   cudaSetDevice(h->device);
   const int W = h->nwalk, den = h->cv_den, m = (W + den - 1) / den;
   launch_force_bias_mixed(h);
-  k_cv_features32<<<(W + CV_FWALK - 1) / CV_FWALK, 32 * CV_FWALK, 0, h->stream>>>(
-      h->fb32, h->theta32, h->h1phi32, h->ovlp, W, h->N, h->nce, h->G, h->mult, h->cv_ms, h->cv_ms + CV_NF, h->cv_x);
+  k_cv_features32<<<W, 128, 0, h->stream>>>(h->fb32, h->theta32, h->h1phi32, h->ovlp, h->N, h->nce, h->G, h->mult,
+                                            h->cv_ms, h->cv_ms + CV_NF, h->cv_x);
   const int mlp_launches = mlp_forward_on(h->cv_mlp, h->cv_x, W, h->cv_f, h->stream, false);
   k_cv_select<<<(m + 127) / 128, 128, 0, h->stream>>>(h->cv_idx, W, den, h->seed, tag, h->d_step);
   launch_local_energy_mixed_subset(h, h->cv_idx, m, h->cv_esub);
