@@ -165,6 +165,14 @@ int afqmc_launch_count(const afqmc_handle* h, long* count);
 int afqmc_timer_start(afqmc_handle* h);
 int afqmc_timer_stop(afqmc_handle* h, double* ms);
 
+/* Failure-detection check: runs, on the handle's stream, one bounded device
+ * wait of the kind the tensor-core pipelines use (an mbarrier wait that gives
+ * up after ~2 s, records a code and returns instead of hanging) on a barrier
+ * that nothing arrives at.  Returns AFQMC_ERR_TIMEOUT once that wait has run
+ * out, with the handle still usable; no copy or tensor memory is involved.
+ * No counterpart in the reference (its CPU path has no device waits). */
+int afqmc_check_wait_timeout(afqmc_handle* h);
+
 /* Synchronise the handle's stream. */
 int afqmc_sync(afqmc_handle* h);
 
@@ -309,10 +317,11 @@ const char* afqmc_graph_last_error(void);
 
 /* ---- allocation-free orthonormalisation ----
  * No counterpart in the reference.  For callers that cannot allocate GPU
- * memory when they call it: code running under CUDA stream capture (where
- * cudaMalloc is not allowed), hosts whose device memory belongs to another
- * allocator, latency-bound loops that must not touch the allocator.  Same
- * Householder QR as afqmc_orthonormalize, on caller-owned device buffers:
+ * memory when they call it: hosts whose device memory belongs to another
+ * allocator (a framework's caching pool, a service that budgets the whole GPU
+ * up front), and latency-bound loops that must stay out of the allocator,
+ * whose cudaMalloc / cudaFree synchronise the device.  Same Householder QR as
+ * afqmc_orthonormalize, on caller-owned device buffers:
  *   dets:     device, [nwalk][ncols][norb] complex double, column-major per walker
  *             (ncols = nalpha for rhf_walker, else nalpha + nbeta, alpha first); in/out
  *   overlaps: device, [nwalk] complex double; divided by prod diag(R) (squared
@@ -322,9 +331,12 @@ const char* afqmc_graph_last_error(void);
  * every GPU loading the library keeps until exit; walkers go through it in
  * batches, and one walker's det (norb x ncols) must fit, else AFQMC_ERR_ARG.
  * The first call on a device looks up the array's address (with that device
- * current) and must come before any stream capture.  All calls share the array:
- * calls that overlap on the GPU race and must be serialised by the caller.
- * Nothing is allocated (no cudaMalloc / cudaFree).  On failure the message is
+ * current) and should come before any stream capture; after cudaDeviceReset
+ * that address is stale, so do not call this again on a reset device.  All
+ * calls share the array: calls that overlap on the GPU race and must be
+ * serialised by the caller.  Nothing is allocated (no cudaMalloc / cudaFree).
+ * A CUDA error already pending when it is called is returned as
+ * AFQMC_ERR_CUDA with a message saying so.  On failure the message is
  * afqmc_last_error(NULL). */
 int afqmc_orthonormalize_noalloc(void* dets, void* overlaps, int nwalk, int norb, int nalpha, int nbeta,
                                  int rhf_walker, void* stream);

@@ -8,6 +8,7 @@ energy of each 50-step block of a 4-rank run, checked by the reference's
 tests/testEnergy.py:108-121), and writes ``tests/golden/ref_<name>.npz``.
 
 Usage: python tests/golden/make_reference_fixtures.py [REFERENCE_ROOT]
+(default: $VMC_REFERENCE_ROOT, else /root/reference)
 """
 import json
 import os
@@ -43,6 +44,6 @@ def convert(ref_root, name):
 
 
 if __name__ == "__main__":
-    root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("VMC_REFERENCE_ROOT", "/root/reference")
     for n in FIXTURES:
         print(convert(root, n))

@@ -1,0 +1,182 @@
+"""GPU parity at the benchmark workloads' own shapes, against the FP64 oracle.
+
+Shapes:
+  * N=120, nalpha=nbeta=20, nchol=600 (the timed workload), UHF trial and walkers;
+  * N=160, nalpha=nbeta=36, nchol=480: more than 128 orbitals and more than 32
+    occupied orbitals per spin (column-chunked propagators, the block
+    Gauss-Jordan overlap kernel);
+  * N=200, nalpha=nbeta=30, nchol=1000 (the control-variate workload's system).
+
+Each case starts a small walker batch from perturbed trial determinants, runs
+the steps with identical host fields on the GPU and in the oracle (QR every 5
+steps), and compares walker dets, overlaps and weights after the last step and
+every walker's local energy.  FP64 form: <= 1e-10 relative (the FP64 parity
+bar).  Mixed form, per result (the FP32 propagation carries ~1e-6 relative per
+step into every column; a weight is a ratio of determinants over all 2n
+columns): dets <= 2e-5 relative, weights <= 5e-7 x 2n per step, each walker's
+E_L within 2e-6 of max |E_L|, and the weighted mixed energy within 0.1 mEh.
+"""
+import numpy as np
+import pytest
+
+from oracle import afqmc_oracle as O
+from vmc_gb300 import synthetic as S
+
+pytestmark = pytest.mark.gpu
+
+_SYS = {}
+
+
+def system(name):
+    if name not in _SYS:
+        if name == "n120":
+            s = S.workload("cfg2")
+        elif name == "n160":
+            s = S.make_system(160, 36, 480, 20261203 + 160, "uhf")
+        elif name == "n200":
+            s = S.workload("cfg4")
+        else:
+            raise ValueError(name)
+        N, n = s["norb"], s["nalpha"]
+        oh = O.Hamiltonian(N, n, n, s["ecore"], s["h1"], s["h1mod"], s["chol"])
+        ot = O.Trial(oh, s["trial"], s["phi_a"], s["phi_b"])
+        _SYS[name] = (oh, ot)
+    return _SYS[name]
+
+
+@pytest.fixture(scope="module")
+def A():
+    from vmc_gb300 import afqmc
+    afqmc.lib()
+    return afqmc
+
+
+def rel(a, b):
+    return float(np.abs(np.asarray(a) - np.asarray(b)).max() / np.abs(np.asarray(b)).max())
+
+
+_ORACLE = {}
+
+
+def oracle_run(name, W, steps, seed):
+    """Oracle walkers after `steps` FP64 steps (QR every 5), the fields used and
+    the oracle's local energies; cached per case so several GPU variants share it."""
+    key = (name, W, steps, seed)
+    if key in _ORACLE:
+        return _ORACLE[key]
+    oh, ot = system(name)
+    rng = np.random.default_rng(seed)
+    base = O._ref_dets(oh, ot.phi, False)
+    dets0 = base[None] + 0.05 * (rng.standard_normal((W,) + base.shape) + 1j * rng.standard_normal((W,) + base.shape))
+    xs = [rng.standard_normal((W, oh.nchol)) for _ in range(steps)]
+    e0 = O.hf_energy(ot, oh, ot.phi, False).real
+    ow = O.Walkers(oh, False, dets0.copy())
+    ow.overlaps = O.overlap(ot, ow)
+    prop = O.Propagator(oh, ot.phi, 0.005, mode="fp64")
+    for k in range(steps):
+        O.step(ot, oh, prop, ow, xs[k], e0, 1e9)
+        if (k + 1) % 5 == 0:
+            O.orthogonalize(ow)
+    el = O.local_energy(ot, ow, oh)
+    _ORACLE[key] = (dets0, xs, e0, ow, el)
+    return _ORACLE[key]
+
+
+def gpu_run(A, name, W, steps, seed, precision, tuning=None):
+    oh, ot = system(name)
+    dets0, xs, e0, ow, el = oracle_run(name, W, steps, seed)
+    gh = A.Hamiltonian(oh.norb, oh.nalpha, oh.nbeta, oh.ecore, oh.h1, oh.h1mod, oh.chol)
+    gt = A.UHF(gh, ot.phi[0], ot.phi[1])
+    wk = A.DQMCWalkers(gh, gt, W, False, 0.005, precision=precision)
+    if tuning:
+        A.set_tuning(wk, **tuning)
+    wk.set_det(dets0)
+    for k in range(steps):
+        wk.propagate_phaseless(xs[k], e0)
+        if (k + 1) % 5 == 0:
+            wk.orthogonalize()
+    d, o, w = wk.get_det()
+    g_el = wk.ham_and_overlap()
+    wk.close()
+    return (d, o, w, g_el), (ow, el)
+
+
+def check_fp64(got, ref):
+    (d, o, w, g_el), (ow, el) = got, ref
+    errs = dict(dets=rel(d, ow.dets), ovl=rel(o, ow.overlaps), w=rel(w, ow.weights), el=rel(g_el, el))
+    assert max(errs.values()) < 1e-10, errs
+    return errs
+
+
+def check_mixed(got, ref, n_occ, steps, qr_signs):
+    (d, o, w, g_el), (ow, el) = got, ref
+    if qr_signs:
+        # Cholesky-QR returns Householder's Q up to column signs, carried by the
+        # stored overlap; compare the sign-free quantities column by column
+        s = np.sign(np.real(np.einsum("wpc,wpc->wc", d.conj(), ow.dets)))
+        d = d * s[:, None, :]
+        o = o * np.prod(s, axis=1)
+    e_g = (w * g_el.real).sum() / w.sum()
+    e_o = (ow.weights * el.real).sum() / ow.weights.sum()
+    errs = dict(dets=rel(d, ow.dets), ovl=rel(o, ow.overlaps), w=rel(w, ow.weights),
+                el=float(np.abs(g_el - el).max() / np.abs(el).max()), e_mEh=abs(e_g - e_o) * 1e3)
+    assert errs["dets"] < 2e-5, errs
+    assert errs["w"] < 5e-7 * n_occ * steps, errs
+    assert errs["ovl"] < 5e-7 * n_occ * steps, errs
+    assert errs["el"] < 2e-6, errs
+    assert errs["e_mEh"] < 0.1, errs
+    return errs
+
+
+def test_timed_shape_fp64(A):
+    """N=120, n=20, G=600: 10 steps (QR at 5 and 10), 32 walkers, FP64 form."""
+    got, ref = gpu_run(A, "n120", 32, 10, 1, "fp64")
+    print(check_fp64(got, ref))
+
+
+MIXED_VARIANTS = {
+    # the kernels the timed run's autotuner picks at this size class
+    "tensor": dict(prop="tensor", ovl=3, qr="cholesky"),
+    "tensor_bn256": dict(bn_fb=256, bn_vhs=256, prop="tensor", ovl=3, qr="cholesky"),
+    # the other choices it can make there
+    "smem_warp_householder": dict(bn_fb=64, bn_vhs=64, prop="smem", ovl=1, qr="householder"),
+    "chunked_cta": dict(prop="chunked", ovl=2, qr="cholesky"),
+}
+
+
+@pytest.mark.parametrize("variant", sorted(MIXED_VARIANTS))
+def test_timed_shape_mixed(A, variant):
+    """N=120, n=20, G=600: the same 10 steps in the mixed form, per kernel variant."""
+    t = MIXED_VARIANTS[variant]
+    got, ref = gpu_run(A, "n120", 32, 10, 1, "mixed", t)
+    print(variant, check_mixed(got, ref, 40, 10, t["qr"] == "cholesky"))
+
+
+def test_above_128_orbitals_fp64(A):
+    """N=160, n=36 (> 32 per spin): FP64 column-chunked propagator, block
+    Gauss-Jordan overlap, Householder QR; 5 steps, 12 walkers."""
+    got, ref = gpu_run(A, "n160", 12, 5, 2, "fp64")
+    print(check_fp64(got, ref))
+
+
+@pytest.mark.parametrize("variant", ["chunked_cta", "chunked_cta_householder"])
+def test_above_128_orbitals_mixed(A, variant):
+    """N=160, n=36: FP32 column-chunked propagator, block Gauss-Jordan overlap."""
+    t = dict(prop="chunked", ovl=2, qr="householder" if variant.endswith("householder") else "cholesky")
+    got, ref = gpu_run(A, "n160", 12, 5, 2, "mixed", t)
+    print(variant, check_mixed(got, ref, 72, 5, t["qr"] == "cholesky"))
+
+
+def test_control_variate_system_fp64(A):
+    """N=200, n=30, G=1000: 5 steps, 8 walkers, FP64 form."""
+    got, ref = gpu_run(A, "n200", 8, 5, 3, "fp64")
+    print(check_fp64(got, ref))
+
+
+@pytest.mark.parametrize("variant", ["auto", "chunked_warp"])
+def test_control_variate_system_mixed(A, variant):
+    """N=200, n=30, G=1000: the mixed form's default choices at this size, and
+    the FP32 column-chunked propagator with the warp-per-matrix LU."""
+    t = None if variant == "auto" else dict(prop="chunked", ovl=1, qr="cholesky")
+    got, ref = gpu_run(A, "n200", 8, 5, 3, "mixed", t)
+    print(variant, check_mixed(got, ref, 60, 5, True))

@@ -18,7 +18,8 @@ import pytest
 from vmc_gb300 import inputs
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF = os.environ.get("VMC_REFERENCE_ROOT", "/root/reference")
+# the reference checkout, when one is at hand (VMC_REFERENCE_ROOT); the tests that read it skip otherwise
+REF = os.environ.get("VMC_REFERENCE_ROOT", "")
 
 
 def test_trial_readers(tmp_path):
@@ -49,6 +50,8 @@ def test_run_options_and_samples(tmp_path):
 
 @pytest.mark.parametrize("name", ["rhf_rhf", "uhf_uhf_ui"])
 def test_hdf5_reader_matches_fixtures(name):
+    if not REF:
+        pytest.skip("VMC_REFERENCE_ROOT not set")
     d = os.path.join(REF, "tests", "DQMC", name)
     if not os.path.exists(os.path.join(d, "FCIDUMP_chol")):
         pytest.skip("reference run directory not present")

@@ -79,6 +79,7 @@ def lib():
                            ("afqmc_stage_time", [vp, ctypes.c_char_p, dp]),
                            ("afqmc_launch_count", [vp, ctypes.POINTER(ctypes.c_long)]),
                            ("afqmc_sync", [vp]),
+                           ("afqmc_check_wait_timeout", [vp]),
                            ("afqmc_timer_start", [vp]),
                            ("afqmc_timer_stop", [vp, dp]),
                            ("afqmc_run", [vp, ctypes.POINTER(_RunOpts), vp, vp, ctypes.POINTER(_RunStats)]),
@@ -347,6 +348,12 @@ class DQMCWalkers:
 
     def sync(self):
         self._check(lib().afqmc_sync(self.h))
+
+    def check_wait_timeout(self):
+        """Run one bounded device wait that nothing completes (afqmc_check_wait_timeout);
+        returns the status code (AFQMC_ERR_TIMEOUT = 4 expected) and the message."""
+        rc = lib().afqmc_check_wait_timeout(self.h)
+        return rc, (lib().afqmc_last_error(self.h) or b"").decode()
 
     def timer_start(self):
         self._check(lib().afqmc_timer_start(self.h))

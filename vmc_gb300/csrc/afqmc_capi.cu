@@ -7,6 +7,8 @@
 
 #include <algorithm>
 #include <complex>
+#include <map>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -196,6 +198,19 @@ namespace afqmc {
 bool check_launch(afqmc_handle* h, const char* what) { return after_launch(h, what) == AFQMC_OK; }
 void set_global_error(const std::string& msg) { g_create_err = msg; }
 int take_device_error(afqmc_handle* h) { return device_error(h); }
+
+bool smem_optin_fn(const void* kernel, int bytes) {
+  static std::mutex mu;
+  static std::map<std::pair<const void*, int>, int> done;  // (kernel, device) -> bytes set
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return false;
+  std::lock_guard<std::mutex> lk(mu);
+  int& cur = done[std::make_pair(kernel, dev)];
+  if (cur >= bytes) return true;
+  if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes) != cudaSuccess) return false;
+  cur = bytes;
+  return true;
+}
 }  // namespace afqmc
 
 extern "C" {
@@ -253,6 +268,8 @@ int afqmc_create(const afqmc_ham* ham, const afqmc_trial* trial, const afqmc_opt
   int rc;
   cudaError_t ce = cudaSetDevice(h->device);
   if (ce != cudaSuccess) { std::string m = cudaGetErrorString(ce); delete h; return fail(nullptr, AFQMC_ERR_CUDA, "cudaSetDevice: " + m); }
+  ce = cudaDeviceGetAttribute(&h->nsm, cudaDevAttrMultiProcessorCount, h->device);
+  if (ce != cudaSuccess) { std::string m = cudaGetErrorString(ce); delete h; return fail(nullptr, AFQMC_ERR_CUDA, "cudaDeviceGetAttribute: " + m); }
   ce = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
   if (ce != cudaSuccess) { std::string m = cudaGetErrorString(ce); delete h; return fail(nullptr, AFQMC_ERR_CUDA, "cudaStreamCreate: " + m); }
 
@@ -887,6 +904,17 @@ int afqmc_timer_stop(afqmc_handle* h, double* ms) {
   CK(cudaEventElapsedTime(&t, h->timer[0], h->timer[1]));
   *ms = t;
   return AFQMC_OK;
+}
+
+int afqmc_check_wait_timeout(afqmc_handle* h) {
+  if (!h) return AFQMC_ERR_ARG;
+  cudaSetDevice(h->device);
+  int rc = device_error(h);  // an earlier recorded error is reported, not masked
+  if (rc != AFQMC_OK) return rc;
+  afqmc::launch_wait_probe(h);
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(h->stream));
+  return device_error(h);
 }
 
 int afqmc_sync(afqmc_handle* h) {

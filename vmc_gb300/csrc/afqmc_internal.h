@@ -60,6 +60,7 @@ struct afqmc_handle {
   // sizes
   int N = 0, na = 0, nb = 0, G = 0, T = 0, nsp = 1, int_type = 0;
   int nwalk = 0, rhf_walker = 0, precision = 0, device = 0;
+  int nsm = 0;          // SMs of the device (persistent grids)
   int ncw = 0;          // walker det columns (na, or na + nb)
   int nchan = 0, mult = 1, nce = 0;
   afqmc::Channel chan[2];
@@ -215,8 +216,19 @@ void split_rows(afqmc_handle* h, const double* src, long lds, int rows, int K, i
 void split_rows(afqmc_handle* h, const float* src, long lds, int rows, int K, int kpad, int pattern,
                 __nv_bfloat16* dst);
 void launch_local_energy_mixed(afqmc_handle* h);
+void launch_wait_probe(afqmc_handle* h);  // one bounded mbarrier wait that nothing completes
 
 // error helper used by kernels' launchers
 bool check_launch(afqmc_handle* h, const char* what);
+
+// Raise `kernel`'s dynamic shared-memory limit to at least `bytes` on the
+// current device.  The attribute belongs to one device, so the set-up is
+// remembered per (kernel, device), under a lock: handles on different devices
+// or host threads each get it.  Returns false if CUDA refused it.
+bool smem_optin_fn(const void* kernel, int bytes);
+template <class F>
+inline bool smem_optin(F* kernel, int bytes) {
+  return smem_optin_fn((const void*)kernel, bytes);
+}
 
 }  // namespace afqmc

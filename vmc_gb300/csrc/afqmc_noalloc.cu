@@ -1,13 +1,13 @@
 // Allocation-free Householder orthonormalisation of walker determinants.
 //
 // This entry point has no counterpart in the reference.  It exists for callers
-// that cannot allocate GPU memory at the time they call it: code running while
-// a CUDA stream is being captured into a graph (where cudaMalloc is not
-// allowed), hosts whose device memory is owned by another allocator (a
-// framework's caching pool, a memory-budgeted service), and latency-bound
-// loops that must not hit the allocator.  The caller passes the walker
-// determinants and overlaps in its own device memory; the Q workspace of the
-// QR lives in a fixed file-scope device array, so nothing is allocated.
+// that cannot allocate GPU memory at the time they call it: hosts whose device
+// memory is owned by another allocator (a framework's caching pool, a service
+// that budgets every byte of the GPU up front), and latency-bound loops that
+// must not enter the allocator, whose cudaMalloc / cudaFree synchronise the
+// device.  The caller passes the walker determinants and overlaps in its own
+// device memory; the Q workspace of the QR lives in a fixed file-scope device
+// array, so nothing is allocated.
 //
 // The array holds AFQMC_NOALLOC_QR_SCRATCH complex doubles (8 MiB); every GPU
 // that loads this library keeps it until the process exits.  Walkers are
@@ -16,7 +16,10 @@
 // array and it keeps the last call's contents (the kernel rewrites the part it
 // uses before reading it), so calls that overlap on the GPU -- on different
 // streams, or from different host threads -- race on it and must be serialised
-// by the caller.
+// by the caller.  The first call on a device looks up the array's device
+// address with that device current and keeps it; cudaDeviceReset discards the
+// library's device memory, so the kept address is stale after a reset and the
+// entry point must not be used on that device again in the same process.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -63,14 +66,19 @@ int afqmc_orthonormalize_noalloc(void* dets, void* overlaps, int nwalk, int norb
     return noalloc_fail(AFQMC_ERR_ARG, "one walker determinant (" + std::to_string(per_walker) +
                                            " complex) exceeds the fixed scratch of " +
                                            std::to_string(AFQMC_NOALLOC_QR_SCRATCH) + " complex");
+  // an error left pending by earlier, unrelated work is reported as such, not
+  // as a failure of this call's launches
+  cudaError_t e = cudaPeekAtLastError();
+  if (e != cudaSuccess)
+    return noalloc_fail(AFQMC_ERR_CUDA, std::string("an earlier CUDA error is pending: ") + cudaGetErrorString(e));
   int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
+  e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return noalloc_fail(AFQMC_ERR_CUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
   if (dev < 0 || dev >= kMaxDevices) return noalloc_fail(AFQMC_ERR_ARG, "device ordinal out of range");
   double2* scratch;
   {
     // first call on this device (with it current): look up the device address
-    // of the array; do it before any stream capture
+    // of the array; this first call should come before any stream capture
     std::lock_guard<std::mutex> lk(g_mu);
     if (!g_scratch_addr[dev]) {
       void* p = nullptr;

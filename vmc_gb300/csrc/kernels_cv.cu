@@ -145,8 +145,13 @@ __global__ void k_cv_estimate(const double* __restrict__ weights, const float* _
   __shared__ double s_part[32][NV];
   double v[NV] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
   for (int w = threadIdx.x; w < W; w += blockDim.x) {
-    v[0] += weights[w];
-    v[1] += weights[w] * (double)f(w);
+    // dead walkers are skipped, not multiplied by 0: their prediction may be
+    // non-finite (a walker that died of a non-finite overlap)
+    const double wt = weights[w];
+    if (wt != 0.0) {
+      v[0] += wt;
+      v[1] += wt * (double)f(w);
+    }
   }
   for (int i = threadIdx.x; i < m; i += blockDim.x) {
     const int w = idx[i];

@@ -265,11 +265,7 @@ void launch_local_energy_mixed_subset(afqmc_handle* h, const int* d_idx, int m, 
   const int Kn = h->N;
   if (d_idx) launch_split_theta_gather(h, d_idx, m);
   else split_rows(h, h->theta32, Kn, 2 * m * h->nce, Kn, h->ke_pad, 1, h->thetaE);
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(k_tc_exchange, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ex_smem(128));
-    attr = true;
-  }
+  smem_optin(k_tc_exchange, (int)ex_smem(128));
   ExArgs a[2];
   size_t smem = 0;
   int gt = 1, wt = 1;

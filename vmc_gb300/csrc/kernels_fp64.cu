@@ -538,11 +538,7 @@ void launch_overlap_theta(afqmc_handle* h, bool only_live) {
     const int nm = (nmax + 3) / 4 * 4;
 #define OW_LAUNCH(F, NMV, MBV)                                                                                \
   {                                                                                                          \
-    static bool attr = false;                                                                                \
-    if (!attr) {                                                                                             \
-      cudaFuncSetAttribute(k_overlap_lu<F, NMV, MBV>, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024); \
-      attr = true;                                                                                           \
-    }                                                                                                        \
+    smem_optin(k_overlap_lu<F, NMV, MBV>, 160 * 1024);                                                       \
     k_overlap_lu<F, NMV, MBV><<<grid, OW_WARPS * 32, smem, h->stream>>>(                                     \
         h->psi, h->psi32, h->phi, h->theta, h->theta32, h->det, h->weights, h->nwalk, h->N, h->ncw, h->nce,  \
         h->chan[0],                                                                                          \
@@ -573,11 +569,7 @@ void launch_overlap_theta(afqmc_handle* h, bool only_live) {
     return;
   }
   size_t smem = (size_t)nmax * 2 * nmax * sizeof(double2) + nmax * sizeof(double2);
-  static bool attr_set = false;
-  if (!attr_set) {
-    cudaFuncSetAttribute(k_overlap_theta, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    attr_set = true;
-  }
+  smem_optin(k_overlap_theta, 200 * 1024);
   dim3 grid(h->nwalk, h->nchan);
   k_overlap_theta<<<grid, 256, smem, h->stream>>>(h->psi, h->phi, h->theta, h->theta32, h->det, h->weights, h->N,
                                                   h->ncw, h->nce, h->chan[0], h->chan[1],
@@ -1019,11 +1011,7 @@ void launch_ortho(afqmc_handle* h) {
 void launch_ortho_core(afqmc_handle* h) {
   const size_t smem = 2 * (size_t)h->N * std::max(h->na, h->nb) * sizeof(double2);
   if (smem <= 200 * 1024) {
-    static bool attr = false;
-    if (!attr) {
-      cudaFuncSetAttribute(k_ortho<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-      attr = true;
-    }
+    smem_optin(k_ortho<true>, 200 * 1024);
     k_ortho<true><<<h->nwalk, 256, smem, h->stream>>>(h->psi, h->qwork, h->ovlp, h->N, h->ncw, h->na, h->nb,
                                                       h->rhf_walker);
   } else {
@@ -1127,11 +1115,7 @@ __global__ void k_energy_final(const double* __restrict__ theta, const double* _
 void launch_local_energy(afqmc_handle* h) {
   const int nmax = std::max(h->chan[0].n, h->nchan > 1 ? h->chan[1].n : 0);
   const size_t smem = ((size_t)h->nce * h->N + (size_t)h->nchan * nmax * nmax) * sizeof(double2);
-  static bool attr_set = false;
-  if (!attr_set) {
-    cudaFuncSetAttribute(k_energy, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
-    attr_set = true;
-  }
+  smem_optin(k_energy, 220 * 1024);
   const int gper = (h->nchol_ene + h->nechunk - 1) / h->nechunk;
   dim3 grid(h->nwalk, h->nechunk);
   k_energy<<<grid, 256, smem, h->stream>>>(h->theta, h->rot, h->epart, h->N, h->nce, h->nchol_ene, gper,
@@ -1143,11 +1127,7 @@ void launch_local_energy(afqmc_handle* h) {
 
 void launch_propagate(afqmc_handle* h) {
   const size_t smem = 3 * (size_t)h->N * PROP_CH * sizeof(double2);
-  static bool attr_set = false;
-  if (!attr_set) {
-    cudaFuncSetAttribute(k_propagate, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    attr_set = true;
-  }
+  smem_optin(k_propagate, 200 * 1024);
   const int threads = std::min(256, ((h->N + 31) / 32) * 32);
   dim3 grid(h->nwalk, h->nchunks);
   k_propagate<<<grid, threads, smem, h->stream>>>(h->psi, h->V, h->expm, h->weights, h->d_chunks, h->N, h->ncw,

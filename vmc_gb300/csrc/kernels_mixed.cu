@@ -156,13 +156,8 @@ static void launch_tc_bn(afqmc_handle* h, const CUtensorMap& ta, const CUtensorM
                          const Epi& epi) {
   constexpr int ST = 4;
   const int smem = tc::GemmPSmem<BN, ST>::TOTAL;
-  static bool attr = false;
-  static int nsm = 0;
-  if (!attr) {
-    cudaFuncSetAttribute(tc::k_tc_gemm_p<BN, ST, Epi>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, h->device);
-    attr = true;
-  }
+  smem_optin(tc::k_tc_gemm_p<BN, ST, Epi>, smem);
+  const int nsm = h->nsm;
   // persistent: one CTA per SM (or per tile when there are fewer tiles)
   const int tiles = ((N + BN - 1) / BN) * ((M + tc::BM - 1) / tc::BM);
   const int grid = std::max(1, std::min(tiles, nsm > 0 ? nsm : tiles));
@@ -585,11 +580,7 @@ void launch_propagate_mixed(afqmc_handle* h) {
   }
   if (h->N <= PS_NMAX && h->tune_prop != 2) {
     const size_t smem = ((size_t)h->N * h->N + 2 * (size_t)h->N * PS_CW) * sizeof(float2);
-    static bool attr2 = false;
-    if (!attr2) {
-      cudaFuncSetAttribute(k_prop32_smem, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
-      attr2 = true;
-    }
+    smem_optin(k_prop32_smem, 220 * 1024);
     const int threads = ((h->N + PS_RB - 1) / PS_RB) * (PS_CW / PS_CB);
     dim3 grid(h->nwalk, h->nspV);
     k_prop32_smem<<<grid, threads, smem, h->stream>>>(h->psi, h->psi32, h->V32, h->expm32, h->tri, h->weights, h->N,
@@ -598,11 +589,7 @@ void launch_propagate_mixed(afqmc_handle* h) {
     return;
   }
   const size_t smem = 2 * (size_t)h->N * PCH32 * sizeof(float2);
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(k_propagate32, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    attr = true;
-  }
+  smem_optin(k_propagate32, 200 * 1024);
   const int threads = ((h->N + 31) / 32) * 32;
   dim3 grid(h->nwalk, h->nchunks32);
   k_propagate32<<<grid, threads, smem, h->stream>>>(h->psi, h->psi32, h->V32, h->expm32, h->weights, h->d_chunks32, h->N,
@@ -653,5 +640,24 @@ void launch_vhs_gemm(afqmc_handle* h, int bn) {
     EpiV32 epi{h->V32, h->T, h->nspV, s, (float)sqrt(h->dt)};
     launch_tc(h, h->tm_LT[s], h->tm_x_bn, bn, h->T, 2 * h->nwalk, h->kv_pad, epi);
   }
+}
+}  // namespace afqmc
+
+namespace afqmc {
+// Check of the bounded-wait path: one thread waits, with the same bounded
+// mbarrier wait as the tensor-core pipelines, on a barrier that nothing
+// arrives at.  No copy is issued and no tensor memory is held, so when the
+// wait gives up (after tc::WAIT_NS) the kernel records the code and returns.
+constexpr int WAIT_PROBE_CODE = 90;
+__global__ void k_wait_probe(int* err) {
+  __shared__ uint64_t bar;
+  if (threadIdx.x != 0) return;
+  tc::mbar_init(&bar, 1);
+  tc::fence_mbar_init();
+  tc::mbar_wait(&bar, 0, err, WAIT_PROBE_CODE);
+}
+void launch_wait_probe(afqmc_handle* h) {
+  k_wait_probe<<<1, 32, 0, h->stream>>>(h->d_err);
+  h->launches++;
 }
 }  // namespace afqmc

@@ -294,12 +294,8 @@ __global__ void __launch_bounds__(MF_THREADS)
 int mlp_forward_on(afqmc_mlp* m, const float* X, int B, float* Y, cudaStream_t st, bool keep) {
   const int H = m->H, nin = m->nin;
   if (H <= MF_THREADS && mf_smem(nin, H) <= 220 * 1024) {
-    static size_t attr = 0;
     const size_t smem = mf_smem(nin, H);
-    if (smem > attr) {
-      cudaFuncSetAttribute(k_mlp_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      attr = smem;
-    }
+    smem_optin(k_mlp_fwd, (int)smem);
     k_mlp_fwd<<<(B + MF_RB - 1) / MF_RB, MF_THREADS, smem, st>>>(
         X, B, nin, H, m->Pb, m->P + m->o_b1(), m->Pb + m->o_W2(), m->P + m->o_b2(), m->Pb + m->o_w3(),
         m->P + m->o_b3(), Y, keep ? m->Z1 : nullptr, keep ? m->H1 : nullptr, keep ? m->Z2 : nullptr,

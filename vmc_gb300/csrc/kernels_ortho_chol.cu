@@ -188,11 +188,7 @@ bool ortho_chol_available(const afqmc_handle* h) {
 }
 
 void launch_ortho_chol(afqmc_handle* h) {
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(k_ortho_chol, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    attr = true;
-  }
+  smem_optin(k_ortho_chol, 200 * 1024);
   const int nmax = std::max(h->na, h->rhf_walker ? 0 : h->nb);
   k_ortho_chol<<<h->nwalk, OC_THREADS, ortho_chol_smem(h), h->stream>>>(h->psi, h->psi32, h->ovlp, h->weights, h->N,
                                                                          h->ncw, h->na, h->nb, h->rhf_walker, nmax);

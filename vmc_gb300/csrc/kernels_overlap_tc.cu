@@ -415,11 +415,7 @@ bool setup_ovl_tc(afqmc_handle* h) {
 }
 
 void launch_overlap_m_tc(afqmc_handle* h) {
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(k_ovl_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
-    attr = true;
-  }
+  smem_optin(k_ovl_tc, 220 * 1024);
   OzArgs g;
   g.psi = h->psi;
   g.bimg = h->ovl_bimg;

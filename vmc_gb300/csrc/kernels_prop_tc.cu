@@ -445,11 +445,7 @@ bool setup_prop_tc(afqmc_handle* h) {
 bool prop_tc_available(const afqmc_handle* h) { return h->N <= 128 && h->pt_img != nullptr; }
 
 void launch_propagate_tc(afqmc_handle* h) {
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(k_prop_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, PT_SMEM);
-    attr = true;
-  }
+  smem_optin(k_prop_tc, PT_SMEM);
   dim3 grid(h->nwalk, h->nspV);
   k_prop_tc<<<grid, PT_THREADS, PT_SMEM, h->stream>>>(h->psi, h->psi32, h->V32, h->pt_img, h->pt_voff, h->weights, h->N,
                                                h->ncw, h->na, h->nspV, h->real_expm ? 1 : 0, h->d_err);
