@@ -208,6 +208,35 @@ typedef struct afqmc_run_stats {
 int afqmc_run(afqmc_handle* h, const afqmc_run_opts* opts, double* total_weights, double* total_energies,
               afqmc_run_stats* stats);
 
+/* afqmc_run, and per block the two other columns of the reference's afqmc.dat
+ * rows (MixedEstimator.cpp:423-425, :530-544): block_eshift[nsweeps], the
+ * energy shift of the measured step (row 0: the initial energy), and
+ * block_wall[nsweeps], seconds since the walker set-up began (with
+ * device_blocks this waits for each block).  Either pointer may be NULL. */
+int afqmc_run_blocks(afqmc_handle* h, const afqmc_run_opts* opts, double* total_weights, double* total_energies,
+                     double* block_eshift, double* block_wall, afqmc_run_stats* stats);
+
+/* ---- mixed one-body reduced density matrix ----
+ * The reference's weighted mixed estimate of the 1-RDM: the mean over live
+ * walkers and measurements, weighted by the walker weights, of each walker's
+ * sample (psi_s (Phi_s^T psi_s)^-1 Phi_s^T)^T, real part (DQMC/RHF.cpp:64-67,
+ * DQMC/UHF.cpp:68-72, DQMC/MixedEstimator.cpp:488-510, written by :52-110).
+ * afqmc_rdm_enable(h, 1) allocates the running sums (once) and makes afqmc_run
+ * (both paths) and afqmc_block_end add every measurement after equilibration
+ * (step dt > 10 and step > burnIter nsteps, counted from afqmc_block_setup on
+ * the device); afqmc_rdm_accumulate adds the current walkers unconditionally
+ * (asynchronous).  afqmc_rdm_get writes rdm [nout][norb][norb] row-major
+ * (nout = 1, the sum over spins, for AFQMC_INT_R; 2, up then down, for
+ * AFQMC_INT_U) and the cumulative weight; either pointer may be NULL.  For a
+ * trial/integral pairing whose reference trial has no matching override (UHF
+ * trial with restricted integrals, RHF trial with unrestricted ones), the
+ * reference leaves its sample at zero; this library returns the same
+ * spin-summed or per-spin estimate as for the other pairings. */
+int afqmc_rdm_enable(afqmc_handle* h, int on);
+int afqmc_rdm_reset(afqmc_handle* h);
+int afqmc_rdm_accumulate(afqmc_handle* h);
+int afqmc_rdm_get(afqmc_handle* h, double* rdm, double* cumulative_weight);
+
 /* The reference's field order for one emulated rank: std::mt19937(seed) and nwalk
  * std::normal_distribution<double>(0, 1) objects (DQMC/DQMCWalker.h:18). */
 typedef struct afqmc_refrng afqmc_refrng;

@@ -77,6 +77,12 @@ def build():
     subprocess.check_call(["g++", "-O2", "-std=c++17", "-shared", "-fPIC",
                            os.path.join(_HERE, "fieldgen.cpp"), "-o", tmp])
     os.replace(tmp, so)
+    # the C++ restatement of the walker step (CPU baseline; oracle/cpu_port.py)
+    so = os.path.join(out, "libcpustep.so")
+    tmp = so + ".tmp%d" % os.getpid()
+    subprocess.check_call(["g++", "-O3", "-std=c++17", "-fopenmp", "-fcx-limited-range", "-shared", "-fPIC",
+                           os.path.join(_HERE, "cpu_step.cpp"), "-o", tmp])
+    os.replace(tmp, so)
 
 
 class RankRNG:
@@ -502,6 +508,50 @@ def orthogonalize(walkers):
 # ---------------------------------------------------------------------------
 # the driver (calcMixedEstimatorLongProp) with emulated MPI ranks
 # ---------------------------------------------------------------------------
+def one_rdm_samples(trial, walkers, int_type="r"):
+    """Each walker's 1-RDM sample, real part: (psi_s (Phi_s^T psi_s)^-1 Phi_s^T)^T
+    per spin (RHF.cpp:64-67, UHF.cpp:68-72).  Restricted integrals: the sum over
+    the two spins, shape (W, 1, N, N); unrestricted: (W, 2, N, N).  The
+    restricted walker's second spin is its first (DQMCWalker.cpp:487), which the
+    channel multiplicity counts."""
+    th, mult = thetas(trial, walkers)
+    W, N = walkers.nwalk, walkers.dets.shape[1]
+    nout = 1 if int_type == "r" else 2
+    out = np.zeros((W, nout, N, N))
+    for s, t in th:
+        samp = np.einsum("pi,wqi->wpq", trial.phi[s], t).real  # [p][q] = sum_i Phi[p, i] theta[q, i]
+        if nout == 1:
+            out[:, 0] += mult * samp
+        else:
+            out[:, s] += samp
+            if mult == 2:
+                out[:, 1 - s] += samp
+    return out
+
+
+class OneRDM:
+    """The reference's running weighted mean of the 1-RDM samples over live
+    walkers and measurements (MixedEstimator.cpp:488-510), updated walker by
+    walker: rdm <- (rdm cum + w sample) / (cum + w), cum <- cum + w."""
+
+    def __init__(self, N, int_type="r"):
+        self.rdm = np.zeros((1 if int_type == "r" else 2, N, N))
+        self.cum = 0.0
+        self.int_type = int_type
+
+    def add(self, trial, walkers):
+        live = np.nonzero(walkers.weights != 0.0)[0]
+        if len(live) == 0:
+            return
+        sub = walkers.copy()
+        sub.dets = walkers.dets[live]
+        samples = one_rdm_samples(trial, sub, self.int_type)
+        for j, w in enumerate(live):
+            wt = walkers.weights[w]
+            self.rdm = (self.rdm * self.cum + wt * samples[j]) / (self.cum + wt)
+            self.cum += wt
+
+
 def truncate_cholesky(trial, ham, ref_phi, rhf_walker, threshold):
     """ncholEne / delta selection (MixedEstimator.cpp:363-384)."""
     e_ref = hf_energy(trial, ham, ref_phi, rhf_walker, ham.nchol)
@@ -516,14 +566,16 @@ def truncate_cholesky(trial, ham, ref_phi, rhf_walker, threshold):
 
 def run(ham, trial, ref_phi, rhf_walker, seed, nprocs=1, nwalk=20, dt=0.005, nsteps=50,
         nsweeps=50, ortho_steps=20, cholesky_threshold=1e-3, burn_iter=0,
-        weight_cap=-1.0, mode="ref", max_steps=None, right_phi=None):
+        weight_cap=-1.0, mode="ref", max_steps=None, right_phi=None, one_rdm=False):
     """Restatement of calcMixedEstimatorLongProp (MixedEstimator.cpp:309-660).
 
     Emulates ``nprocs`` MPI ranks in lockstep: rank r has mt19937(seed + r) and
     ``nwalk`` walkers; the sums of MixedEstimator.cpp:420, :473, :536 run over
     all ranks; the comb (:559-635) gathers in rank order and draws zeta from rank
     0's generator.  Returns (totalWeights, totalEnergies) per block, i.e. the
-    samples.dat columns (:678-683).
+    samples.dat columns (:678-683).  one_rdm: the info dict also holds the
+    mixed 1-RDM ("one_rdm", "rdm_weight") accumulated at the measurements after
+    equilibration (:491-510).
     """
     nchol_ene, delta, e_ref = truncate_cholesky(trial, ham, ref_phi, rhf_walker, cholesky_threshold)
     ham.nchol_ene = nchol_ene
@@ -545,6 +597,7 @@ def run(ham, trial, ref_phi, rhf_walker, seed, nprocs=1, nwalk=20, dt=0.005, nst
     e_est = tot_e[0]
     cap = weight_cap if weight_cap > 0 else max(100.0, nwalk / 10.0)
     nlarge = 0
+    rdm = OneRDM(ham.norb, ham.int_type) if one_rdm else None
     last = nsweeps * nsteps if max_steps is None else min(nsweeps * nsteps, max_steps + 1)
     for st in range(1, last):
         if st * dt < 10.0:
@@ -558,6 +611,8 @@ def run(ham, trial, ref_phi, rhf_walker, seed, nprocs=1, nwalk=20, dt=0.005, nst
             orthogonalize(wk)
         if st % nsteps == 0:
             block = st // nsteps
+            if rdm is not None and st * dt > 10.0 and st > burn_iter * nsteps:
+                rdm.add(trial, wk)
             el = np.zeros(wk.nwalk)
             live = wk.weights != 0.0
             if live.any():
@@ -587,4 +642,7 @@ def run(ham, trial, ref_phi, rhf_walker, seed, nprocs=1, nwalk=20, dt=0.005, nst
             wk.dets = wk.dets[index]
             wk.overlaps = wk.overlaps[index]
             wk.weights = np.full(P * nwalk, total / P / nwalk)
-    return tot_w, tot_e, {"nchol_ene": nchol_ene, "delta": delta, "e_ref": e_ref, "nlarge": nlarge}
+    info = {"nchol_ene": nchol_ene, "delta": delta, "e_ref": e_ref, "nlarge": nlarge}
+    if rdm is not None:
+        info.update(one_rdm=rdm.rdm, rdm_weight=rdm.cum)
+    return tot_w, tot_e, info

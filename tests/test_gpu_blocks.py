@@ -65,13 +65,17 @@ def test_device_blocks_reproduce_host_loop(A, precision):
     for dev in (False, True):
         wk = make(A, s, W, precision)
         tw, te, st = wk.run(nsteps=10, nsweeps=6, ortho_steps=5, seed=11, nprocs=4, field_source="device",
-                            cholesky_threshold=1e-3, device_blocks=dev)
+                            cholesky_threshold=1e-3, device_blocks=dev, block_info=True)
         out.append((tw, te, st, wk.get_det()))
     (tw0, te0, st0, g0), (tw1, te1, st1, g1) = out
     assert np.abs(tw1 - tw0).max() <= 1e-10 * np.abs(tw0).max()
     assert np.abs(te1 - te0).max() <= 1e-10 * np.abs(te0).max()
     assert st1["n_large_deviations"] == st0["n_large_deviations"]
     assert np.abs(g1[0] - g0[0]).max() <= 1e-8 * np.abs(g0[0]).max()
+    # afqmc.dat's eshift column: read from the device in the host loop,
+    # reconstructed from the block ring with device blocks; the same numbers
+    assert np.abs(st1["eshift"] - st0["eshift"]).max() <= 1e-9 * np.abs(st0["eshift"]).max()
+    assert np.all(np.diff(st0["walltime"]) >= 0) and np.all(np.diff(st1["walltime"]) >= 0)
 
 
 def test_block_graph_equals_calls(A):

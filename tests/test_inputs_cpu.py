@@ -64,3 +64,71 @@ def test_hdf5_reader_matches_fixtures(name):
     t = inputs.read_trials(d, ints["norb"], ints["nalpha"], ints["nbeta"])
     assert set(t) == {k.replace("_txt", "") for k in z.files if k.endswith("_txt")}
     assert inputs.run_options(cfg)["nsteps"] == int(cfg["sampling"]["nsteps"])
+
+
+def _slater_spin_rdm_file(path, N, na, nb, seed):
+    """spinRDM.0.0.txt of a Slater determinant: Gamma_abcd = g_ac g_bd - g_ad g_bc
+    over spin orbitals (2i alpha, 2i + 1 beta), one line per a < b, c < d."""
+    rng = np.random.default_rng(seed)
+    ca = np.linalg.qr(rng.standard_normal((N, N)))[0][:, :na]
+    cb = np.linalg.qr(rng.standard_normal((N, N)))[0][:, :nb]
+    g = np.zeros((2 * N, 2 * N))
+    g[0::2, 0::2] = ca @ ca.T
+    g[1::2, 1::2] = cb @ cb.T
+    with open(path, "w") as f:
+        for a in range(2 * N):
+            for b in range(a + 1, 2 * N):
+                for c in range(2 * N):
+                    for d in range(c + 1, 2 * N):
+                        v = g[a, c] * g[b, d] - g[a, d] * g[b, c]
+                        if abs(v) > 1e-14:
+                            f.write("%d %d %d %d %.17e\n" % (a, b, c, d, v))
+    return ca @ ca.T, cb @ cb.T
+
+
+def test_spin_rdm_reader(tmp_path):
+    """The 1-RDM contracted from a determinant's 2-RDM is its density matrix."""
+    N, na, nb = 5, 3, 2
+    p = tmp_path / "spinRDM.0.0.txt"
+    ga, gb = _slater_spin_rdm_file(str(p), N, na, nb, 3)
+    green = inputs.read_spin_rdm(str(p), N, na, nb)
+    assert green.shape == (2, N, N)
+    assert np.allclose(green[0], ga, atol=1e-12) and np.allclose(green[1], gb, atol=1e-12)
+
+
+def test_blocking_and_afqmc_dat(tmp_path):
+    """blocking.tmp: the weighted mean, the block-size-1 error equals the
+    weighted standard error written out directly, the plateau rule; afqmc.dat:
+    header, one row per block, '-' in the cumulative column during
+    equilibration (step dt < 10), the running weighted average after it."""
+    rng = np.random.default_rng(5)
+    n = 140
+    tw = 80 + rng.random(n)
+    te = -76.0 + 0.01 * rng.standard_normal(n)
+    res = inputs.write_blocking(str(tmp_path / "blocking.tmp"), tw, te, burn_iter=0)
+    assert res is not None
+    w, e = tw[40:], te[40:]
+    mean, err, rows = inputs.blocking(w, e)
+    assert abs(mean - (w * e).sum() / w.sum()) < 1e-12
+    v1, v2 = w.sum(), (w ** 2).sum()
+    m1 = (w * e).sum() / v1
+    se1 = np.sqrt((w * (e - m1) ** 2).sum() / (v1 - v2 / v1) / (len(w) - 1))
+    assert rows[0][:2] == (1, 100) and abs(rows[0][3] - se1) < 1e-15
+    assert [r[0] for r in rows] == [1, 2, 5, 10, 20, 50]
+    txt = open(tmp_path / "blocking.tmp").read().splitlines()
+    assert txt[0] == "Number of samples: 100" and txt[1].startswith("Mean energy: -7.")
+    assert inputs.write_blocking(str(tmp_path / "none.tmp"), tw[:40], te[:40]) is None
+    stats = dict(e_ref=-75.98, delta=1e-4, nchol_ene=30, n_large_deviations=2,
+                 eshift=np.full(n, -76.0), walltime=np.linspace(0.1, 5.0, n))
+    p = tmp_path / "afqmc.dat"
+    inputs.write_afqmc_dat(str(p), tw, te, stats, dt=0.005, nsteps=50, nchol=60)
+    lines = open(p).read().splitlines()
+    rows = [l for l in lines if not l.startswith("#")]
+    assert len(rows) == n
+    assert "Using truncated Cholesky with 30 vectors" in lines[2]
+    # step 40 x 50 x 0.005 = 10: blocks < 40 are equilibration
+    assert rows[39].split()[5] == "-" and rows[40].split()[5] != "-"
+    assert abs(float(rows[40].split()[5]) - te[40]) < 1e-8
+    cum = (tw[40:42] * te[40:42]).sum() / tw[40:42].sum()
+    assert abs(float(rows[41].split()[5]) - cum) < 1e-8
+    assert lines[-1] == "# Number of large deviations:  2"

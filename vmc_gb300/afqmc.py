@@ -80,6 +80,9 @@ def lib():
                            ("afqmc_launch_count", [vp, ctypes.POINTER(ctypes.c_long)]),
                            ("afqmc_sync", [vp]),
                            ("afqmc_check_wait_timeout", [vp]),
+                           ("afqmc_rdm_enable", [vp, ip]),
+                           ("afqmc_rdm_reset", [vp]),
+                           ("afqmc_rdm_accumulate", [vp]),
                            ("afqmc_timer_start", [vp]),
                            ("afqmc_timer_stop", [vp, dp]),
                            ("afqmc_run", [vp, ctypes.POINTER(_RunOpts), vp, vp, ctypes.POINTER(_RunStats)]),
@@ -349,6 +352,28 @@ class DQMCWalkers:
     def sync(self):
         self._check(lib().afqmc_sync(self.h))
 
+    # --- mixed 1-RDM estimator (MixedEstimator.cpp:488-510) ---
+    def rdm_enable(self, on=True):
+        self._check(lib().afqmc_rdm_enable(self.h, int(bool(on))))
+
+    def rdm_reset(self):
+        self._check(lib().afqmc_rdm_reset(self.h))
+
+    def rdm_accumulate(self):
+        self._check(lib().afqmc_rdm_accumulate(self.h))
+
+    def rdm(self):
+        """(rdm, cumulative weight): rdm (1, N, N) spin-summed for restricted
+        integrals, (2, N, N) up / down for unrestricted ones."""
+        N = self.ham.norb
+        nout = 1 if self.ham.int_type == "r" else 2
+        r = np.zeros((nout, N, N))
+        cw = ctypes.c_double()
+        L = lib()
+        L.afqmc_rdm_get.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(ctypes.c_double)]
+        self._check(L.afqmc_rdm_get(self.h, r.ctypes.data, ctypes.byref(cw)))
+        return r, cw.value
+
     def check_wait_timeout(self):
         """Run one bounded device wait that nothing completes (afqmc_check_wait_timeout);
         returns the status code (AFQMC_ERR_TIMEOUT = 4 expected) and the message."""
@@ -364,22 +389,36 @@ class DQMCWalkers:
         return ms.value
 
     def run(self, nsteps=50, nsweeps=50, ortho_steps=20, seed=4321, nprocs=1, burn_iter=0,
-            field_source="reference", comb=True, cholesky_threshold=1e-3, max_steps=0, device_blocks=False):
+            field_source="reference", comb=True, cholesky_threshold=1e-3, max_steps=0, device_blocks=False,
+            block_info=False):
         """calcMixedEstimatorLongProp from the current walkers (DQMC/MixedEstimator.cpp:309-660).
 
-        Returns (total_weights, total_energies, stats) -- the samples.dat columns."""
+        Returns (total_weights, total_energies, stats) -- the samples.dat columns.
+        block_info: stats also holds "eshift" and "walltime" per block (the other
+        afqmc.dat columns; inputs.write_afqmc_dat)."""
         o = _RunOpts(int(nprocs), int(nsteps), int(nsweeps), int(ortho_steps), int(burn_iter), int(seed),
                      0 if field_source == "reference" else 1, int(bool(comb)), float(cholesky_threshold),
                      int(max_steps), int(bool(device_blocks)))
         tw = np.zeros(nsweeps)
         te = np.zeros(nsweeps)
         st = _RunStats()
-        self._check(lib().afqmc_run(self.h, ctypes.byref(o), tw.ctypes.data, te.ctypes.data, ctypes.byref(st)))
-        return tw, te, dict(nchol_ene=st.nchol_ene, delta=st.delta, e_ref=st.e_ref,
-                            n_large_deviations=st.n_large_deviations)
+        if block_info:
+            es, wl = np.zeros(nsweeps), np.zeros(nsweeps)
+            L = lib()
+            L.afqmc_run_blocks.argtypes = [ctypes.c_void_p, ctypes.POINTER(_RunOpts)] + [ctypes.c_void_p] * 4 + \
+                [ctypes.POINTER(_RunStats)]
+            self._check(L.afqmc_run_blocks(self.h, ctypes.byref(o), tw.ctypes.data, te.ctypes.data, es.ctypes.data,
+                                           wl.ctypes.data, ctypes.byref(st)))
+        else:
+            self._check(lib().afqmc_run(self.h, ctypes.byref(o), tw.ctypes.data, te.ctypes.data,
+                                        ctypes.byref(st)))
+        out = dict(nchol_ene=st.nchol_ene, delta=st.delta, e_ref=st.e_ref, n_large_deviations=st.n_large_deviations)
+        if block_info:
+            out.update(eshift=es, walltime=wl)
+        return tw, te, out
 
 
-def from_reference_inputs(ham_arrays, trials, cfg, nprocs=1, precision="ref32", device=0):
+def from_reference_inputs(ham_arrays, trials, cfg, nprocs=1, precision="ref32", device=0, green=None):
     """Build ``DQMCWalkers`` the way executables/DQMC.cpp:74-153 does for the
     RHF/UHF phaseless path.
 
@@ -389,7 +428,10 @@ def from_reference_inputs(ham_arrays, trials, cfg, nprocs=1, precision="ref32", 
     rhf.txt / uhf.txt contents.  cfg: the afqmc.json dict.  The left trial is
     cfg["wavefunction"]["left"]; the walkers start at the right trial's
     determinant (waveRight.getSample); the mean-field reference is rhf.txt for
-    the restricted walker and uhf.txt otherwise (MixedEstimator.cpp:338-350)."""
+    the restricted walker and uhf.txt otherwise (MixedEstimator.cpp:338-350).
+    green: optional [2][norb][norb] mean-field Green's function replacing the
+    reference determinant's in the mean-field shifts (the spinRDM.0.0.txt
+    override, DQMCWalker.cpp:39-58; inputs.read_spin_rdm)."""
     left = trials[cfg["wavefunction"]["left"]]
     right = trials[cfg["wavefunction"]["right"]]
     it = cfg["system"].get("intType", "r")
@@ -408,7 +450,7 @@ def from_reference_inputs(ham_arrays, trials, cfg, nprocs=1, precision="ref32", 
     ref_t = mk(trials["rhf" if rhf_walker else "uhf"])
     nwalk = int(s.get("nwalk", 100))
     wk = DQMCWalkers(ham, mk(left), nwalk * nprocs, rhf_walker, float(s.get("dt", 0.1)), precision=precision,
-                     ref=(ref_t.phi_a, ref_t.phi_b), weight_cap=max(100.0, nwalk / 10.0),
+                     ref=(ref_t.phi_a, ref_t.phi_b), green=green, weight_cap=max(100.0, nwalk / 10.0),
                      pop_target=nwalk * nprocs, device=device)
     rt = mk(right)
     init = np.concatenate([rt.phi_a, rt.phi_b], axis=1) if not rhf_walker else rt.phi_a

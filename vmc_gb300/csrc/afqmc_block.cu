@@ -172,6 +172,7 @@ void launch_block_end(afqmc_handle* h, int comb) {
   k_block_measure<<<1, 32, 0, h->stream>>>(h->eloc, h->weights, h->scal, h->blk, h->blk_zeta, h->d_step, h->seed,
                                             h->nwalk, h->dt, h->d_err);
   h->launches++;
+  launch_rdm_accumulate(h, true);  // no-op unless the 1-RDM estimator is on
   if (comb) launch_comb_moves(h);
 }
 

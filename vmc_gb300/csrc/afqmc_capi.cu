@@ -180,7 +180,8 @@ void release(afqmc_handle* h) {
                   h->thetaB, h->xB, h->fb32, h->V32, h->expm32, h->d_chunks32, h->rotE, h->thetaE,
                   h->xc, h->cv_x, h->cv_idx, h->cv_esub, h->cv_f, h->cv_ms, h->cv_out, h->d_step, h->psi32,
                   h->pt_img, h->comb_cum, h->comb_idx, h->comb_ovl, h->blk, h->blk_zeta, h->wpart,
-                  h->ovl_tau, h->ovl_bimg, h->ovl_M, h->theta32, h->mf32, h->h1phi32, h->pt_voff};
+                  h->ovl_tau, h->ovl_bimg, h->ovl_M, h->theta32, h->mf32, h->h1phi32, h->pt_voff,
+                  h->rdm_acc, h->rdm_part};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (h->host_pinned) cudaFreeHost(h->host_pinned);
@@ -528,6 +529,7 @@ int afqmc_create(const afqmc_ham* ham, const afqmc_trial* trial, const afqmc_opt
     return rc;                                                     \
   }
   UP(phi, phi);
+  h->phi_host = phi;
   UP(rot, rot);
   UP(h1phi, h1phi);
   UP(LT, LT);
@@ -818,10 +820,10 @@ int afqmc_local_energy(afqmc_handle* h, double* eloc) {
   if (!h) return AFQMC_ERR_ARG;
   cudaSetDevice(h->device);
   const int nmax = std::max(h->chan[0].n, h->nchan > 1 ? h->chan[1].n : 0);
-  const size_t smem = ((size_t)h->nce * h->N + (size_t)h->nchan * nmax * nmax) * sizeof(double2);
+  const size_t fbytes = (size_t)h->nchan * nmax * nmax * sizeof(double2);
   const bool mixed = h->precision == AFQMC_PREC_MIXED;
-  if (!mixed && smem > 220 * 1024)
-    return fail(h, AFQMC_ERR_UNSUPPORTED, "FP64 local energy: theta does not fit in shared memory");
+  if (!mixed && fbytes > 220 * 1024)
+    return fail(h, AFQMC_ERR_UNSUPPORTED, "FP64 local energy: the n x n exchange blocks do not fit in shared memory");
   cudaEvent_t e0;
   stage_begin(h, afqmc::ST_ENERGY, &e0);
   if (mixed) afqmc::launch_local_energy_mixed(h);

@@ -17,6 +17,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <chrono>
 #include <random>
 #include <string>
 #include <vector>
@@ -59,9 +60,15 @@ double afqmc_refrng_uniform(afqmc_refrng* r) {
   return u(r->gen);
 }
 
-int afqmc_run(afqmc_handle* h, const afqmc_run_opts* o, double* total_weights, double* total_energies,
-              afqmc_run_stats* stats) {
+static int run_impl(afqmc_handle* h, const afqmc_run_opts* o, double* total_weights, double* total_energies,
+                    double* block_eshift, double* block_wall, afqmc_run_stats* stats) {
   if (!h || !o || !total_weights || !total_energies) return AFQMC_ERR_ARG;
+  // wall clock of the afqmc.dat rows: from the start of the walker set-up, as
+  // the reference's calcInitTime (MixedEstimator.cpp:397)
+  const auto t_start = std::chrono::steady_clock::now();
+  const auto wall = [&]() {
+    return std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
+  };
   const int P = o->nprocs > 0 ? o->nprocs : 1;
   if (h->nwalk % P != 0) {
     h->err = "nwalk of the handle must be a multiple of nprocs";
@@ -116,6 +123,14 @@ int afqmc_run(afqmc_handle* h, const afqmc_run_opts* o, double* total_weights, d
   for (int w = 0; w < W; ++w) wsum_e += el[2 * w];
   total_weights[0] = (double)nwalk * P;
   total_energies[0] = wsum_e / total_weights[0] + delta;
+  if (block_eshift) {
+    for (int b = 0; b < nsweeps; ++b) block_eshift[b] = 0.0;
+    block_eshift[0] = total_energies[0];  // row 0 prints the initial energy in the eshift column
+  }
+  if (block_wall) {
+    for (int b = 0; b < nsweeps; ++b) block_wall[b] = 0.0;
+    block_wall[0] = wall();
+  }
 
   std::vector<afqmc_refrng*> rngs;
   for (int r = 0; r < P; ++r) rngs.push_back(afqmc_refrng_create(o->seed + (unsigned)r, nwalk));
@@ -156,7 +171,13 @@ int afqmc_run(afqmc_handle* h, const afqmc_run_opts* o, double* total_weights, d
       afqmc_graph* g = nullptr;
       afqmc_handle* hs[1] = {h};
       RUN(afqmc_graph_capture_blocks(hs, 1, nsteps, o->ortho_steps, o->comb, &g));
-      for (long b = 0; b < nblk && rc == AFQMC_OK; ++b) rc = afqmc_graph_launch(g);
+      for (long b = 0; b < nblk && rc == AFQMC_OK; ++b) {
+        rc = afqmc_graph_launch(g);
+        if (rc == AFQMC_OK && block_wall) {  // one wait per block, only when its time is asked for
+          rc = afqmc_sync(h);
+          if (b + 1 < nsweeps) block_wall[b + 1] = wall();
+        }
+      }
       afqmc_graph_destroy(g);
       if (rc != AFQMC_OK) {
         h->err = afqmc_graph_last_error();
@@ -169,10 +190,15 @@ int afqmc_run(afqmc_handle* h, const afqmc_run_opts* o, double* total_weights, d
     }
     std::vector<double> bw(nblk), be(nblk);
     RUN(afqmc_block_results(h, (int)nblk, bw.data(), be.data(), &nlarge));
+    double est = e_est;
     for (long b = 0; b < nblk; ++b)
       if (b + 1 < nsweeps) {
         total_weights[b + 1] = bw[b];
         total_energies[b + 1] = be[b];
+        // the eshift of the measured step: the estimate before this block's
+        // update and the block's total weight (MixedEstimator.cpp:474, :545)
+        if (block_eshift) block_eshift[b + 1] = est - 0.1 * log(bw[b] / ((double)nwalk * P)) / dt;
+        est = 0.9 * est + 0.1 * be[b];
       }
   }
   for (long step = o->device_blocks ? last : 1; step < last; ++step) {
@@ -214,6 +240,8 @@ int afqmc_run(afqmc_handle* h, const afqmc_run_opts* o, double* total_weights, d
       if (block < nsweeps) {
         total_weights[block] = total_weight;
         total_energies[block] = wE / total_weight;
+        if (block_eshift) block_eshift[block] = eshift;
+        if (block_wall) block_wall[block] = wall();
       }
       const double tb = wE / total_weight;
       if (step * dt < 10.0 || step < (long)o->burn_iter * nsteps) {
@@ -226,6 +254,14 @@ int afqmc_run(afqmc_handle* h, const afqmc_run_opts* o, double* total_weights, d
         avg_e = num / den;
       }
       e_est = 0.9 * e_est + 0.1 * tb;
+      // mixed 1-RDM of the measured walkers, after equilibration (MixedEstimator.cpp:491)
+      if (h->rdm_on && step * dt > 10.0 && step > (long)o->burn_iter * nsteps) {
+        afqmc::launch_rdm_accumulate(h, false);
+        if (cudaGetLastError() != cudaSuccess) {
+          h->err = "1-RDM accumulation launch failed";
+          return AFQMC_ERR_CUDA;
+        }
+      }
       if (o->comb) {
         RUN(afqmc_get_walkers(h, dets.data(), ovl.data(), nullptr));
         cum[0] = wts[0];
@@ -258,6 +294,16 @@ int afqmc_run(afqmc_handle* h, const afqmc_run_opts* o, double* total_weights, d
   }
   return AFQMC_OK;
 #undef RUN
+}
+
+int afqmc_run(afqmc_handle* h, const afqmc_run_opts* o, double* total_weights, double* total_energies,
+              afqmc_run_stats* stats) {
+  return run_impl(h, o, total_weights, total_energies, nullptr, nullptr, stats);
+}
+
+int afqmc_run_blocks(afqmc_handle* h, const afqmc_run_opts* o, double* total_weights, double* total_energies,
+                     double* block_eshift, double* block_wall, afqmc_run_stats* stats) {
+  return run_impl(h, o, total_weights, total_energies, block_eshift, block_wall, stats);
 }
 
 }  // extern "C"

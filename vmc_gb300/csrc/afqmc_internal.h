@@ -173,6 +173,12 @@ struct afqmc_handle {
   int cv_nslots = 4096, cv_den = 8;
   float cv_ymean = 0.f, cv_ystd = 1.f;
   struct afqmc_mlp* cv_mlp = nullptr;
+  // mixed 1-RDM estimator: running sums of sum_w w Re theta_w [nce*N] and of
+  // the weights (slot nce*N), per-chunk partial sums, trial orbitals on the host
+  bool rdm_on = false;
+  double* rdm_acc = nullptr;   // [nce*N + 1]
+  double* rdm_part = nullptr;  // [RDM_CHUNKS][nce*N + 1]
+  std::vector<double> phi_host;  // [nce][N] channel trial orbitals
 };
 
 namespace afqmc {
@@ -217,6 +223,10 @@ void split_rows(afqmc_handle* h, const float* src, long lds, int rows, int K, in
                 __nv_bfloat16* dst);
 void launch_local_energy_mixed(afqmc_handle* h);
 void launch_wait_probe(afqmc_handle* h);  // one bounded mbarrier wait that nothing completes
+// ---- mixed 1-RDM estimator (afqmc_rdm.cu) ----
+// add sum_w w Re theta_w of the live walkers to the running sums; gated: only
+// when the step counted on the device satisfies step dt > 10 and step > burn
+void launch_rdm_accumulate(afqmc_handle* h, bool gated);
 
 // error helper used by kernels' launchers
 bool check_launch(afqmc_handle* h, const char* what);

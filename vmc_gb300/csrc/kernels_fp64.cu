@@ -1033,19 +1033,25 @@ void launch_ortho_buffers(double2* psi, double2* qwork, double2* ovlp, int nwalk
 //       + 1/2 sum_{g < ncholEne} [(mult sum_s c_sg)^2 - mult sum_s sum_ij f_sg[i,j] f_sg[j,i]]
 // f_sg = rot_s[g] theta_s (n x n), c_sg = tr f_sg.  One CTA per (walker, g chunk).
 // ---------------------------------------------------------------------------
+// THS: the walker's theta staged in shared memory (when nce N complex fit
+// beside the f blocks); otherwise it is read from global memory, where the
+// CTA's repeated reads of the same walker hit L2
+template <bool THS>
 __global__ void k_energy(const double* __restrict__ theta, const double* __restrict__ rot,
                          double2* __restrict__ epart, int N, int nce, int Gene, int gper, int nechunk,
                          Channel c0, Channel c1, int nchan, int mult) {
   const int w = blockIdx.x;
   const int gs = blockIdx.y * gper, ge = min(Gene, gs + gper);
   extern __shared__ double2 sm[];
-  double2* th = sm;                                   // [nce*N]
-  double2* f = sm + (size_t)nce * N;                  // [nchan][nmax*nmax]
+  double2* th = sm;                                   // [nce*N] (THS)
+  double2* f = THS ? sm + (size_t)nce * N : sm;       // [nchan][nmax*nmax]
   const int nmax = max(c0.n, nchan > 1 ? c1.n : 0);
   const double* tre = theta + (size_t)(2 * w) * nce * N;
   const double* tim = tre + (size_t)nce * N;
-  for (int e = threadIdx.x; e < nce * N; e += blockDim.x) th[e] = make_double2(tre[e], tim[e]);
-  __syncthreads();
+  if (THS) {
+    for (int e = threadIdx.x; e < nce * N; e += blockDim.x) th[e] = make_double2(tre[e], tim[e]);
+    __syncthreads();
+  }
   double2 xacc = make_double2(0.0, 0.0);  // sum of f[i][j] f[j][i] over this thread's entries
   double2 coul = make_double2(0.0, 0.0);  // thread 0: sum_g (mult sum_s c_sg)^2
   for (int g = gs; g < ge; ++g) {
@@ -1056,11 +1062,20 @@ __global__ void k_energy(const double* __restrict__ theta, const double* __restr
       for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
         const int i = e / n, j = e % n;
         const double* r = rg + (size_t)(ch.col_off + i) * N;
-        const double2* t = th + (size_t)(ch.col_off + j) * N;
         double re = 0.0, im = 0.0;
-        for (int p = 0; p < N; ++p) {
-          re = fma(r[p], t[p].x, re);
-          im = fma(r[p], t[p].y, im);
+        if (THS) {
+          const double2* t = th + (size_t)(ch.col_off + j) * N;
+          for (int p = 0; p < N; ++p) {
+            re = fma(r[p], t[p].x, re);
+            im = fma(r[p], t[p].y, im);
+          }
+        } else {
+          const double* tr = tre + (size_t)(ch.col_off + j) * N;
+          const double* ti = tim + (size_t)(ch.col_off + j) * N;
+          for (int p = 0; p < N; ++p) {
+            re = fma(r[p], tr[p], re);
+            im = fma(r[p], ti[p], im);
+          }
         }
         f[s * nmax * nmax + i * n + j] = make_double2(re, im);
       }
@@ -1092,6 +1107,8 @@ __global__ void k_energy(const double* __restrict__ theta, const double* __restr
         make_double2(0.5 * (coul.x - mult * xacc.x), 0.5 * (coul.y - mult * xacc.y));
 }
 
+constexpr size_t ENERGY_SMEM_MAX = 220 * 1024;
+
 __global__ void k_energy_final(const double* __restrict__ theta, const double* __restrict__ h1phi,
                                const double2* __restrict__ epart, double2* __restrict__ eloc, int N, int nce,
                                int nechunk, int mult, double ecore) {
@@ -1114,12 +1131,19 @@ __global__ void k_energy_final(const double* __restrict__ theta, const double* _
 
 void launch_local_energy(afqmc_handle* h) {
   const int nmax = std::max(h->chan[0].n, h->nchan > 1 ? h->chan[1].n : 0);
-  const size_t smem = ((size_t)h->nce * h->N + (size_t)h->nchan * nmax * nmax) * sizeof(double2);
-  smem_optin(k_energy, 220 * 1024);
+  const size_t fbytes = (size_t)h->nchan * nmax * nmax * sizeof(double2);
+  const size_t smem = (size_t)h->nce * h->N * sizeof(double2) + fbytes;
   const int gper = (h->nchol_ene + h->nechunk - 1) / h->nechunk;
   dim3 grid(h->nwalk, h->nechunk);
-  k_energy<<<grid, 256, smem, h->stream>>>(h->theta, h->rot, h->epart, h->N, h->nce, h->nchol_ene, gper,
-                                           h->nechunk, h->chan[0], h->chan[1], h->nchan, h->mult);
+  if (smem <= ENERGY_SMEM_MAX) {
+    smem_optin(k_energy<true>, ENERGY_SMEM_MAX);
+    k_energy<true><<<grid, 256, smem, h->stream>>>(h->theta, h->rot, h->epart, h->N, h->nce, h->nchol_ene, gper,
+                                                   h->nechunk, h->chan[0], h->chan[1], h->nchan, h->mult);
+  } else {
+    smem_optin(k_energy<false>, ENERGY_SMEM_MAX);
+    k_energy<false><<<grid, 256, fbytes, h->stream>>>(h->theta, h->rot, h->epart, h->N, h->nce, h->nchol_ene,
+                                                      gper, h->nechunk, h->chan[0], h->chan[1], h->nchan, h->mult);
+  }
   k_energy_final<<<h->nwalk, 256, 0, h->stream>>>(h->theta, h->h1phi, h->epart, h->eloc, h->N, h->nce,
                                                   h->nechunk, h->mult, h->ecore);
   h->launches += 2;
