@@ -1,29 +1,38 @@
 #!/usr/bin/env python3
 """Walker-steps/s of the phaseless AFQMC step on one GB300 (one JSON line).
 
-Workload (default): norb=120, nalpha=nbeta=20, nchol=600 synthetic Hamiltonian
-(vmc_gb300/synthetic.py), UHF trial and UHF walkers, 2048 walkers, dt=0.005.
-One step = force bias, fields, VHS, propagator, overlap and weights of every
-walker, the walkers orthonormalised every 5 steps, and an energy estimate.
+Workload (default, the metric's configuration): norb=120, nalpha=nbeta=20,
+nchol=600 synthetic Hamiltonian (vmc_gb300/synthetic.py: Cholesky variance
+sigma_g^2 / norb, see `config.generator`), UHF trial and UHF walkers, 2048
+walkers, dt=0.005.  One step = force bias, fields, VHS, propagator, overlap and
+weights of every live walker, the walkers orthonormalised every 5 steps, an
+energy estimate every step, and the reference's comb reconfiguration every 50
+steps (its measurement cadence), which keeps the population alive.
 
-Forms, all on the same GPU and workload:
+`value` counts live walker-steps only (walkers with weight > 1e-8 when a step
+begins; dead walkers are not propagated), from the library's device counter,
+over the device time of the timed steps.
+
+Forms, all on the same GPU:
   headline ("value"): mixed precision + control variate, an energy estimate
-      every step (MLP for every walker + exact local energy of 1 walker in 8);
-  fp64_every_step: the plain FP64 form, exact local energy of every walker every
-      step (the metric's comparison);
-  mixed_every50 / fp64_every50: both forms at the reference's own measurement
-      cadence (every sampling.nsteps = 50 steps, exact energies).
-energy_error_mEh: |mixed-estimator energy of the mixed form - that of the FP64
-form| after 40 steps from the same walkers with identical fields (the FP64 form
-equals the FP64 oracle to 1e-10).
+      every step (network for every walker, exact local energy of 1 walker in
+      8, Horvitz-Thompson correction);
+  mixed_fp64_lu_qr: the same with the overlap inverse / log-determinant and the
+      walker QR in FP64 (block Gauss-Jordan, Householder);
+  fp64_every_step: the plain FP64 form, exact local energy of every walker
+      every step (the metric's comparison);
+  mixed_every50 / fp64_every50: both forms at the reference's cadence;
+  cfg1 / cfg3 / cfg4: the other workloads (see `forms`).
+energy_check: over 100 steps with identical fields, the headline estimator and
+the mixed form's exact energy against the FP64 form's exact energy.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 
---impl reference times the CPU restatement of the reference's path (the
-oracle port: the reference's own C++ needs Boost, HDF5 and MPI, absent here)
-on all host cores, same workload and metric.  Under torchrun every rank runs
-an independent replica; rank 0 prints value = walker-steps of all ranks / max
-time.
+--impl reference times the C++ restatement of the reference's walker step
+(oracle/cpu_step.cpp; the reference's own C++ needs Boost, HDF5 and MPI, absent
+here) on all host cores, same workload and metric.  Under torchrun every rank
+runs an independent replica; rank 0 prints value = walker-steps of all ranks /
+max time.
 """
 import argparse
 import json
@@ -43,6 +52,16 @@ METRIC = "AFQMC walker-steps/s, mixed vs FP64 on same GB300, at ≤0.1 mEh energ
 ORTHO_EVERY = 5
 REF_CADENCE = 50
 STAGES = ["fb", "fields", "vhs", "prop", "overlap", "weights", "ortho", "energy"]
+# the reference's published per-core rate at its rhf_rhf regression size
+# (N=13, 5/5 electrons, 64 Cholesky vectors; 20 walkers x 2499 steps in
+# 1.34078 s of propagation on a Xeon Gold 6254, tests/DQMC/rhf_rhf/afqmc.ref)
+REF_PUBLISHED_PER_CORE = 20 * 2499 / 1.34078
+GENERATOR = ("Cholesky entries N(0, sigma_g^2 / norb), sigma_g = 0.5 exp(-g/20): the workload text's variance "
+             "divided by norb, which keeps sum_g ||L_g||^2 near 10 (as the reference's H2O fixture) instead of "
+             "growing with norb; the FLOP count is unchanged")
+DTYPE = ("split-BF16 (3 passes, FP32 accumulation) force bias, VHS, propagator and exchange on tcgen05; overlap "
+         "matrix from exact BF16 slices (FP64-grade); double-FP32 (~48-bit) LU, FP32 theta; Cholesky-QR with FP32 "
+         "Gram/Cholesky/R^-1 and a compensated double-FP32 Q; FP64 weights, phases and determinant products")
 
 
 def parse():
@@ -66,8 +85,6 @@ def parse():
 def dist_env():
     return (int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")),
             int(os.environ.get("LOCAL_RANK", "0")))
-
-
 
 
 def fp32_nominal_tflops(sm_mhz=2070.0):
@@ -174,45 +191,80 @@ def peaks():
     return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
 
 
-def cpu_baseline(sysd, nwalk_sample=32, steps=4, seconds_cap=30.0, nchol_ene=None):
-    """The oracle port (numpy complex128 + the reference's FP32 VHS) on the host cores;
-    local energies with the same Cholesky truncation as the GPU run."""
+def host_threads():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def cpu_port_rate(sysd, nchol_ene, threads, walkers_per_thread=8, steps=10, energy_every=1):
+    """The C++ restatement of the reference's walker step (oracle/cpu_step.cpp:
+    the reference's FP32 VHS, FP64 elsewhere) on `threads` host threads, one
+    OpenMP thread per core standing in for one MPI rank per core, each with
+    `walkers_per_thread` walkers: (walker-steps/s with an exact energy every
+    `energy_every` steps, the same without energies, seconds, sample text)."""
     from oracle import afqmc_oracle as O
+    from oracle import cpu_port as C
     N, na, nb = sysd["norb"], sysd["nalpha"], sysd["nbeta"]
     oh = O.Hamiltonian(N, na, nb, sysd["ecore"], sysd["h1"], sysd["h1mod"], sysd["chol"])
     ot = O.Trial(oh, sysd["trial"], sysd["phi_a"], sysd["phi_b"])
+    rw = sysd["trial"] == "rhf"
     prop = O.Propagator(oh, ot.phi, 0.005, mode="ref")
-    wk = O.Walkers(oh, False, np.repeat(O._ref_dets(oh, ot.phi, False)[None], nwalk_sample, axis=0))
-    wk.overlaps = O.overlap(ot, wk)
-    rng = np.random.default_rng(0)
-    e0 = O.hf_energy(ot, oh, ot.phi, False).real
-    t0 = time.perf_counter()
-    done = 0
-    for st in range(1, steps + 1):
-        O.step(ot, oh, prop, wk, rng.standard_normal((nwalk_sample, oh.nchol)), e0, 100.0)
-        if st % ORTHO_EVERY == 0:
-            O.orthogonalize(wk)
-        done += nwalk_sample
-        if time.perf_counter() - t0 > seconds_cap:
-            break
-    t_step = (time.perf_counter() - t0) / done
-    te = time.perf_counter()
-    O.local_energy(ot, wk, oh, nchol_ene)
-    t_el = (time.perf_counter() - te) / nwalk_sample
-    per_ws = t_step + t_el  # energy every step, as the headline form
-    return {"value": 1.0 / per_ws, "unit": "walker-steps/s", "cores": os.cpu_count(), "kind": "port",
-            "sample": "%d walkers x %d steps of the same workload + one exact local energy per walker-step "
-                      "(oracle port: numpy complex128 with the reference's FP32 VHS, all BLAS threads)"
-                      % (nwalk_sample, done // nwalk_sample),
-            "every50_value": 1.0 / (t_step + t_el / REF_CADENCE)}
+    W = walkers_per_thread * threads
+    cw = C.CpuWalkers(oh, ot, prop, rw, W, nthreads=threads, nchol_ene=nchol_ene)
+    cw.set_walkers(np.repeat(O._ref_dets(oh, ot.phi, rw)[None], W, axis=0))
+    e0 = O.hf_energy(ot, oh, ot.phi, rw).real
+    t_step, t_qr, t_e, ws = cw.run_timed(steps, ORTHO_EVERY, energy_every, e0, max(100.0, W / 10.0))
+    cw.close()
+    total = t_step + t_qr + t_e
+    return (ws / total, ws / (t_step + t_qr), total,
+            "%d walkers (%d per thread) x %d steps of the same workload, QR every %d, exact local energy "
+            "(%d Cholesky vectors) every %d step(s)" % (W, walkers_per_thread, steps, ORTHO_EVERY, nchol_ene,
+                                                         energy_every))
 
 
-def make_walkers(A, sysd, form, device, nwalk=None):
+def cpu_calibration():
+    """The same C++ step at the reference's rhf_rhf regression size (its own
+    fixture: N=13, 5/5, 64 Cholesky vectors, RHF walkers, 20 walkers, one
+    thread), timed as the reference times its propagation (the step loop only),
+    beside the reference's published per-core rate."""
+    from oracle import afqmc_oracle as O
+    from oracle import cpu_port as C
+    from tests import refcases
+    c = refcases.load("rhf_rhf")
+    oh, ot, rw = c["ham"], c["trial"], c["rhf_walker"]
+    prop = O.Propagator(oh, c["ref_phi"], float(c["cfg"]["sampling"]["dt"]), mode="ref")
+    cw = C.CpuWalkers(oh, ot, prop, rw, 20, nthreads=1)
+    cw.set_walkers(np.repeat(O._ref_dets(oh, c["ref_phi"], rw)[None], 20, axis=0))
+    t_step, _, _, ws = cw.run_timed(1500, 20, 50, O.hf_energy(ot, oh, c["ref_phi"], rw).real)
+    cw.close()
+    rate = ws / t_step
+    return {"fixture": "rhf_rhf (N=13, 5/5, 64 Cholesky vectors, RHF walkers)", "port_per_core": rate,
+            "reference_published_per_core": REF_PUBLISHED_PER_CORE,
+            "reference_hardware": "Xeon Gold 6254 @ 3.10 GHz (tests/DQMC/rhf_rhf/afqmc.ref)",
+            "port_over_reference": rate / REF_PUBLISHED_PER_CORE,
+            "representative": bool(rate * 3.0 >= REF_PUBLISHED_PER_CORE)}
+
+
+def cpu_baseline(sysd, nchol_ene, threads=None):
+    threads = threads or host_threads()
+    v, v_noe, secs, sample = cpu_port_rate(sysd, nchol_ene, threads)
+    cal = cpu_calibration()
+    return {"value": v, "unit": "walker-steps/s", "cores": threads, "kind": "port", "sample": sample,
+            "every50_value": 1.0 / (1.0 / v_noe + (1.0 / v - 1.0 / v_noe) / REF_CADENCE),
+            "seconds": secs,
+            "code": "oracle/cpu_step.cpp: C++ restatement of the reference's walker step (FP32 VHS as the "
+                    "reference, FP64 elsewhere), g++ -O3 -fopenmp, one thread per core",
+            "calibration": cal}
+
+
+def make_walkers(A, sysd, form, device, nwalk=None, seed=20261203):
     N, na, nb = sysd["norb"], sysd["nalpha"], sysd["nbeta"]
     gh = A.Hamiltonian(N, na, nb, sysd["ecore"], sysd["h1"], sysd["h1mod"], sysd["chol"])
     gt = A.UHF(gh, sysd["phi_a"], sysd["phi_b"]) if sysd["trial"] == "uhf" else A.RHF(gh, sysd["phi_a"])
     return A.DQMCWalkers(gh, gt, nwalk or sysd["walkers"], sysd["trial"] == "rhf", 0.005, precision=form,
-                         device=device, seed=20261203)
+                         device=device, seed=seed)
 
 
 def cholesky_truncation(wk, G, threshold=1e-3):
@@ -232,11 +284,25 @@ def energy_all(A, wk):
     wk._check(A.lib().afqmc_local_energy(wk.h, None))
 
 
-def timed(A, wk, k0, K, energy, cv=None):
-    """K steps on the device; energy in {"cv", "every", "every50"}; returns (ms, launches, stage ms)."""
+class Comb:
+    """The reference's comb every REF_CADENCE steps (MixedEstimator.cpp:559-635),
+    on the device, with zetas from a seeded host generator."""
+
+    def __init__(self, seed=99):
+        self.rng = np.random.default_rng(seed)
+
+    def __call__(self, wk):
+        wk.comb(float(self.rng.random()))
+
+
+def timed(A, wk, k0, K, energy, cv=None, comb=None):
+    """K steps on the device; energy in {"cv", "every", "every50"}; the comb
+    every REF_CADENCE steps when given.  Returns (ms, launches, stage ms, live
+    walker-steps)."""
     wk.sync()
     wk.enable_timing(True)
     l0 = wk.launch_count()
+    n0 = wk.walker_steps()
     wk.timer_start()
     for k in range(k0, k0 + K):
         wk.propagate_phaseless(None)
@@ -246,80 +312,173 @@ def timed(A, wk, k0, K, energy, cv=None):
             cv.measure(tag=k, slot=k % 4096)
         elif energy == "every" or (k + 1) % REF_CADENCE == 0:
             energy_all(A, wk)
+        if comb is not None and (k + 1) % REF_CADENCE == 0:
+            comb(wk)
     ms = wk.timer_stop()
     launches = wk.launch_count() - l0
     stage = {s: wk.stage_time(s) for s in STAGES}
     wk.enable_timing(False)
-    return ms, launches, stage
+    live = wk.walker_steps() - n0
+    return ms, launches, stage, live
 
 
-def energy_error(A, sysd, device, tuned, nw=256, steps=40):
-    """Mixed vs FP64 form from the same walkers with identical host fields; the
-    mixed form runs the kernel variants the timed run uses (`tuned`)."""
+def energy_check(A, sysd, device, tuned, cv, nchol_ene, nw=256, steps=100):
+    """The energy error of the headline estimator.  From the same walkers and
+    with identical host fields (fixed eshift, QR every 5): per step the FP64
+    form's exact mixed energy sum_w w E_L / sum_w w, the mixed form's exact one,
+    and the mixed form's control-variate estimate (the trained network
+    attached to this handle; Horvitz-Thompson correction).  Reported: the mean
+    and largest |mixed exact - FP64| (the precision error, deterministic), and
+    the mean of (estimate - FP64) with its standard error over the steps (the
+    estimator's noise averages out; its mean is the bias plus the precision
+    error)."""
+    from vmc_gb300 import cv as CV
     rng = np.random.default_rng(11)
-    xs = [rng.standard_normal((nw, sysd["nchol"])) for _ in range(steps)]
-    out = {}
-    for form in ("mixed", "fp64"):
-        wk = make_walkers(A, sysd, form, device, nw)
-        if form == "mixed":
-            A.set_tuning(wk, **tuned)
-        e0 = wk.ham_and_overlap().real.mean()
-        for k in range(steps):
-            wk.propagate_phaseless(xs[k], e0)
+    wm = make_walkers(A, sysd, "mixed", device, nw)
+    A.set_tuning(wm, **tuned)
+    wf = make_walkers(A, sysd, "fp64", device, nw)
+    for w in (wm, wf):
+        w.set_nchol_ene(nchol_ene)
+    cv.attach(wm)
+    e0 = wf.ham_and_overlap().real.mean()
+    ef, em = [], []
+    for k in range(steps):
+        xi = rng.standard_normal((nw, sysd["nchol"]))
+        for w in (wm, wf):
+            w.propagate_phaseless(xi, e0)
             if (k + 1) % ORTHO_EVERY == 0:
-                wk.orthogonalize()
-        _, _, w = wk.get_det()
-        el = wk.ham_and_overlap().real
-        out[form] = (w * el).sum() / w.sum()
-        wk.close()
-    return abs(out["mixed"] - out["fp64"]) * 1e3, out
+                w.orthogonalize()
+        CV.measure(wm, tag=70000 + k, slot=k)
+        out = []
+        for w in (wf, wm):
+            _, _, wt = w.get_det()
+            el = w.ham_and_overlap().real
+            out.append((wt * el).sum() / wt.sum())
+        ef.append(out[0])
+        em.append(out[1])
+    r = CV.results(wm, steps)
+    wm.close()
+    wf.close()
+    ef, em = np.array(ef), np.array(em)
+    d_prec = (em - ef) * 1e3
+    d_cv = (r[:, 1] - ef) * 1e3
+    d_ratio = (r[:, 0] - ef) * 1e3
+    return {"walkers": nw, "steps": steps, "nchol_energy": nchol_ene,
+            "precision_error_mEh_mean": float(abs(d_prec.mean())), "precision_error_mEh_max": float(abs(d_prec).max()),
+            "estimate_minus_fp64_mEh_mean": float(d_cv.mean()),
+            "estimate_minus_fp64_mEh_stderr": float(d_cv.std(ddof=1) / np.sqrt(steps)),
+            "estimate_noise_mEh_per_step": float(d_cv.std(ddof=1)),
+            "ratio_form_minus_fp64_mEh_mean": float(d_ratio.mean()),
+            "within_0p1_mEh": bool(abs(d_prec).max() <= 0.1 and abs(d_cv.mean()) <= 0.1
+                                   + 3 * d_cv.std(ddof=1) / np.sqrt(steps)),
+            "estimator": "E_cv = [sum_w w f_w + sum_S pi_w^-1 w (E_w - f_w)] / sum_w w (Horvitz-Thompson)"}
 
 
-def main_multisystem(args, local):
-    """Uneven multi-system batch: 16 synthetic systems, norb ~ U[40, 200],
-    nocc = round(norb / 6), nchol = 5 norb, 256 walkers each, mixed form,
-    each system autotuned for its size class, all advanced by one CUDA graph
-    (10 steps + QR every 5 per replay)."""
-    from vmc_gb300 import afqmc as A
-    from vmc_gb300 import synthetic as S
-    systems = S.multi_system_batch()
+def train_cv(A, wk, hidden=256, n_eq=120, n_skip=20, epochs=20, seed=3):
+    """Equilibrate the walkers (device fields, QR every 5) collecting features
+    and exact energies of a stratified 1/8 subsample after step n_skip, then
+    train the network and attach it."""
+    from vmc_gb300.cv import ControlVariate
+    cv = ControlVariate(wk, hidden=hidden, den=8, seed=seed)
+    for k in range(n_eq):
+        wk.propagate_phaseless(None)
+        if (k + 1) % ORTHO_EVERY == 0:
+            wk.orthogonalize()
+        if k >= n_skip:
+            cv.collect()
+    loss, n = cv.train(epochs=epochs, batch=512, lr=1e-3)
+    return cv, loss, n
+
+
+def tune_cache():
     cache = os.environ.get("AFQMC_TUNE_CACHE", os.path.join(os.path.expanduser("~"), ".cache", "vmc_gb300",
                                                             "autotune.txt"))
     os.makedirs(os.path.dirname(cache), exist_ok=True)
+    return cache
+
+
+def form_single(A, sysd, device, precision, steps, energy, cv_train=None, nchol_ene=None):
+    """A workload's own timed line (autotuned kernels, device fields, QR every
+    5, the comb every 50): value over live walker-steps."""
+    W, G = sysd["walkers"], sysd["nchol"]
+    wk = make_walkers(A, sysd, precision, device)
+    tuned = None
+    if precision == "mixed":
+        tuned, _ = A.autotune(wk, tune_cache())
+    n_ene = nchol_ene or cholesky_truncation(wk, G)
+    wk.set_nchol_ene(n_ene)
+    e0 = wk.ham_and_overlap().real.mean()
+    wk.set_energy_estimate(e0, e0)
+    cv, info = None, {}
+    if energy == "cv":
+        n_eq, n_skip = cv_train
+        cv, loss, n = train_cv(A, wk, n_eq=n_eq, n_skip=n_skip)
+        info = {"cv_train_steps": n_eq, "cv_train_samples": n, "cv_train_mse_std_units": loss}
+    for k in range(3):
+        wk.propagate_phaseless(None)
+        if cv is not None:
+            cv.measure(tag=k, slot=k)
+    comb = Comb()
+    ms, launches, stage, live = timed(A, wk, 3, steps, energy, cv, comb)
+    wk.close()
+    N, na = sysd["norb"], sysd["nalpha"]
+    fl = flops_model(N, na, sysd["nbeta"], G)
+    out = {"workload": "norb=%d nalpha=nbeta=%d nchol=%d walkers=%d %s" % (N, na, G, W, sysd["trial"].upper()),
+           "form": precision + (" + control variate" if energy == "cv" else ""), "energy": energy,
+           "value": live / (ms / 1e3), "live_fraction": live / (W * steps), "ms_per_step": ms / steps,
+           "steps": steps, "nchol_energy": n_ene, "tuning": tuned, "gpu_launches": launches,
+           "achieved_tflops_algorithmic": fl["step"] * live / (ms / 1e3) / 1e12,
+           "stage_ms_per_step": {k: v / steps for k, v in stage.items()}}
+    out.update(info)
+    return out
+
+
+def form_multisystem(A, device, reps=3):
+    """Uneven multi-system batch: 16 synthetic systems, norb ~ U[40, 200],
+    nocc = round(norb / 6), nchol = 5 norb, 256 walkers each, mixed form, each
+    system autotuned for its size class, all advanced by one CUDA graph per
+    replay (10 steps + QR every 5; no energy in the timed region)."""
+    from vmc_gb300 import synthetic as S
+    systems = S.multi_system_batch()
     hs, flops = [], 0.0
     for sd in systems:
         n = sd["nalpha"]
         gh = A.Hamiltonian(sd["norb"], n, n, sd["ecore"], sd["h1"], sd["h1mod"], sd["chol"])
         gt = A.UHF(gh, sd["phi_a"], sd["phi_b"])
-        wk = A.DQMCWalkers(gh, gt, sd["walkers"], False, 0.005, precision="mixed", device=local, seed=7 + len(hs))
-        A.autotune(wk, cache)
+        wk = A.DQMCWalkers(gh, gt, sd["walkers"], False, 0.005, precision="mixed", device=device, seed=7 + len(hs))
+        A.autotune(wk, tune_cache())
         e0 = wk.ham_and_overlap().real.mean()
         wk.set_energy_estimate(e0, e0)
         hs.append(wk)
         flops += flops_model(sd["norb"], n, n, sd["nchol"])["step"] * sd["walkers"]
     g = A.StepGraph(hs, 10, ortho_every=5)
-    for _ in range(max(1, args.warmup // 10 + 1)):
-        g.launch()
-    reps = max(1, args.steps // 10)
+    g.launch()
     for h in hs:
         h.sync()
-    t0 = time.perf_counter()
+    n0 = sum(h.walker_steps() for h in hs)
     hs[0].timer_start()
     for _ in range(reps):
         g.launch()
     ms = hs[0].timer_stop()
     for h in hs:
         h.sync()
-    wall = time.perf_counter() - t0
+    live = sum(h.walker_steps() for h in hs) - n0
     W = sum(sd["walkers"] for sd in systems)
-    out = {"metric": METRIC, "value": W * 10 * reps / (ms / 1e3), "unit": "walker-steps/s", "n_gpus": 1,
-           "steps": 10 * reps, "warmup": args.warmup, "ms_per_step": ms / (10 * reps), "higher_is_better": True,
-           "scaling": "weak", "vs_baseline": None, "dtype": "bf16x3 / f32 / f64", "data": "synthetic",
-           "config": {"workload": "cfg3: 16 systems, norb %s, 256 walkers each, UHF, mixed form, one CUDA graph"
-                                  % sorted(sd["norb"] for sd in systems),
-                      "graph_nodes": g.nodes(), "ortho_every": 5, "energy": "none in the timed region"},
-           "achieved_tflops_algorithmic": flops * 10 * reps / (ms / 1e3) / 1e12, "wall_s": wall}
-    print(json.dumps(out))
+    out = {"workload": "16 systems, norb %s, 256 walkers each, UHF, mixed form, one CUDA graph"
+                       % sorted(sd["norb"] for sd in systems),
+           "value": live / (ms / 1e3), "live_fraction": live / (W * 10 * reps), "ms_per_step": ms / (10 * reps),
+           "graph_nodes": g.nodes(), "energy": "none in the timed region",
+           "achieved_tflops_algorithmic": flops * 10 * reps / (ms / 1e3) / 1e12}
+    g.close()
+    for h in hs:
+        h.close()
+    return out
+
+
+# DRAM bytes of one launch of the tensor-core propagator on this workload
+# (dram__bytes_read.sum + dram__bytes_write.sum of one ncu capture of k_prop_tc,
+# 2048 walkers x 2 spins); a recorded constant, refreshed with each capture
+PROP_TC_DRAM_BYTES = {"cfg2": 198.0e6 + 179.0e6}
 
 
 def main():
@@ -327,11 +486,8 @@ def main():
     rank, world, local = dist_env()
     if args.impl == "reference":
         return main_reference(args, rank, world)
-    if args.workload == "cfg3":
-        return main_multisystem(args, local)
     from vmc_gb300 import afqmc as A
     from vmc_gb300 import synthetic as S
-    from vmc_gb300.cv import ControlVariate
     if world > 1:
         import torch
         import torch.distributed as dist
@@ -342,25 +498,16 @@ def main():
     A.lib()
     A._bind_cv(A.lib())
 
-    # --- headline: mixed + control variate, energy estimate every step ---
+    # --- headline: mixed + control variate, energy estimate every step, comb every 50 ---
     wk = make_walkers(A, sysd, "mixed", local)
-    cache = os.environ.get("AFQMC_TUNE_CACHE", os.path.join(os.path.expanduser("~"), ".cache", "vmc_gb300",
-                                                            "autotune.txt"))
-    os.makedirs(os.path.dirname(cache), exist_ok=True)
-    tuned, tune_report = A.autotune(wk, cache)
+    tuned, tune_report = A.autotune(wk, tune_cache())
     nchol_ene = cholesky_truncation(wk, G)
     e0 = wk.ham_and_overlap().real.mean()
     wk.set_energy_estimate(e0, e0)
-    cv = ControlVariate(wk, hidden=256, den=8, seed=3)
     n_eq, n_skip = (25, 20) if args.profile else (120, 20)
-    for k in range(n_eq):  # equilibration; training data from steps 20.. (untimed)
-        wk.propagate_phaseless(None)
-        if (k + 1) % ORTHO_EVERY == 0:
-            wk.orthogonalize()
-        if k >= n_skip:
-            cv.collect()
-    cv_loss, cv_n = cv.train(epochs=1 if args.profile else 20, batch=512, lr=1e-3)
+    cv, cv_loss, cv_n = train_cv(A, wk, n_eq=n_eq, n_skip=n_skip, epochs=1 if args.profile else 20)
     k0 = n_eq
+    comb = Comb()
     for k in range(k0, k0 + args.warmup):
         wk.propagate_phaseless(None)
         cv.measure(tag=k, slot=k % 4096)
@@ -368,22 +515,26 @@ def main():
     if world > 1:
         dist.barrier()
     clk = Clocks(local)
-    ms, launches, stage = timed(A, wk, k0, args.steps, "cv", cv)
+    ms, launches, stage, live = timed(A, wk, k0, args.steps, "cv", cv, comb)
     clocks = clk.stop()
     if world > 1:
         import torch
         t = torch.tensor([ms], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = float(t.item())
-    value = W * args.steps * world / (ms / 1e3)
+        t = torch.tensor([live], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.SUM)
+        live = float(t.item())
+    value = live / (ms / 1e3)
+    live_fraction = live / (W * args.steps * world)
     k0 += args.steps
 
     if args.profile:
         print(json.dumps({"profile_run": True, "ms_per_step": ms / args.steps, "launches": launches,
                           "stage_ms_per_step": {k: v / args.steps for k, v in stage.items()}}))
         return
-    # end to end through the public API with host buffers: fields H2D, weights and the
-    # step's energy estimate D2H every step
+    # end to end through the public API with host buffers: the step's fields H2D,
+    # the weights and the step's energy estimate D2H, every step
     rng = np.random.default_rng(1)
     import torch
     xis = []
@@ -392,26 +543,44 @@ def main():
         t.numpy()[:] = rng.standard_normal((W, G))
         xis.append(t.numpy())
     wbuf = np.zeros(W)
-    ebuf = np.zeros(4)
+    ebuf = np.zeros(6)
     wk.sync()
+    n0 = wk.walker_steps()
     t0 = time.perf_counter()
     for k in range(args.steps):
         wk.propagate_phaseless(xis[k % 2])
         if (k + 1) % ORTHO_EVERY == 0:
             wk.orthogonalize()
         cv.measure(tag=k0 + k, slot=0)
+        if (k + 1) % REF_CADENCE == 0:
+            comb(wk)
         A.lib().afqmc_get_walkers(wk.h, None, None, wbuf.ctypes.data)
         A.lib().afqmc_cv_results(wk.h, ebuf.ctypes.data, 1)
     wk.sync()
     e2e_s = time.perf_counter() - t0
-    e2e = {"value": W * args.steps * world / e2e_s, "unit": "walker-steps/s",
-           "h2d_bytes_per_step": W * G * 8, "d2h_bytes_per_step": W * 8 + 32, "host_fields": "page-locked"}
+    e2e_live = wk.walker_steps() - n0
+    e2e = {"value": e2e_live * world / e2e_s, "unit": "walker-steps/s",
+           "h2d_bytes_per_step": W * G * 8, "d2h_bytes_per_step": W * 8 + 48, "host_fields": "page-locked",
+           "live_fraction": e2e_live / (W * args.steps)}
+    k0 += args.steps
 
     forms = {}
+    err = None
     if not args.quick:
-        # mixed at the reference cadence (energy every 50 steps)
-        ms_m50, _, _ = timed(A, wk, k0, REF_CADENCE, "every50")
-        forms["mixed_every50"] = {"value": W * REF_CADENCE / (ms_m50 / 1e3), "ms_per_step": ms_m50 / REF_CADENCE}
+        # mixed at the reference cadence (exact energy of every walker every 50 steps)
+        ms_m50, _, _, live_m50 = timed(A, wk, k0, REF_CADENCE, "every50", comb=comb)
+        forms["mixed_every50"] = {"value": live_m50 / (ms_m50 / 1e3), "ms_per_step": ms_m50 / REF_CADENCE,
+                                  "live_fraction": live_m50 / (W * REF_CADENCE)}
+        k0 += REF_CADENCE
+        # the mixed form with the overlap inverse / log-det and the QR in FP64
+        A.set_tuning(wk, ovl=2, qr="householder")
+        ms_f64, _, st_f64, live_f64 = timed(A, wk, k0, args.steps, "cv", cv, comb)
+        forms["mixed_fp64_lu_qr"] = {
+            "value": live_f64 / (ms_f64 / 1e3), "ms_per_step": ms_f64 / args.steps,
+            "live_fraction": live_f64 / (W * args.steps),
+            "precision": "as the headline, with the n x n overlap inverse and log-determinant by FP64 block "
+                         "Gauss-Jordan and the walker QR by FP64 Householder",
+            "stage_ms_per_step": {s: v / args.steps for s, v in st_f64.items()}}
         wk.close()
         # the plain FP64 form: warm-up 1 step, time 3 steps with an exact energy every step
         wf = make_walkers(A, sysd, "fp64", local)
@@ -420,17 +589,23 @@ def main():
         wf.set_energy_estimate(ef, ef)
         wf.propagate_phaseless(None)
         kf = 3
-        ms_f, _, stage_f = timed(A, wf, 1, kf, "every")
-        forms["fp64_every_step"] = {"value": W * kf / (ms_f / 1e3), "ms_per_step": ms_f / kf,
+        ms_f, _, stage_f, live_f = timed(A, wf, 1, kf, "every")
+        forms["fp64_every_step"] = {"value": live_f / (ms_f / 1e3), "ms_per_step": ms_f / kf,
+                                    "live_fraction": live_f / (W * kf),
                                     "stage_ms_per_step": {s: v / kf for s, v in stage_f.items()}}
         step_ms = (ms_f - stage_f["energy"]) / kf
-        forms["fp64_every50"] = {"value": W / ((step_ms + stage_f["energy"] / kf / REF_CADENCE) / 1e3),
+        lf = live_f / (W * kf)
+        forms["fp64_every50"] = {"value": W * lf / ((step_ms + stage_f["energy"] / kf / REF_CADENCE) / 1e3),
                                  "ms_per_step": step_ms + stage_f["energy"] / kf / REF_CADENCE}
         wf.close()
-        err_meh, err_e = energy_error(A, sysd, local, tuned)
+        err = energy_check(A, sysd, local, tuned, cv, nchol_ene)
+        # the other workloads, each on its own line of `forms`
+        forms["cfg1"] = {"fp64": form_single(A, S.workload("cfg1"), local, "fp64", 200, "every50"),
+                         "mixed": form_single(A, S.workload("cfg1"), local, "mixed", 200, "every50")}
+        forms["cfg3"] = form_multisystem(A, local)
+        forms["cfg4"] = form_single(A, S.workload("cfg4"), local, "mixed", args.steps, "cv", cv_train=(200, 0))
     else:
         wk.close()
-        err_meh, err_e = None, None
 
     fl = flops_model(N, na, nb, G)
     pk, src = peaks()
@@ -458,23 +633,26 @@ def main():
                          "bound_ms": bound_ms, "frac": bound_ms / t}
     dom = max(("vhs", "prop"), key=lambda s: stage[s])
     achieved = per_launch[dom] / (stage_roof[dom]["ms_per_launch"] / 1e3) / 1e12
-    # DRAM bytes per launch of the dominant kernel from one ncu capture of this workload
-    # (dram__bytes_read.sum + dram__bytes_write.sum; profiles/k_prop_tc_cfg2.md)
-    traffic = {"prop": 198.0e6 + 179.0e6}.get(dom) if args.workload == "cfg2" else None
+    traffic = PROP_TC_DRAM_BYTES.get(args.workload) if dom == "prop" else None
     roof = {"bound": "tensor", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-            "frac": achieved / peak, "traffic": traffic, "traffic_unit": "bytes per launch (ncu capture)",
+            "frac": achieved / peak, "traffic": traffic,
+            "traffic_source": "dram__bytes_read.sum + dram__bytes_write.sum per launch of k_prop_tc, one ncu "
+                              "capture of this workload (recorded constant)" if traffic else None,
             "peak_source": "%s bf16 sustained (MEASURED_PEAKS.json); algorithmic FLOPs of the stage per launch "
                            "/ its CUDA-event time; the largest tensor-core stage (every stage against the executed "
-                           "cost of its parts in stage_roofline; FP32 peak nominal)"
-                           % src,
+                           "cost of its parts in stage_roofline; FP32 peak nominal)" % src,
             "stage_roofline": stage_roof}
     out = {"metric": METRIC, "value": value, "unit": "walker-steps/s", "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
-           "vs_baseline": None, "dtype": "bf16x3 contractions / f32 propagator / f64 inverse, det, QR, weights",
-           "data": "synthetic (seeded generator, vmc_gb300/synthetic.py)",
-           "config": {"workload": "%s: norb=%d nalpha=nbeta=%d nchol=%d walkers=%d UHF trial and walkers dt=0.005"
-                                  % (args.workload, N, na, G, W),
-                      "form": "mixed + control variate (energy estimate every step, exact on 1/8)",
+           "vs_baseline": None, "dtype": DTYPE, "data": "synthetic (seeded generator, vmc_gb300/synthetic.py)",
+           "config": {"workload": "%s: norb=%d nalpha=nbeta=%d nchol=%d walkers=%d %s trial and walkers dt=0.005; "
+                                  "generator: Cholesky variance sigma_g^2/norb"
+                                  % (args.workload, N, na, G, W, sysd["trial"].upper()),
+                      "generator": GENERATOR,
+                      "form": "mixed + control variate (energy estimate every step: network for every walker, "
+                              "exact on 1/8, Horvitz-Thompson correction), comb every %d steps" % REF_CADENCE,
+                      "counted": "live walker-steps (weight > 1e-8 when the step begins), device counter",
+                      "live_fraction": live_fraction,
                       "ortho_every": ORTHO_EVERY, "fields": "device Philox",
                       "nchol_energy": nchol_ene, "autotune": tuned, "autotune_report": tune_report,
                       "l2": "inputs larger than L2 (walker state + split operands + VHS %.0f MB per step)"
@@ -483,11 +661,13 @@ def main():
                       "cv": {"train_samples": cv_n, "train_mse_std_units": cv_loss}},
            "forms": forms,
            "speedup_vs_fp64": (value / forms["fp64_every_step"]["value"]) if forms else None,
-           "energy_error_mEh": err_meh, "energy_check": err_e,
+           "energy_check": err,
+           "energy_error_mEh": (max(err["precision_error_mEh_max"], abs(err["estimate_minus_fp64_mEh_mean"]))
+                                if err else None),
            "stage_ms_per_step": {k: v / args.steps for k, v in stage.items()},
            "roofline": roof, "e2e": e2e, "gpu_launches": launches, "clocks": clocks}
     if rank == 0 and not args.no_cpu_baseline:
-        out["cpu_baseline"] = cpu_baseline(sysd, nchol_ene=nchol_ene)
+        out["cpu_baseline"] = cpu_baseline(sysd, nchol_ene)
     if rank == 0:
         print(json.dumps(out))
     if world > 1:
@@ -504,22 +684,29 @@ def reference_truncation(sysd, threshold=1e-3):
 
 
 def main_reference(args, rank, world):
+    """The reference's path on the host cores: the C++ restatement of its walker
+    step with all host threads, each step a bounded sample of the workload."""
     if rank != 0:
         return
     from vmc_gb300 import synthetic as S
     sysd = S.workload(args.workload)
-    cb = cpu_baseline(sysd, nwalk_sample=32, steps=max(2, min(args.steps, 6)), nchol_ene=reference_truncation(sysd))
+    nchol_ene = reference_truncation(sysd)
+    cb = cpu_baseline(sysd, nchol_ene)
     N, na, G, W = sysd["norb"], sysd["nalpha"], sysd["nchol"], sysd["walkers"]
     out = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": "walker-steps/s",
            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f64 (FP32 VHS as the reference)", "data": "synthetic",
-           "config": {"workload": "%s: norb=%d nalpha=nbeta=%d nchol=%d walkers=%d UHF trial and walkers dt=0.005"
-                                  % (args.workload, N, na, G, W),
-                      "ortho_every": ORTHO_EVERY, "energy": "exact local energy every step"},
+           "config": {"workload": "%s: norb=%d nalpha=nbeta=%d nchol=%d walkers=%d %s trial and walkers dt=0.005; "
+                                  "generator: Cholesky variance sigma_g^2/norb"
+                                  % (args.workload, N, na, G, W, sysd["trial"].upper()),
+                      "generator": GENERATOR,
+                      "ortho_every": ORTHO_EVERY, "energy": "exact local energy every step",
+                      "nchol_energy": nchol_ene},
            "cpu_baseline": cb,
            "e2e": {"value": cb["value"], "unit": "walker-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
            "note": "the reference's own C++ (DQMC/*.cpp) needs Boost, HDF5 and MPI, absent here; this arm times "
-                   "the oracle port of the same path on all host cores"}
+                   "the C++ restatement of the same path (oracle/cpu_step.cpp) on all host cores, calibrated "
+                   "against the reference's published per-core rate at its rhf_rhf size (cpu_baseline.calibration)"}
     print(json.dumps(out))
 
 

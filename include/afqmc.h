@@ -157,6 +157,11 @@ int afqmc_prop_info(afqmc_handle* h, double* mf, double* prop_constant, double* 
 int afqmc_enable_timing(afqmc_handle* h, int on);
 int afqmc_stage_time(afqmc_handle* h, const char* stage, double* ms);
 
+/* Walker-steps propagated since creation: the sum over steps of the walkers
+ * that were live (weight > 1e-8) when the step began; dead walkers are not
+ * propagated and not counted.  Synchronises the handle's stream. */
+int afqmc_walker_steps(afqmc_handle* h, double* propagated);
+
 /* Kernels launched by this handle since creation (device work items). */
 int afqmc_launch_count(const afqmc_handle* h, long* count);
 

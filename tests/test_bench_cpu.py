@@ -1,5 +1,7 @@
 """bench.py on the CPU: its work models, and the reference arm's JSON line
-(the oracle port timed on the host cores) on the smallest workload."""
+(the C++ restatement of the walker step timed on the host cores, with its
+calibration against the reference's published per-core rate) on the smallest
+workload."""
 import json
 import os
 import subprocess
@@ -36,6 +38,8 @@ def test_reference_arm_line():
     assert cb["kind"] in ("port", "reference") and cb["cores"] >= 1 and cb["value"] == line["value"]
     assert line["e2e"] == {"value": line["value"], "unit": "walker-steps/s", "h2d_bytes_per_step": 0,
                            "d2h_bytes_per_step": 0}
+    cal = cb["calibration"]
+    assert cal["port_per_core"] > 0 and abs(cal["reference_published_per_core"] - 37277.0) < 1.0
 
 
 def _undefined_globals(path):

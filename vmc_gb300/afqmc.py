@@ -344,6 +344,14 @@ class DQMCWalkers:
         self._check(lib().afqmc_stage_time(self.h, stage.encode(), ctypes.byref(ms)))
         return ms.value
 
+    def walker_steps(self):
+        """Walker-steps propagated so far (live walkers only; afqmc_walker_steps)."""
+        v = ctypes.c_double()
+        L = lib()
+        L.afqmc_walker_steps.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double)]
+        self._check(L.afqmc_walker_steps(self.h, ctypes.byref(v)))
+        return v.value
+
     def launch_count(self):
         c = ctypes.c_long()
         self._check(lib().afqmc_launch_count(self.h, ctypes.byref(c)))

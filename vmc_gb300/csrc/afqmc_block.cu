@@ -199,9 +199,10 @@ int afqmc_block_setup(afqmc_handle* h, int nprocs, int nsteps, double e_estimate
   if (h->nwalk % nprocs != 0) return fail_blk(h, AFQMC_ERR_ARG, "afqmc_block_setup: nwalk not a multiple of nprocs");
   {
     const int nmax = std::max(h->chan[0].n, h->nchan > 1 ? h->chan[1].n : 0);
-    const size_t smem = ((size_t)h->nce * h->N + (size_t)h->nchan * nmax * nmax) * sizeof(double2);
-    if (h->precision != AFQMC_PREC_MIXED && smem > 220 * 1024)
-      return fail_blk(h, AFQMC_ERR_UNSUPPORTED, "FP64 local energy: theta does not fit in shared memory");
+    const size_t fbytes = (size_t)h->nchan * nmax * nmax * sizeof(double2);
+    if (h->precision != AFQMC_PREC_MIXED && fbytes > 220 * 1024)
+      return fail_blk(h, AFQMC_ERR_UNSUPPORTED,
+                      "FP64 local energy: the n x n exchange blocks do not fit in shared memory");
   }
   cudaSetDevice(h->device);
   if (nzeta > 0) {

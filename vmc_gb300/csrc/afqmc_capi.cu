@@ -505,7 +505,7 @@ int afqmc_create(const afqmc_ham* ham, const afqmc_trial* trial, const afqmc_opt
   ALLOC(eloc, W);
   ALLOC(scal, (size_t)afqmc::S_NSLOTS);
   ALLOC(d_chunks, (size_t)h->nchunks);
-  ALLOC(wpart, 2 * (size_t)afqmc::WT_MAXPARTS);
+  ALLOC(wpart, 3 * (size_t)afqmc::WT_MAXPARTS);
   ALLOC(comb_cum, W);
   ALLOC(comb_idx, W);
   ALLOC(comb_ovl, W);
@@ -905,6 +905,14 @@ int afqmc_timer_stop(afqmc_handle* h, double* ms) {
   float t = 0.f;
   CK(cudaEventElapsedTime(&t, h->timer[0], h->timer[1]));
   *ms = t;
+  return AFQMC_OK;
+}
+
+int afqmc_walker_steps(afqmc_handle* h, double* propagated) {
+  if (!h || !propagated) return AFQMC_ERR_ARG;
+  cudaSetDevice(h->device);
+  CK(cudaMemcpyAsync(propagated, h->scal + afqmc::S_NLIVE, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
   return AFQMC_OK;
 }
 

@@ -45,6 +45,7 @@ enum {
   S_ESHIFT = 0, S_EEST = 1, S_SUMW = 2, S_NCAP = 3,
   S_AVGE = 4, S_AVGE_EQL = 5, S_NUM = 6, S_DEN = 7, S_NUM_EQL = 8, S_DEN_EQL = 9,
   S_DELTA = 10, S_NLARGE = 11, S_STEP0 = 12, S_BURN = 13, S_BLOCK = 14, S_NPROCS = 15, S_NZETA = 16,
+  S_NLIVE = 20,  // walker-steps propagated since the handle was created (live walkers, w > 1e-8)
   S_NSLOTS = 24
 };
 constexpr int BLK_MAX = 65536;  // block ring capacity (samples of one run)

@@ -831,9 +831,11 @@ __global__ void __launch_bounds__(WT_THREADS)
   const double sdt = sqrt(dt);
   double sumw = 0.0;
   double ncap = 0.0;
+  double nlive = 0.0;
   for (int w = blockIdx.x * WT_THREADS + threadIdx.x; w < W; w += gridDim.x * WT_THREADS) {
     double wt = weights[w];
     if (wt > 1.0e-8) {
+      nlive += 1.0;
       double2 on = det[2 * w];
       if (nchan > 1) on = cmul(on, det[2 * w + 1]);
       if (mult == 2) on = cmul(on, on);
@@ -854,24 +856,29 @@ __global__ void __launch_bounds__(WT_THREADS)
   }
   sumw = block_sum(sumw);
   ncap = block_sum(ncap);
+  nlive = block_sum(nlive);
   if (threadIdx.x == 0) {
-    part[2 * blockIdx.x] = sumw;
-    part[2 * blockIdx.x + 1] = ncap;
+    part[3 * blockIdx.x] = sumw;
+    part[3 * blockIdx.x + 1] = ncap;
+    part[3 * blockIdx.x + 2] = nlive;
   }
 }
 
 __global__ void k_weights_final(const double* __restrict__ part, int nparts, double* __restrict__ scal, double dt,
                                 double target, unsigned long long* __restrict__ stepp) {
-  double sumw = 0.0, ncap = 0.0;
+  double sumw = 0.0, ncap = 0.0, nlive = 0.0;
   for (int b = threadIdx.x; b < nparts; b += blockDim.x) {
-    sumw += part[2 * b];
-    ncap += part[2 * b + 1];
+    sumw += part[3 * b];
+    ncap += part[3 * b + 1];
+    nlive += part[3 * b + 2];
   }
   sumw = block_sum(sumw);
   ncap = block_sum(ncap);
+  nlive = block_sum(nlive);
   if (threadIdx.x == 0) {
     scal[S_SUMW] = sumw;
     scal[S_NCAP] += ncap;
+    scal[S_NLIVE] += nlive;
     scal[S_ESHIFT] = scal[S_EEST] - 0.1 * log(sumw / target) / dt;
     *stepp += 1;  // the device field stream's step counter (graph replays advance it)
   }

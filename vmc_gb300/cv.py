@@ -55,11 +55,30 @@ class ControlVariate:
                                          self.ymean, self.ystd, self.den))
         return loss, len(Ys)
 
+    def attach(self, walkers):
+        """Use the trained network, with its training set's scalings, on another
+        handle of the same system (mixed form, nwalk <= the network's batch)."""
+        L = A.lib()
+        walkers._check(L.afqmc_cv_attach(walkers.h, self.mlp.h, self.xmean.ctypes.data, self.xstd.ctypes.data,
+                                         self.ymean, self.ystd, self.den))
+
     def measure(self, tag, slot):
         self.wk._check(A.lib().afqmc_cv_measure(self.wk.h, int(tag), int(slot)))
 
     def results(self, nslots):
         """(nslots, 6): E_cv, E_cv (HT), E_sub (HT), E_sub (ratio), sum_w, sum_w (subsample)."""
-        out = np.zeros((nslots, 6))
-        self.wk._check(A.lib().afqmc_cv_results(self.wk.h, out.ctypes.data, int(nslots)))
-        return out
+        return results(self.wk, nslots)
+
+
+def measure(walkers, tag, slot):
+    """Control-variate measurement on a handle the network is attached to."""
+    walkers._check(A.lib().afqmc_cv_measure(walkers.h, int(tag), int(slot)))
+
+
+def results(walkers, nslots):
+    """(nslots, 6) control-variate results of a handle: E_cv (ratio correction),
+    E_cv (Horvitz-Thompson correction, exactly unbiased), E_sub (HT), E_sub
+    (ratio), sum of weights, sum of subsample weights."""
+    out = np.zeros((nslots, 6))
+    walkers._check(A.lib().afqmc_cv_results(walkers.h, out.ctypes.data, int(nslots)))
+    return out
