@@ -71,3 +71,10 @@ def test_two_ranks_match_single_process():
         assert np.allclose(r[8], ctot / 2 / nwalk)
     # a zero-weight walker is never selected
     assert 3 not in idx
+    # the moves: each rank receives exactly the foreign sources of its new
+    # walkers, once each, and sends what the other rank receives from it
+    s0, r0 = ranks.comb_moves(idx, nwalk, 2, 0)
+    s1, r1 = ranks.comb_moves(idx, nwalk, 2, 1)
+    assert np.array_equal(s0.get(1, []), r1.get(0, np.array([], int)) - 0 * nwalk)
+    assert np.array_equal(s1.get(0, []), r0.get(1, np.array([], int)) - nwalk)
+    assert sum(len(v) for v in r0.values()) == len(np.unique(idx[:nwalk][idx[:nwalk] >= nwalk]))

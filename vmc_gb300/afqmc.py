@@ -246,6 +246,12 @@ class DQMCWalkers:
         self._check(lib().afqmc_get_walkers(self.h, _ptr(d), _ptr(o), _ptr(w)))
         return self.from_serial(d), o, w
 
+    def weights(self):
+        """The walker weights alone (no determinant copy)."""
+        w = np.zeros(self.nwalk)
+        self._check(lib().afqmc_get_walkers(self.h, None, None, _ptr(w)))
+        return w
+
     def to_serial(self, d):
         N, na, nb = self.ham.norb, self.ham.nalpha, self.ham.nbeta
         a = d[:, :, :na]

@@ -31,7 +31,7 @@ class ControlVariate:
     def collect(self):
         """Features of the current walkers and exact E_L of a subsample (training data)."""
         feats = A.cv_features(self.wk)
-        _, _, w = self.wk.get_det()
+        w = self.wk.weights()
         idx = self.stratified()
         idx = idx[w[idx] > 0]
         if len(idx) == 0:

@@ -5,10 +5,11 @@ the sum of weights for the population-control shift (:472-475,
 MPI_Allreduce), the weighted energy sum at measurement (:535-538) and the comb
 reconfiguration (:559-635: MPI_Gather of weights, overlaps and dets to rank 0,
 systematic resampling with one uniform zeta from rank 0's generator,
-MPI_Scatter back, MPI_Bcast of the total weight).  These helpers do the same
-with torch.distributed collectives (NCCL between GPUs, gloo on CPU), one rank
-per GPU; every rank ends with the walkers the single-process comb over the
-concatenated population would give it.  Walker data stay in the reference's
+MPI_Scatter back, MPI_Bcast of the total weight).  These helpers give every
+rank the walkers the single-process comb over the concatenated population
+would give it, with torch.distributed (NCCL between GPUs, gloo on CPU), one
+rank per GPU: the weights are all-gathered, every rank computes the same
+resampling, and only the walkers that change rank move, point to point.  Walker data stay in the reference's
 serial layout (``DQMCWalkers.get_det``/``set_det``).
 """
 import numpy as np
@@ -37,11 +38,35 @@ def comb_indices(weights_all, zeta, nwalk, nprocs):
     return np.minimum(idx, len(weights_all) - 1), tot
 
 
+def comb_moves(idx, nwalk, nprocs, rank):
+    """The walker moves of one rank for the comb with source indices idx (every
+    rank computes the same idx from the gathered weights, so the moves need no
+    negotiation).  Returns (sends, recvs): sends[q] = this rank's local walker
+    indices that rank q's new walkers copy (each once), recvs[q] = the global
+    indices this rank copies from rank q (each once), both sorted."""
+    sends, recvs = {}, {}
+    mine = idx[rank * nwalk:(rank + 1) * nwalk]
+    for q in range(nprocs):
+        if q == rank:
+            continue
+        theirs = np.unique(idx[q * nwalk:(q + 1) * nwalk])
+        s = theirs[theirs // nwalk == rank] - rank * nwalk
+        if len(s):
+            sends[q] = s
+        rv = np.unique(mine[mine // nwalk == q])
+        if len(rv):
+            recvs[q] = rv
+    return sends, recvs
+
+
 def distributed_comb(dets, overlaps, weights, zeta, dist):
     """Comb over all ranks; returns this rank's new (dets, overlaps, weights).
 
     dets: (nwalk, L) complex (serial layout), overlaps (nwalk,) complex,
-    weights (nwalk,); zeta is used from rank 0 (broadcast)."""
+    weights (nwalk,); zeta is used from rank 0 (broadcast).  Only the weights
+    are gathered (nwalk P doubles); each walker chosen by another rank then
+    travels once, point to point, as one packed message per peer (its dets
+    and overlap), instead of every rank gathering every walker."""
     import torch
     P, r = dist.get_world_size(), dist.get_rank()
     nwalk = len(weights)
@@ -51,15 +76,36 @@ def distributed_comb(dets, overlaps, weights, zeta, dist):
     dist.all_gather(w_all, torch.as_tensor(np.asarray(weights, np.float64)))
     w_all = torch.cat(w_all).numpy()
     idx, tot = comb_indices(w_all, float(z.item()), nwalk, P)
-    # every rank contributes its walkers; the receivers pick their sources
-    d = torch.view_as_real(torch.as_tensor(np.ascontiguousarray(dets, np.complex128)))
-    o = torch.view_as_real(torch.as_tensor(np.ascontiguousarray(overlaps, np.complex128)))
-    d_all = [torch.zeros_like(d) for _ in range(P)]
-    o_all = [torch.zeros_like(o) for _ in range(P)]
-    dist.all_gather(d_all, d)
-    dist.all_gather(o_all, o)
-    d_all = torch.view_as_complex(torch.cat(d_all)).numpy()
-    o_all = torch.view_as_complex(torch.cat(o_all)).numpy()
+    d = np.ascontiguousarray(dets, np.complex128)
+    o = np.ascontiguousarray(overlaps, np.complex128)
+    L = d.shape[1]
+    sends, recvs = comb_moves(idx, nwalk, P, r)
+
+    def pack(rows):  # (n, 2 L + 2) doubles: the walker's dets, then its overlap
+        return np.concatenate([d[rows].view(np.float64), o[rows].view(np.float64).reshape(-1, 2)], axis=1)
+
+    reqs, bufs = [], {}
+    for q, rows in sends.items():
+        t = torch.from_numpy(np.ascontiguousarray(pack(rows)))
+        bufs[("s", q)] = t
+        reqs.append(dist.isend(t, dst=q))
+    for q, src in recvs.items():
+        t = torch.zeros((len(src), 2 * L + 2), dtype=torch.float64)
+        bufs[("r", q)] = t
+        reqs.append(dist.irecv(t, src=q))
+    for q in reqs:
+        q.wait()
     mine = idx[r * nwalk:(r + 1) * nwalk]
+    new_d = np.empty_like(d)
+    new_o = np.empty_like(o)
+    for k, s in enumerate(mine):
+        q = s // nwalk
+        if q == r:
+            new_d[k] = d[s - r * nwalk]
+            new_o[k] = o[s - r * nwalk]
+        else:
+            row = bufs[("r", q)].numpy()[np.searchsorted(recvs[q], s)]
+            new_d[k] = row[:2 * L].view(np.complex128)
+            new_o[k] = row[2 * L:].view(np.complex128)[0]
     new_w = np.full(nwalk, tot / P / nwalk)
-    return d_all[mine], o_all[mine], new_w
+    return new_d, new_o, new_w
