@@ -161,14 +161,15 @@ def test_above_128_orbitals_fp64(A):
     print(check_fp64(got, ref))
 
 
-@pytest.mark.parametrize("variant", ["chunked_cta", "chunked_cta_householder"])
+@pytest.mark.parametrize("variant", ["chunked_cta", "chunked_cta_householder", "tensor_cta"])
 def test_above_128_orbitals_mixed(A, variant):
     """N=160, n=36: FP32 column-chunked propagator, block Gauss-Jordan overlap.
     This system is not a benchmark workload and its energy bound follows from
     the per-result ones: with 72 electrons, |E_L| ~ 75 Eh and a spread of ~4 Eh
     over 12 walkers, the weight bound (1.8e-4) times the spread alone allows
     0.7 mEh; 0.3 mEh is asserted (0.11 measured)."""
-    t = dict(prop="chunked", ovl=2, qr="householder" if variant.endswith("householder") else "cholesky")
+    t = dict(prop="tensor" if variant.startswith("tensor") else "chunked", ovl=2,
+             qr="householder" if variant.endswith("householder") else "cholesky")
     got, ref = gpu_run(A, "n160", 12, 5, 2, "mixed", t)
     print(variant, check_mixed(got, ref, 72, 5, t["qr"] == "cholesky", e_bound_mEh=0.3))
 
@@ -179,10 +180,12 @@ def test_control_variate_system_fp64(A):
     print(check_fp64(got, ref))
 
 
-@pytest.mark.parametrize("variant", ["auto", "chunked_warp"])
+@pytest.mark.parametrize("variant", ["auto", "chunked_warp", "tensor"])
 def test_control_variate_system_mixed(A, variant):
-    """N=200, n=30, G=1000: the mixed form's default choices at this size, and
-    the FP32 column-chunked propagator with the warp-per-matrix LU."""
-    t = None if variant == "auto" else dict(prop="chunked", ovl=1, qr="cholesky")
+    """N=200, n=30, G=1000: the mixed form's default choices at this size, the
+    FP32 column-chunked propagator with the warp-per-matrix LU, and the
+    tensor-core propagator of streamed tiles."""
+    t = {"auto": None, "chunked_warp": dict(prop="chunked", ovl=1, qr="cholesky"),
+         "tensor": dict(prop="tensor", qr="cholesky")}[variant]
     got, ref = gpu_run(A, "n200", 8, 5, 3, "mixed", t)
     print(variant, check_mixed(got, ref, 60, 5, True))

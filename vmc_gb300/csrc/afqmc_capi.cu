@@ -181,7 +181,7 @@ void release(afqmc_handle* h) {
                   h->xc, h->cv_x, h->cv_idx, h->cv_esub, h->cv_f, h->cv_ms, h->cv_out, h->d_step, h->psi32,
                   h->pt_img, h->comb_cum, h->comb_idx, h->comb_ovl, h->blk, h->blk_zeta, h->wpart,
                   h->ovl_tau, h->ovl_bimg, h->ovl_M, h->theta32, h->mf32, h->h1phi32, h->pt_voff,
-                  h->rdm_acc, h->rdm_part};
+                  h->rdm_acc, h->rdm_part, h->pb_img, h->pb_scratch};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (h->host_pinned) cudaFreeHost(h->host_pinned);
@@ -490,6 +490,11 @@ int afqmc_create(const afqmc_ham* ham, const afqmc_trial* trial, const afqmc_opt
     if (N <= 128) {
       ALLOC(pt_img, (size_t)nsp * 2 * 128 * 256);
       ALLOC(pt_voff, (size_t)T);
+    } else if (afqmc::prop_tcb_supported(N)) {
+      const size_t ib = afqmc::prop_tcb_img_bytes(N);
+      h->pb_slots = (int)std::min<size_t>((size_t)std::max(h->nsm, 1), W * (size_t)h->nspV);
+      ALLOC(pb_img, (size_t)nsp * ib);
+      ALLOC(pb_scratch, (size_t)h->pb_slots * ib);
     }
     if (afqmc::ovl_tc_wanted(h)) {
       const size_t nm = std::max(h->chan[0].n, h->nchan > 1 ? h->chan[1].n : 0);

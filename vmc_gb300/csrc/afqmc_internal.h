@@ -158,6 +158,11 @@ struct afqmc_handle {
   double* blk_zeta = nullptr;   // [BLK_MAX]
   __nv_bfloat16* pt_img = nullptr;
   uint2* pt_voff = nullptr;  // [T] swizzled scatter offsets of the packed triangle (tensor-core propagator)
+  // tensor-core propagator for 128 < N <= 512: the B - I tile image per spin
+  // and one V-image scratch slot per persistent CTA
+  uint8_t* pb_img = nullptr;
+  uint8_t* pb_scratch = nullptr;
+  int pb_slots = 0;
   // tensor-core overlap matrices (exact BF16 slices): trial-orbital scales
   // [channel][BNP], the swizzled trial-slice images [channel][bytes], and M
   double* ovl_tau = nullptr;
@@ -208,6 +213,11 @@ bool setup_ovl_tc(afqmc_handle* h);
 void launch_overlap_m_tc(afqmc_handle* h);
 bool prop_tc_available(const afqmc_handle* h);
 void launch_propagate_tc(afqmc_handle* h);
+size_t prop_tcb_img_bytes(int N);  // one matrix's tile image, 128 < N <= 512
+bool prop_tcb_supported(int N);
+bool setup_prop_tcb(afqmc_handle* h);
+bool prop_tcb_available(const afqmc_handle* h);
+void launch_propagate_tcb(afqmc_handle* h);
 void launch_block_end(afqmc_handle* h, int comb);
 bool ortho_chol_available(const afqmc_handle* h);
 void launch_ortho_chol(afqmc_handle* h);

@@ -435,16 +435,23 @@ __global__ void __launch_bounds__(PT_THREADS, 1)
 }
 
 bool setup_prop_tc(afqmc_handle* h) {
-  if (h->N > 128 || !h->pt_img) return true;
+  if (h->N > 128) return setup_prop_tcb(h);
+  if (!h->pt_img) return true;
   dim3 grid(128 * PT_K / 256, h->nsp);
   k_pt_image<<<grid, 256, 0, h->stream>>>(h->expm32, h->pt_img, h->N);
   k_pt_voff<<<(h->T + 255) / 256, 256, 0, h->stream>>>(h->tri, h->pt_voff, h->T);
   return cudaGetLastError() == cudaSuccess;
 }
 
-bool prop_tc_available(const afqmc_handle* h) { return h->N <= 128 && h->pt_img != nullptr; }
+bool prop_tc_available(const afqmc_handle* h) {
+  return (h->N <= 128 && h->pt_img != nullptr) || prop_tcb_available(h);
+}
 
 void launch_propagate_tc(afqmc_handle* h) {
+  if (h->N > 128) {  // streamed tiles (kernels_prop_tcb.cu)
+    launch_propagate_tcb(h);
+    return;
+  }
   smem_optin(k_prop_tc, PT_SMEM);
   dim3 grid(h->nwalk, h->nspV);
   k_prop_tc<<<grid, PT_THREADS, PT_SMEM, h->stream>>>(h->psi, h->psi32, h->V32, h->pt_img, h->pt_voff, h->weights, h->N,
