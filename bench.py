@@ -326,7 +326,10 @@ def energy_check(A, sysd, device, wm, cv, nchol_ene, steps=100):
     """The energy error of the headline form, on the headline handle itself
     (its equilibrated walkers, the trained network attached).  Its walkers are
     copied into an FP64 handle; both then run `steps` steps with identical host
-    fields and a fixed eshift (QR every 5).  Per step: the FP64 form's exact
+    fields and a fixed eshift (QR every 5), at the production cadence: every
+    REF_CADENCE steps the comb reconfigures the mixed handle's walkers and the
+    FP64 handle restarts from them (a precision error accumulates over at most
+    REF_CADENCE steps, as between the reference's combs).  Per step: the FP64 form's exact
     mixed energy sum_w w E_L / sum_w w, the mixed form's exact one, the mixed
     form's control-variate estimate (Horvitz-Thompson and ratio corrections)
     and the plain 1/8 subsample estimate.  Reported: the precision error of
@@ -344,6 +347,7 @@ def energy_check(A, sysd, device, wm, cv, nchol_ene, steps=100):
     wf.set_det(d, overlaps=o, weights=w)
     e0 = float((w * wm.ham_and_overlap().real).sum() / w.sum())
     ef, em = [], []
+    zeta = np.random.default_rng(12)
     for k in range(steps):
         xi = rng.standard_normal((nw, sysd["nchol"]))
         for h in (wm, wf):
@@ -358,6 +362,10 @@ def energy_check(A, sysd, device, wm, cv, nchol_ene, steps=100):
             out.append((wt * el).sum() / wt.sum())
         ef.append(out[0])
         em.append(out[1])
+        if (k + 1) % REF_CADENCE == 0:
+            wm.comb(float(zeta.random()))
+            d, o, w = wm.get_det()
+            wf.set_det(d, overlaps=o, weights=w)
     r = CV.results(wm, steps)
     wf.close()
     ef, em = np.array(ef), np.array(em)

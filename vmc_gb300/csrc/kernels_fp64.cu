@@ -258,9 +258,21 @@ __global__ void __launch_bounds__(OW_WARPS * 32, (F32 && MB && NM <= 20) ? 7 : 1
   float2* ah = (float2*)wbase;   // mixed form: [n][n] high parts, then [n][n] low parts
   float2* al = ah + (size_t)nmax * nmax;
   int* perm = (int*)(wbase + (size_t)nmax * nmax * sizeof(double2));
+  // mixed form with an FP32 walker copy: M is formed in double-FP32 from the
+  // FP32 walker values and the trial orbitals split into FP32 pairs (staged
+  // as such, so the product loop does no FP64 work)
+  constexpr bool MDF = F32 && !MB;
+  float2* phs2 = (float2*)ow_raw;  // MDF: [n][N] (high, low) of the channel orbitals
   if (!MB) {
     const double* ph = phi + (size_t)ch.col_off * N;
-    for (int e = threadIdx.x; e < n * N; e += blockDim.x) phs[e] = ph[e];
+    for (int e = threadIdx.x; e < n * N; e += blockDim.x) {
+      if constexpr (MDF) {
+        const df32 d = df_from_double(ph[e]);
+        phs2[e] = make_float2(d.h, d.l);
+      } else {
+        phs[e] = ph[e];
+      }
+    }
     __syncthreads();
   }
   const int w = blockIdx.x * OW_WARPS + warp;
@@ -274,6 +286,51 @@ __global__ void __launch_bounds__(OW_WARPS * 32, (F32 && MB && NM <= 20) ? 7 : 1
       ah[e] = make_float2(v.x, v.z);
       al[e] = make_float2(v.y, v.w);
     }
+  } else if constexpr (MDF) {  // M = Phi^T psi, compensated: Dot2 on the high parts, the low parts in FP32
+    constexpr int OW_RI = NM / 4, OW_RJ = (NM + 7) / 8;
+    const int li = lane >> 3, lj = lane & 7;
+    const float2* ps32 = psi32 + (size_t)w * ncw * N + (size_t)ch.psi_off * N;
+    float sh[OW_RI][OW_RJ][2], sl[OW_RI][OW_RJ][2];
+#pragma unroll
+    for (int x = 0; x < OW_RI; ++x)
+#pragma unroll
+      for (int y = 0; y < OW_RJ; ++y)
+#pragma unroll
+        for (int c = 0; c < 2; ++c) sh[x][y][c] = sl[x][y][c] = 0.f;
+    for (int p = 0; p < N; ++p) {
+      float2 v[OW_RJ];
+#pragma unroll
+      for (int y = 0; y < OW_RJ; ++y) {
+        const int j = lj + 8 * y;
+        v[y] = j < n ? ps32[(size_t)j * N + p] : make_float2(0.f, 0.f);
+      }
+#pragma unroll
+      for (int x = 0; x < OW_RI; ++x) {
+        const int i = li + 4 * x;
+        const float2 f = i < n ? phs2[i * N + p] : make_float2(0.f, 0.f);
+#pragma unroll
+        for (int y = 0; y < OW_RJ; ++y) {
+#pragma unroll
+          for (int c = 0; c < 2; ++c) {
+            const float xv = c == 0 ? v[y].x : v[y].y;
+            const float pr = __fmul_rn(f.x, xv);
+            const float pe = fmaf(f.x, xv, -pr);  // f.x xv = pr + pe exactly
+            float t, e;
+            df_two_sum(sh[x][y][c], pr, t, e);
+            sh[x][y][c] = t;
+            sl[x][y][c] = fmaf(f.y, xv, __fadd_rn(sl[x][y][c], __fadd_rn(e, pe)));
+          }
+        }
+      }
+    }
+#pragma unroll
+    for (int x = 0; x < OW_RI; ++x)
+#pragma unroll
+      for (int y = 0; y < OW_RJ; ++y) {
+        const int i = li + 4 * x, j = lj + 8 * y;
+        if (i < n && j < n)
+          st_dfc(ah, al, i * n + j, {df_fast(sh[x][y][0], sl[x][y][0]), df_fast(sh[x][y][1], sl[x][y][1])});
+      }
   } else {  // M = Phi^T psi
     constexpr int OW_RI = NM / 4, OW_RJ = (NM + 7) / 8;
     const int li = lane >> 3, lj = lane & 7;
