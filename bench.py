@@ -22,7 +22,8 @@ Forms, all on the same GPU:
   fp64_every_step: the plain FP64 form, exact local energy of every walker
       every step (the metric's comparison);
   mixed_every50 / fp64_every50: both forms at the reference's cadence;
-  cfg1 / cfg3 / cfg4: the other workloads (see `forms`).
+  cfg1 / cfg3 / cfg4 / cfg5: the other workloads (see `forms`; cfg5 with its
+      energy error against the FP64 form).
 energy_check: over 100 steps with identical fields, the headline estimator and
 the mixed form's exact energy against the FP64 form's exact energy.
 
@@ -446,6 +447,43 @@ def form_single(A, sysd, device, precision, steps, energy, cv_train=None, nchol_
     return out
 
 
+def form_large(A, device, steps=50, nw_check=16, check_steps=10):
+    """The large-system workload (norb=400, nalpha=nbeta=60, nchol=2400, 1024
+    walkers): the mixed form timed at the reference's cadence (exact energy of
+    every walker and the comb every 50 steps), and its energy error against the
+    FP64 form on nw_check walkers after check_steps steps with identical host
+    fields (QR every 5), both from the same perturbed trial determinants."""
+    from vmc_gb300 import synthetic as S
+    sysd = S.workload("cfg5")
+    out = form_single(A, sysd, device, "mixed", steps, "every50")
+    rng = np.random.default_rng(21)
+    base = np.concatenate([sysd["phi_a"], sysd["phi_b"]], axis=1).astype(np.complex128)
+    d0 = base[None] + 0.02 * (rng.standard_normal((nw_check,) + base.shape)
+                              + 1j * rng.standard_normal((nw_check,) + base.shape))
+    xs = [rng.standard_normal((nw_check, sysd["nchol"])) for _ in range(check_steps)]
+    res = {}
+    for form in ("mixed", "fp64"):
+        wk = make_walkers(A, sysd, form, device, nw_check)
+        if form == "mixed":
+            A.set_tuning(wk, **(out["tuning"] or {}))
+        wk.set_nchol_ene(out["nchol_energy"])
+        wk.set_det(d0)
+        e0 = float(wk.ham_and_overlap().real.mean())
+        for k in range(check_steps):
+            wk.propagate_phaseless(xs[k], e0)
+            if (k + 1) % ORTHO_EVERY == 0:
+                wk.orthogonalize()
+        w = wk.weights()
+        el = wk.ham_and_overlap().real
+        res[form] = ((w * el).sum() / w.sum(), el)
+        wk.close()
+    out["energy_error_mEh"] = abs(res["mixed"][0] - res["fp64"][0]) * 1e3
+    out["energy_check"] = {"walkers": nw_check, "steps": check_steps, "e_fp64": res["fp64"][0],
+                           "e_mixed": res["mixed"][0],
+                           "max_walker_el_diff_mEh": float(np.abs(res["mixed"][1] - res["fp64"][1]).max() * 1e3)}
+    return out
+
+
 def form_multisystem(A, device, reps=3):
     """Uneven multi-system batch: 16 synthetic systems, norb ~ U[40, 200],
     nocc = round(norb / 6), nchol = 5 norb, 256 walkers each, mixed form, each
@@ -618,6 +656,7 @@ def main():
                          "mixed": form_single(A, S.workload("cfg1"), local, "mixed", 200, "every50")}
         forms["cfg3"] = form_multisystem(A, local)
         forms["cfg4"] = form_single(A, S.workload("cfg4"), local, "mixed", args.steps, "cv", cv_train=(200, 0))
+        forms["cfg5"] = form_large(A, local)
     else:
         wk.close()
 

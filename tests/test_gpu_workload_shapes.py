@@ -5,7 +5,10 @@ Shapes:
   * N=160, nalpha=nbeta=36, nchol=480: more than 128 orbitals and more than 32
     occupied orbitals per spin (column-chunked propagators, the block
     Gauss-Jordan overlap kernel);
-  * N=200, nalpha=nbeta=30, nchol=1000 (the control-variate workload's system).
+  * N=200, nalpha=nbeta=30, nchol=1000 (the control-variate workload's system);
+  * N=400, nalpha=nbeta=60, nchol=2400 (the large-system workload; one step of
+    two walkers: four row tiles in the tensor-core propagator, the block
+    Gauss-Jordan overlap, the FP64 energy reading theta from L2).
 
 Each case starts a small walker batch from perturbed trial determinants, runs
 the steps with identical host fields on the GPU and in the oracle (QR every 5
@@ -37,6 +40,8 @@ def system(name):
             s = S.make_system(160, 36, 480, 20261203 + 160, "uhf")
         elif name == "n200":
             s = S.workload("cfg4")
+        elif name == "n400":
+            s = S.workload("cfg5")
         else:
             raise ValueError(name)
         N, n = s["norb"], s["nalpha"]
@@ -126,6 +131,11 @@ def check_mixed(got, ref, n_occ, steps, qr_signs, e_bound_mEh=0.1):
     assert errs["w"] < 5e-7 * n_occ * steps, errs
     assert errs["ovl"] < 5e-7 * n_occ * steps, errs
     assert errs["el"] < 2e-6, errs
+    if e_bound_mEh is None:
+        # the bound the per-result ones imply: every E_L within 2e-6 of max
+        # |E_L|, the weights within their bound times the spread of E_L
+        e_bound_mEh = 1e3 * (2e-6 * np.abs(el).max() + 5e-7 * n_occ * steps * np.ptp(el.real))
+    errs["e_bound_mEh"] = e_bound_mEh
     assert errs["e_mEh"] < e_bound_mEh, errs
     return errs
 
@@ -189,3 +199,16 @@ def test_control_variate_system_mixed(A, variant):
          "tensor": dict(prop="tensor", qr="cholesky")}[variant]
     got, ref = gpu_run(A, "n200", 8, 5, 3, "mixed", t)
     print(variant, check_mixed(got, ref, 60, 5, True))
+
+
+def test_large_system_fp64(A):
+    """N=400, n=60, G=2400: one step of 2 walkers, FP64 form."""
+    got, ref = gpu_run(A, "n400", 2, 1, 4, "fp64")
+    print(check_fp64(got, ref))
+
+
+def test_large_system_mixed(A):
+    """N=400, n=60, G=2400: the same step in the mixed form with the
+    tensor-core propagator (4 row tiles, two column passes per spin)."""
+    got, ref = gpu_run(A, "n400", 2, 1, 4, "mixed", dict(prop="tensor"))
+    print(check_mixed(got, ref, 120, 1, False, e_bound_mEh=None))

@@ -41,7 +41,7 @@ def build(verbose=False, extra=()):
     with ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
         logs = list(ex.map(compile_one, zip(srcs, objs)))
     tmp = LIB + ".tmp%d" % os.getpid()
-    cmd = [nvcc] + ARCH + ["-shared", "-o", tmp] + objs
+    cmd = [nvcc] + ARCH + ["-shared", "-o", tmp] + objs + ["-lpthread"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s%s" % (r.stdout, r.stderr))

@@ -10,6 +10,7 @@
 #include <map>
 #include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "afqmc_internal.h"
@@ -308,17 +309,30 @@ int afqmc_create(const afqmc_ham* ham, const afqmc_trial* trial, const afqmc_opt
     const int ld = (beta && trial->kind == AFQMC_TRIAL_UHF) ? nb : na;
     for (int i = 0; i < ch.n; ++i)
       for (int p = 0; p < N; ++p) phi[(size_t)(ch.col_off + i) * N + p] = src[(size_t)p * ld + i];
-    for (int g = 0; g < G; ++g) {
-      const double* L = ham->chol + ((size_t)ch.lspin * G + g) * NN;
-      double* r = rot.data() + (size_t)g * h->nce * N;
-      for (int q = 0; q < N; ++q)
-        for (int i = 0; i < ch.n; ++i) {
-          const double a = phi[(size_t)(ch.col_off + i) * N + q];
-          if (a == 0.0) continue;
-          double* ri = r + (size_t)(ch.col_off + i) * N;
-          const double* Lq = L + (size_t)q * N;
-          for (int p = 0; p < N; ++p) ri[p] += a * Lq[p];
-        }
+    // G N^2 n multiply-adds (23 G at N = 400): the Cholesky vectors are split
+    // over host threads, each writing its own rows of rot
+    auto rotate = [&](int g0, int g1) {
+      for (int g = g0; g < g1; ++g) {
+        const double* L = ham->chol + ((size_t)ch.lspin * G + g) * NN;
+        double* r = rot.data() + (size_t)g * h->nce * N;
+        for (int q = 0; q < N; ++q)
+          for (int i = 0; i < ch.n; ++i) {
+            const double a = phi[(size_t)(ch.col_off + i) * N + q];
+            if (a == 0.0) continue;
+            double* ri = r + (size_t)(ch.col_off + i) * N;
+            const double* Lq = L + (size_t)q * N;
+            for (int p = 0; p < N; ++p) ri[p] += a * Lq[p];
+          }
+      }
+    };
+    const double work = (double)G * N * N * ch.n;
+    const int nthr = work < 5e7 ? 1 : (int)std::max(1u, std::min(32u, std::thread::hardware_concurrency()));
+    if (nthr == 1) {
+      rotate(0, G);
+    } else {
+      std::vector<std::thread> pool;
+      for (int t = 0; t < nthr; ++t) pool.emplace_back(rotate, (int)((long)G * t / nthr), (int)((long)G * (t + 1) / nthr));
+      for (auto& th : pool) th.join();
     }
     const double* h1s = ham->h1 + (size_t)ch.lspin * NN;
     for (int i = 0; i < ch.n; ++i)

@@ -243,7 +243,7 @@ __global__ void __launch_bounds__(OW_WARPS * 32, (F32 && MB && NM <= 20) ? 7 : 1
                  double* __restrict__ theta, float* __restrict__ theta32, double2* __restrict__ det,
                  const double* __restrict__ weights, int W, int N, int ncw, int nce, Channel c0, Channel c1,
                  int only_live, int nmax, const float4* __restrict__ mbuf, __nv_bfloat16* __restrict__ thetaB,
-                 int kf_pad) {
+                 int kf_pad, int m_from32) {
   static_assert(F32 || !MB, "M formed beforehand only in the mixed form");
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int s = blockIdx.y;
@@ -258,15 +258,17 @@ __global__ void __launch_bounds__(OW_WARPS * 32, (F32 && MB && NM <= 20) ? 7 : 1
   float2* ah = (float2*)wbase;   // mixed form: [n][n] high parts, then [n][n] low parts
   float2* al = ah + (size_t)nmax * nmax;
   int* perm = (int*)(wbase + (size_t)nmax * nmax * sizeof(double2));
-  // mixed form with an FP32 walker copy: M is formed in double-FP32 from the
-  // FP32 walker values and the trial orbitals split into FP32 pairs (staged
-  // as such, so the product loop does no FP64 work)
-  constexpr bool MDF = F32 && !MB;
+  // mixed form above 128 orbitals (m_from32): M is formed in double-FP32 from
+  // the FP32 walker values and the trial orbitals split into FP32 pairs
+  // (staged as such, so the product loop does no FP64 work).  Up to 128
+  // orbitals M comes from the FP64 walker, as the tensor-core overlap forms
+  // it, so the two choices give the same overlap for any walker.
+  const bool MDF = F32 && !MB && m_from32;
   float2* phs2 = (float2*)ow_raw;  // MDF: [n][N] (high, low) of the channel orbitals
   if (!MB) {
     const double* ph = phi + (size_t)ch.col_off * N;
     for (int e = threadIdx.x; e < n * N; e += blockDim.x) {
-      if constexpr (MDF) {
+      if (MDF) {
         const df32 d = df_from_double(ph[e]);
         phs2[e] = make_float2(d.h, d.l);
       } else {
@@ -286,7 +288,7 @@ __global__ void __launch_bounds__(OW_WARPS * 32, (F32 && MB && NM <= 20) ? 7 : 1
       ah[e] = make_float2(v.x, v.z);
       al[e] = make_float2(v.y, v.w);
     }
-  } else if constexpr (MDF) {  // M = Phi^T psi, compensated: Dot2 on the high parts, the low parts in FP32
+  } else if (MDF) {  // M = Phi^T psi, compensated: Dot2 on the high parts, the low parts in FP32
     constexpr int OW_RI = NM / 4, OW_RJ = (NM + 7) / 8;
     const int li = lane >> 3, lj = lane & 7;
     const float2* ps32 = psi32 + (size_t)w * ncw * N + (size_t)ch.psi_off * N;
@@ -599,7 +601,7 @@ void launch_overlap_theta(afqmc_handle* h, bool only_live) {
     k_overlap_lu<F, NMV, MBV><<<grid, OW_WARPS * 32, smem, h->stream>>>(                                     \
         h->psi, h->psi32, h->phi, h->theta, h->theta32, h->det, h->weights, h->nwalk, h->N, h->ncw, h->nce,  \
         h->chan[0],                                                                                          \
-        h->chan[1], only_live ? 1 : 0, nmax, h->ovl_M, F ? h->thetaB : nullptr, h->kf_pad);                   \
+        h->chan[1], only_live ? 1 : 0, nmax, h->ovl_M, F ? h->thetaB : nullptr, h->kf_pad, h->N > 128 ? 1 : 0); \
   }
 #define OW_NM(F, MBV)                          \
   switch (nm) {                                \
