@@ -301,7 +301,8 @@ int afqmc_autotune(afqmc_handle* h, const char* cache_path, char* report, int re
 int afqmc_tuning(const afqmc_handle* h, int* bn_fb, int* bn_vhs, int* prop, int* ovl, int* qr);
 /* Set the choices directly (a value <= 0 keeps the current one).  bn_*: 64, 128
  * or 256; prop: 1 V in shared memory (N <= 128), 2 column-chunked, 3 tensor
- * core (N <= 128); ovl: 1 warp per matrix, 2 CTA per matrix, 3 warp per
+ * core (N <= 512; streamed tiles above 128), 4 tensor core with the walker
+ * operand stored MN-major (N <= 128); ovl: 1 warp per matrix, 2 CTA per matrix, 3 warp per
  * matrix with M = Phi^T psi formed on the tensor cores from exact BF16 slices
  * (mixed form, N <= 128, n <= 32; FP64-grade); qr (walker
  * orthonormalisation): 1 Householder with the reference's (Eigen's) column

@@ -129,10 +129,44 @@ def test_energy_error_tensor_propagator(A):
     assert abs(e_g - e_o) < 1e-4, (e_g, e_o)
 
 
-def test_tensor_choice_rejected_when_unavailable(A):
-    s = S.make_system(136, 4, 40, 4646, "uhf")
-    gh = A.Hamiltonian(136, 4, 4, s["ecore"], s["h1"], s["h1mod"], s["chol"])
-    gt = A.UHF(gh, s["phi_a"][:, :4], s["phi_b"][:, :4])
-    wk = A.DQMCWalkers(gh, gt, 8, False, 0.005, precision="mixed")
-    with pytest.raises(Exception):
-        A.set_tuning(wk, prop="tensor")
+def test_tensor_choice_limits(A):
+    """The MN-major variant covers N <= 128 and the tensor-core choice N <= 512
+    (streamed tiles above 128); beyond them the choice is refused."""
+    for N, tensor_ok in ((136, True), (520, False)):
+        s = S.make_system(N, 4, 40, 4646, "uhf")
+        gh = A.Hamiltonian(N, 4, 4, s["ecore"], s["h1"], s["h1mod"], s["chol"])
+        gt = A.UHF(gh, s["phi_a"][:, :4], s["phi_b"][:, :4])
+        wk = A.DQMCWalkers(gh, gt, 8, False, 0.005, precision="mixed")
+        with pytest.raises(Exception):
+            A.set_tuning(wk, prop="tensor_mn")
+        if tensor_ok:
+            A.set_tuning(wk, prop="tensor")
+        else:
+            with pytest.raises(Exception):
+                A.set_tuning(wk, prop="tensor")
+        wk.close()
+
+
+@pytest.mark.parametrize("name", ["uhf", "rhf", "wide", "n128"])
+def test_mn_major_walker_operand_equals_k_major(A, name):
+    """The propagator with the walker operand stored MN-major (16-byte chunk
+    stores) forms the same BF16 splits, issues the same MMAs in the same order
+    and sums the same FP32 values as the K-major one: the steps are equal."""
+    oh, ot, rw = system(name)
+    W = 96
+    dets = start_dets(oh, ot, rw, W, 12)
+    w0 = np.ones(W)
+    w0[::5] = 0.0
+    xi = np.random.default_rng(13).standard_normal((W, oh.nchol))
+    e0 = O.hf_energy(ot, oh, ot.phi, rw).real
+    out = {}
+    for prop in ("tensor", "tensor_mn"):
+        wk = walkers(A, oh, ot, rw, W, prop)
+        wk.set_det(dets, weights=w0)
+        for _ in range(3):
+            wk.propagate_phaseless(xi, e0)
+        out[prop] = wk.get_det()
+        wk.close()
+    (d3, o3, w3), (d4, o4, w4) = out["tensor"], out["tensor_mn"]
+    assert rel(d4, d3) <= 1e-12 and rel(w4, w3) <= 1e-12, (rel(d4, d3), rel(w4, w3))
+    assert np.array_equal(d4[::5], dets[::5])

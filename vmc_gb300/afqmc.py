@@ -654,7 +654,7 @@ def autotune(wk, cache_path=None):
             buf.value.decode())
 
 
-PROP_VARIANTS = {"smem": 1, "chunked": 2, "tensor": 3}
+PROP_VARIANTS = {"smem": 1, "chunked": 2, "tensor": 3, "tensor_mn": 4}
 QR_VARIANTS = {"householder": 1, "cholesky": 2}
 
 

@@ -133,7 +133,8 @@ struct afqmc_handle {
   int nchunks32 = 0;
   CUtensorMap tm_rot, tm_LT[2];
   CUtensorMap tm_theta_bn[3], tm_x_bn[3];  // B operands with box heights 64, 128, 256
-  // autotuned choices (afqmc_autotune): GEMM N-tiles; propagator 0 auto / 1 SMEM / 2 chunked / 3 tcgen05;
+  // autotuned choices (afqmc_autotune): GEMM N-tiles; propagator 0 auto / 1 SMEM / 2 chunked / 3 tcgen05 /
+  // 4 tcgen05 with the walker operand MN-major (N <= 128);
   // overlap 0 auto / 1 warp per matrix / 2 block per matrix
   int tune_bn_fb = 128, tune_bn_vhs = 128, tune_prop = 0, tune_ovl = 0;
   int tune_qr = 0;  // walker QR: 0 auto (Cholesky-QR in the mixed form when it fits), 1 Householder, 2 Cholesky-QR
@@ -213,6 +214,8 @@ bool setup_ovl_tc(afqmc_handle* h);
 void launch_overlap_m_tc(afqmc_handle* h);
 bool prop_tc_available(const afqmc_handle* h);
 void launch_propagate_tc(afqmc_handle* h);
+bool prop_tc2_available(const afqmc_handle* h);  // N <= 128, MN-major X operand
+void launch_propagate_tc2(afqmc_handle* h);
 size_t prop_tcb_img_bytes(int N);  // one matrix's tile image, 128 < N <= 512
 bool prop_tcb_supported(int N);
 bool setup_prop_tcb(afqmc_handle* h);

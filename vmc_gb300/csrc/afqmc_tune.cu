@@ -101,15 +101,17 @@ int afqmc_autotune(afqmc_handle* h, const char* cache_path, char* report, int re
     const size_t bytes = (size_t)h->nwalk * h->ncw * h->N * sizeof(double2);
     cudaMemcpyAsync(h->qwork, h->psi, bytes, cudaMemcpyDeviceToDevice, h->stream);
     best = 1e30f;
-    const int cands[3] = {3, 1, 2};
+    const int cands[4] = {4, 3, 1, 2};
     for (int c : cands) {
-      if ((c == 1 && h->N > 128) || (c == 3 && !afqmc::prop_tc_available(h))) continue;
+      if ((c == 1 && h->N > 128) || (c == 3 && !afqmc::prop_tc_available(h)) ||
+          (c == 4 && !afqmc::prop_tc2_available(h)))
+        continue;
       h->tune_prop = c;
       const float t = time_ms(h, [&] {
         afqmc::launch_propagate_mixed(h);
         cudaMemcpyAsync(h->psi, h->qwork, bytes, cudaMemcpyDeviceToDevice, h->stream);
       }, 2);
-      rep << "prop" << (c == 1 ? "_smem" : c == 2 ? "_chunk" : "_tc") << "=" << t << "ms ";
+      rep << "prop" << (c == 1 ? "_smem" : c == 2 ? "_chunk" : c == 3 ? "_tc" : "_tc_mn") << "=" << t << "ms ";
       if (t < best) { best = t; h->tune_prop_best = c; }
     }
     h->tune_prop = h->tune_prop_best;
@@ -151,9 +153,10 @@ int afqmc_set_tuning(afqmc_handle* h, int bn_fb, int bn_vhs, int prop, int ovl, 
   if (!h) return AFQMC_ERR_ARG;
   auto bn_ok = [](int b) { return b <= 0 || b == 64 || b == 128 || b == 256; };
   const bool mixed = h->precision == AFQMC_PREC_MIXED;
-  if (!bn_ok(bn_fb) || !bn_ok(bn_vhs) || prop > 3 || ovl > 3 || ((bn_fb > 0 || bn_vhs > 0 || prop > 0) && !mixed) ||
+  if (!bn_ok(bn_fb) || !bn_ok(bn_vhs) || prop > 4 || ovl > 3 || ((bn_fb > 0 || bn_vhs > 0 || prop > 0) && !mixed) ||
       (ovl == 3 && !afqmc::ovl_tc_available(h)) ||
-      ((prop == 1) && h->N > 128) || (prop == 3 && !afqmc::prop_tc_available(h)) || qr > 2 ||
+      ((prop == 1) && h->N > 128) || (prop == 3 && !afqmc::prop_tc_available(h)) ||
+      (prop == 4 && !afqmc::prop_tc2_available(h)) || qr > 2 ||
       (qr == 2 && !afqmc::ortho_chol_available(h))) {
     h->err = "afqmc_set_tuning: choice not available for this handle";
     return AFQMC_ERR_ARG;

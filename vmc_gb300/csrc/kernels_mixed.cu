@@ -574,6 +574,10 @@ __global__ void __launch_bounds__(256, 1)
 }
 
 void launch_propagate_mixed(afqmc_handle* h) {
+  if (h->tune_prop == 4 && prop_tc2_available(h)) {
+    launch_propagate_tc2(h);
+    return;
+  }
   if (h->tune_prop == 3 && prop_tc_available(h)) {
     launch_propagate_tc(h);
     return;

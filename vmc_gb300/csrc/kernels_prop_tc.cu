@@ -459,4 +459,269 @@ void launch_propagate_tc(afqmc_handle* h) {
   h->launches++;
 }
 
+
+// ---------------------------------------------------------------------------
+// The same propagator with the B operand (the walker's columns X) MN-major:
+// element (B row n, K = orbital p) at
+//   (n / 64) * 16 KB + (p / 8) * 1 KB + (p % 8) * 128 B + chunk ((n % 64) / 8 XOR p % 8) * 16 B + (n % 8) * 2 B
+// (128-byte swizzle; the descriptor's leading byte offset is the 16 KB between
+// 64-row groups, its stride byte offset the 1 KB between groups of 8 K
+// positions).  A thread owns one K position (orbital p = TMEM lane) and whole
+// 8-row chunks of B rows, so it writes its part of X as 16-byte vector stores
+// of packed BF16 pairs (a chunk of 8 values: 4 conversions per half and 2
+// stores) instead of 16 two-byte stores.  The 10 chunks of an 80-row pass are
+// split 2-3-2-3 over the four warps that share each TMEM lane quadrant.
+// ---------------------------------------------------------------------------
+constexpr int P2_B_HALF = 2 * 16384;   // two 64-row groups x K = 128
+constexpr int P2_SMEM = 2 * PT_A_BYTES + 2 * P2_B_HALF + 64 + 1024;
+constexpr int P2_MAXCH = 3;            // 8-row chunks per thread (10 over 4 groups)
+
+__device__ __forceinline__ uint32_t p2_chunk_off(int c, int p) {
+  return (uint32_t)((c >> 3) * 16384 + (p >> 3) * 1024 + (p & 7) * 128 + (((c & 7) ^ (p & 7)) << 4));
+}
+
+__device__ __forceinline__ uint32_t p2_pack_bf16(float a, float b) {
+  const __nv_bfloat162 v = __floats2bfloat162_rn(a, b);
+  return *reinterpret_cast<const uint32_t*>(&v);
+}
+
+// 8 consecutive B rows (chunk c) at K = p: split BF16, two 16-byte stores
+__device__ __forceinline__ void p2_store_chunk(uint8_t* sB, int c, int p, const float* v) {
+  uint32_t h[4], l[4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    h[i] = p2_pack_bf16(v[2 * i], v[2 * i + 1]);
+    const __nv_bfloat162 hb = *reinterpret_cast<const __nv_bfloat162*>(&h[i]);
+    l[i] = p2_pack_bf16(v[2 * i] - __low2float(hb), v[2 * i + 1] - __high2float(hb));
+  }
+  const uint32_t o = p2_chunk_off(c, p);
+  *(uint4*)(sB + o) = make_uint4(h[0], h[1], h[2], h[3]);
+  *(uint4*)(sB + P2_B_HALF + o) = make_uint4(l[0], l[1], l[2], l[3]);
+}
+
+template <bool CPLX>
+__device__ __forceinline__ void p2_issue(uint32_t tmem, uint8_t* sA, uint8_t* sB, int nc) {
+  const uint32_t idesc = tc::idesc_bf16(128, nc) | (1u << 16);  // B MN-major
+  const uint32_t dah = tc::sdesc_lo(tc::smem_u32(sA)), dal = dah + (PT_A_BYTES >> 4);
+  // leading byte offset 16 KB (between 64-row groups of B)
+  const uint32_t dbh = ((tc::smem_u32(sB) & 0x3FFFFu) >> 4) | ((uint32_t)(16384 >> 4) << 16);
+  const uint32_t dbl = dbh + (P2_B_HALF >> 4);
+#pragma unroll
+  for (int s = 0; s < 8; ++s) {
+    const uint32_t ao = (uint32_t)((s >> 2) * 128 * 128 + (s & 3) * 32) >> 4;
+    const uint32_t ai = ao + (uint32_t)((2 * 128 * 128) >> 4);
+    const uint32_t bo = (uint32_t)(s * 2048) >> 4;  // two groups of 8 K positions per K step of 16
+#pragma unroll
+    for (int pass = 0; pass < 3; ++pass) {
+      const uint32_t a = pass == 1 ? dal : dah;
+      const uint64_t b = tc::sdesc_from_lo((pass == 2 ? dbl : dbh) + bo);
+      tc::mma_bf16(tmem + (uint32_t)(pass * PT_NCMAX), tc::sdesc_from_lo(a + ao), b, idesc, s > 0 ? 1u : 0u);
+      if (CPLX)
+        tc::mma_bf16(tmem + (uint32_t)((3 + pass) * PT_NCMAX), tc::sdesc_from_lo(a + ai), b, idesc,
+                     s > 0 ? 1u : 0u);
+    }
+  }
+}
+
+__device__ __forceinline__ bool p2_product(uint8_t* sA, uint8_t* sB, int nc, bool cplx, uint32_t tmem, uint64_t* bar,
+                                           uint32_t& phase, int* err) {
+  pt_fence_proxy();
+  tc::tc_fence_before();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    tc::tc_fence_after();
+    if (cplx) p2_issue<true>(tmem, sA, sB, nc);
+    else p2_issue<false>(tmem, sA, sB, nc);
+    tc::mma_commit(bar);
+  }
+  const bool ok = pt_wait(bar, phase, err, 21);
+  tc::tc_fence_after();
+  return ok;
+}
+
+// 8 columns of TMEM tiles at ta and tb (this thread's lane), one wait
+__device__ __forceinline__ void p2_ld8x2(uint32_t ta, uint32_t tb, float* a, float* b) {
+  uint32_t u[8], w[8];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%16];\n"
+      "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%8,%9,%10,%11,%12,%13,%14,%15}, [%17];\n"
+      "tcgen05.wait::ld.sync.aligned;\n"
+      : "=r"(u[0]), "=r"(u[1]), "=r"(u[2]), "=r"(u[3]), "=r"(u[4]), "=r"(u[5]), "=r"(u[6]), "=r"(u[7]),
+        "=r"(w[0]), "=r"(w[1]), "=r"(w[2]), "=r"(w[3]), "=r"(w[4]), "=r"(w[5]), "=r"(w[6]), "=r"(w[7])
+      : "r"(ta), "r"(tb)
+      : "memory");
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    a[i] = __uint_as_float(u[i]);
+    b[i] = __uint_as_float(w[i]);
+  }
+}
+
+// v = the product's 8 columns of chunk c at row lane base tlane: the three
+// passes (tiles p and 3 + p) summed in FP32; Re = C1 re - C2 im, Im = C1 im + C2 re
+__device__ __forceinline__ void p2_chunk(uint32_t tlane, int c, bool cplx, float* v) {
+#pragma unroll
+  for (int pass = 0; pass < 3; ++pass) {
+    float a[8], b[8];
+    const uint32_t ta = tlane + (uint32_t)(pass * PT_NCMAX + 8 * c);
+    p2_ld8x2(ta, ta + (uint32_t)(3 * PT_NCMAX), a, b);
+#pragma unroll
+    for (int i = 0; i < 8; i += 2) {
+      const float re = cplx ? a[i] - b[i + 1] : a[i];
+      const float im = cplx ? a[i + 1] + b[i] : a[i + 1];
+      v[i] = pass == 0 ? re : v[i] + re;
+      v[i + 1] = pass == 0 ? im : v[i + 1] + im;
+    }
+  }
+}
+
+__global__ void __launch_bounds__(PT_THREADS, 1)
+    k_prop_tc2(double2* __restrict__ psi, float2* __restrict__ psi32, const float* __restrict__ Vp,
+               const __nv_bfloat16* __restrict__ img, const uint2* __restrict__ voff,
+               const double* __restrict__ weights, int N, int ncw, int na, int nspV, int realB, int* err) {
+  const int w = blockIdx.x;
+  if (!(weights[w] > 1.0e-8)) return;
+  const int sp = blockIdx.y;
+  extern __shared__ uint8_t p2_raw[];
+  uint8_t* smem = (uint8_t*)(((uintptr_t)p2_raw + 1023) & ~(uintptr_t)1023);
+  uint8_t* sA = smem;                    // hi at 0, lo at PT_A_BYTES
+  uint8_t* sB = smem + 2 * PT_A_BYTES;   // hi at 0, lo at P2_B_HALF
+  uint64_t* bar_ld = (uint64_t*)(sB + 2 * P2_B_HALF);
+  uint64_t* bar_mma = bar_ld + 1;
+  uint32_t* tmem_holder = (uint32_t*)(bar_mma + 1);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (threadIdx.x == 0) {
+    tc::mbar_init(bar_ld, 1);
+    tc::mbar_init(bar_mma, 1);
+    tc::fence_mbar_init();
+  }
+  if (warp == 0) tc::tmem_alloc(tmem_holder, PT_TMEM_COLS);
+  for (int e = threadIdx.x; e < 2 * P2_B_HALF / 16; e += blockDim.x) ((uint4*)sB)[e] = make_uint4(0, 0, 0, 0);
+  if (realB)
+    for (int e = threadIdx.x; e < PT_A_BYTES / 16; e += blockDim.x) {
+      const int h = e / (PT_A_BYTES / 32), o = e % (PT_A_BYTES / 32);
+      ((uint4*)(sA + h * PT_A_BYTES + PT_A_BYTES / 2))[o] = make_uint4(0, 0, 0, 0);
+    }
+  tc::tc_fence_before();
+  __syncthreads();
+  tc::tc_fence_after();
+  const uint32_t tmem = *tmem_holder;
+  uint32_t ph_ld = 0, ph_mma = 0;
+  bool ok = true;
+
+  const int p = ((warp & 3) << 5) | lane;  // orbital row = TMEM lane = K position of X
+  const int g = warp >> 2;
+  const uint32_t tlane = tmem + ((uint32_t)((warp & 3) * 32) << 16);
+
+  const int T = N * (N + 1) / 2;
+  const float* vre = Vp + ((size_t)(w * nspV + sp) * 2) * T;
+  const float* vim = vre + T;
+  const __nv_bfloat16* im = img + (size_t)sp * 2 * PT_IMG;
+  const int col_lo = nspV == 1 ? 0 : (sp == 0 ? 0 : na);
+  const int col_hi = nspV == 1 ? ncw : (sp == 0 ? na : ncw);
+  double2* pw = psi + (size_t)w * ncw * N;
+  float2* pw32 = psi32 + (size_t)w * ncw * N;
+
+  for (int c0 = col_lo; c0 < col_hi && ok; c0 += PT_NCMAX / 2) {
+    const int ncols = min(PT_NCMAX / 2, col_hi - c0);
+    const int nc = ((2 * ncols + 15) / 16) * 16;
+    const int C = nc / 8;                                  // chunks of this pass
+    const int cs = (g * C) / PT_NG, ce = ((g + 1) * C) / PT_NG;  // this group's chunks
+    float x[P2_MAXCH][8], acc[P2_MAXCH][8];
+    __syncthreads();
+    pt_issue_image(sA, im, bar_ld, realB != 0);
+#pragma unroll
+    for (int q = 0; q < P2_MAXCH; ++q) {
+      if (cs + q >= ce) break;
+#pragma unroll
+      for (int jj = 0; jj < 4; ++jj) {
+        const int j = 4 * (cs + q) + jj;  // complex column: B rows 2j, 2j + 1
+        float2 v = make_float2(0.f, 0.f);
+        if (j < ncols && p < N) v = pw32[(size_t)(c0 + j) * N + p];
+        x[q][2 * jj] = v.x;
+        x[q][2 * jj + 1] = v.y;
+      }
+      if (p < N) p2_store_chunk(sB, cs + q, p, x[q]);
+    }
+    if (!(ok = pt_wait(bar_ld, ph_ld, err, 22))) break;
+    // B psi = psi + (B - I) psi
+    if (!(ok = p2_product(sA, sB, nc, !realB, tmem, bar_mma, ph_mma, err))) break;
+#pragma unroll
+    for (int q = 0; q < P2_MAXCH; ++q) {
+      if (cs + q >= ce) break;
+      float t[8];
+      p2_chunk(tlane, cs + q, !realB, t);
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        x[q][i] += t[i];
+        acc[q][i] = x[q][i];
+      }
+    }
+    pt_load_V(sA, vre, vim, voff, T);
+    for (int k = 1; k <= 5 && ok; ++k) {
+#pragma unroll
+      for (int q = 0; q < P2_MAXCH; ++q) {
+        if (cs + q >= ce) break;
+        if (p < N) p2_store_chunk(sB, cs + q, p, x[q]);
+      }
+      if (!(ok = p2_product(sA, sB, nc, true, tmem, bar_mma, ph_mma, err))) break;
+      const float inv = 1.f / (float)k;
+#pragma unroll
+      for (int q = 0; q < P2_MAXCH; ++q) {
+        if (cs + q >= ce) break;
+        p2_chunk(tlane, cs + q, true, x[q]);
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+          x[q][i] *= inv;
+          acc[q][i] += x[q][i];
+        }
+      }
+    }
+    if (!ok) break;
+    // B (sum) = sum + (B - I) sum
+    pt_issue_image(sA, im, bar_ld, realB != 0);
+#pragma unroll
+    for (int q = 0; q < P2_MAXCH; ++q) {
+      if (cs + q >= ce) break;
+      if (p < N) p2_store_chunk(sB, cs + q, p, acc[q]);
+    }
+    if (!(ok = pt_wait(bar_ld, ph_ld, err, 22))) break;
+    if (!(ok = p2_product(sA, sB, nc, !realB, tmem, bar_mma, ph_mma, err))) break;
+#pragma unroll
+    for (int q = 0; q < P2_MAXCH; ++q) {
+      if (cs + q >= ce) break;
+      float t[8];
+      p2_chunk(tlane, cs + q, !realB, t);
+      if (p < N) {
+#pragma unroll
+        for (int jj = 0; jj < 4; ++jj) {
+          const int j = 4 * (cs + q) + jj;
+          if (j < ncols) {
+            const float re = acc[q][2 * jj] + t[2 * jj], imv = acc[q][2 * jj + 1] + t[2 * jj + 1];
+            const size_t o = (size_t)(c0 + j) * N + p;
+            pw[o] = make_double2(df_f2d_bits(re), df_f2d_bits(imv));
+            pw32[o] = make_float2(re, imv);
+          }
+        }
+      }
+    }
+  }
+  tc::tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    tc::tc_fence_after();
+    tc::tmem_dealloc(tmem, PT_TMEM_COLS);
+  }
+}
+
+void launch_propagate_tc2(afqmc_handle* h) {
+  smem_optin(k_prop_tc2, P2_SMEM);
+  dim3 grid(h->nwalk, h->nspV);
+  k_prop_tc2<<<grid, PT_THREADS, P2_SMEM, h->stream>>>(h->psi, h->psi32, h->V32, h->pt_img, h->pt_voff, h->weights,
+                                                      h->N, h->ncw, h->na, h->nspV, h->real_expm ? 1 : 0, h->d_err);
+  h->launches++;
+}
+
+bool prop_tc2_available(const afqmc_handle* h) { return h->N <= 128 && h->pt_img != nullptr; }
+
 }  // namespace afqmc
