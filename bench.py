@@ -527,9 +527,10 @@ def form_multisystem(A, device, reps=3):
 
 
 # DRAM bytes of one launch of the tensor-core propagator on this workload
-# (dram__bytes_read.sum + dram__bytes_write.sum of one ncu capture of k_prop_tc,
-# 2048 walkers x 2 spins); a recorded constant, refreshed with each capture
-PROP_TC_DRAM_BYTES = {"cfg2": 198.0e6 + 179.0e6}
+# (dram__bytes_read.sum + dram__bytes_write.sum of one ncu capture, 2048 walkers
+# x 2 spins): k_prop_tc2 197.8 + 179.6 MB, k_prop_tc 198 + 179 MB; a recorded
+# constant, refreshed with each capture
+PROP_TC_DRAM_BYTES = {"cfg2": 197.8e6 + 179.6e6}
 
 
 def main():
@@ -691,8 +692,9 @@ def main():
     traffic = PROP_TC_DRAM_BYTES.get(args.workload) if dom == "prop" else None
     roof = {"bound": "tensor", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
             "frac": achieved / peak, "traffic": traffic,
-            "traffic_source": "dram__bytes_read.sum + dram__bytes_write.sum per launch of k_prop_tc, one ncu "
-                              "capture of this workload (recorded constant)" if traffic else None,
+            "traffic_source": "dram__bytes_read.sum + dram__bytes_write.sum per launch of the tensor-core "
+                              "propagator (k_prop_tc2), one ncu capture of this workload (recorded constant)"
+                              if traffic else None,
             "peak_source": "%s bf16 sustained (MEASURED_PEAKS.json); algorithmic FLOPs of the stage per launch "
                            "/ its CUDA-event time; the largest tensor-core stage (every stage against the executed "
                            "cost of its parts in stage_roofline; FP32 peak nominal)" % src,

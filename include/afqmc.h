@@ -302,9 +302,11 @@ int afqmc_tuning(const afqmc_handle* h, int* bn_fb, int* bn_vhs, int* prop, int*
 /* Set the choices directly (a value <= 0 keeps the current one).  bn_*: 64, 128
  * or 256; prop: 1 V in shared memory (N <= 128), 2 column-chunked, 3 tensor
  * core (N <= 512; streamed tiles above 128), 4 tensor core with the walker
- * operand stored MN-major (N <= 128); ovl: 1 warp per matrix, 2 CTA per matrix, 3 warp per
- * matrix with M = Phi^T psi formed on the tensor cores from exact BF16 slices
- * (mixed form, N <= 128, n <= 32; FP64-grade); qr (walker
+ * operand stored MN-major (N <= 128); ovl: 1 warp per matrix, 2 CTA per matrix
+ * (FP64 Gauss-Jordan), 3 warp per matrix with M = Phi^T psi formed on the
+ * tensor cores from exact BF16 slices (mixed form, N <= 128, n <= 32;
+ * FP64-grade), 4 CTA per matrix in double-FP32 (mixed form; the default there
+ * above 32 electrons per channel); qr (walker
  * orthonormalisation): 1 Householder with the reference's (Eigen's) column
  * signs, 2 Cholesky-QR in FP64 (mixed form; the same Q up to column signs,
  * which the overlaps carry, so every physical result is unchanged; the

@@ -27,11 +27,16 @@ def A():
     return afqmc
 
 
-@pytest.mark.parametrize("kind", ["uhf", "rhf"])
+@pytest.mark.parametrize("kind", ["uhf", "rhf", "large"])
 def test_cholesky_qr_equals_householder_up_to_column_signs(A, kind):
+    """"large": N = 300 with 45 + 44 electrons, whose spin block does not fit
+    shared memory as FP32 pairs: the variant that keeps it in L2."""
     if kind == "uhf":
         s = S.make_system(40, 7, 150, 4242, "uhf")
         na, nb, rw = 7, 6, False
+    elif kind == "large":
+        s = S.make_system(300, 45, 40, 4141, "uhf")
+        na, nb, rw = 45, 44, False
     else:
         s = S.make_system(36, 6, 130, 4343, "rhf")
         na = nb = 6
@@ -39,7 +44,7 @@ def test_cholesky_qr_equals_householder_up_to_column_signs(A, kind):
     N = s["norb"]
     oh = O.Hamiltonian(N, na, nb, s["ecore"], s["h1"], s["h1mod"], s["chol"])
     ot = O.Trial(oh, s["trial"], s["phi_a"][:, :na], s["phi_b"][:, :nb])
-    W = 48
+    W = 12 if kind == "large" else 48
     rng = np.random.default_rng(5)
     base = O._ref_dets(oh, ot.phi, rw)
     dets = base[None] + 0.1 * (rng.standard_normal((W,) + base.shape) + 1j * rng.standard_normal((W,) + base.shape))
@@ -78,6 +83,7 @@ def test_cholesky_qr_equals_householder_up_to_column_signs(A, kind):
     assert np.abs(oc / ref_o - 1).max() < 1e-10
     ref_h = O.overlap(ot, O.Walkers(oh, rw, dh))
     assert np.abs(oh_ / ref_h - 1).max() < 1e-10
-    assert np.abs(elh - el_ref).max() < 2e-5
-    assert np.abs(elc - el_ref).max() < 2e-5
+    tol_el = max(2e-5, 2e-7 * np.abs(el_ref).max())  # FP32-grade exchange: relative for large |E_L|
+    assert np.abs(elh - el_ref).max() < tol_el
+    assert np.abs(elc - el_ref).max() < tol_el
     assert np.abs(w1c - w1h).max() <= 1e-6 * np.abs(w1h).max()

@@ -171,14 +171,15 @@ def test_above_128_orbitals_fp64(A):
     print(check_fp64(got, ref))
 
 
-@pytest.mark.parametrize("variant", ["chunked_cta", "chunked_cta_householder", "tensor_cta"])
+@pytest.mark.parametrize("variant", ["chunked_cta", "chunked_cta_householder", "tensor_cta", "tensor_cta_df32"])
 def test_above_128_orbitals_mixed(A, variant):
-    """N=160, n=36: FP32 column-chunked propagator, block Gauss-Jordan overlap.
+    """N=160, n=36: FP32 column-chunked or tensor-core propagator, block
+    Gauss-Jordan overlap in FP64 or in double-FP32.
     This system is not a benchmark workload and its energy bound follows from
     the per-result ones: with 72 electrons, |E_L| ~ 75 Eh and a spread of ~4 Eh
     over 12 walkers, the weight bound (1.8e-4) times the spread alone allows
     0.7 mEh; 0.3 mEh is asserted (0.11 measured)."""
-    t = dict(prop="tensor" if variant.startswith("tensor") else "chunked", ovl=2,
+    t = dict(prop="tensor" if variant.startswith("tensor") else "chunked", ovl=4 if variant.endswith("df32") else 2,
              qr="householder" if variant.endswith("householder") else "cholesky")
     got, ref = gpu_run(A, "n160", 12, 5, 2, "mixed", t)
     print(variant, check_mixed(got, ref, 72, 5, t["qr"] == "cholesky", e_bound_mEh=0.3))

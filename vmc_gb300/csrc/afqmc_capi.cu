@@ -182,7 +182,7 @@ void release(afqmc_handle* h) {
                   h->xc, h->cv_x, h->cv_idx, h->cv_esub, h->cv_f, h->cv_ms, h->cv_out, h->d_step, h->psi32,
                   h->pt_img, h->comb_cum, h->comb_idx, h->comb_ovl, h->blk, h->blk_zeta, h->wpart,
                   h->ovl_tau, h->ovl_bimg, h->ovl_M, h->theta32, h->mf32, h->h1phi32, h->pt_voff,
-                  h->rdm_acc, h->rdm_part, h->pb_img, h->pb_scratch};
+                  h->rdm_acc, h->rdm_part, h->pb_img, h->pb_scratch, h->phi2};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (h->host_pinned) cudaFreeHost(h->host_pinned);
@@ -496,6 +496,7 @@ int afqmc_create(const afqmc_ham* ham, const afqmc_trial* trial, const afqmc_opt
     ALLOC(fb32, W * 2 * G);
     ALLOC(mf32, (size_t)G);
     ALLOC(h1phi32, (size_t)h->nce * N);
+    ALLOC(phi2, (size_t)h->nce * N);
     ALLOC(V32, W * h->nspV * 2 * (size_t)T);
     ALLOC(expm32, (size_t)nsp * 2 * NN);
     ALLOC(d_chunks32, h->chunks32.size());

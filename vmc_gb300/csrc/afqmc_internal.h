@@ -89,6 +89,7 @@ struct afqmc_handle {
   double* rot = nullptr;      // [G][nce*N]           rot[g][(col)*N + p] = (Phi^T L_g)[i, p]
   double* h1phi = nullptr;    // [nce][N]             (h1 Phi)[p, i]
   float2* h1phi32 = nullptr;  // [nce][N]             double-FP32 copy (mixed form: features, one-body energy)
+  float2* phi2 = nullptr;     // [nce][N]             double-FP32 copy of phi (mixed form: overlap matrices)
   double* LT = nullptr;       // [nsp][T][G]          packed lower-triangle Cholesky, FP64
   float* LT32 = nullptr;      // [nsp][T][G]          FP32 copy (REF32)
   int2* tri = nullptr;        // [T]                  packed index -> (i, j), j <= i
@@ -135,7 +136,8 @@ struct afqmc_handle {
   CUtensorMap tm_theta_bn[3], tm_x_bn[3];  // B operands with box heights 64, 128, 256
   // autotuned choices (afqmc_autotune): GEMM N-tiles; propagator 0 auto / 1 SMEM / 2 chunked / 3 tcgen05 /
   // 4 tcgen05 with the walker operand MN-major (N <= 128);
-  // overlap 0 auto / 1 warp per matrix / 2 block per matrix
+  // overlap 0 auto / 1 warp per matrix / 2 block per matrix (FP64) / 3 warp per matrix, M on the tensor cores /
+  // 4 block per matrix in double-FP32 (mixed form)
   int tune_bn_fb = 128, tune_bn_vhs = 128, tune_prop = 0, tune_ovl = 0;
   int tune_qr = 0;  // walker QR: 0 auto (Cholesky-QR in the mixed form when it fits), 1 Householder, 2 Cholesky-QR
   int tune_prop_best = 0, tune_ovl_best = 0;

@@ -120,14 +120,15 @@ int afqmc_autotune(afqmc_handle* h, const char* cache_path, char* report, int re
   {
     const int nmax = std::max(h->chan[0].n, h->nchan > 1 ? h->chan[1].n : 0);
     float best = 1e30f;
-    const int cands[3] = {3, 1, 2};
+    const int cands[4] = {3, 1, 4, 2};
     for (int c : cands) {
       if (c == 1 && (nmax > 32 || (size_t)nmax * h->N * 8 + 4 * ((size_t)nmax * nmax * 24 + 4 * nmax + 16) > 160 * 1024))
         continue;
       if (c == 3 && !afqmc::ovl_tc_available(h)) continue;
+      if (c == 4 && h->precision != AFQMC_PREC_MIXED) continue;
       h->tune_ovl = c;
       const float t = time_ms(h, [&] { afqmc::launch_overlap_theta(h, false); }, 3);
-      rep << "ovl" << (c == 1 ? "_warp" : c == 2 ? "_block" : "_tc") << "=" << t << "ms ";
+      rep << "ovl" << (c == 1 ? "_warp" : c == 2 ? "_block" : c == 3 ? "_tc" : "_block_df32") << "=" << t << "ms ";
       if (t < best) { best = t; h->tune_ovl_best = c; }
     }
     h->tune_ovl = h->tune_ovl_best;
@@ -153,7 +154,7 @@ int afqmc_set_tuning(afqmc_handle* h, int bn_fb, int bn_vhs, int prop, int ovl, 
   if (!h) return AFQMC_ERR_ARG;
   auto bn_ok = [](int b) { return b <= 0 || b == 64 || b == 128 || b == 256; };
   const bool mixed = h->precision == AFQMC_PREC_MIXED;
-  if (!bn_ok(bn_fb) || !bn_ok(bn_vhs) || prop > 4 || ovl > 3 || ((bn_fb > 0 || bn_vhs > 0 || prop > 0) && !mixed) ||
+  if (!bn_ok(bn_fb) || !bn_ok(bn_vhs) || prop > 4 || ovl > 4 || (ovl == 4 && !mixed) || ((bn_fb > 0 || bn_vhs > 0 || prop > 0) && !mixed) ||
       (ovl == 3 && !afqmc::ovl_tc_available(h)) ||
       ((prop == 1) && h->N > 128) || (prop == 3 && !afqmc::prop_tc_available(h)) ||
       (prop == 4 && !afqmc::prop_tc2_available(h)) || qr > 2 ||

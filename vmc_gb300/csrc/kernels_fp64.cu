@@ -582,6 +582,11 @@ void launch_psi_to_f32(afqmc_handle* h) {
   h->launches++;
 }
 
+__global__ void k_overlap_gj_df32(const float2* __restrict__ psi32, const float2* __restrict__ phi2,
+                                  float* __restrict__ theta32, double2* __restrict__ det,
+                                  const double* __restrict__ weights, int N, int ncw, int nce, Channel c0, Channel c1,
+                                  int only_live);
+
 void launch_overlap_theta(afqmc_handle* h, bool only_live) {
   h->fb_current = false;  // theta changes
   h->thetaB_from_lu = false;  // set below when the FP32 LU writes the force bias's operand too
@@ -589,7 +594,7 @@ void launch_overlap_theta(afqmc_handle* h, bool only_live) {
   const size_t per_warp = ow_per_warp(nmax);
   const size_t smem_lu = (((size_t)nmax * h->N * sizeof(double) + 15) & ~(size_t)15) + OW_WARPS * per_warp;
   const bool mtc = h->tune_ovl == 3 && ovl_tc_available(h);  // M on the tensor cores
-  if (nmax <= 32 && h->tune_ovl != 2 && (mtc || smem_lu <= 160 * 1024)) {
+  if (nmax <= 32 && h->tune_ovl != 2 && h->tune_ovl != 4 && (mtc || smem_lu <= 160 * 1024)) {
     const size_t smem = mtc ? OW_WARPS * per_warp : smem_lu;
     const bool f32 = h->precision == AFQMC_PREC_MIXED && h->psi32;
     if (mtc) launch_overlap_m_tc(h);
@@ -628,12 +633,124 @@ void launch_overlap_theta(afqmc_handle* h, bool only_live) {
     return;
   }
   size_t smem = (size_t)nmax * 2 * nmax * sizeof(double2) + nmax * sizeof(double2);
-  smem_optin(k_overlap_theta, 200 * 1024);
   dim3 grid(h->nwalk, h->nchan);
+  if (h->precision == AFQMC_PREC_MIXED && h->psi32 && h->phi2 && h->tune_ovl != 2) {  // double-FP32 elimination
+    smem_optin(k_overlap_gj_df32, 200 * 1024);
+    k_overlap_gj_df32<<<grid, 256, smem, h->stream>>>(h->psi32, h->phi2, h->theta32, h->det, h->weights, h->N, h->ncw,
+                                                      h->nce, h->chan[0], h->chan[1], only_live ? 1 : 0);
+    h->launches++;
+    return;
+  }
+  smem_optin(k_overlap_theta, 200 * 1024);
   k_overlap_theta<<<grid, 256, smem, h->stream>>>(h->psi, h->phi, h->theta, h->theta32, h->det, h->weights, h->N,
                                                   h->ncw, h->nce, h->chan[0], h->chan[1],
                                                   only_live ? 1 : 0, h->precision == AFQMC_PREC_MIXED ? 1 : 0);
   h->launches++;
+}
+
+// Mixed form, more than 32 electrons per channel: the same block Gauss-Jordan
+// with no FP64 work in its loops.  M = Phi^T psi from the FP32 walker copy and
+// the trial orbitals as FP32 pairs (Dot2: exact products by FMA, TwoSum
+// accumulation, ~2^-48 relative); the elimination in double-FP32 complex
+// arithmetic (pivot search on the high parts), so the determinant -- the
+// product of the pivots, formed in double-FP32 and converted once -- stays
+// FP64-grade; theta = psi M^-1 in FP32 from the FP32 walker and the high parts
+// of the inverse.  One CTA per (walker, channel); [n][2n] pairs in shared memory.
+__device__ __forceinline__ df32c gj_ld(const float4* a, int e) {
+  const float4 v = a[e];
+  return {{v.x, v.y}, {v.z, v.w}};
+}
+__device__ __forceinline__ void gj_st(float4* a, int e, df32c v) { a[e] = make_float4(v.r.h, v.r.l, v.i.h, v.i.l); }
+
+__global__ void k_overlap_gj_df32(const float2* __restrict__ psi32, const float2* __restrict__ phi2,
+                                  float* __restrict__ theta32, double2* __restrict__ det,
+                                  const double* __restrict__ weights, int N, int ncw, int nce, Channel c0, Channel c1,
+                                  int only_live) {
+  const int w = blockIdx.x;
+  const Channel ch = blockIdx.y == 0 ? c0 : c1;
+  if (only_live && !(weights[w] > 1.0e-8)) return;
+  extern __shared__ float4 gj_sm[];
+  const int n = ch.n, n2 = 2 * n;
+  float4* a = gj_sm;             // [n][2n]
+  float4* fcol = gj_sm + n * n2;  // [n]
+  __shared__ int s_piv;
+  const float2* ps = psi32 + (size_t)w * ncw * N + (size_t)ch.psi_off * N;
+  const float2* ph = phi2 + (size_t)ch.col_off * N;
+  for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+    const int i = e / n, j = e % n;
+    float sr = 0.f, cr = 0.f, si = 0.f, ci = 0.f;
+    for (int p = 0; p < N; ++p) {
+      const float2 f = ph[i * N + p];
+      const float2 v = ps[j * N + p];
+      dot2_acc(sr, cr, f.x, f.y, v.x);
+      dot2_acc(si, ci, f.x, f.y, v.y);
+    }
+    gj_st(a, i * n2 + j, {df_fast(sr, cr), df_fast(si, ci)});
+    gj_st(a, i * n2 + n + j, {{i == j ? 1.f : 0.f, 0.f}, {0.f, 0.f}});
+  }
+  __syncthreads();
+  df32c detv = {{1.f, 0.f}, {0.f, 0.f}};  // meaningful in thread 0
+  for (int k = 0; k < n; ++k) {
+    if (threadIdx.x < 32) {
+      float best = -1.f;
+      int bi = k;
+      for (int i = k + threadIdx.x; i < n; i += 32) {
+        const float4 v = a[i * n2 + k];
+        const float m = v.x * v.x + v.z * v.z;
+        if (m > best) { best = m; bi = i; }
+      }
+      for (int off = 16; off > 0; off >>= 1) {
+        const float ob = __shfl_down_sync(0xffffffffu, best, off);
+        const int oi = __shfl_down_sync(0xffffffffu, bi, off);
+        if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+      }
+      if (threadIdx.x == 0) s_piv = bi;
+    }
+    __syncthreads();
+    const int pr = s_piv;
+    if (pr != k) {
+      for (int j = threadIdx.x; j < n2; j += blockDim.x) {
+        const float4 t = a[k * n2 + j];
+        a[k * n2 + j] = a[pr * n2 + j];
+        a[pr * n2 + j] = t;
+      }
+    }
+    __syncthreads();
+    const df32c pv = gj_ld(a, k * n2 + k);
+    if (threadIdx.x == 0) {
+      detv = dfc_mul(detv, pv);
+      if (pr != k) detv = {df_neg(detv.r), df_neg(detv.i)};
+    }
+    const df32c inv = dfc_recip(pv);
+    for (int i = threadIdx.x; i < n; i += blockDim.x) fcol[i] = a[i * n2 + k];
+    __syncthreads();
+    for (int j = k + threadIdx.x; j < n2; j += blockDim.x) gj_st(a, k * n2 + j, dfc_mul(gj_ld(a, k * n2 + j), inv));
+    __syncthreads();
+    for (int e = threadIdx.x; e < n * (n2 - k); e += blockDim.x) {
+      const int i = e / (n2 - k), j = k + e % (n2 - k);
+      if (i == k) continue;
+      const float4 f = fcol[i];
+      gj_st(a, i * n2 + j, dfc_fms(gj_ld(a, i * n2 + j), {{f.x, f.y}, {f.z, f.w}}, gj_ld(a, k * n2 + j)));
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0)
+    det[2 * w + blockIdx.y] = make_double2(df_to_double_bits(detv.r), df_to_double_bits(detv.i));
+  // theta[p][j] = sum_i psi[p][i] Minv[i][j], FP32
+  float* tre = theta32 + (size_t)(2 * w) * nce * N + (size_t)ch.col_off * N;
+  float* tim = tre + (size_t)nce * N;
+  for (int e = threadIdx.x; e < N * n; e += blockDim.x) {
+    const int j = e / N, p = e % N;
+    float re = 0.f, im = 0.f;
+    for (int i = 0; i < n; ++i) {
+      const float2 v = ps[i * N + p];
+      const float4 m = a[i * n2 + n + j];
+      re = fmaf(v.x, m.x, fmaf(-v.y, m.z, re));
+      im = fmaf(v.x, m.z, fmaf(v.y, m.x, im));
+    }
+    tre[j * N + p] = re;
+    tim[j * N + p] = im;
+  }
 }
 
 // overlap = prod_s det_s^mult (used after set_walkers)

@@ -612,6 +612,7 @@ bool setup_mixed(afqmc_handle* h) {
   // the force bias's theta operand: its padding columns stay zero when the LU writes it
   cudaMemsetAsync(h->thetaB, 0, (size_t)h->nwalk * 2 * h->kf_pad * sizeof(__nv_bfloat16), h->stream);
   k_to_df32<<<(h->nce * h->N + 255) / 256, 256, 0, h->stream>>>(h->h1phi, h->h1phi32, h->nce * h->N);
+  k_to_df32<<<(h->nce * h->N + 255) / 256, 256, 0, h->stream>>>(h->phi, h->phi2, h->nce * h->N);
   bool ok = setup_prop_tc(h) && setup_ovl_tc(h) && make_tmap_bf16(&h->tm_rot, h->rotA, h->G, h->kf_pad, tc::BM);
   const int bns[3] = {64, 128, 256};
   for (int i = 0; i < 3 && ok; ++i)

@@ -178,18 +178,151 @@ __global__ void __launch_bounds__(OC_THREADS)
   }
 }
 
+// The same factorisation for walker blocks too large to stage in shared
+// memory (N x n beyond ~200 KB as pairs, e.g. N = 400, n = 60): the block
+// stays in global memory (L2).  The Gram matrix comes from the FP32 copy
+// (the high part of every stored number) with one warp per (i, j) pair and
+// lanes over the orbitals; Cholesky and X = R^-1 are as above; Q = A X runs in
+// place with one thread per orbital row p: Q(p, j) needs A(p, i) for i <= j
+// only, so the thread forms its row's columns from the last to the first and
+// overwrites each A(p, j) once it is no longer needed (no other thread reads
+// row p).
+__global__ void __launch_bounds__(OC_THREADS)
+    k_ortho_chol_g(double2* __restrict__ psi, float2* __restrict__ psi32, double2* __restrict__ ovlp,
+                   const double* __restrict__ weights, int N, int ncw, int na, int nb, int rhf_walker, int nmax) {
+  const int w = blockIdx.x;
+  if (!(weights[w] > 1.0e-8)) return;
+  extern __shared__ float2 ocg_sm[];
+  float2* R = ocg_sm;                   // [nmax][nmax]
+  float2* X = R + (size_t)nmax * nmax;  // [nmax][nmax]
+  __shared__ int s_bad;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  double fac = 1.0;  // thread 0
+  const int nblk = rhf_walker ? 1 : 2;
+  for (int b = 0; b < nblk; ++b) {
+    const int off = b == 0 ? 0 : na, n = b == 0 ? na : nb;
+    if (n == 0) continue;
+    double2* Ag = psi + ((size_t)w * ncw + off) * N;
+    float2* Ag32 = psi32 + ((size_t)w * ncw + off) * N;
+    __syncthreads();  // R, X free (previous block done)
+    if (tid == 0) s_bad = 0;
+    for (int e = warp; e < n * n; e += OC_THREADS / 32) {
+      const int i = e / n, j = e % n;
+      if (i > j) continue;  // warp-uniform
+      const float2* ai = Ag32 + (size_t)i * N;
+      const float2* aj = Ag32 + (size_t)j * N;
+      float sr = 0.f, si = 0.f;
+      for (int p = lane; p < N; p += 32) {
+        const float2 x = ai[p], y = aj[p];
+        sr += x.x * y.x + x.y * y.y;
+        si += x.x * y.y - x.y * y.x;
+      }
+      sr = warp_sumf(sr);
+      si = warp_sumf(si);
+      if (lane == 0) R[i * n + j] = make_float2(sr, si);
+    }
+    __syncthreads();
+    if (warp == 0) {
+      bool bad = false;
+      for (int k = 0; k < n; ++k) {
+        float dkk = 0.f;
+        if (lane == 0) {
+          float d = R[k * n + k].x;
+          for (int m = 0; m < k; ++m) {
+            const float2 r = R[m * n + k];
+            d -= r.x * r.x + r.y * r.y;
+          }
+          if (!(d > 0.f) || !isfinite(d)) {
+            bad = true;
+            d = 1.f;
+          }
+          dkk = sqrtf(d);
+          R[k * n + k] = make_float2(dkk, 0.f);
+        }
+        dkk = __shfl_sync(0xffffffffu, dkk, 0);
+        const float inv = 1.f / dkk;
+        for (int j = k + 1 + lane; j < n; j += 32) {
+          float2 g = R[k * n + j];
+          for (int m = 0; m < k; ++m) {
+            const float2 a = R[m * n + k], c = R[m * n + j];
+            g.x -= a.x * c.x + a.y * c.y;
+            g.y -= a.x * c.y - a.y * c.x;
+          }
+          R[k * n + j] = make_float2(g.x * inv, g.y * inv);
+        }
+        __syncwarp();
+      }
+      if (lane == 0 && bad) s_bad = 1;
+    }
+    __syncthreads();
+    if (s_bad) continue;
+    for (int j = tid; j < n; j += OC_THREADS) {
+      X[j * n + j] = make_float2(1.f / R[j * n + j].x, 0.f);
+      for (int i = j - 1; i >= 0; --i) {
+        float2 t = make_float2(0.f, 0.f);
+        for (int m = i + 1; m <= j; ++m) {
+          const float2 r = R[i * n + m], x = X[m * n + j];
+          t.x += r.x * x.x - r.y * x.y;
+          t.y += r.x * x.y + r.y * x.x;
+        }
+        const float inv = 1.f / R[i * n + i].x;
+        X[i * n + j] = make_float2(-t.x * inv, -t.y * inv);
+      }
+    }
+    __syncthreads();
+    for (int p = tid; p < N; p += OC_THREADS) {
+      for (int j = n - 1; j >= 0; --j) {
+        float sr = 0.f, cr = 0.f, si = 0.f, ci = 0.f;
+        for (int i = 0; i <= j; ++i) {
+          const double2 v = Ag[(size_t)i * N + p];
+          const df32 re = df_split_bits(v.x), im = df_split_bits(v.y);
+          const float2 x = X[i * n + j];
+          dot2_acc(sr, cr, re.h, re.l, x.x);
+          dot2_acc(sr, cr, -im.h, -im.l, x.y);
+          dot2_acc(si, ci, re.h, re.l, x.y);
+          dot2_acc(si, ci, im.h, im.l, x.x);
+        }
+        const double2 q = make_double2(df_to_double_bits(df_fast(sr, cr)), df_to_double_bits(df_fast(si, ci)));
+        Ag[(size_t)j * N + p] = q;
+        Ag32[(size_t)j * N + p] = make_float2(df_split_bits(q.x).h, df_split_bits(q.y).h);
+      }
+    }
+    if (tid == 0)
+      for (int k = 0; k < n; ++k) fac *= (double)X[k * n + k].x;
+  }
+  if (tid == 0) {
+    if (rhf_walker) fac *= fac;
+    const double2 o = ovlp[w];
+    ovlp[w] = make_double2(o.x * fac, o.y * fac);
+  }
+}
+
+size_t ortho_chol_g_smem(const afqmc_handle* h) {
+  const size_t nmax = (size_t)std::max(h->na, h->rhf_walker ? 0 : h->nb);
+  return 2 * nmax * nmax * sizeof(float2);
+}
+
 size_t ortho_chol_smem(const afqmc_handle* h) {
   const size_t nmax = (size_t)std::max(h->na, h->rhf_walker ? 0 : h->nb);
   return (2 * nmax * (size_t)(h->N | 1) + 2 * nmax * nmax) * sizeof(float2);
 }
 
 bool ortho_chol_available(const afqmc_handle* h) {
-  return h->precision == AFQMC_PREC_MIXED && h->psi32 && ortho_chol_smem(h) <= 200 * 1024;
+  return h->precision == AFQMC_PREC_MIXED && h->psi32 &&
+         (ortho_chol_smem(h) <= 200 * 1024 || ortho_chol_g_smem(h) <= 200 * 1024);
 }
 
 void launch_ortho_chol(afqmc_handle* h) {
-  smem_optin(k_ortho_chol, 200 * 1024);
   const int nmax = std::max(h->na, h->rhf_walker ? 0 : h->nb);
+  if (ortho_chol_smem(h) > 200 * 1024) {  // the block stays in L2
+    smem_optin(k_ortho_chol_g, 200 * 1024);
+    k_ortho_chol_g<<<h->nwalk, OC_THREADS, ortho_chol_g_smem(h), h->stream>>>(h->psi, h->psi32, h->ovlp, h->weights,
+                                                                              h->N, h->ncw, h->na, h->nb,
+                                                                              h->rhf_walker, nmax);
+    h->launches++;
+    return;
+  }
+  smem_optin(k_ortho_chol, 200 * 1024);
   k_ortho_chol<<<h->nwalk, OC_THREADS, ortho_chol_smem(h), h->stream>>>(h->psi, h->psi32, h->ovlp, h->weights, h->N,
                                                                          h->ncw, h->na, h->nb, h->rhf_walker, nmax);
   h->launches++;
