@@ -72,7 +72,7 @@ def test_autotune_choices_and_cache(A, tmp_path):
     cache = str(tmp_path / "tune.txt")
     ch, rep = A.autotune(b, cache)
     assert ch["bn_fb"] in (64, 128, 256) and ch["bn_vhs"] in (64, 128, 256)
-    assert ch["prop"] in (1, 2, 3) and ch["ovl"] in (1, 2, 3) and ch["qr"] in (1, 2)
+    assert ch["prop"] in (1, 2, 3, 4) and ch["ovl"] in (1, 2, 3, 4) and ch["qr"] in (1, 2)
     c = make(A, s, 300, "mixed", 3)
     ch2, rep2 = A.autotune(c, cache)
     assert ch2 == ch and rep2.startswith("cached")

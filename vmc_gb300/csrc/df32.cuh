@@ -142,6 +142,38 @@ __device__ __forceinline__ df32c dfc_mul(df32c a, df32c b) {
   const df32 z = {0.f, 0.f};
   return dfc_fma({z, z}, a, b);
 }
+// Packed pairs: one float2 instruction (FADD2 / FMUL2 / FFMA2, sm_100 and
+// later) computes both components with the per-component rounding of the
+// scalar _rn forms, so a packed sequence that does the scalar steps in the
+// same order gives the same bits with half the instructions.
+__device__ __forceinline__ float2 f2_neg(float2 a) { return make_float2(-a.x, -a.y); }
+__device__ __forceinline__ void df2_two_sum(float2 a, float2 b, float2& s, float2& e) {
+  s = __fadd2_rn(a, b);
+  const float2 bb = __fadd2_rn(s, f2_neg(a));
+  e = __fadd2_rn(__fadd2_rn(a, f2_neg(__fadd2_rn(s, f2_neg(bb)))), __fadd2_rn(b, f2_neg(bb)));
+}
+// complex x - a b with each operand held as planes: (Re, Im) of the high
+// parts in one float2, of the low parts in another.  Component for component
+// the operations and their order of dfc_fms: Re = x.r + (-a.r) b.r + (-a.i)(-b.i),
+// Im = x.i + (-a.r) b.i + (-a.i) b.r.
+__device__ __forceinline__ void dfc_fms_planes(float2& xh, float2& xl, float2 ah, float2 al, float2 bh, float2 bl) {
+  const float2 a1h = make_float2(-ah.x, -ah.x), a1l = make_float2(-al.x, -al.x);
+  const float2 a2h = make_float2(-ah.y, -ah.y), a2l = make_float2(-al.y, -al.y);
+  const float2 b2h = make_float2(-bh.y, bh.x), b2l = make_float2(-bl.y, bl.x);
+  const float2 p1 = __fmul2_rn(a1h, bh), e1 = __ffma2_rn(a1h, bh, f2_neg(p1));
+  const float2 p2 = __fmul2_rn(a2h, b2h), e2 = __ffma2_rn(a2h, b2h, f2_neg(p2));
+  float2 s1, t1, s2, t2;
+  df2_two_sum(xh, p1, s1, t1);
+  df2_two_sum(s1, p2, s2, t2);
+  float2 lo = __fadd2_rn(__fadd2_rn(xl, t1), __fadd2_rn(t2, __fadd2_rn(e1, e2)));
+  lo = __ffma2_rn(a1h, bl, lo);
+  lo = __ffma2_rn(a1l, bh, lo);
+  lo = __ffma2_rn(a2h, b2l, lo);
+  lo = __ffma2_rn(a2l, b2h, lo);
+  xh = __fadd2_rn(s2, lo);
+  xl = __fadd2_rn(lo, f2_neg(__fadd2_rn(xh, f2_neg(s2))));
+}
+
 // 2^k as an FP32 number, |k| <= 126
 __device__ __forceinline__ float df_pow2(int k) { return __int_as_float((127 + k) << 23); }
 // 1 / p: p scaled by a power of two so that max(|Re p|, |Im p|) is in [1, 2),

@@ -142,8 +142,15 @@ __global__ void k_overlap_theta(const double2* __restrict__ psi, const double* _
 constexpr int OW_WARPS = 4;
 // shared memory of one warp: the n x n matrix (FP64 complex, or the mixed
 // form's high and low FP32 planes: 16 bytes an entry either way) and the pivots
+// (the mixed form's low-part plane starts on a 16-byte boundary and is sized
+// for n rows of n rounded up to 4 FP32 pairs: the inverse's two FP32 planes
+// are written over it and read with 16-byte loads)
+__host__ __device__ inline size_t ow_lo_off(int nmax) { return (size_t)((nmax * nmax + 1) & ~1) * sizeof(float2); }
+__host__ __device__ inline size_t ow_perm_off(int nmax) {
+  return ow_lo_off(nmax) + (size_t)nmax * ((nmax + 3) & ~3) * sizeof(float2);
+}
 __host__ __device__ inline size_t ow_per_warp(int nmax) {
-  return ((size_t)nmax * nmax * sizeof(double2) + nmax * sizeof(int) + 15) & ~(size_t)15;
+  return (ow_perm_off(nmax) + nmax * sizeof(int) + 15) & ~(size_t)15;
 }
 
 __device__ __forceinline__ df32c ld_dfc(const float2* ah, const float2* al, int e) {
@@ -199,7 +206,10 @@ __device__ double2 lu_df32(float2* ah, float2* al, int* perm, int n, int lane) {
       const int dq = 32 / rem, dr = 32 - dq * rem;  // 32 entries = dq rows + dr columns
       int i = k + 1 + lane / rem, j = k + 1 + lane % rem;
       for (int e = lane; e < rem * rem; e += 32) {
-        st_dfc(ah, al, i * n + j, dfc_fms(ld_dfc(ah, al, i * n + j), ld_dfc(ah, al, i * n + k), ld_dfc(ah, al, k * n + j)));
+        float2 xh = ah[i * n + j], xl = al[i * n + j];
+        dfc_fms_planes(xh, xl, ah[i * n + k], al[i * n + k], ah[k * n + j], al[k * n + j]);
+        ah[i * n + j] = xh;
+        al[i * n + j] = xl;
         i += dq;
         j += dr;
         if (j >= n) {
@@ -256,8 +266,8 @@ __global__ void __launch_bounds__(OW_WARPS * 32, (F32 && MB && NM <= 20) ? 7 : 1
   unsigned char* wbase = ow_raw + phs_bytes + warp * per_warp;
   double2* a = (double2*)wbase;  // FP64 form: [n][n] LU, row-major
   float2* ah = (float2*)wbase;   // mixed form: [n][n] high parts, then [n][n] low parts
-  float2* al = ah + (size_t)nmax * nmax;
-  int* perm = (int*)(wbase + (size_t)nmax * nmax * sizeof(double2));
+  float2* al = (float2*)(wbase + ow_lo_off(nmax));
+  int* perm = (int*)(wbase + ow_perm_off(nmax));
   // mixed form above 128 orbitals (m_from32): M is formed in double-FP32 from
   // the FP32 walker values and the trial orbitals split into FP32 pairs
   // (staged as such, so the product loop does no FP64 work).  Up to 128
@@ -441,9 +451,15 @@ __global__ void __launch_bounds__(OW_WARPS * 32, (F32 && MB && NM <= 20) ? 7 : 1
     // z[k]; then every orbital row
     // of theta is psi32[p][:] G.  n solves instead of N, and the row products
     // read G by broadcast.  The solves use the FP32 high parts of the factors.
-    float2* G = al;  // [n][n], over the low parts (no longer needed)
+    // G is stored as two planes, Re and Im, rows of NM floats, over the low
+    // parts (no longer needed); a row product takes four columns of each plane
+    // per 16-byte load and forms pairs of columns with packed FMAs:
+    // re(c, c+1) += x.re G_re(c, c+1) - x.im G_im(c, c+1),
+    // im(c, c+1) += x.re G_im(c, c+1) + x.im G_re(c, c+1).
+    float* Gr = (float*)al;
+    float* Gi = Gr + n * NM;
+    float2 r[NM];
     if (lane < n) {
-      float2 r[NM];
 #pragma unroll
       for (int j = 0; j < NM; ++j) r[j] = make_float2(j == lane ? 1.f : 0.f, 0.f);
 #pragma unroll
@@ -458,8 +474,8 @@ __global__ void __launch_bounds__(OW_WARPS * 32, (F32 && MB && NM <= 20) ? 7 : 1
               t.y -= r[i].x * u.y + r[i].y * u.x;
             }
           const float2 d = ah[j * n + j];
-          const float den = d.x * d.x + d.y * d.y;
-          r[j] = make_float2((t.x * d.x + t.y * d.y) / den, (t.y * d.x - t.x * d.y) / den);
+          const float rd = __frcp_rn(fmaf(d.x, d.x, d.y * d.y));
+          r[j] = make_float2(fmaf(t.x, d.x, t.y * d.y) * rd, fmaf(t.y, d.x, -t.x * d.y) * rd);
         }
       }
 #pragma unroll
@@ -478,25 +494,41 @@ __global__ void __launch_bounds__(OW_WARPS * 32, (F32 && MB && NM <= 20) ? 7 : 1
       }
 #pragma unroll
       for (int k = 0; k < NM; ++k)
-        if (k < n) G[lane * n + perm[k]] = r[k];
+        if (k < n) {
+          Gr[lane * NM + perm[k]] = r[k].x;
+          Gi[lane * NM + perm[k]] = r[k].y;
+        }
     }
     __syncwarp();
     const float2* p32 = psi32 + (size_t)w * ncw * N + (size_t)ch.psi_off * N;
     for (int p = lane; p < N; p += 32) {
+      float2 are[NM / 2], aim[NM / 2];
+#pragma unroll
+      for (int c = 0; c < NM / 2; ++c) are[c] = aim[c] = make_float2(0.f, 0.f);
+      float2 xnext = p32[p];
+#pragma unroll 1
+      for (int j = 0; j < n; ++j) {
+        const float2 x = xnext;
+        if (j + 1 < n) xnext = p32[(size_t)(j + 1) * N + p];
+        const float2 xr = make_float2(x.x, x.x), xi = make_float2(x.y, x.y), xin = make_float2(-x.y, -x.y);
+        const float4* gr4 = (const float4*)(Gr + j * NM);
+        const float4* gi4 = (const float4*)(Gi + j * NM);
+#pragma unroll
+        for (int q = 0; q < NM / 4; ++q) {
+          const float4 gr = gr4[q], gi = gi4[q];
+          const float2 r0 = make_float2(gr.x, gr.y), r1 = make_float2(gr.z, gr.w);
+          const float2 i0 = make_float2(gi.x, gi.y), i1 = make_float2(gi.z, gi.w);
+          are[2 * q] = __ffma2_rn(xin, i0, __ffma2_rn(xr, r0, are[2 * q]));
+          aim[2 * q] = __ffma2_rn(xi, r0, __ffma2_rn(xr, i0, aim[2 * q]));
+          are[2 * q + 1] = __ffma2_rn(xin, i1, __ffma2_rn(xr, r1, are[2 * q + 1]));
+          aim[2 * q + 1] = __ffma2_rn(xi, r1, __ffma2_rn(xr, i1, aim[2 * q + 1]));
+        }
+      }
       float2 acc[NM];
 #pragma unroll
-      for (int c = 0; c < NM; ++c) acc[c] = make_float2(0.f, 0.f);
-#pragma unroll 2
-      for (int j = 0; j < n; ++j) {
-        const float2 x = p32[(size_t)j * N + p];
-        const float2* gj = G + j * n;
-#pragma unroll
-        for (int c = 0; c < NM; ++c)
-          if (c < n) {
-            const float2 gv = gj[c];
-            acc[c].x += x.x * gv.x - x.y * gv.y;
-            acc[c].y += x.x * gv.y + x.y * gv.x;
-          }
+      for (int c = 0; c < NM / 2; ++c) {
+        acc[2 * c] = make_float2(are[c].x, aim[c].x);
+        acc[2 * c + 1] = make_float2(are[c].y, aim[c].y);
       }
 #pragma unroll
       for (int c = 0; c < NM; ++c)

@@ -379,10 +379,20 @@ __global__ void __launch_bounds__(PB_THREADS, 1)
         ++ndone;
         tc::tc_fence_after();
         if (!ok) break;
-        // the product's rows of this thread: Re = C1 re - C2 im, Im = C1 im + C2 re
+        // the product's rows of this thread: Re = C1 re - C2 im, Im = C1 im + C2 re.
+        // The Taylor sums of the row tile are fetched first, in one batch of
+        // independent loads (element by element, each load would wait for the
+        // previous element's store), then combined and stored.
         const float inv = prod >= 1 && prod <= 5 ? 1.f / (float)prod : 1.f;
         for (int m = 0; m < MT; ++m) {
           const int p = 128 * m + pl;
+          float2 accs[CW / 2];
+#pragma unroll
+          for (int q = 0; q < CW / 2; ++q) {
+            const int j = g * (CW / 2) + q;
+            accs[q] = (p < N && j < ncols) ? pw32[(size_t)j * N + p] : make_float2(0.f, 0.f);
+          }
+#pragma unroll
           for (int c8 = 0; c8 < CW / 8; ++c8) {
             const int col = g * CW + 8 * c8;  // first B row of the chunk
             if (col >= 2 * ncols) break;      // warp-uniform
@@ -397,7 +407,7 @@ __global__ void __launch_bounds__(PB_THREADS, 1)
               const float re = cplx ? c1[2 * q] - c2[2 * q + 1] : c1[2 * q];
               const float im = cplx ? c1[2 * q + 1] + c2[2 * q] : c1[2 * q + 1];
               float2* a = pw32 + (size_t)j * N + p;
-              float2 acc = *a;
+              float2 acc = accs[4 * c8 + q];
               float xr, xi;
               if (prod == 0) {  // B psi = psi + (B - I) psi: the Taylor sum starts from it
                 xr = acc.x + re;
