@@ -199,7 +199,15 @@ __device__ double2 lu_df32(float2* ah, float2* al, int* perm, int n, int lane) {
     }
     __syncwarp();
     const df32c inv = dfc_recip(ld_dfc(ah, al, k * n + k));
-    for (int i = k + 1 + lane; i < n; i += 32) st_dfc(ah, al, i * n + k, dfc_mul(ld_dfc(ah, al, i * n + k), inv));
+    const float2 ivh = make_float2(inv.r.h, inv.i.h), ivl = make_float2(inv.r.l, inv.i.l);
+    for (int i = k + 1 + lane; i < n; i += 32) {
+      // x inv as 0 - (-x) inv: the operations and order of dfc_mul(x, inv)
+      const float2 xh = ah[i * n + k], xl = al[i * n + k];
+      float2 yh = make_float2(0.f, 0.f), yl = yh;
+      dfc_fms_planes(yh, yl, f2_neg(xh), f2_neg(xl), ivh, ivl);
+      ah[i * n + k] = yh;
+      al[i * n + k] = yl;
+    }
     __syncwarp();
     const int rem = n - k - 1;
     if (rem > 0) {
@@ -291,6 +299,13 @@ __global__ void __launch_bounds__(OW_WARPS * 32, (F32 && MB && NM <= 20) ? 7 : 1
   if (w >= W) return;
   if (only_live && !(weights[w] > 1.0e-8)) return;
   const double2* ps = psi + (size_t)w * ncw * N + (size_t)ch.psi_off * N;
+  if constexpr (F32) {
+    // the FP32 walker block that the theta products read last, towards L2
+    // now, so that those reads wait on L2 rather than DRAM
+    const char* pb = (const char*)(psi32 + (size_t)w * ncw * N + (size_t)ch.psi_off * N);
+    for (size_t o = (size_t)lane * 128; o < (size_t)n * N * sizeof(float2); o += 32 * 128)
+      asm volatile("prefetch.global.L2 [%0];" ::"l"(pb + o));
+  }
   if constexpr (MB) {
     const float4* mb = mbuf + ((size_t)w * 2 + s) * nmax * nmax;
     for (int e = lane; e < n * n; e += 32) {
@@ -430,16 +445,17 @@ __global__ void __launch_bounds__(OW_WARPS * 32, (F32 && MB && NM <= 20) ? 7 : 1
     }
   }
   if (lane == 0) det[2 * w + s] = detv;
-  // perm[k]: row swapped with k at step k -> final row order of P M
-  if (lane == 0) {
-    int order[NM];
-    for (int i = 0; i < n; ++i) order[i] = i;
-    for (int k = 0; k < n; ++k) {
-      const int t = order[k];
-      order[k] = order[perm[k]];
-      order[perm[k]] = t;
+  // perm[k]: row swapped with k at step k -> final row order of P M: lane q
+  // follows final position q back through the swaps, last to first, to the
+  // row that started there (all lanes at once, no per-lane array)
+  {
+    int pos = lane;
+    for (int t = n - 1; t >= 0; --t) {
+      const int pt = perm[t];
+      pos = pos == t ? pt : (pos == pt ? t : pos);
     }
-    for (int k = 0; k < n; ++k) perm[k] = order[k];
+    __syncwarp();
+    if (lane < n) perm[lane] = pos;
   }
   __syncwarp();
   // theta[p][:] = psi[p][:] M^-1 ; with P M = L U: w U = psi[p], z L = w, theta[perm[k]] = z[k]
