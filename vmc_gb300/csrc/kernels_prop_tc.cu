@@ -35,6 +35,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <algorithm>
+
 #include "afqmc_internal.h"
 #include "device_common.cuh"
 #include "df32.cuh"
@@ -500,11 +502,14 @@ __device__ __forceinline__ void p2_store_chunk(uint8_t* sB, int c, int p, const 
 }
 
 template <bool CPLX>
-__device__ __forceinline__ void p2_issue(uint32_t tmem, uint8_t* sA, uint8_t* sB, int nc) {
+// nc B rows from byte boffs of each B half (0, or 16384: the second MN
+// group) into TMEM columns dcol + (tile) x 80
+__device__ __forceinline__ void p2_issue(uint32_t tmem, uint8_t* sA, uint8_t* sB, int nc, uint32_t dcol = 0,
+                                         uint32_t boffs = 0) {
   const uint32_t idesc = tc::idesc_bf16(128, nc) | (1u << 16);  // B MN-major
   const uint32_t dah = tc::sdesc_lo(tc::smem_u32(sA)), dal = dah + (PT_A_BYTES >> 4);
   // leading byte offset 16 KB (between 64-row groups of B)
-  const uint32_t dbh = ((tc::smem_u32(sB) & 0x3FFFFu) >> 4) | ((uint32_t)(16384 >> 4) << 16);
+  const uint32_t dbh = ((tc::smem_u32(sB + boffs) & 0x3FFFFu) >> 4) | ((uint32_t)(16384 >> 4) << 16);
   const uint32_t dbl = dbh + (P2_B_HALF >> 4);
 #pragma unroll
   for (int s = 0; s < 8; ++s) {
@@ -515,28 +520,57 @@ __device__ __forceinline__ void p2_issue(uint32_t tmem, uint8_t* sA, uint8_t* sB
     for (int pass = 0; pass < 3; ++pass) {
       const uint32_t a = pass == 1 ? dal : dah;
       const uint64_t b = tc::sdesc_from_lo((pass == 2 ? dbl : dbh) + bo);
-      tc::mma_bf16(tmem + (uint32_t)(pass * PT_NCMAX), tc::sdesc_from_lo(a + ao), b, idesc, s > 0 ? 1u : 0u);
+      tc::mma_bf16(tmem + dcol + (uint32_t)(pass * PT_NCMAX), tc::sdesc_from_lo(a + ao), b, idesc, s > 0 ? 1u : 0u);
       if (CPLX)
-        tc::mma_bf16(tmem + (uint32_t)((3 + pass) * PT_NCMAX), tc::sdesc_from_lo(a + ai), b, idesc,
+        tc::mma_bf16(tmem + dcol + (uint32_t)((3 + pass) * PT_NCMAX), tc::sdesc_from_lo(a + ai), b, idesc,
                      s > 0 ? 1u : 0u);
     }
   }
 }
 
+// One product of all B rows.  With two halves (pp) the rows sit in the two
+// MN groups (48 rows in the first, nc - 48 from the start of the second) and
+// are issued as two MMA sets into TMEM columns [0, 48) and [48, nc) of each tile.
 __device__ __forceinline__ bool p2_product(uint8_t* sA, uint8_t* sB, int nc, bool cplx, uint32_t tmem, uint64_t* bar,
-                                           uint32_t& phase, int* err) {
+                                           uint32_t& phase, int* err, bool pp = false) {
   pt_fence_proxy();
   tc::tc_fence_before();
   __syncthreads();
   if (threadIdx.x == 0) {
     tc::tc_fence_after();
-    if (cplx) p2_issue<true>(tmem, sA, sB, nc);
-    else p2_issue<false>(tmem, sA, sB, nc);
+    if (pp) {
+      if (cplx) {
+        p2_issue<true>(tmem, sA, sB, 48);
+        p2_issue<true>(tmem, sA, sB, nc - 48, 48u, 16384u);
+      } else {
+        p2_issue<false>(tmem, sA, sB, 48);
+        p2_issue<false>(tmem, sA, sB, nc - 48, 48u, 16384u);
+      }
+    } else if (cplx) {
+      p2_issue<true>(tmem, sA, sB, nc);
+    } else {
+      p2_issue<false>(tmem, sA, sB, nc);
+    }
     tc::mma_commit(bar);
   }
   const bool ok = pt_wait(bar, phase, err, 21);
   tc::tc_fence_after();
   return ok;
+}
+
+// named barrier of the 256 threads of half hf (barrier 1 + hf), and the same
+// with an AND of v over those threads
+__device__ __forceinline__ void p2_half_sync(int hf) {
+  asm volatile("bar.sync %0, 256;" ::"r"(1 + hf) : "memory");
+}
+__device__ __forceinline__ bool p2_half_and(bool v, int hf) {
+  uint32_t r;
+  asm volatile(
+      "{\n .reg .pred p, q;\n setp.ne.u32 p, %1, 0;\n bar.red.and.pred q, %2, 256, p;\n selp.u32 %0, 1, 0, q;\n}"
+      : "=r"(r)
+      : "r"((uint32_t)v), "r"(1 + hf)
+      : "memory");
+  return r != 0;
 }
 
 // 8 columns of TMEM tiles at ta and tb (this thread's lane), one wait
@@ -578,10 +612,7 @@ __device__ __forceinline__ void p2_chunk(uint32_t tlane, int c, bool cplx, float
 __global__ void __launch_bounds__(PT_THREADS, 1)
     k_prop_tc2(double2* __restrict__ psi, float2* __restrict__ psi32, const float* __restrict__ Vp,
                const __nv_bfloat16* __restrict__ img, const uint2* __restrict__ voff,
-               const double* __restrict__ weights, int N, int ncw, int na, int nspV, int realB, int* err) {
-  const int w = blockIdx.x;
-  if (!(weights[w] > 1.0e-8)) return;
-  const int sp = blockIdx.y;
+               const double* __restrict__ weights, int N, int ncw, int na, int nw, int nspV, int realB, int* err) {
   extern __shared__ uint8_t p2_raw[];
   uint8_t* smem = (uint8_t*)(((uintptr_t)p2_raw + 1023) & ~(uintptr_t)1023);
   uint8_t* sA = smem;                    // hi at 0, lo at PT_A_BYTES
@@ -614,93 +645,116 @@ __global__ void __launch_bounds__(PT_THREADS, 1)
   const uint32_t tlane = tmem + ((uint32_t)((warp & 3) * 32) << 16);
 
   const int T = N * (N + 1) / 2;
-  const float* vre = Vp + ((size_t)(w * nspV + sp) * 2) * T;
-  const float* vim = vre + T;
-  const __nv_bfloat16* im = img + (size_t)sp * 2 * PT_IMG;
-  const int col_lo = nspV == 1 ? 0 : (sp == 0 ? 0 : na);
-  const int col_hi = nspV == 1 ? ncw : (sp == 0 ? na : ncw);
-  double2* pw = psi + (size_t)w * ncw * N;
-  float2* pw32 = psi32 + (size_t)w * ncw * N;
+  const int nunits = nw * nspV;
+  int img_sp = -1;  // spin block whose B - I image A holds (-1: A holds a V)
+  for (int unit = blockIdx.x; unit < nunits && ok; unit += gridDim.x) {
+    const int w = unit / nspV, sp = unit - w * nspV;
+    {
+      // the next unit's FP32 walker block and V towards L2 while this one runs
+      const int nu = unit + gridDim.x;
+      if (nu < nunits) {
+        const int w2 = nu / nspV, sp2 = nu - w2 * nspV;
+        const char* pb = (const char*)(psi32 + (size_t)w2 * ncw * N);
+        const char* vb = (const char*)(Vp + ((size_t)(w2 * nspV + sp2) * 2) * T);
+        const size_t pbytes = (size_t)ncw * N * sizeof(float2), vbytes = (size_t)2 * T * sizeof(float);
+        for (size_t o = (size_t)threadIdx.x * 128; o < pbytes; o += (size_t)blockDim.x * 128)
+          asm volatile("prefetch.global.L2 [%0];" ::"l"(pb + o));
+        for (size_t o = (size_t)threadIdx.x * 128; o < vbytes; o += (size_t)blockDim.x * 128)
+          asm volatile("prefetch.global.L2 [%0];" ::"l"(vb + o));
+      }
+    }
+    if (!(weights[w] > 1.0e-8)) continue;
+    const float* vre = Vp + ((size_t)(w * nspV + sp) * 2) * T;
+    const float* vim = vre + T;
+    const __nv_bfloat16* im = img + (size_t)sp * 2 * PT_IMG;
+    const int col_lo = nspV == 1 ? 0 : (sp == 0 ? 0 : na);
+    const int col_hi = nspV == 1 ? ncw : (sp == 0 ? na : ncw);
+    double2* pw = psi + (size_t)w * ncw * N;
+    float2* pw32 = psi32 + (size_t)w * ncw * N;
 
-  for (int c0 = col_lo; c0 < col_hi && ok; c0 += PT_NCMAX / 2) {
-    const int ncols = min(PT_NCMAX / 2, col_hi - c0);
-    const int nc = ((2 * ncols + 15) / 16) * 16;
-    const int C = nc / 8;                                  // chunks of this pass
-    const int cs = (g * C) / PT_NG, ce = ((g + 1) * C) / PT_NG;  // this group's chunks
-    float x[P2_MAXCH][8], acc[P2_MAXCH][8];
-    __syncthreads();
-    pt_issue_image(sA, im, bar_ld, realB != 0);
-#pragma unroll
-    for (int q = 0; q < P2_MAXCH; ++q) {
-      if (cs + q >= ce) break;
-#pragma unroll
-      for (int jj = 0; jj < 4; ++jj) {
-        const int j = 4 * (cs + q) + jj;  // complex column: B rows 2j, 2j + 1
-        float2 v = make_float2(0.f, 0.f);
-        if (j < ncols && p < N) v = pw32[(size_t)(c0 + j) * N + p];
-        x[q][2 * jj] = v.x;
-        x[q][2 * jj + 1] = v.y;
-      }
-      if (p < N) p2_store_chunk(sB, cs + q, p, x[q]);
-    }
-    if (!(ok = pt_wait(bar_ld, ph_ld, err, 22))) break;
-    // B psi = psi + (B - I) psi
-    if (!(ok = p2_product(sA, sB, nc, !realB, tmem, bar_mma, ph_mma, err))) break;
-#pragma unroll
-    for (int q = 0; q < P2_MAXCH; ++q) {
-      if (cs + q >= ce) break;
-      float t[8];
-      p2_chunk(tlane, cs + q, !realB, t);
-#pragma unroll
-      for (int i = 0; i < 8; ++i) {
-        x[q][i] += t[i];
-        acc[q][i] = x[q][i];
-      }
-    }
-    pt_load_V(sA, vre, vim, voff, T);
-    for (int k = 1; k <= 5 && ok; ++k) {
+    for (int c0 = col_lo; c0 < col_hi && ok; c0 += PT_NCMAX / 2) {
+      const int ncols = min(PT_NCMAX / 2, col_hi - c0);
+      const int nc = ((2 * ncols + 15) / 16) * 16;
+      const int C = nc / 8;                                  // chunks of this pass
+      const int cs = (g * C) / PT_NG, ce = ((g + 1) * C) / PT_NG;  // this group's chunks
+      float x[P2_MAXCH][8], acc[P2_MAXCH][8];
+      __syncthreads();
+      const bool copy = img_sp != sp;  // A still holds this spin block's image after the last product
+      if (copy) pt_issue_image(sA, im, bar_ld, realB != 0);
 #pragma unroll
       for (int q = 0; q < P2_MAXCH; ++q) {
         if (cs + q >= ce) break;
-        if (p < N) p2_store_chunk(sB, cs + q, p, x[q]);
-      }
-      if (!(ok = p2_product(sA, sB, nc, true, tmem, bar_mma, ph_mma, err))) break;
-      const float inv = 1.f / (float)k;
-#pragma unroll
-      for (int q = 0; q < P2_MAXCH; ++q) {
-        if (cs + q >= ce) break;
-        p2_chunk(tlane, cs + q, true, x[q]);
-#pragma unroll
-        for (int i = 0; i < 8; ++i) {
-          x[q][i] *= inv;
-          acc[q][i] += x[q][i];
-        }
-      }
-    }
-    if (!ok) break;
-    // B (sum) = sum + (B - I) sum
-    pt_issue_image(sA, im, bar_ld, realB != 0);
-#pragma unroll
-    for (int q = 0; q < P2_MAXCH; ++q) {
-      if (cs + q >= ce) break;
-      if (p < N) p2_store_chunk(sB, cs + q, p, acc[q]);
-    }
-    if (!(ok = pt_wait(bar_ld, ph_ld, err, 22))) break;
-    if (!(ok = p2_product(sA, sB, nc, !realB, tmem, bar_mma, ph_mma, err))) break;
-#pragma unroll
-    for (int q = 0; q < P2_MAXCH; ++q) {
-      if (cs + q >= ce) break;
-      float t[8];
-      p2_chunk(tlane, cs + q, !realB, t);
-      if (p < N) {
 #pragma unroll
         for (int jj = 0; jj < 4; ++jj) {
-          const int j = 4 * (cs + q) + jj;
-          if (j < ncols) {
-            const float re = acc[q][2 * jj] + t[2 * jj], imv = acc[q][2 * jj + 1] + t[2 * jj + 1];
-            const size_t o = (size_t)(c0 + j) * N + p;
-            pw[o] = make_double2(df_f2d_bits(re), df_f2d_bits(imv));
-            pw32[o] = make_float2(re, imv);
+          const int j = 4 * (cs + q) + jj;  // complex column: B rows 2j, 2j + 1
+          float2 v = make_float2(0.f, 0.f);
+          if (j < ncols && p < N) v = pw32[(size_t)(c0 + j) * N + p];
+          x[q][2 * jj] = v.x;
+          x[q][2 * jj + 1] = v.y;
+        }
+        if (p < N) p2_store_chunk(sB, cs + q, p, x[q]);
+      }
+      if (copy && !(ok = pt_wait(bar_ld, ph_ld, err, 22))) break;
+      // B psi = psi + (B - I) psi
+      if (!(ok = p2_product(sA, sB, nc, !realB, tmem, bar_mma, ph_mma, err))) break;
+#pragma unroll
+      for (int q = 0; q < P2_MAXCH; ++q) {
+        if (cs + q >= ce) break;
+        float t[8];
+        p2_chunk(tlane, cs + q, !realB, t);
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+          x[q][i] += t[i];
+          acc[q][i] = x[q][i];
+        }
+      }
+      img_sp = -1;
+      pt_load_V(sA, vre, vim, voff, T);
+      for (int k = 1; k <= 5 && ok; ++k) {
+#pragma unroll
+        for (int q = 0; q < P2_MAXCH; ++q) {
+          if (cs + q >= ce) break;
+          if (p < N) p2_store_chunk(sB, cs + q, p, x[q]);
+        }
+        if (!(ok = p2_product(sA, sB, nc, true, tmem, bar_mma, ph_mma, err))) break;
+        const float inv = 1.f / (float)k;
+#pragma unroll
+        for (int q = 0; q < P2_MAXCH; ++q) {
+          if (cs + q >= ce) break;
+          p2_chunk(tlane, cs + q, true, x[q]);
+#pragma unroll
+          for (int i = 0; i < 8; ++i) {
+            x[q][i] *= inv;
+            acc[q][i] += x[q][i];
+          }
+        }
+      }
+      if (!ok) break;
+      // B (sum) = sum + (B - I) sum
+      pt_issue_image(sA, im, bar_ld, realB != 0);
+#pragma unroll
+      for (int q = 0; q < P2_MAXCH; ++q) {
+        if (cs + q >= ce) break;
+        if (p < N) p2_store_chunk(sB, cs + q, p, acc[q]);
+      }
+      if (!(ok = pt_wait(bar_ld, ph_ld, err, 22))) break;
+      if (!(ok = p2_product(sA, sB, nc, !realB, tmem, bar_mma, ph_mma, err))) break;
+      img_sp = sp;
+#pragma unroll
+      for (int q = 0; q < P2_MAXCH; ++q) {
+        if (cs + q >= ce) break;
+        float t[8];
+        p2_chunk(tlane, cs + q, !realB, t);
+        if (p < N) {
+#pragma unroll
+          for (int jj = 0; jj < 4; ++jj) {
+            const int j = 4 * (cs + q) + jj;
+            if (j < ncols) {
+              const float re = acc[q][2 * jj] + t[2 * jj], imv = acc[q][2 * jj + 1] + t[2 * jj + 1];
+              const size_t o = (size_t)(c0 + j) * N + p;
+              pw[o] = make_double2(df_f2d_bits(re), df_f2d_bits(imv));
+              pw32[o] = make_float2(re, imv);
+            }
           }
         }
       }
@@ -714,11 +768,16 @@ __global__ void __launch_bounds__(PT_THREADS, 1)
   }
 }
 
+
+
 void launch_propagate_tc2(afqmc_handle* h) {
   smem_optin(k_prop_tc2, P2_SMEM);
-  dim3 grid(h->nwalk, h->nspV);
+  // persistent: one CTA per SM takes (walker, V block) units in turn
+  const int units = h->nwalk * h->nspV;
+  const int grid = std::max(1, std::min(units, h->nsm > 0 ? h->nsm : units));
   k_prop_tc2<<<grid, PT_THREADS, P2_SMEM, h->stream>>>(h->psi, h->psi32, h->V32, h->pt_img, h->pt_voff, h->weights,
-                                                      h->N, h->ncw, h->na, h->nspV, h->real_expm ? 1 : 0, h->d_err);
+                                                      h->N, h->ncw, h->na, h->nwalk, h->nspV, h->real_expm ? 1 : 0,
+                                                      h->d_err);
   h->launches++;
 }
 
