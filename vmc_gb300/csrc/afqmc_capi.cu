@@ -443,7 +443,8 @@ int afqmc_create(const afqmc_ham* ham, const afqmc_trial* trial, const afqmc_opt
     h->nchunks32 = (int)h->chunks32.size();
   }
   const bool mixed = h->precision == AFQMC_PREC_MIXED;
-  h->kf_pad = (3 * h->nce * N + 63) / 64 * 64;
+  h->kf_seg = (h->nce * N + 63) / 64 * 64;
+  h->kf_pad = 3 * h->kf_seg;
   h->kv_pad = (3 * G + 63) / 64 * 64;
   h->ke_pad = (3 * N + 63) / 64 * 64;
   h->nechunk = std::max(1, std::min(G, (4 * 152 + h->nwalk - 1) / h->nwalk));
@@ -491,7 +492,7 @@ int afqmc_create(const afqmc_ham* ham, const afqmc_trial* trial, const afqmc_opt
   if (mixed) {
     ALLOC(rotA, (size_t)G * h->kf_pad);
     ALLOC(LTA, (size_t)nsp * T * h->kv_pad);
-    ALLOC(thetaB, W * 2 * h->kf_pad);
+    ALLOC(thetaB, W * 2 * 2 * h->kf_seg);
     ALLOC(xB, W * 2 * h->kv_pad);
     ALLOC(fb32, W * 2 * G);
     ALLOC(mf32, (size_t)G);
@@ -571,7 +572,7 @@ int afqmc_create(const afqmc_ham* ham, const afqmc_trial* trial, const afqmc_opt
     UP(expm32, e32);
     UP(d_chunks32, h->chunks32);
     ce = cudaMemsetAsync(h->xB, 0, W * 2 * h->kv_pad * sizeof(__nv_bfloat16), h->stream);
-    if (ce == cudaSuccess) ce = cudaMemsetAsync(h->thetaB, 0, W * 2 * h->kf_pad * sizeof(__nv_bfloat16), h->stream);
+    if (ce == cudaSuccess) ce = cudaMemsetAsync(h->thetaB, 0, W * 2 * 2 * h->kf_seg * sizeof(__nv_bfloat16), h->stream);
     if (ce != cudaSuccess || !afqmc::setup_mixed(h)) {
       g_create_err = ce != cudaSuccess ? cudaGetErrorString(ce) : "tensor map encoding failed";
       release(h);

@@ -122,9 +122,10 @@ struct afqmc_handle {
   // mixed-precision form
   int* d_err = nullptr;              // error code of bounded device waits (0 = none)
   int kf_pad = 0, kv_pad = 0;        // padded split-K lengths of the force-bias / VHS GEMMs
-  __nv_bfloat16* rotA = nullptr;     // [G][kf_pad]       [hi | hi | lo] of rot
+  int kf_seg = 0;                    // force bias: nce N rounded up to 64; kf_pad = 3 kf_seg
+  __nv_bfloat16* rotA = nullptr;     // [G][kf_pad]       [hi | hi | lo] of rot, segments kf_seg apart
   __nv_bfloat16* LTA = nullptr;      // [nsp][T][kv_pad]  [hi | hi | lo] of LT
-  __nv_bfloat16* thetaB = nullptr;   // [2W][kf_pad]      [hi | lo | hi] of theta planes
+  __nv_bfloat16* thetaB = nullptr;   // [2W][2 kf_seg]    [hi | lo] of theta planes (the GEMM reads hi twice)
   __nv_bfloat16* xB = nullptr;       // [2W][kv_pad]      [hi | lo | hi] of field planes
   float* fb32 = nullptr;             // [W][2][G]
   float* V32 = nullptr;              // [W][nspV][2][T]   packed VHS, re / im planes
@@ -233,9 +234,11 @@ void launch_force_bias_mixed(afqmc_handle* h);
 void launch_fields_mixed(afqmc_handle* h, bool device_rng);
 void launch_vhs_mixed(afqmc_handle* h);
 void launch_propagate_mixed(afqmc_handle* h);
-void split_rows(afqmc_handle* h, const double* src, long lds, int rows, int K, int kpad, int pattern,
+void split_rows(afqmc_handle* h, const double* src, long lds, int rows, int K, int kpad, int pattern, int seg,
+                int nseg,
                 __nv_bfloat16* dst);
-void split_rows(afqmc_handle* h, const float* src, long lds, int rows, int K, int kpad, int pattern,
+void split_rows(afqmc_handle* h, const float* src, long lds, int rows, int K, int kpad, int pattern, int seg,
+                int nseg,
                 __nv_bfloat16* dst);
 void launch_local_energy_mixed(afqmc_handle* h);
 void launch_wait_probe(afqmc_handle* h);  // one bounded mbarrier wait that nothing completes

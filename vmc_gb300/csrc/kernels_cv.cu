@@ -49,9 +49,25 @@ __global__ void k_cv_features32(const float* __restrict__ fb32, const float* __r
   float* o = out + (size_t)w * CV_NF;
   for (int g = threadIdx.x; g < 64; g += blockDim.x) o[g] = g < G ? fb32[(size_t)(2 * w) * G + g] : 0.f;
   const float* tre = theta + (size_t)(2 * w) * nce * N;
-  float e1 = 0.f;
-  for (int k = threadIdx.x; k < nce * N; k += blockDim.x) e1 = fmaf(tre[k], h1phi32[k].x, e1);
-  e1 = warp_sumf(e1);
+  // four elements per step: one 16-byte load of theta, two of the (high, low)
+  // pairs of h1 Phi (high parts used), four independent partial sums
+  const int K = nce * N;
+  float p0 = 0.f, p1 = 0.f, p2 = 0.f, p3 = 0.f;
+  int k0 = 0;
+  if ((((uintptr_t)tre) & 15) == 0) {
+    const float4* t4 = (const float4*)tre;
+    const float4* h4 = (const float4*)h1phi32;
+    for (int k = threadIdx.x; k < K / 4; k += blockDim.x) {
+      const float4 t = t4[k], ha = h4[2 * k], hb = h4[2 * k + 1];
+      p0 = fmaf(t.x, ha.x, p0);
+      p1 = fmaf(t.y, ha.z, p1);
+      p2 = fmaf(t.z, hb.x, p2);
+      p3 = fmaf(t.w, hb.z, p3);
+    }
+    k0 = K / 4 * 4;
+  }
+  for (int k = k0 + threadIdx.x; k < K; k += blockDim.x) p0 = fmaf(tre[k], h1phi32[k].x, p0);
+  float e1 = warp_sumf((p0 + p1) + (p2 + p3));
   if ((threadIdx.x & 31) == 0) s_part[threadIdx.x >> 5] = e1;
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -112,26 +128,43 @@ __global__ void k_cv_select(int* __restrict__ idx, int W, int den, uint64_t seed
 }
 
 // dst rows (i, plane, c) = split of theta rows of walker idx[i] ([hi | lo | hi]
-// along p, zeros to kpad); one block per (i, plane) covering its nce rows
+// along p, zeros to kpad).  Grid (m x 2 (i, plane), row blocks of GT_ROWS);
+// every thread writes pairs of adjacent positions (one 8-byte load, one
+// 4-byte store) when N and kpad are even, single positions otherwise; all the
+// rows of the block are one flat loop of independent iterations.
+constexpr int GT_ROWS = 8;
 __global__ void k_split_theta_gather(const float* __restrict__ theta, const int* __restrict__ idx, int m, int nce,
                                      int N, int kpad, __nv_bfloat16* __restrict__ dst) {
   const int ip = blockIdx.x;  // (i, plane)
   const int i = ip >> 1, plane = ip & 1;
-  const float* s = theta + ((size_t)idx[i] * 2 + plane) * nce * N;
-  __nv_bfloat16* d = dst + (size_t)ip * nce * kpad;
-  const __nv_bfloat16 z = __float2bfloat16_rn(0.f);
-  for (int c = 0; c < nce; ++c) {
-    const float* sr = s + (size_t)c * N;
-    __nv_bfloat16* dr = d + (size_t)c * kpad;
-    for (int p = threadIdx.x; p < N; p += blockDim.x) {
-      const float x = sr[p];
-      const __nv_bfloat16 hi = __float2bfloat16_rn(x);
-      const __nv_bfloat16 lo = __float2bfloat16_rn(x - __bfloat162float(hi));
-      dr[p] = hi;
-      dr[N + p] = lo;
-      dr[2 * N + p] = hi;
+  const int c0 = blockIdx.y * GT_ROWS, rows = min(GT_ROWS, nce - c0);
+  const float* s = theta + ((size_t)idx[i] * 2 + plane) * nce * N + (size_t)c0 * N;
+  __nv_bfloat16* d = dst + (size_t)ip * nce * kpad + (size_t)c0 * kpad;
+  if (((N | kpad) & 1) == 0) {
+    const int hk = kpad / 2;
+    for (int e = threadIdx.x; e < rows * hk; e += blockDim.x) {
+      const int c = e / hk, k = 2 * (e - c * hk);
+      __nv_bfloat162 v = __floats2bfloat162_rn(0.f, 0.f);
+      if (k < 3 * N) {
+        const int seg = k / N, pp = k - seg * N;
+        const float2 x = *(const float2*)(s + (size_t)c * N + pp);
+        const __nv_bfloat162 hi = __floats2bfloat162_rn(x.x, x.y);
+        v = seg == 1 ? __floats2bfloat162_rn(x.x - __low2float(hi), x.y - __high2float(hi)) : hi;
+      }
+      *(__nv_bfloat162*)(d + (size_t)c * kpad + k) = v;
     }
-    for (int k = 3 * N + threadIdx.x; k < kpad; k += blockDim.x) dr[k] = z;
+  } else {
+    for (int e = threadIdx.x; e < rows * kpad; e += blockDim.x) {
+      const int c = e / kpad, k = e - c * kpad;
+      __nv_bfloat16 v = __float2bfloat16_rn(0.f);
+      if (k < 3 * N) {
+        const int seg = k / N, pp = k - seg * N;
+        const float x = s[(size_t)c * N + pp];
+        const __nv_bfloat16 hi = __float2bfloat16_rn(x);
+        v = seg == 1 ? __float2bfloat16_rn(x - __bfloat162float(hi)) : hi;
+      }
+      d[(size_t)c * kpad + k] = v;
+    }
   }
 }
 
@@ -200,7 +233,8 @@ namespace afqmc {
 void launch_local_energy_mixed_subset(afqmc_handle* h, const int* d_idx, int m, double2* out);
 
 void launch_split_theta_gather(afqmc_handle* h, const int* d_idx, int m) {
-  k_split_theta_gather<<<m * 2, 128, 0, h->stream>>>(h->theta32, d_idx, m, h->nce, h->N, h->ke_pad, h->thetaE);
+  dim3 grid(m * 2, (h->nce + GT_ROWS - 1) / GT_ROWS);
+  k_split_theta_gather<<<grid, 256, 0, h->stream>>>(h->theta32, d_idx, m, h->nce, h->N, h->ke_pad, h->thetaE);
   h->launches++;
 }
 }

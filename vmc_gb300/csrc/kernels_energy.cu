@@ -221,7 +221,28 @@ __global__ void k_energy_assemble(const float* __restrict__ theta, const float2*
   const float* tre = theta + (size_t)(2 * ws) * nce * N;
   const float* tim = tre + (size_t)nce * N;
   float sr = 0.f, cr = 0.f, si = 0.f, ci = 0.f;
-  for (int k = threadIdx.x; k < nce * N; k += blockDim.x) {
+  const int K = nce * N;
+  int k0 = 0;
+  if (((((uintptr_t)tre) | ((uintptr_t)tim)) & 15) == 0) {
+    // four elements per step: 16-byte loads of both planes and of two (high,
+    // low) pairs of h1 Phi, all issued before the compensated sums use them
+    const float4* r4 = (const float4*)tre;
+    const float4* i4 = (const float4*)tim;
+    const float4* h4 = (const float4*)h1phi;
+    for (int k = threadIdx.x; k < K / 4; k += blockDim.x) {
+      const float4 a = r4[k], b = i4[k], ha = h4[2 * k], hb = h4[2 * k + 1];
+      dot2_acc(sr, cr, ha.x, ha.y, a.x);
+      dot2_acc(si, ci, ha.x, ha.y, b.x);
+      dot2_acc(sr, cr, ha.z, ha.w, a.y);
+      dot2_acc(si, ci, ha.z, ha.w, b.y);
+      dot2_acc(sr, cr, hb.x, hb.y, a.z);
+      dot2_acc(si, ci, hb.x, hb.y, b.z);
+      dot2_acc(sr, cr, hb.z, hb.w, a.w);
+      dot2_acc(si, ci, hb.z, hb.w, b.w);
+    }
+    k0 = K / 4 * 4;
+  }
+  for (int k = k0 + threadIdx.x; k < K; k += blockDim.x) {
     const float2 hp = h1phi[k];
     dot2_acc(sr, cr, hp.x, hp.y, tre[k]);
     dot2_acc(si, ci, hp.x, hp.y, tim[k]);
@@ -264,7 +285,7 @@ void launch_split_theta_gather(afqmc_handle* h, const int* d_idx, int m);
 void launch_local_energy_mixed_subset(afqmc_handle* h, const int* d_idx, int m, double2* out) {
   const int Kn = h->N;
   if (d_idx) launch_split_theta_gather(h, d_idx, m);
-  else split_rows(h, h->theta32, Kn, 2 * m * h->nce, Kn, h->ke_pad, 1, h->thetaE);
+  else split_rows(h, h->theta32, Kn, 2 * m * h->nce, Kn, h->ke_pad, 1, Kn, 3, h->thetaE);
   smem_optin(k_tc_exchange, (int)ex_smem(128));
   ExArgs a[2];
   size_t smem = 0;

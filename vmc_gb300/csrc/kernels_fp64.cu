@@ -261,7 +261,7 @@ __global__ void __launch_bounds__(OW_WARPS * 32, (F32 && MB && NM <= 20) ? 7 : 1
                  double* __restrict__ theta, float* __restrict__ theta32, double2* __restrict__ det,
                  const double* __restrict__ weights, int W, int N, int ncw, int nce, Channel c0, Channel c1,
                  int only_live, int nmax, const float4* __restrict__ mbuf, __nv_bfloat16* __restrict__ thetaB,
-                 int kf_pad, int m_from32) {
+                 int kf_seg, int m_from32) {
   static_assert(F32 || !MB, "M formed beforehand only in the mixed form");
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int s = blockIdx.y;
@@ -553,11 +553,11 @@ __global__ void __launch_bounds__(OW_WARPS * 32, (F32 && MB && NM <= 20) ? 7 : 1
           tim[(size_t)c * N + p] = acc[c].y;
         }
       if (thetaB) {
-        // the force bias's operand: rows (w, re) and (w, im), [hi | lo | hi] along
-        // K = nce N (what k_split_rows would write from theta32)
-        const int Kf = nce * N;
-        __nv_bfloat16* br = thetaB + (size_t)(2 * w) * kf_pad + (size_t)ch.col_off * N + p;
-        __nv_bfloat16* bi = br + kf_pad;
+        // the force bias's operand: rows (w, re) and (w, im) of 2 kf_seg
+        // columns, [hi | lo] with the segments kf_seg apart (what k_split_rows
+        // writes from theta32 with two segments)
+        __nv_bfloat16* br = thetaB + (size_t)(2 * w) * 2 * kf_seg + (size_t)ch.col_off * N + p;
+        __nv_bfloat16* bi = br + 2 * kf_seg;
 #pragma unroll
         for (int c = 0; c < NM; ++c)
           if (c < n) {
@@ -567,11 +567,9 @@ __global__ void __launch_bounds__(OW_WARPS * 32, (F32 && MB && NM <= 20) ? 7 : 1
             const __nv_bfloat16 il = __float2bfloat16_rn(acc[c].y - __bfloat162float(ih));
             const size_t o = (size_t)c * N;
             br[o] = rh;
-            br[o + Kf] = rl;
-            br[o + 2 * Kf] = rh;
+            br[o + kf_seg] = rl;
             bi[o] = ih;
-            bi[o + Kf] = il;
-            bi[o + 2 * Kf] = ih;
+            bi[o + kf_seg] = il;
           }
       }
     }
@@ -654,7 +652,7 @@ void launch_overlap_theta(afqmc_handle* h, bool only_live) {
     k_overlap_lu<F, NMV, MBV><<<grid, OW_WARPS * 32, smem, h->stream>>>(                                     \
         h->psi, h->psi32, h->phi, h->theta, h->theta32, h->det, h->weights, h->nwalk, h->N, h->ncw, h->nce,  \
         h->chan[0],                                                                                          \
-        h->chan[1], only_live ? 1 : 0, nmax, h->ovl_M, F ? h->thetaB : nullptr, h->kf_pad, h->N > 128 ? 1 : 0); \
+        h->chan[1], only_live ? 1 : 0, nmax, h->ovl_M, F ? h->thetaB : nullptr, h->kf_seg, h->N > 128 ? 1 : 0); \
   }
 #define OW_NM(F, MBV)                          \
   switch (nm) {                                \
@@ -1045,7 +1043,10 @@ __global__ void k_propagate(double2* __restrict__ psi, const double* __restrict_
 // Per-walker part over many CTAs (the FP64 transcendentals of one walker are
 // the cost; one SM would take ~0.1 ms for 2048 walkers); each CTA writes its
 // partial sums, which k_weights_final adds in CTA order.
-constexpr int WT_THREADS = 128;
+// one warp per CTA: the per-walker work is FP64 transcendentals, whose pipe is
+// narrow, so the walkers are spread over as many SMs as possible (64 CTAs for
+// 2048 walkers rather than 16)
+constexpr int WT_THREADS = 32;
 __global__ void __launch_bounds__(WT_THREADS)
     k_weights(double* __restrict__ weights, double2* __restrict__ ovlp, const double2* __restrict__ det,
               const double2* __restrict__ shift, const double2* __restrict__ fbterm, const double* __restrict__ scal,

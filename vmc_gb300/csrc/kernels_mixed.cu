@@ -84,13 +84,15 @@ __device__ __forceinline__ void split_bf16(float x, __nv_bfloat16& hi, __nv_bflo
   lo = __float2bfloat16_rn(x - __bfloat162float(hi));
 }
 
-// dst[r][0:3K] = pattern of src[r][0:K] (FP64, row stride lds); pattern 0:
-// [hi | hi | lo] (the static side), 1: [hi | lo | hi] (the per-step side).
-// Columns 3K .. kpad-1 are zero.  Grid (column blocks, rows); each thread
-// splits one source element and writes its three copies.
+// dst[r] = segments of src[r][0:K] (row stride lds), seg columns apart: with
+// nseg = 3, pattern 0 is [hi | hi | lo] (the static side) and pattern 1
+// [hi | lo | hi] (the per-step side); nseg = 2 is [hi | lo] (a per-step side
+// whose GEMM reads its first segment again for the third).  Columns of a
+// segment beyond K and columns nseg seg .. kpad-1 are zero.  Grid (column
+// blocks, rows); each thread splits one source element and writes its copies.
 template <class T>
-__global__ void k_split_rows(const T* __restrict__ src, long lds, int rows, int K, int kpad, int pattern,
-                             __nv_bfloat16* __restrict__ dst) {
+__global__ void k_split_rows(const T* __restrict__ src, long lds, int rows, int K, int kpad, int pattern, int seg,
+                             int nseg, __nv_bfloat16* __restrict__ dst) {
   const int r = blockIdx.y;
   const T* s = src + (long)r * lds;
   __nv_bfloat16* d = dst + (long)r * kpad;
@@ -98,31 +100,32 @@ __global__ void k_split_rows(const T* __restrict__ src, long lds, int rows, int 
     __nv_bfloat16 hi, lo;
     split_bf16(s[k], hi, lo);
     d[k] = hi;
-    d[K + k] = pattern == 0 ? hi : lo;
-    d[2 * K + k] = pattern == 0 ? lo : hi;
+    d[seg + k] = pattern == 0 ? hi : lo;
+    if (nseg == 3) d[2 * seg + k] = pattern == 0 ? lo : hi;
   }
   const __nv_bfloat16 z = __float2bfloat16_rn(0.f);
-  for (int c = 3 * K + blockIdx.x * blockDim.x + threadIdx.x; c < kpad; c += gridDim.x * blockDim.x) d[c] = z;
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < kpad; c += gridDim.x * blockDim.x)
+    if (c >= nseg * seg || c % seg >= K) d[c] = z;
 }
 
 template <class T>
-static void split_rows_t(afqmc_handle* h, const T* src, long lds, int rows, int K, int kpad, int pattern,
-                         __nv_bfloat16* dst) {
+static void split_rows_t(afqmc_handle* h, const T* src, long lds, int rows, int K, int kpad, int pattern, int seg,
+                         int nseg, __nv_bfloat16* dst) {
   const int cb = std::max(1, std::min(8, (K + 255) / 256));
   for (int r0 = 0; r0 < rows; r0 += 65535) {
     dim3 grid(cb, std::min(65535, rows - r0));
-    k_split_rows<T><<<grid, 256, 0, h->stream>>>(src + (long)r0 * lds, lds, rows - r0, K, kpad, pattern,
+    k_split_rows<T><<<grid, 256, 0, h->stream>>>(src + (long)r0 * lds, lds, rows - r0, K, kpad, pattern, seg, nseg,
                                                  dst + (long)r0 * kpad);
     h->launches++;
   }
 }
-void split_rows(afqmc_handle* h, const double* src, long lds, int rows, int K, int kpad, int pattern,
-                __nv_bfloat16* dst) {
-  split_rows_t(h, src, lds, rows, K, kpad, pattern, dst);
+void split_rows(afqmc_handle* h, const double* src, long lds, int rows, int K, int kpad, int pattern, int seg,
+                int nseg, __nv_bfloat16* dst) {
+  split_rows_t(h, src, lds, rows, K, kpad, pattern, seg, nseg, dst);
 }
-void split_rows(afqmc_handle* h, const float* src, long lds, int rows, int K, int kpad, int pattern,
-                __nv_bfloat16* dst) {
-  split_rows_t(h, src, lds, rows, K, kpad, pattern, dst);
+void split_rows(afqmc_handle* h, const float* src, long lds, int rows, int K, int kpad, int pattern, int seg,
+                int nseg, __nv_bfloat16* dst) {
+  split_rows_t(h, src, lds, rows, K, kpad, pattern, seg, nseg, dst);
 }
 
 // ---------------------------------------------------------------------------
@@ -153,7 +156,7 @@ struct EpiV32 {
 
 template <int BN, class Epi>
 static void launch_tc_bn(afqmc_handle* h, const CUtensorMap& ta, const CUtensorMap& tb, int M, int N, int K,
-                         const Epi& epi) {
+                         const Epi& epi, int kwrap_b) {
   constexpr int ST = 4;
   const int smem = tc::GemmPSmem<BN, ST>::TOTAL;
   smem_optin(tc::k_tc_gemm_p<BN, ST, Epi>, smem);
@@ -161,7 +164,7 @@ static void launch_tc_bn(afqmc_handle* h, const CUtensorMap& ta, const CUtensorM
   // persistent: one CTA per SM (or per tile when there are fewer tiles)
   const int tiles = ((N + BN - 1) / BN) * ((M + tc::BM - 1) / tc::BM);
   const int grid = std::max(1, std::min(tiles, nsm > 0 ? nsm : tiles));
-  tc::k_tc_gemm_p<BN, ST, Epi><<<grid, tc::GP_THREADS, smem, h->stream>>>(ta, tb, M, N, K, epi, h->d_err);
+  tc::k_tc_gemm_p<BN, ST, Epi><<<grid, tc::GP_THREADS, smem, h->stream>>>(ta, tb, M, N, K, epi, h->d_err, kwrap_b);
   h->launches++;
 }
 
@@ -169,23 +172,23 @@ static void launch_tc_bn(afqmc_handle* h, const CUtensorMap& ta, const CUtensorM
 // tbs holds the B-operand tensor maps of the three box heights.
 template <class Epi>
 static void launch_tc(afqmc_handle* h, const CUtensorMap& ta, const CUtensorMap* tbs, int bn, int M, int N, int K,
-                      const Epi& epi) {
-  if (bn == 64) launch_tc_bn<64>(h, ta, tbs[0], M, N, K, epi);
-  else if (bn == 256) launch_tc_bn<256>(h, ta, tbs[2], M, N, K, epi);
-  else launch_tc_bn<128>(h, ta, tbs[1], M, N, K, epi);
+                      const Epi& epi, int kwrap_b = 0) {
+  if (bn == 64) launch_tc_bn<64>(h, ta, tbs[0], M, N, K, epi, kwrap_b);
+  else if (bn == 256) launch_tc_bn<256>(h, ta, tbs[2], M, N, K, epi, kwrap_b);
+  else launch_tc_bn<128>(h, ta, tbs[1], M, N, K, epi, kwrap_b);
 }
 
 // theta planes (FP64) -> split BF16 operand rows (w, plane)
 void launch_theta_split(afqmc_handle* h) {
   const int K = h->nce * h->N;
-  split_rows(h, h->theta32, K, 2 * h->nwalk, K, h->kf_pad, 1, h->thetaB);
+  split_rows(h, h->theta32, K, 2 * h->nwalk, K, 2 * h->kf_seg, 1, h->kf_seg, 2, h->thetaB);
 }
 
 void launch_force_bias_mixed(afqmc_handle* h) {
   if (h->fb_current) return;  // already computed from this theta (control-variate features)
   if (!h->thetaB_from_lu) launch_theta_split(h);
   EpiFB epi{h->fb32, h->G, (float)h->mult};
-  launch_tc(h, h->tm_rot, h->tm_theta_bn, h->tune_bn_fb, h->G, 2 * h->nwalk, h->kf_pad, epi);
+  launch_tc(h, h->tm_rot, h->tm_theta_bn, h->tune_bn_fb, h->G, 2 * h->nwalk, h->kf_pad, epi, 2 * h->kf_seg);
   h->fb_current = true;
 }
 
@@ -604,24 +607,24 @@ void launch_propagate_mixed(afqmc_handle* h) {
 // static operands of the mixed form, from the FP64 device copies
 bool setup_mixed(afqmc_handle* h) {
   const int Kf = h->nce * h->N;
-  split_rows(h, h->rot, Kf, h->G, Kf, h->kf_pad, 0, h->rotA);
+  split_rows(h, h->rot, Kf, h->G, Kf, h->kf_pad, 0, h->kf_seg, 3, h->rotA);
   for (int s = 0; s < h->nsp; ++s)
-    split_rows(h, h->LT + (size_t)s * h->T * h->G, h->G, h->T, h->G, h->kv_pad, 0,
+    split_rows(h, h->LT + (size_t)s * h->T * h->G, h->G, h->T, h->G, h->kv_pad, 0, h->G, 3,
                h->LTA + (size_t)s * h->T * h->kv_pad);
   k_split_mf<<<(h->G + 127) / 128, 128, 0, h->stream>>>(h->mf, h->mf32, h->G);
   // the force bias's theta operand: its padding columns stay zero when the LU writes it
-  cudaMemsetAsync(h->thetaB, 0, (size_t)h->nwalk * 2 * h->kf_pad * sizeof(__nv_bfloat16), h->stream);
+  cudaMemsetAsync(h->thetaB, 0, (size_t)h->nwalk * 2 * 2 * h->kf_seg * sizeof(__nv_bfloat16), h->stream);
   k_to_df32<<<(h->nce * h->N + 255) / 256, 256, 0, h->stream>>>(h->h1phi, h->h1phi32, h->nce * h->N);
   k_to_df32<<<(h->nce * h->N + 255) / 256, 256, 0, h->stream>>>(h->phi, h->phi2, h->nce * h->N);
   bool ok = setup_prop_tc(h) && setup_ovl_tc(h) && make_tmap_bf16(&h->tm_rot, h->rotA, h->G, h->kf_pad, tc::BM);
   const int bns[3] = {64, 128, 256};
   for (int i = 0; i < 3 && ok; ++i)
-    ok = make_tmap_bf16(&h->tm_theta_bn[i], h->thetaB, 2 * h->nwalk, h->kf_pad, bns[i]) &&
+    ok = make_tmap_bf16(&h->tm_theta_bn[i], h->thetaB, 2 * h->nwalk, 2 * h->kf_seg, bns[i]) &&
          make_tmap_bf16(&h->tm_x_bn[i], h->xB, 2 * h->nwalk, h->kv_pad, bns[i]);
   for (int s = 0; s < h->nsp && ok; ++s)
     ok = make_tmap_bf16(&h->tm_LT[s], h->LTA + (size_t)s * h->T * h->kv_pad, h->T, h->kv_pad, tc::BM);
   // local energy: rot split along p, [G][nce][ke_pad]; tiles of whole (g, walker) blocks
-  split_rows(h, h->rot, h->N, h->G * h->nce, h->N, h->ke_pad, 0, h->rotE);
+  split_rows(h, h->rot, h->N, h->G * h->nce, h->N, h->ke_pad, 0, h->N, 3, h->rotE);
   for (int s = 0; s < h->nchan && ok; ++s) {
     const int n = h->chan[s].n;
     h->ex_gbox[s] = std::max(1, 128 / n);
@@ -638,7 +641,7 @@ namespace afqmc {
 // single GEMMs for the autotuner (operands must be current)
 void launch_fb_gemm(afqmc_handle* h, int bn) {
   EpiFB epi{h->fb32, h->G, (float)h->mult};
-  launch_tc(h, h->tm_rot, h->tm_theta_bn, bn, h->G, 2 * h->nwalk, h->kf_pad, epi);
+  launch_tc(h, h->tm_rot, h->tm_theta_bn, bn, h->G, 2 * h->nwalk, h->kf_pad, epi, 2 * h->kf_seg);
 }
 void launch_vhs_gemm(afqmc_handle* h, int bn) {
   for (int s = 0; s < h->nspV; ++s) {

@@ -178,7 +178,10 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
 // each) run the epilogue of tile i while the MMAs of tile i + 1 proceed; the
 // accumulators are handed over by acc_full (MMA commit) and acc_empty (the 128
 // epilogue threads).  Every wait is bounded; on a timeout the roles leave
-// their loops, issued loads land, and TMEM is freed.
+// their loops, issued loads land, and TMEM is freed.  kwrap_b > 0: the B
+// operand holds K columns [0, kwrap_b) only and K blocks at or beyond kwrap_b
+// read B from kwrap_b columns earlier (a [hi | lo] operand read as
+// [hi | lo | hi] against A's [hi | hi | lo]).
 template <int BN, int STAGES>
 struct GemmPSmem {
   static constexpr int A_BYTES = BM * BK * 2;
@@ -192,7 +195,7 @@ constexpr int GP_THREADS = 192;
 template <int BN, int STAGES, class Epi>
 __global__ void __launch_bounds__(GP_THREADS, 1)
     k_tc_gemm_p(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, int M, int N,
-                int K, Epi epi, int* err) {
+                int K, Epi epi, int* err, int kwrap_b = 0) {
   using L = GemmPSmem<BN, STAGES>;
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
@@ -241,7 +244,8 @@ __global__ void __launch_bounds__(GP_THREADS, 1)
           uint8_t* a = smem + s * L::STAGE_BYTES;
           mbar_expect_tx(&full[s], L::STAGE_BYTES);
           tma_load_2d(a, &tmA, &full[s], kb * BK, m0);
-          tma_load_2d(a + L::A_BYTES, &tmB, &full[s], kb * BK, n0);
+          const int kx = kb * BK;
+          tma_load_2d(a + L::A_BYTES, &tmB, &full[s], kwrap_b > 0 && kx >= kwrap_b ? kx - kwrap_b : kx, n0);
         }
       }
       // the loads already issued land before the CTA releases its shared memory
