@@ -1040,12 +1040,17 @@ __global__ void k_propagate(double2* __restrict__ psi, const double* __restrict_
 // weights (DQMCWalker.cpp:495-502, MixedEstimator.cpp:461-475): importance
 // function, phaseless projection, cap, sum of weights, next eshift.  One CTA.
 // ---------------------------------------------------------------------------
-// Per-walker part over many CTAs (the FP64 transcendentals of one walker are
-// the cost; one SM would take ~0.1 ms for 2048 walkers); each CTA writes its
-// partial sums, which k_weights_final adds in CTA order.
-// one warp per CTA: the per-walker work is FP64 transcendentals, whose pipe is
-// narrow, so the walkers are spread over as many SMs as possible (64 CTAs for
-// 2048 walkers rather than 16)
+// Per-walker part over many CTAs, one warp each (the per-walker work is a
+// chain of FP64 operations whose latency sets the kernel's time); each CTA
+// writes its partial sums, which k_weights_final adds in CTA order.
+//
+// The reference forms imp = exp(ex) ratio, ph = exp(-sdt shift) ratio,
+// th = arg(ph) and val = |imp| cos(th).  The same value by identity, with one
+// real exponential and one sine / cosine pair instead of two complex
+// exponentials, an arctangent, a hypotenuse and a cosine:
+//   |imp| = exp(Re ex) |ratio|,  th = arg(ratio) - sdt Im(shift),
+//   val = exp(Re ex) Re(ratio exp(-i sdt Im(shift))).
+// (A non-finite ratio gives a non-finite val, which the window sets to 0.)
 constexpr int WT_THREADS = 32;
 __global__ void __launch_bounds__(WT_THREADS)
     k_weights(double* __restrict__ weights, double2* __restrict__ ovlp, const double2* __restrict__ det,
@@ -1066,11 +1071,10 @@ __global__ void __launch_bounds__(WT_THREADS)
       if (mult == 2) on = cmul(on, on);
       const double2 ratio = cdiv(on, ovlp[w]);
       const double2 sh = shift[w], ft = fbterm[w];
-      const double2 ex = make_double2(-sdt * sh.x + ft.x + dt * (eshift + c0r), -sdt * sh.y + ft.y + dt * c0i);
-      const double2 imp = cmul(cexp_d(ex), ratio);
-      const double2 ph = cmul(cexp_d(make_double2(-sdt * sh.x, -sdt * sh.y)), ratio);
-      const double th = atan2(ph.y, ph.x);
-      double val = hypot(imp.x, imp.y) * cos(th);
+      const double exr = -sdt * sh.x + ft.x + dt * (eshift + c0r);
+      double sa, ca;
+      sincos(sdt * sh.y, &sa, &ca);
+      double val = exp(exr) * (ratio.x * ca + ratio.y * sa);
       if (val < 1.0e-3 || val > 100.0 || isnan(val)) val = 0.0;
       wt *= val;
       if (wt > cap) { wt = 0.0; ncap += 1.0; }
