@@ -191,6 +191,9 @@ void release(afqmc_handle* h) {
   if (h->timer[0]) { cudaEventDestroy(h->timer[0]); cudaEventDestroy(h->timer[1]); }
   for (int s = 0; s < afqmc::ST_N; ++s)
     for (auto& e : h->ev[s]) { cudaEventDestroy(e.first); cudaEventDestroy(e.second); }
+  if (h->cv_fork) cudaEventDestroy(h->cv_fork);
+  if (h->cv_join) cudaEventDestroy(h->cv_join);
+  if (h->cv_side) cudaStreamDestroy(h->cv_side);
   if (h->stream) cudaStreamDestroy(h->stream);
 }
 

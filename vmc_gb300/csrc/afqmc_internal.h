@@ -183,6 +183,8 @@ struct afqmc_handle {
   int cv_nslots = 4096, cv_den = 8;
   float cv_ymean = 0.f, cv_ystd = 1.f;
   struct afqmc_mlp* cv_mlp = nullptr;
+  cudaStream_t cv_side = nullptr;      // the subsample's exact energies, beside the force bias
+  cudaEvent_t cv_fork = nullptr, cv_join = nullptr;
   // mixed 1-RDM estimator: running sums of sum_w w Re theta_w [nce*N] and of
   // the weights (slot nce*N), per-chunk partial sums, trial orbitals on the host
   bool rdm_on = false;

@@ -294,6 +294,12 @@ int afqmc_cv_attach(afqmc_handle* h, afqmc_mlp* m, const float* mean, const floa
     return AFQMC_ERR_UNSUPPORTED;
   }
   cudaSetDevice(h->device);
+  if (!h->cv_side && (cudaStreamCreateWithFlags(&h->cv_side, cudaStreamNonBlocking) != cudaSuccess ||
+                      cudaEventCreateWithFlags(&h->cv_fork, cudaEventDisableTiming) != cudaSuccess ||
+                      cudaEventCreateWithFlags(&h->cv_join, cudaEventDisableTiming) != cudaSuccess)) {
+    h->err = "cv_attach: stream or event creation failed";
+    return AFQMC_ERR_CUDA;
+  }
   h->cv_mlp = m;
   h->cv_den = den;
   h->cv_ymean = ymean;
@@ -313,12 +319,26 @@ int afqmc_cv_measure(afqmc_handle* h, uint64_t tag, int slot) {
   if (!h || !h->cv_mlp || slot < 0 || slot >= h->cv_nslots) return AFQMC_ERR_ARG;
   cudaSetDevice(h->device);
   const int W = h->nwalk, den = h->cv_den, m = (W + den - 1) / den;
+  // Two branches that need only theta and the walkers: the force bias, the
+  // features and the network on the handle's stream, and the subsample's exact
+  // energies on a side stream, so that the exchange GEMM's CTAs fill the SMs
+  // that the force-bias GEMM (one CTA per output tile, fewer tiles than SMs)
+  // leaves idle.  The estimate waits for both.
+  cudaEventRecord(h->cv_fork, h->stream);
+  cudaStreamWaitEvent(h->cv_side, h->cv_fork, 0);
   launch_force_bias_mixed(h);
+  {
+    cudaStream_t main_stream = h->stream;
+    h->stream = h->cv_side;
+    k_cv_select<<<(m + 127) / 128, 128, 0, h->stream>>>(h->cv_idx, W, den, h->seed, tag, h->d_step);
+    launch_local_energy_mixed_subset(h, h->cv_idx, m, h->cv_esub);
+    h->stream = main_stream;
+  }
+  cudaEventRecord(h->cv_join, h->cv_side);
   k_cv_features32<<<W, 128, 0, h->stream>>>(h->fb32, h->theta32, h->h1phi32, h->ovlp, h->N, h->nce, h->G, h->mult,
                                             h->cv_ms, h->cv_ms + CV_NF, h->cv_x);
   const int mlp_launches = mlp_forward_on(h->cv_mlp, h->cv_x, W, h->cv_f, h->stream, false);
-  k_cv_select<<<(m + 127) / 128, 128, 0, h->stream>>>(h->cv_idx, W, den, h->seed, tag, h->d_step);
-  launch_local_energy_mixed_subset(h, h->cv_idx, m, h->cv_esub);
+  cudaStreamWaitEvent(h->stream, h->cv_join, 0);
   k_cv_estimate<<<1, 256, 0, h->stream>>>(h->weights, h->cv_f, h->cv_ymean, h->cv_ystd, h->cv_idx, h->cv_esub, W, m, den,
                                            h->cv_out + 6 * (size_t)slot);
   h->launches += 3 + mlp_launches;  // features, select, estimate and the MLP (the rest count themselves)

@@ -189,33 +189,45 @@ static dim3 g2(int M, int N) { return dim3((N + 63) / 64, (M + 63) / 64); }
 // The whole forward pass for MF_RB walkers per CTA, one hidden unit per thread
 // (H <= MF_THREADS): the same FP32 multiply-add chains over k in the same order,
 // bias, SiLU and output reduction as the layer kernels above, so the results
-// are bit-identical, in one launch.  Both BF16 weight matrices are copied into
-// shared memory once, transposed ([k][o]: thread o loads its own row and
-// stores along o, conflict-free, and reads its column the same way);
-// activations are kept as [unit][walker] so one 128-bit broadcast load feeds
-// four walkers.  Z1, H1, Z2, H2 (for backward) are written when non-null.
+// are bit-identical, in one launch.  Thread o reads its own weight row straight
+// from global memory (L1/L2: every CTA reads the same 164 KB), 8 weights per
+// 16-byte load where the row allows it, each weight feeding the 16 walkers of
+// the CTA; activations are kept in shared memory as [unit][walker] so one
+// 128-bit broadcast load feeds four walkers.  Z1, H1, Z2, H2 (for backward)
+// are written when non-null.
 constexpr int MF_RB = 16, MF_THREADS = 256;
-static size_t mf_smem(int nin, int H) {
-  return (size_t)(nin + H) * H * sizeof(__nv_bfloat16) + (size_t)MF_RB * (nin + 2 * H) * sizeof(float) + 16;
+static size_t mf_smem(int nin, int H) { return (size_t)MF_RB * (nin + 2 * H) * sizeof(float) + 16; }
+
+__device__ __forceinline__ void mf_fma_k(const float* __restrict__ inT, int k, float w, float* acc) {
+  const float4* x = reinterpret_cast<const float4*>(inT + (size_t)k * MF_RB);
+#pragma unroll
+  for (int q = 0; q < MF_RB / 4; ++q) {
+    const float4 v = x[q];
+    acc[4 * q] = fmaf(v.x, w, acc[4 * q]);
+    acc[4 * q + 1] = fmaf(v.y, w, acc[4 * q + 1]);
+    acc[4 * q + 2] = fmaf(v.z, w, acc[4 * q + 2]);
+    acc[4 * q + 3] = fmaf(v.w, w, acc[4 * q + 3]);
+  }
 }
 
-__device__ __forceinline__ void mf_layer(const float* __restrict__ inT, int K, int H, const __nv_bfloat16* WT,
+// acc[b] = sum_k in[k][b] Wrow[k], k ascending (the layer kernels' order)
+__device__ __forceinline__ void mf_layer(const float* __restrict__ inT, int K, const __nv_bfloat16* __restrict__ Wrow,
                                          float* acc) {
-  const int o = threadIdx.x;
 #pragma unroll
   for (int b = 0; b < MF_RB; ++b) acc[b] = 0.f;
-  for (int k = 0; k < K; ++k) {
-    const float w = __bfloat162float(WT[k * H + o]);
-    const float4* x = reinterpret_cast<const float4*>(inT + (size_t)k * MF_RB);
+  int k = 0;
+  if ((K & 7) == 0 && (((uintptr_t)Wrow) & 15) == 0) {
+    const uint4* w8 = reinterpret_cast<const uint4*>(Wrow);
+    uint4 nxt = w8[0];
+    for (; k < K; k += 8) {
+      const uint4 u = nxt;
+      if (k + 8 < K) nxt = w8[(k >> 3) + 1];
+      const __nv_bfloat16* e = reinterpret_cast<const __nv_bfloat16*>(&u);
 #pragma unroll
-    for (int q = 0; q < MF_RB / 4; ++q) {
-      const float4 v = x[q];
-      acc[4 * q] = fmaf(v.x, w, acc[4 * q]);
-      acc[4 * q + 1] = fmaf(v.y, w, acc[4 * q + 1]);
-      acc[4 * q + 2] = fmaf(v.z, w, acc[4 * q + 2]);
-      acc[4 * q + 3] = fmaf(v.w, w, acc[4 * q + 3]);
+      for (int i = 0; i < 8; ++i) mf_fma_k(inT, k + i, __bfloat162float(e[i]), acc);
     }
   }
+  for (; k < K; ++k) mf_fma_k(inT, k, __bfloat162float(Wrow[k]), acc);
 }
 
 __global__ void __launch_bounds__(MF_THREADS)
@@ -227,32 +239,15 @@ __global__ void __launch_bounds__(MF_THREADS)
   float* XT = mf_sm;                 // [nin][MF_RB]
   float* H1T = XT + MF_RB * nin;     // [H][MF_RB]
   float* H2T = H1T + MF_RB * H;      // [H][MF_RB]
-  __nv_bfloat16* W1T = reinterpret_cast<__nv_bfloat16*>(H2T + MF_RB * H);  // [nin][H]
-  __nv_bfloat16* W2T = W1T + (size_t)nin * H;                                // [H][H]
   const int b0 = blockIdx.x * MF_RB, nb = min(MF_RB, B - b0), o = threadIdx.x;
   for (int e = threadIdx.x; e < MF_RB * nin; e += blockDim.x) {
     const int b = e / nin, k = e - b * nin;
     XT[k * MF_RB + b] = b < nb ? X[(size_t)(b0 + b) * nin + k] : 0.f;
   }
-  if (o < H) {
-    const __nv_bfloat16* r1 = W1 + (size_t)o * nin;
-    for (int k = 0; k < nin; ++k) W1T[k * H + o] = r1[k];
-    const __nv_bfloat16* r2 = W2 + (size_t)o * H;
-    if ((H & 7) == 0) {
-      for (int k8 = 0; k8 < H; k8 += 8) {
-        const uint4 v = *reinterpret_cast<const uint4*>(r2 + k8);
-        const __nv_bfloat16* e = reinterpret_cast<const __nv_bfloat16*>(&v);
-#pragma unroll
-        for (int i = 0; i < 8; ++i) W2T[(k8 + i) * H + o] = e[i];
-      }
-    } else {
-      for (int k = 0; k < H; ++k) W2T[k * H + o] = r2[k];
-    }
-  }
   __syncthreads();
   float acc[MF_RB];
   if (o < H) {
-    mf_layer(XT, nin, H, W1T, acc);
+    mf_layer(XT, nin, W1 + (size_t)o * nin, acc);
 #pragma unroll
     for (int b = 0; b < MF_RB; ++b) {
       const float z = acc[b] + b1[o];
@@ -266,7 +261,7 @@ __global__ void __launch_bounds__(MF_THREADS)
   }
   __syncthreads();
   if (o < H) {
-    mf_layer(H1T, H, H, W2T, acc);
+    mf_layer(H1T, H, W2 + (size_t)o * H, acc);
 #pragma unroll
     for (int b = 0; b < MF_RB; ++b) {
       const float z = acc[b] + b2[o];
