@@ -152,6 +152,17 @@ __device__ __forceinline__ void df2_two_sum(float2 a, float2 b, float2& s, float
   const float2 bb = __fadd2_rn(s, f2_neg(a));
   e = __fadd2_rn(__fadd2_rn(a, f2_neg(__fadd2_rn(s, f2_neg(bb)))), __fadd2_rn(b, f2_neg(bb)));
 }
+// dot2_acc on both components of (s, c) at once: component k accumulates
+// ah.k b.k with the low part al.k, in dot2_acc's operations and order
+__device__ __forceinline__ void dot2_acc2(float2& s, float2& c, float2 ah, float2 al, float2 b) {
+  const float2 p = __fmul2_rn(ah, b);
+  const float2 pe = __ffma2_rn(ah, b, f2_neg(p));
+  float2 t, e;
+  df2_two_sum(s, p, t, e);
+  s = t;
+  c = __fadd2_rn(c, __fadd2_rn(e, pe));
+  c = __ffma2_rn(al, b, c);
+}
 // complex x - a b with each operand held as planes: (Re, Im) of the high
 // parts in one float2, of the low parts in another.  Component for component
 // the operations and their order of dfc_fms: Re = x.r + (-a.r) b.r + (-a.i)(-b.i),

@@ -628,10 +628,12 @@ void launch_psi_to_f32(afqmc_handle* h) {
   h->launches++;
 }
 
-__global__ void k_overlap_gj_df32(const float2* __restrict__ psi32, const float2* __restrict__ phi2,
-                                  float* __restrict__ theta32, double2* __restrict__ det,
-                                  const double* __restrict__ weights, int N, int ncw, int nce, Channel c0, Channel c1,
-                                  int only_live);
+constexpr int GJ_THREADS = 1024;  // k_overlap_gj_df32: one CTA of 32 warps per matrix
+__global__ void __launch_bounds__(GJ_THREADS)
+    k_overlap_gj_df32(const float2* __restrict__ psi32, const float2* __restrict__ phi2,
+                      float* __restrict__ theta32, double2* __restrict__ det,
+                      const double* __restrict__ weights, int N, int ncw, int nce, Channel c0, Channel c1,
+                      int only_live);
 
 void launch_overlap_theta(afqmc_handle* h, bool only_live) {
   h->fb_current = false;  // theta changes
@@ -682,7 +684,7 @@ void launch_overlap_theta(afqmc_handle* h, bool only_live) {
   dim3 grid(h->nwalk, h->nchan);
   if (h->precision == AFQMC_PREC_MIXED && h->psi32 && h->phi2 && h->tune_ovl != 2) {  // double-FP32 elimination
     smem_optin(k_overlap_gj_df32, 200 * 1024);
-    k_overlap_gj_df32<<<grid, 256, smem, h->stream>>>(h->psi32, h->phi2, h->theta32, h->det, h->weights, h->N, h->ncw,
+    k_overlap_gj_df32<<<grid, GJ_THREADS, smem, h->stream>>>(h->psi32, h->phi2, h->theta32, h->det, h->weights, h->N, h->ncw,
                                                       h->nce, h->chan[0], h->chan[1], only_live ? 1 : 0);
     h->launches++;
     return;
@@ -701,17 +703,27 @@ void launch_overlap_theta(afqmc_handle* h, bool only_live) {
 // arithmetic (pivot search on the high parts), so the determinant -- the
 // product of the pivots, formed in double-FP32 and converted once -- stays
 // FP64-grade; theta = psi M^-1 in FP32 from the FP32 walker and the high parts
-// of the inverse.  One CTA per (walker, channel); [n][2n] pairs in shared memory.
+// of the inverse.  One CTA of 32 warps per (walker, channel); [n][2n] entries in
+// shared memory, each as (Re hi, Im hi, Re lo, Im lo): the high and the low
+// planes of the packed float2 arithmetic (dfc_fms_planes: the scalar
+// double-FP32 sequence's bits with half the instructions).
+__device__ __forceinline__ void gj_st(float4* a, int e, df32c v) { a[e] = make_float4(v.r.h, v.i.h, v.r.l, v.i.l); }
 __device__ __forceinline__ df32c gj_ld(const float4* a, int e) {
   const float4 v = a[e];
-  return {{v.x, v.y}, {v.z, v.w}};
+  return {{v.x, v.z}, {v.y, v.w}};
 }
-__device__ __forceinline__ void gj_st(float4* a, int e, df32c v) { a[e] = make_float4(v.r.h, v.r.l, v.i.h, v.i.l); }
+// x - a b (all four float4 entries in the layout above)
+__device__ __forceinline__ float4 gj_fms(float4 x, float4 a, float4 b) {
+  float2 xh = make_float2(x.x, x.y), xl = make_float2(x.z, x.w);
+  dfc_fms_planes(xh, xl, make_float2(a.x, a.y), make_float2(a.z, a.w), make_float2(b.x, b.y), make_float2(b.z, b.w));
+  return make_float4(xh.x, xh.y, xl.x, xl.y);
+}
 
-__global__ void k_overlap_gj_df32(const float2* __restrict__ psi32, const float2* __restrict__ phi2,
-                                  float* __restrict__ theta32, double2* __restrict__ det,
-                                  const double* __restrict__ weights, int N, int ncw, int nce, Channel c0, Channel c1,
-                                  int only_live) {
+__global__ void __launch_bounds__(GJ_THREADS)
+    k_overlap_gj_df32(const float2* __restrict__ psi32, const float2* __restrict__ phi2,
+                      float* __restrict__ theta32, double2* __restrict__ det,
+                      const double* __restrict__ weights, int N, int ncw, int nce, Channel c0, Channel c1,
+                      int only_live) {
   const int w = blockIdx.x;
   const Channel ch = blockIdx.y == 0 ? c0 : c1;
   if (only_live && !(weights[w] > 1.0e-8)) return;
@@ -724,14 +736,20 @@ __global__ void k_overlap_gj_df32(const float2* __restrict__ psi32, const float2
   const float2* ph = phi2 + (size_t)ch.col_off * N;
   for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
     const int i = e / n, j = e % n;
-    float sr = 0.f, cr = 0.f, si = 0.f, ci = 0.f;
+    // dot2_acc of the real and of the imaginary part, as one packed sequence
+    float2 sv = make_float2(0.f, 0.f), cv = sv;
     for (int p = 0; p < N; ++p) {
       const float2 f = ph[i * N + p];
       const float2 v = ps[j * N + p];
-      dot2_acc(sr, cr, f.x, f.y, v.x);
-      dot2_acc(si, ci, f.x, f.y, v.y);
+      const float2 fh = make_float2(f.x, f.x), fl = make_float2(f.y, f.y);
+      const float2 pr = __fmul2_rn(fh, v);
+      const float2 pe = __ffma2_rn(fh, v, f2_neg(pr));
+      float2 t, er;
+      df2_two_sum(sv, pr, t, er);
+      sv = t;
+      cv = __ffma2_rn(fl, v, __fadd2_rn(cv, __fadd2_rn(er, pe)));
     }
-    gj_st(a, i * n2 + j, {df_fast(sr, cr), df_fast(si, ci)});
+    gj_st(a, i * n2 + j, {df_fast(sv.x, cv.x), df_fast(sv.y, cv.y)});
     gj_st(a, i * n2 + n + j, {{i == j ? 1.f : 0.f, 0.f}, {0.f, 0.f}});
   }
   __syncthreads();
@@ -742,7 +760,7 @@ __global__ void k_overlap_gj_df32(const float2* __restrict__ psi32, const float2
       int bi = k;
       for (int i = k + threadIdx.x; i < n; i += 32) {
         const float4 v = a[i * n2 + k];
-        const float m = v.x * v.x + v.z * v.z;
+        const float m = v.x * v.x + v.y * v.y;
         if (m > best) { best = m; bi = i; }
       }
       for (int off = 16; off > 0; off >>= 1) {
@@ -770,13 +788,17 @@ __global__ void k_overlap_gj_df32(const float2* __restrict__ psi32, const float2
     const df32c inv = dfc_recip(pv);
     for (int i = threadIdx.x; i < n; i += blockDim.x) fcol[i] = a[i * n2 + k];
     __syncthreads();
-    for (int j = k + threadIdx.x; j < n2; j += blockDim.x) gj_st(a, k * n2 + j, dfc_mul(gj_ld(a, k * n2 + j), inv));
+    // x inv as 0 - (-x) inv: the operations and order of dfc_mul(x, inv)
+    const float4 ninv = make_float4(inv.r.h, inv.i.h, inv.r.l, inv.i.l);
+    for (int j = k + threadIdx.x; j < n2; j += blockDim.x) {
+      const float4 x = a[k * n2 + j];
+      a[k * n2 + j] = gj_fms(make_float4(0.f, 0.f, 0.f, 0.f), make_float4(-x.x, -x.y, -x.z, -x.w), ninv);
+    }
     __syncthreads();
     for (int e = threadIdx.x; e < n * (n2 - k); e += blockDim.x) {
       const int i = e / (n2 - k), j = k + e % (n2 - k);
       if (i == k) continue;
-      const float4 f = fcol[i];
-      gj_st(a, i * n2 + j, dfc_fms(gj_ld(a, i * n2 + j), {{f.x, f.y}, {f.z, f.w}}, gj_ld(a, k * n2 + j)));
+      a[i * n2 + j] = gj_fms(a[i * n2 + j], fcol[i], a[k * n2 + j]);
     }
     __syncthreads();
   }
@@ -791,8 +813,8 @@ __global__ void k_overlap_gj_df32(const float2* __restrict__ psi32, const float2
     for (int i = 0; i < n; ++i) {
       const float2 v = ps[i * N + p];
       const float4 m = a[i * n2 + n + j];
-      re = fmaf(v.x, m.x, fmaf(-v.y, m.z, re));
-      im = fmaf(v.x, m.z, fmaf(v.y, m.x, im));
+      re = fmaf(v.x, m.x, fmaf(-v.y, m.y, re));
+      im = fmaf(v.x, m.y, fmaf(v.y, m.x, im));
     }
     tre[j * N + p] = re;
     tim[j * N + p] = im;
@@ -1095,15 +1117,17 @@ __global__ void __launch_bounds__(WT_THREADS)
 
 __global__ void k_weights_final(const double* __restrict__ part, int nparts, double* __restrict__ scal, double dt,
                                 double target, unsigned long long* __restrict__ stepp) {
+  // one warp: lane sums the partials lane, lane + 32, ... in order, then a
+  // butterfly (a fixed order either way)
   double sumw = 0.0, ncap = 0.0, nlive = 0.0;
-  for (int b = threadIdx.x; b < nparts; b += blockDim.x) {
+  for (int b = threadIdx.x; b < nparts; b += 32) {
     sumw += part[3 * b];
     ncap += part[3 * b + 1];
     nlive += part[3 * b + 2];
   }
-  sumw = block_sum(sumw);
-  ncap = block_sum(ncap);
-  nlive = block_sum(nlive);
+  sumw = warp_sum(sumw);
+  ncap = warp_sum(ncap);
+  nlive = warp_sum(nlive);
   if (threadIdx.x == 0) {
     scal[S_SUMW] = sumw;
     scal[S_NCAP] += ncap;
@@ -1120,7 +1144,7 @@ void launch_weights(afqmc_handle* h) {
   const int nb = weights_parts(h);
   k_weights<<<nb, WT_THREADS, 0, h->stream>>>(h->weights, h->ovlp, h->det, h->shift, h->fbterm, h->scal, h->nwalk,
                                                h->nchan, h->mult, h->dt, cr, ci, h->weight_cap, h->wpart);
-  k_weights_final<<<1, 256, 0, h->stream>>>(h->wpart, nb, h->scal, h->dt, h->pop_target, h->d_step);
+  k_weights_final<<<1, 32, 0, h->stream>>>(h->wpart, nb, h->scal, h->dt, h->pop_target, h->d_step);
   h->launches += 2;
 }
 

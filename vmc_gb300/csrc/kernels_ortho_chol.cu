@@ -153,15 +153,16 @@ __global__ void __launch_bounds__(OC_THREADS)
     // Q = A X: Q[j][p] = sum_{i <= j} A[i][p] X[i][j], compensated
     for (int e = tid; e < n * N; e += OC_THREADS) {
       const int j = e / N, p = e % N;
-      float sr = 0.f, cr = 0.f, si = 0.f, ci = 0.f;
+      // (Re, Im) of Q accumulated as one packed pair: the four dot2_acc calls
+      // per term (Re += h.re x.re, Re -= h.im x.im, Im += h.re x.im, Im += h.im
+      // x.re) in two packed calls, each component in its scalar order
+      float2 s2 = make_float2(0.f, 0.f), c2 = s2;
       for (int i = 0; i <= j; ++i) {
         const float2 h = Ah[(size_t)i * ld + p], l = Al[(size_t)i * ld + p], x = X[i * n + j];
-        dot2_acc(sr, cr, h.x, l.x, x.x);
-        dot2_acc(sr, cr, -h.y, -l.y, x.y);
-        dot2_acc(si, ci, h.x, l.x, x.y);
-        dot2_acc(si, ci, h.y, l.y, x.x);
+        dot2_acc2(s2, c2, make_float2(h.x, h.x), make_float2(l.x, l.x), x);
+        dot2_acc2(s2, c2, make_float2(-h.y, h.y), make_float2(-l.y, l.y), make_float2(x.y, x.x));
       }
-      const df32 qr = df_fast(sr, cr), qi = df_fast(si, ci);
+      const df32 qr = df_fast(s2.x, c2.x), qi = df_fast(s2.y, c2.y);
       const double2 q = make_double2(df_to_double_bits(qr), df_to_double_bits(qi));
       Ag[e] = q;
       // the FP32 copy is the stored double rounded to nearest, as everywhere
@@ -272,17 +273,15 @@ __global__ void __launch_bounds__(OC_THREADS)
     __syncthreads();
     for (int p = tid; p < N; p += OC_THREADS) {
       for (int j = n - 1; j >= 0; --j) {
-        float sr = 0.f, cr = 0.f, si = 0.f, ci = 0.f;
+        float2 s2 = make_float2(0.f, 0.f), c2 = s2;  // (Re, Im) packed, as above
         for (int i = 0; i <= j; ++i) {
           const double2 v = Ag[(size_t)i * N + p];
           const df32 re = df_split_bits(v.x), im = df_split_bits(v.y);
           const float2 x = X[i * n + j];
-          dot2_acc(sr, cr, re.h, re.l, x.x);
-          dot2_acc(sr, cr, -im.h, -im.l, x.y);
-          dot2_acc(si, ci, re.h, re.l, x.y);
-          dot2_acc(si, ci, im.h, im.l, x.x);
+          dot2_acc2(s2, c2, make_float2(re.h, re.h), make_float2(re.l, re.l), x);
+          dot2_acc2(s2, c2, make_float2(-im.h, im.h), make_float2(-im.l, im.l), make_float2(x.y, x.x));
         }
-        const double2 q = make_double2(df_to_double_bits(df_fast(sr, cr)), df_to_double_bits(df_fast(si, ci)));
+        const double2 q = make_double2(df_to_double_bits(df_fast(s2.x, c2.x)), df_to_double_bits(df_fast(s2.y, c2.y)));
         Ag[(size_t)j * N + p] = q;
         Ag32[(size_t)j * N + p] = make_float2(df_split_bits(q.x).h, df_split_bits(q.y).h);
       }
