@@ -599,25 +599,32 @@ def main():
         t = torch.empty((W, G), dtype=torch.float64, pin_memory=True)
         t.numpy()[:] = rng.standard_normal((W, G))
         xis.append(t.numpy())
-    wbuf = np.zeros(W)
+    from vmc_gb300 import cv as CVM
     ebuf = np.zeros(6)
     wk.sync()
     n0 = wk.walker_steps()
     t0 = time.perf_counter()
+    # pipelined as a caller would: step k + 1 is issued (its fields copied on
+    # the handle's copy stream while step k runs) before step k's estimate is
+    # taken from the result queue
     for k in range(args.steps):
         wk.propagate_phaseless(xis[k % 2])
         if (k + 1) % ORTHO_EVERY == 0:
             wk.orthogonalize()
-        cv.measure(tag=k0 + k, slot=0)
+        cv.measure(tag=k0 + k, slot=k % 2)
         if (k + 1) % REF_CADENCE == 0:
             comb(wk)
-        A.lib().afqmc_get_walkers(wk.h, None, None, wbuf.ctypes.data)
-        A.lib().afqmc_cv_results(wk.h, ebuf.ctypes.data, 1)
+        CVM.result_post(wk, k % 2)
+        if k > 0:
+            CVM.result_take(wk, ebuf)
+    CVM.result_take(wk, ebuf)
     wk.sync()
     e2e_s = time.perf_counter() - t0
     e2e_live = wk.walker_steps() - n0
     e2e = {"value": e2e_live * world / e2e_s, "unit": "walker-steps/s",
-           "h2d_bytes_per_step": W * G * 8, "d2h_bytes_per_step": W * 8 + 48, "host_fields": "page-locked",
+           "h2d_bytes_per_step": W * G * 8, "d2h_bytes_per_step": 48, "host_fields": "page-locked",
+           "result": "each step's control-variate estimate (6 doubles) read back; step k + 1 issued before "
+                     "step k's estimate is taken",
            "live_fraction": e2e_live / (W * args.steps)}
     k0 += args.steps
 

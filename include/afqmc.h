@@ -289,6 +289,14 @@ int afqmc_cv_attach(afqmc_handle* h, afqmc_mlp* m, const float* mean, const floa
  * (ratio), sum of weights, sum of subsample weights}; `tag` seeds the subsample */
 int afqmc_cv_measure(afqmc_handle* h, uint64_t tag, int slot);
 int afqmc_cv_results(afqmc_handle* h, double* out, int nslots);
+/* asynchronous reads of single slots, first in first out (at most 8 posted):
+ * post enqueues a copy of slot `slot` after the work already issued on the
+ * handle; take waits for the oldest posted copy only and writes its 6 doubles
+ * to out.  A caller that issues step k + 1 (whose host fields then reach the
+ * device while step k runs) before taking step k's estimate keeps the device
+ * busy between steps. */
+int afqmc_cv_result_post(afqmc_handle* h, int slot);
+int afqmc_cv_result_take(afqmc_handle* h, double* out);
 
 /* ---- autotuner ----
  * Time the candidate tile shapes and kernel variants of this handle's size class

@@ -92,3 +92,52 @@ def test_control_variate_reduces_variance(A):
     assert gain > 2.0, (gain, r_cv.std(), r_ratio.std(), r_cv_ht.std(), r_ht.std())
     assert r_cv_ht.var() < r_ht.var()
     assert abs(r_cv.mean()) < 4 * r_cv.std() / np.sqrt(len(r_cv)) + 1e-12
+
+
+def test_result_queue_and_host_fields_overlap(A):
+    """The asynchronous result reads (post / take, first in first out) return
+    what the synchronous read returns, and steps with host fields issued ahead
+    of the reads (the copies then overlap the previous step, into the other
+    device field buffer) give the same walkers as the same steps with a
+    synchronous read after each."""
+    from vmc_gb300 import cv as CVM
+    from vmc_gb300.cv import ControlVariate
+    s = S.make_system(24, 4, 60, 616, "uhf")
+    N, n = 24, 4
+    gh = A.Hamiltonian(N, n, n, 0.0, s["h1"], s["h1mod"], s["chol"])
+    gt = A.UHF(gh, s["phi_a"], s["phi_b"])
+    W = 256
+    rng = np.random.default_rng(3)
+    xis = [np.ascontiguousarray(rng.standard_normal((W, 60))) for _ in range(6)]
+    outs = []
+    for pipelined in (False, True):
+        wk = A.DQMCWalkers(gh, gt, W, False, 0.005, precision="mixed", seed=17)
+        e0 = wk.ham_and_overlap().real.mean()
+        wk.set_energy_estimate(e0, e0)
+        cv = ControlVariate(wk, hidden=64, den=8, seed=5)
+        for st in range(1, 41):
+            wk.propagate_phaseless(None)
+            if st > 10:
+                cv.collect()
+        cv.train(epochs=2, batch=128, lr=1e-3)
+        got = []
+        for k in range(6):
+            wk.propagate_phaseless(xis[k])
+            cv.measure(tag=500 + k, slot=k % 2)
+            if pipelined:
+                CVM.result_post(wk, k % 2)
+                if k > 0:
+                    got.append(CVM.result_take(wk).copy())
+            else:
+                got.append(cv.results(2)[k % 2].copy())
+        if pipelined:
+            got.append(CVM.result_take(wk).copy())
+            # the queue returned each step's estimate: the last two are still in their slots
+            last = cv.results(2)
+            assert np.array_equal(got[-1], last[5 % 2]) and np.array_equal(got[-2], last[4 % 2])
+            assert len(got) == 6 and np.all(np.isfinite(np.array(got)))
+        d, o, w = wk.get_det()
+        outs.append((d, w))
+        wk.close()
+    (d0, w0), (d1, w1) = outs
+    assert np.array_equal(d0, d1) and np.array_equal(w0, w1)

@@ -494,7 +494,9 @@ def _bind_cv(L):
                        ("afqmc_local_energy_subset", [vp, vp, ip, vp]),
                        ("afqmc_cv_attach", [vp, vp, vp, vp, ctypes.c_float, ctypes.c_float, ip]),
                        ("afqmc_cv_measure", [vp, ctypes.c_uint64, ip]),
-                       ("afqmc_cv_results", [vp, vp, ip])]:
+                       ("afqmc_cv_results", [vp, vp, ip]),
+                       ("afqmc_cv_result_post", [vp, ip]),
+                       ("afqmc_cv_result_take", [vp, vp])]:
         f = getattr(L, name)
         f.argtypes = args
         f.restype = ctypes.c_int

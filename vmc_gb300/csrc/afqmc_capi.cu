@@ -182,10 +182,18 @@ void release(afqmc_handle* h) {
                   h->xc, h->cv_x, h->cv_idx, h->cv_esub, h->cv_f, h->cv_ms, h->cv_out, h->d_step, h->psi32,
                   h->pt_img, h->comb_cum, h->comb_idx, h->comb_ovl, h->blk, h->blk_zeta, h->wpart,
                   h->ovl_tau, h->ovl_bimg, h->ovl_M, h->theta32, h->mf32, h->h1phi32, h->pt_voff,
-                  h->rdm_acc, h->rdm_part, h->pb_img, h->pb_scratch, h->phi2};
+                  h->rdm_acc, h->rdm_part, h->pb_img, h->pb_scratch, h->phi2, h->xi1};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (h->host_pinned) cudaFreeHost(h->host_pinned);
+  if (h->res_pinned) cudaFreeHost(h->res_pinned);
+  for (int b = 0; b < 2; ++b) {
+    if (h->xi_copied[b]) cudaEventDestroy(h->xi_copied[b]);
+    if (h->xi_read[b]) cudaEventDestroy(h->xi_read[b]);
+  }
+  for (auto& e : h->res_ev)
+    if (e) cudaEventDestroy(e);
+  if (h->copy_stream) cudaStreamDestroy(h->copy_stream);
   for (auto& e : h->stage_ev)
     if (e) cudaEventDestroy(e);
   if (h->timer[0]) { cudaEventDestroy(h->timer[0]); cudaEventDestroy(h->timer[1]); }
@@ -480,6 +488,7 @@ int afqmc_create(const afqmc_ham* ham, const afqmc_trial* trial, const afqmc_opt
   ALLOC(weights, W);
   ALLOC(fb, W * 2 * G);
   ALLOC(xi, W * G);
+  ALLOC(xi1, W * G);
   ALLOC(x, W * 2 * G);
   ALLOC(shift, W);
   ALLOC(fbterm, W);
@@ -539,6 +548,15 @@ int afqmc_create(const afqmc_ham* ham, const afqmc_trial* trial, const afqmc_opt
   ce = cudaMallocHost((void**)&h->host_pinned, 2 * W * G * sizeof(double));
   for (auto& e : h->stage_ev)
     if (ce == cudaSuccess) ce = cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
+  for (int b = 0; b < 2; ++b) {
+    if (ce == cudaSuccess) ce = cudaEventCreateWithFlags(&h->xi_copied[b], cudaEventDisableTiming);
+    if (ce == cudaSuccess) ce = cudaEventCreateWithFlags(&h->xi_read[b], cudaEventDisableTiming);
+  }
+  if (ce == cudaSuccess) ce = cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking);
+  if (ce == cudaSuccess) ce = cudaMallocHost((void**)&h->res_pinned, 8 * 6 * sizeof(double));
+  for (auto& e : h->res_ev)
+    if (ce == cudaSuccess) ce = cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
+  h->xi_cur = h->xi;
   if (ce != cudaSuccess) { g_create_err = cudaGetErrorString(ce); release(h); delete h; return AFQMC_ERR_CUDA; }
   h->host_pinned_bytes = W * G * sizeof(double);
 
@@ -749,26 +767,37 @@ int afqmc_step(afqmc_handle* h, const double* xi, const double* eshift) {
     k_set_scalar<<<1, 1, 0, h->stream>>>(h->scal, afqmc::S_ESHIFT, *eshift);
     h->launches++;
   }
-  cudaPointerAttributes xa;
-  if (xi && cudaPointerGetAttributes(&xa, xi) == cudaSuccess && xa.type == cudaMemoryTypeHost) {
-    // a page-locked (or registered) caller buffer is transferred directly; the
-    // call returns once the transfer is done, so the caller may reuse it
-    CK(cudaMemcpyAsync(h->xi, xi, h->host_pinned_bytes, cudaMemcpyHostToDevice, h->stream));
-    CK(cudaEventRecord(h->stage_ev[h->stage_next], h->stream));
-    CK(cudaEventSynchronize(h->stage_ev[h->stage_next]));
-  } else if (xi) {
-    cudaGetLastError();  // a pageable pointer is not an error
-    // two pinned staging buffers in turn: this step's fields are copied into the
-    // buffer whose last transfer has finished (its event), so the host's copy
-    // overlaps the device's previous step; the transfer itself is stream-ordered
-    // after that step, which still reads the device copy
-    const int b = h->stage_next;
-    h->stage_next ^= 1;
-    CK(cudaEventSynchronize(h->stage_ev[b]));
-    double* stage = h->host_pinned + (size_t)b * h->nwalk * h->G;
-    memcpy(stage, xi, h->host_pinned_bytes);
-    CK(cudaMemcpyAsync(h->xi, stage, h->host_pinned_bytes, cudaMemcpyHostToDevice, h->stream));
-    CK(cudaEventRecord(h->stage_ev[b], h->stream));
+  // host fields go to device buffer xb on the copy stream, which waits only for
+  // the fields kernel that last read xb (two steps ago); the step's fields
+  // kernel waits for the copy.  So the transfer overlaps the device's previous
+  // step whenever the caller issues the next step before waiting for results.
+  const int xb = h->xi_next;
+  if (xi) {
+    h->xi_next ^= 1;
+    double* dst = xb ? h->xi1 : h->xi;
+    CK(cudaStreamWaitEvent(h->copy_stream, h->xi_read[xb], 0));
+    cudaPointerAttributes xa;
+    if (cudaPointerGetAttributes(&xa, xi) == cudaSuccess && xa.type == cudaMemoryTypeHost) {
+      // a page-locked (or registered) caller buffer is transferred directly; the
+      // call returns once the transfer is done, so the caller may reuse it
+      CK(cudaMemcpyAsync(dst, xi, h->host_pinned_bytes, cudaMemcpyHostToDevice, h->copy_stream));
+      CK(cudaEventRecord(h->xi_copied[xb], h->copy_stream));
+      CK(cudaEventSynchronize(h->xi_copied[xb]));
+    } else {
+      cudaGetLastError();  // a pageable pointer is not an error
+      // two pinned staging buffers in turn: this step's fields are copied into the
+      // buffer whose last transfer has finished (its event)
+      const int b = h->stage_next;
+      h->stage_next ^= 1;
+      CK(cudaEventSynchronize(h->stage_ev[b]));
+      double* stage = h->host_pinned + (size_t)b * h->nwalk * h->G;
+      memcpy(stage, xi, h->host_pinned_bytes);
+      CK(cudaMemcpyAsync(dst, stage, h->host_pinned_bytes, cudaMemcpyHostToDevice, h->copy_stream));
+      CK(cudaEventRecord(h->stage_ev[b], h->copy_stream));
+      CK(cudaEventRecord(h->xi_copied[xb], h->copy_stream));
+    }
+    CK(cudaStreamWaitEvent(h->stream, h->xi_copied[xb], 0));
+    h->xi_cur = dst;
   }
   cudaEvent_t e0;
   stage_begin(h, afqmc::ST_FB, &e0);
@@ -779,6 +808,7 @@ int afqmc_step(afqmc_handle* h, const double* xi, const double* eshift) {
   stage_begin(h, afqmc::ST_FIELDS, &e0);
   if (mixed) afqmc::launch_fields_mixed(h, xi == nullptr);
   else afqmc::launch_fields(h, xi == nullptr);
+  if (xi) CK(cudaEventRecord(h->xi_read[xb], h->stream));
   stage_end(h, afqmc::ST_FIELDS, e0);
   stage_begin(h, afqmc::ST_VHS, &e0);
   if (mixed) afqmc::launch_vhs_mixed(h);

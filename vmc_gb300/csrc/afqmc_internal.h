@@ -115,6 +115,20 @@ struct afqmc_handle {
   size_t host_pinned_bytes = 0;   // bytes of one buffer
   cudaEvent_t stage_ev[2] = {nullptr, nullptr};  // recorded after each buffer's copy to the device
   int stage_next = 0;
+  // host fields reach the device on their own stream, into two device buffers
+  // used in turn (xi and xi1), so a copy waits only for the fields kernel that
+  // last read its buffer, not for the device's previous step
+  cudaStream_t copy_stream = nullptr;
+  double* xi1 = nullptr;                             // [W][G] second device field buffer
+  double* xi_cur = nullptr;                          // the buffer this step's fields kernel reads
+  cudaEvent_t xi_copied[2] = {nullptr, nullptr};     // the copy into buffer b is done
+  cudaEvent_t xi_read[2] = {nullptr, nullptr};       // the fields kernel that read buffer b is done
+  int xi_next = 0;
+  // asynchronous reads of control-variate results: a FIFO of pinned 6-double
+  // slots, each with the event of its device-to-host copy
+  double* res_pinned = nullptr;                      // [RES_RING][6]
+  cudaEvent_t res_ev[8] = {};
+  int res_head = 0, res_count = 0;
   int nechunk = 0;
   afqmc::PropChunk* d_chunks = nullptr;
   int nchunks = 0;

@@ -350,6 +350,42 @@ int afqmc_cv_measure(afqmc_handle* h, uint64_t tag, int slot) {
   return AFQMC_OK;
 }
 
+// Asynchronous reads of single result slots, first in first out: post
+// enqueues the 6 doubles of `slot` into one of 8 page-locked entries (after the
+// work already in the handle's stream); take waits for the oldest posted entry
+// only and returns its values, so a caller can issue the next step before it
+// reads this one's estimate.
+int afqmc_cv_result_post(afqmc_handle* h, int slot) {
+  if (!h || slot < 0 || slot >= h->cv_nslots) return AFQMC_ERR_ARG;
+  if (h->res_count >= 8) {
+    h->err = "cv_result_post: eight results are posted and not yet taken";
+    return AFQMC_ERR_ARG;
+  }
+  cudaSetDevice(h->device);
+  const int e = (h->res_head + h->res_count) % 8;
+  if (cudaMemcpyAsync(h->res_pinned + 6 * e, h->cv_out + 6 * (size_t)slot, 6 * sizeof(double),
+                      cudaMemcpyDeviceToHost, h->stream) != cudaSuccess ||
+      cudaEventRecord(h->res_ev[e], h->stream) != cudaSuccess)
+    return AFQMC_ERR_CUDA;
+  ++h->res_count;
+  return AFQMC_OK;
+}
+
+int afqmc_cv_result_take(afqmc_handle* h, double* out) {
+  if (!h || !out) return AFQMC_ERR_ARG;
+  if (h->res_count == 0) {
+    h->err = "cv_result_take: nothing is posted";
+    return AFQMC_ERR_ARG;
+  }
+  cudaSetDevice(h->device);
+  const int e = h->res_head;
+  if (cudaEventSynchronize(h->res_ev[e]) != cudaSuccess) return AFQMC_ERR_CUDA;
+  for (int i = 0; i < 6; ++i) out[i] = h->res_pinned[6 * e + i];
+  h->res_head = (h->res_head + 1) % 8;
+  --h->res_count;
+  return AFQMC_OK;
+}
+
 int afqmc_cv_results(afqmc_handle* h, double* out, int nslots) {
   if (!h || !out || nslots <= 0 || nslots > h->cv_nslots) return AFQMC_ERR_ARG;
   cudaSetDevice(h->device);

@@ -989,7 +989,7 @@ __global__ void k_fields(const double* __restrict__ fb, const double2* __restric
 }
 
 void launch_fields(afqmc_handle* h, bool device_rng) {
-  k_fields<<<h->nwalk, 256, 0, h->stream>>>(h->fb, h->mf, h->xi, h->x, h->x32, h->shift, h->fbterm,
+  k_fields<<<h->nwalk, 256, 0, h->stream>>>(h->fb, h->mf, h->xi_cur, h->x, h->x32, h->shift, h->fbterm,
                                             h->weights, h->G, sqrt(h->dt), device_rng ? 1 : 0, h->seed,
                                             h->d_step, h->precision == AFQMC_PREC_REF32 ? 1 : 0);
   h->launches++;

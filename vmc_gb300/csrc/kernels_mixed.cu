@@ -331,7 +331,7 @@ __global__ void k_fields_mixed(const float* __restrict__ fb, const float4* __res
 void launch_fields_mixed(afqmc_handle* h, bool device_rng) {
   // two warps per walker: each thread takes ~5 pairs of fields, and the four
   // compensated sums need two warp reductions rather than eight
-  k_fields_mixed<<<h->nwalk, 64, 0, h->stream>>>(h->fb32, h->mf32, h->xi, h->xB, h->kv_pad, h->shift, h->fbterm,
+  k_fields_mixed<<<h->nwalk, 64, 0, h->stream>>>(h->fb32, h->mf32, h->xi_cur, h->xB, h->kv_pad, h->shift, h->fbterm,
                                                   h->weights, h->G, (float)sqrt(h->dt), device_rng ? 1 : 0, h->seed,
                                                   h->d_step);
   h->launches++;

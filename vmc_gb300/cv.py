@@ -75,6 +75,18 @@ def measure(walkers, tag, slot):
     walkers._check(A.lib().afqmc_cv_measure(walkers.h, int(tag), int(slot)))
 
 
+def result_post(walkers, slot):
+    """Enqueue an asynchronous read of result slot `slot` (first in first out, at most 8)."""
+    walkers._check(A.lib().afqmc_cv_result_post(walkers.h, int(slot)))
+
+
+def result_take(walkers, out=None):
+    """The oldest posted result (6 values), waiting for its copy only."""
+    out = np.zeros(6) if out is None else out
+    walkers._check(A.lib().afqmc_cv_result_take(walkers.h, out.ctypes.data))
+    return out
+
+
 def results(walkers, nslots):
     """(nslots, 6) control-variate results of a handle: E_cv (ratio correction),
     E_cv (Horvitz-Thompson correction, exactly unbiased), E_sub (HT), E_sub
