@@ -629,11 +629,13 @@ void launch_psi_to_f32(afqmc_handle* h) {
 }
 
 constexpr int GJ_THREADS = 1024;  // k_overlap_gj_df32: one CTA of 32 warps per matrix
+constexpr int GJ_P = 32;          // orbitals per staged chunk of Phi and psi when M is formed
+constexpr int GJ_MAXE = 8;        // entries of M per thread (n^2 <= GJ_MAXE GJ_THREADS)
 __global__ void __launch_bounds__(GJ_THREADS)
     k_overlap_gj_df32(const float2* __restrict__ psi32, const float2* __restrict__ phi2,
                       float* __restrict__ theta32, double2* __restrict__ det,
                       const double* __restrict__ weights, int N, int ncw, int nce, Channel c0, Channel c1,
-                      int only_live);
+                      int only_live, int staged);
 
 void launch_overlap_theta(afqmc_handle* h, bool only_live) {
   h->fb_current = false;  // theta changes
@@ -683,9 +685,15 @@ void launch_overlap_theta(afqmc_handle* h, bool only_live) {
   size_t smem = (size_t)nmax * 2 * nmax * sizeof(double2) + nmax * sizeof(double2);
   dim3 grid(h->nwalk, h->nchan);
   if (h->precision == AFQMC_PREC_MIXED && h->psi32 && h->phi2 && h->tune_ovl != 2) {  // double-FP32 elimination
-    smem_optin(k_overlap_gj_df32, 200 * 1024);
-    k_overlap_gj_df32<<<grid, GJ_THREADS, smem, h->stream>>>(h->psi32, h->phi2, h->theta32, h->det, h->weights, h->N, h->ncw,
-                                                      h->nce, h->chan[0], h->chan[1], only_live ? 1 : 0);
+    // the staged formation of M needs two [n][GJ_P + 1] chunks more and at most
+    // GJ_MAXE entries per thread
+    const size_t smem_st = smem + (size_t)2 * nmax * (GJ_P + 1) * sizeof(float2);
+    const bool staged = smem_st <= 227 * 1024 && (size_t)nmax * nmax <= (size_t)GJ_MAXE * GJ_THREADS;
+    const size_t sm = staged ? smem_st : smem;
+    smem_optin(k_overlap_gj_df32, (int)std::max(sm, (size_t)200 * 1024));
+    k_overlap_gj_df32<<<grid, GJ_THREADS, sm, h->stream>>>(h->psi32, h->phi2, h->theta32, h->det, h->weights, h->N,
+                                                         h->ncw, h->nce, h->chan[0], h->chan[1], only_live ? 1 : 0,
+                                                         staged ? 1 : 0);
     h->launches++;
     return;
   }
@@ -723,7 +731,7 @@ __global__ void __launch_bounds__(GJ_THREADS)
     k_overlap_gj_df32(const float2* __restrict__ psi32, const float2* __restrict__ phi2,
                       float* __restrict__ theta32, double2* __restrict__ det,
                       const double* __restrict__ weights, int N, int ncw, int nce, Channel c0, Channel c1,
-                      int only_live) {
+                      int only_live, int staged) {
   const int w = blockIdx.x;
   const Channel ch = blockIdx.y == 0 ? c0 : c1;
   if (only_live && !(weights[w] > 1.0e-8)) return;
@@ -734,23 +742,62 @@ __global__ void __launch_bounds__(GJ_THREADS)
   __shared__ int s_piv;
   const float2* ps = psi32 + (size_t)w * ncw * N + (size_t)ch.psi_off * N;
   const float2* ph = phi2 + (size_t)ch.col_off * N;
-  for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
-    const int i = e / n, j = e % n;
-    // dot2_acc of the real and of the imaginary part, as one packed sequence
-    float2 sv = make_float2(0.f, 0.f), cv = sv;
-    for (int p = 0; p < N; ++p) {
-      const float2 f = ph[i * N + p];
-      const float2 v = ps[j * N + p];
-      const float2 fh = make_float2(f.x, f.x), fl = make_float2(f.y, f.y);
-      const float2 pr = __fmul2_rn(fh, v);
-      const float2 pe = __ffma2_rn(fh, v, f2_neg(pr));
-      float2 t, er;
-      df2_two_sum(sv, pr, t, er);
-      sv = t;
-      cv = __ffma2_rn(fl, v, __fadd2_rn(cv, __fadd2_rn(er, pe)));
+  // dot2_acc of the real and of the imaginary part, as one packed sequence
+  const auto dot2_step = [](float2& sv, float2& cv, float2 f, float2 v) {
+    const float2 fh = make_float2(f.x, f.x), fl = make_float2(f.y, f.y);
+    const float2 pr = __fmul2_rn(fh, v);
+    const float2 pe = __ffma2_rn(fh, v, f2_neg(pr));
+    float2 t, er;
+    df2_two_sum(sv, pr, t, er);
+    sv = t;
+    cv = __ffma2_rn(fl, v, __fadd2_rn(cv, __fadd2_rn(er, pe)));
+  };
+  if (staged) {
+    // M by chunks of GJ_P orbitals: the chunk's Phi and psi rows are loaded
+    // into shared memory with coalesced reads (row pitch GJ_P + 1 pairs), then
+    // every thread adds the chunk's terms to its entries; the terms are added
+    // in the same orbital order as without staging (padding terms are zero)
+    float2* sPh = reinterpret_cast<float2*>(fcol + n);  // [n][GJ_P + 1]
+    float2* sPs = sPh + n * (GJ_P + 1);                  // [n][GJ_P + 1]
+    float2 sv[GJ_MAXE], cv[GJ_MAXE];
+#pragma unroll
+    for (int q = 0; q < GJ_MAXE; ++q) sv[q] = cv[q] = make_float2(0.f, 0.f);
+    for (int p0 = 0; p0 < N; p0 += GJ_P) {
+      __syncthreads();  // the previous chunk is consumed
+      for (int idx = threadIdx.x; idx < n * GJ_P; idx += blockDim.x) {
+        const int i = idx / GJ_P, pp = idx - i * GJ_P, p = p0 + pp;
+        sPh[i * (GJ_P + 1) + pp] = p < N ? ph[i * N + p] : make_float2(0.f, 0.f);
+        sPs[i * (GJ_P + 1) + pp] = p < N ? ps[i * N + p] : make_float2(0.f, 0.f);
+      }
+      __syncthreads();
+#pragma unroll
+      for (int q = 0; q < GJ_MAXE; ++q) {
+        const int e = threadIdx.x + q * GJ_THREADS;
+        if (e < n * n) {
+          const float2* fr = sPh + (e / n) * (GJ_P + 1);
+          const float2* vr = sPs + (e % n) * (GJ_P + 1);
+#pragma unroll 4
+          for (int pp = 0; pp < GJ_P; ++pp) dot2_step(sv[q], cv[q], fr[pp], vr[pp]);
+        }
+      }
     }
-    gj_st(a, i * n2 + j, {df_fast(sv.x, cv.x), df_fast(sv.y, cv.y)});
-    gj_st(a, i * n2 + n + j, {{i == j ? 1.f : 0.f, 0.f}, {0.f, 0.f}});
+#pragma unroll
+    for (int q = 0; q < GJ_MAXE; ++q) {
+      const int e = threadIdx.x + q * GJ_THREADS;
+      if (e < n * n) {
+        const int i = e / n, j = e % n;
+        gj_st(a, i * n2 + j, {df_fast(sv[q].x, cv[q].x), df_fast(sv[q].y, cv[q].y)});
+        gj_st(a, i * n2 + n + j, {{i == j ? 1.f : 0.f, 0.f}, {0.f, 0.f}});
+      }
+    }
+  } else {
+    for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+      const int i = e / n, j = e % n;
+      float2 sv = make_float2(0.f, 0.f), cv = sv;
+      for (int p = 0; p < N; ++p) dot2_step(sv, cv, ph[i * N + p], ps[j * N + p]);
+      gj_st(a, i * n2 + j, {df_fast(sv.x, cv.x), df_fast(sv.y, cv.y)});
+      gj_st(a, i * n2 + n + j, {{i == j ? 1.f : 0.f, 0.f}, {0.f, 0.f}});
+    }
   }
   __syncthreads();
   df32c detv = {{1.f, 0.f}, {0.f, 0.f}};  // meaningful in thread 0
