@@ -317,13 +317,13 @@ __global__ void __launch_bounds__(OW_WARPS * 32, (F32 && MB && NM <= 20) ? 7 : 1
     constexpr int OW_RI = NM / 4, OW_RJ = (NM + 7) / 8;
     const int li = lane >> 3, lj = lane & 7;
     const float2* ps32 = psi32 + (size_t)w * ncw * N + (size_t)ch.psi_off * N;
-    float sh[OW_RI][OW_RJ][2], sl[OW_RI][OW_RJ][2];
+    // (Re, Im) of each entry as one packed pair: the real and imaginary Dot2
+    // sums in one FP32x2 sequence (each component the scalar sequence)
+    float2 sh[OW_RI][OW_RJ], sl[OW_RI][OW_RJ];
 #pragma unroll
     for (int x = 0; x < OW_RI; ++x)
 #pragma unroll
-      for (int y = 0; y < OW_RJ; ++y)
-#pragma unroll
-        for (int c = 0; c < 2; ++c) sh[x][y][c] = sl[x][y][c] = 0.f;
+      for (int y = 0; y < OW_RJ; ++y) sh[x][y] = sl[x][y] = make_float2(0.f, 0.f);
     for (int p = 0; p < N; ++p) {
       float2 v[OW_RJ];
 #pragma unroll
@@ -335,18 +335,15 @@ __global__ void __launch_bounds__(OW_WARPS * 32, (F32 && MB && NM <= 20) ? 7 : 1
       for (int x = 0; x < OW_RI; ++x) {
         const int i = li + 4 * x;
         const float2 f = i < n ? phs2[i * N + p] : make_float2(0.f, 0.f);
+        const float2 fh = make_float2(f.x, f.x), fl = make_float2(f.y, f.y);
 #pragma unroll
         for (int y = 0; y < OW_RJ; ++y) {
-#pragma unroll
-          for (int c = 0; c < 2; ++c) {
-            const float xv = c == 0 ? v[y].x : v[y].y;
-            const float pr = __fmul_rn(f.x, xv);
-            const float pe = fmaf(f.x, xv, -pr);  // f.x xv = pr + pe exactly
-            float t, e;
-            df_two_sum(sh[x][y][c], pr, t, e);
-            sh[x][y][c] = t;
-            sl[x][y][c] = fmaf(f.y, xv, __fadd_rn(sl[x][y][c], __fadd_rn(e, pe)));
-          }
+          const float2 pr = __fmul2_rn(fh, v[y]);
+          const float2 pe = __ffma2_rn(fh, v[y], f2_neg(pr));  // f.x v = pr + pe exactly
+          float2 t, e;
+          df2_two_sum(sh[x][y], pr, t, e);
+          sh[x][y] = t;
+          sl[x][y] = __ffma2_rn(fl, v[y], __fadd2_rn(sl[x][y], __fadd2_rn(e, pe)));
         }
       }
     }
@@ -356,7 +353,7 @@ __global__ void __launch_bounds__(OW_WARPS * 32, (F32 && MB && NM <= 20) ? 7 : 1
       for (int y = 0; y < OW_RJ; ++y) {
         const int i = li + 4 * x, j = lj + 8 * y;
         if (i < n && j < n)
-          st_dfc(ah, al, i * n + j, {df_fast(sh[x][y][0], sl[x][y][0]), df_fast(sh[x][y][1], sl[x][y][1])});
+          st_dfc(ah, al, i * n + j, {df_fast(sh[x][y].x, sl[x][y].x), df_fast(sh[x][y].y, sl[x][y].y)});
       }
   } else {  // M = Phi^T psi
     constexpr int OW_RI = NM / 4, OW_RJ = (NM + 7) / 8;
