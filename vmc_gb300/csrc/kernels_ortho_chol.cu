@@ -44,6 +44,7 @@
 namespace afqmc {
 
 constexpr int OC_THREADS = 256;
+constexpr int OCG_QT = 64;  // rows of A per tile in the Q product of k_ortho_chol_g
 
 __global__ void __launch_bounds__(OC_THREADS)
     k_ortho_chol(double2* __restrict__ psi, float2* __restrict__ psi32, double2* __restrict__ ovlp,
@@ -183,11 +184,10 @@ __global__ void __launch_bounds__(OC_THREADS)
 // memory (N x n beyond ~200 KB as pairs, e.g. N = 400, n = 60): the block
 // stays in global memory (L2).  The Gram matrix comes from the FP32 copy
 // (the high part of every stored number) with one warp per (i, j) pair and
-// lanes over the orbitals; Cholesky and X = R^-1 are as above; Q = A X runs in
-// place with one thread per orbital row p: Q(p, j) needs A(p, i) for i <= j
-// only, so the thread forms its row's columns from the last to the first and
-// overwrites each A(p, j) once it is no longer needed (no other thread reads
-// row p).
+// lanes over the orbitals; Cholesky and X = R^-1 are as above; Q = A X runs
+// over tiles of rows: a tile's A is split once into FP32 pairs in shared
+// memory, Q(p, j) needs A(p, i) of its own row only, so the tile's Q is
+// written over the tile's rows.
 __global__ void __launch_bounds__(OC_THREADS)
     k_ortho_chol_g(double2* __restrict__ psi, float2* __restrict__ psi32, double2* __restrict__ ovlp,
                    const double* __restrict__ weights, int N, int ncw, int na, int nb, int rhf_walker, int nmax) {
@@ -271,19 +271,44 @@ __global__ void __launch_bounds__(OC_THREADS)
       }
     }
     __syncthreads();
-    for (int p = tid; p < N; p += OC_THREADS) {
-      for (int j = n - 1; j >= 0; --j) {
-        float2 s2 = make_float2(0.f, 0.f), c2 = s2;  // (Re, Im) packed, as above
-        for (int i = 0; i <= j; ++i) {
+    // Q = A X by tiles of OCG_QT rows: the tile's A is split once into
+    // (high, low) pairs in shared memory (entry i of row r at i (OCG_QT + 1) +
+    // r), then thread (row r, group g) forms Q(r, j) for j = g, g + 4, ... --
+    // the same Dot2 terms in the same order as the row-by-row form -- and writes
+    // Q and its FP32 copy over the tile's rows (Q's rows need only their own A)
+    float2* Th = X + (size_t)nmax * nmax;          // [n][OCG_QT + 1]
+    float2* Tl = Th + (size_t)nmax * (OCG_QT + 1);  // [n][OCG_QT + 1]
+    const int rr = tid % OCG_QT, gg = tid / OCG_QT;
+    for (int p0 = 0; p0 < N; p0 += OCG_QT) {
+      __syncthreads();  // the previous tile is consumed
+      for (int e = tid; e < n * OCG_QT; e += OC_THREADS) {
+        const int i = e / OCG_QT, r = e % OCG_QT, p = p0 + r;
+        float2 h = make_float2(0.f, 0.f), l = h;
+        if (p < N) {
           const double2 v = Ag[(size_t)i * N + p];
           const df32 re = df_split_bits(v.x), im = df_split_bits(v.y);
-          const float2 x = X[i * n + j];
-          dot2_acc2(s2, c2, make_float2(re.h, re.h), make_float2(re.l, re.l), x);
-          dot2_acc2(s2, c2, make_float2(-im.h, im.h), make_float2(-im.l, im.l), make_float2(x.y, x.x));
+          h = make_float2(re.h, im.h);
+          l = make_float2(re.l, im.l);
         }
-        const double2 q = make_double2(df_to_double_bits(df_fast(s2.x, c2.x)), df_to_double_bits(df_fast(s2.y, c2.y)));
-        Ag[(size_t)j * N + p] = q;
-        Ag32[(size_t)j * N + p] = make_float2(df_split_bits(q.x).h, df_split_bits(q.y).h);
+        Th[i * (OCG_QT + 1) + r] = h;
+        Tl[i * (OCG_QT + 1) + r] = l;
+      }
+      __syncthreads();
+      const int p = p0 + rr;
+      if (p < N) {
+        for (int jj = gg; jj < n; jj += OC_THREADS / OCG_QT) {
+          float2 s2 = make_float2(0.f, 0.f), c2 = s2;  // (Re, Im) packed
+          for (int i = 0; i <= jj; ++i) {
+            const float2 h = Th[i * (OCG_QT + 1) + rr], l = Tl[i * (OCG_QT + 1) + rr];
+            const float2 x = X[i * n + jj];
+            dot2_acc2(s2, c2, make_float2(h.x, h.x), make_float2(l.x, l.x), x);
+            dot2_acc2(s2, c2, make_float2(-h.y, h.y), make_float2(-l.y, l.y), make_float2(x.y, x.x));
+          }
+          const double2 q =
+              make_double2(df_to_double_bits(df_fast(s2.x, c2.x)), df_to_double_bits(df_fast(s2.y, c2.y)));
+          Ag[(size_t)jj * N + p] = q;
+          Ag32[(size_t)jj * N + p] = make_float2(df_split_bits(q.x).h, df_split_bits(q.y).h);
+        }
       }
     }
     if (tid == 0)
@@ -298,7 +323,7 @@ __global__ void __launch_bounds__(OC_THREADS)
 
 size_t ortho_chol_g_smem(const afqmc_handle* h) {
   const size_t nmax = (size_t)std::max(h->na, h->rhf_walker ? 0 : h->nb);
-  return 2 * nmax * nmax * sizeof(float2);
+  return (2 * nmax * nmax + 2 * nmax * (OCG_QT + 1)) * sizeof(float2);
 }
 
 size_t ortho_chol_smem(const afqmc_handle* h) {
