@@ -127,7 +127,12 @@ int afqmc_force_bias(afqmc_handle* h, double* fb);
  * eshift: if non-NULL, the energy shift for this step; if NULL, the device value
  *         left by the previous step's population control,
  *         eshift = e_estimate - 0.1 ln(sum_w / pop_target) / dt.
- * Asynchronous: returns once the work is queued on the handle's stream. */
+ * Asynchronous: returns once the work is queued on the handle's stream (and,
+ * with host fields, once they have been copied, so the caller may refill its
+ * buffer).  Host fields go to the device on the handle's copy stream, into one
+ * of two device buffers used in turn; the copy waits only for the step two
+ * back to have read that buffer, so it overlaps the previous step when the
+ * caller issues this step before waiting for the previous one's results. */
 int afqmc_step(afqmc_handle* h, const double* xi, const double* eshift);
 
 /* Set the energy estimate used by the device population control, and optionally
