@@ -7,7 +7,7 @@
 // TMA loads 3-D boxes -- gbox Cholesky vectors x n rows of rot, wbox walkers x
 // 2 planes x n columns of theta -- so a 128 x BN tile holds whole n x n blocks
 // f_sg(w) for gbox x wbox (g, w) pairs.  The epilogue copies the tile from TMEM
-// to shared memory and each warp forms, per pair,
+// to shared memory and the CTA forms, per pair,
 //     X = sum_ij f[i][j] f[j][i]   and   c = sum_i f[i][i]     (complex)
 // written to xc[w][s][g].  A small FP64 kernel then assembles
 //     E = ecore + mult sum_s tr(G_s h1) + 1/2 sum_{g<Gene} [(mult sum_s c_sg)^2 - mult sum_s X_sg].
@@ -44,12 +44,24 @@ constexpr int EX_HEAD = 1024;  // barriers and the TMEM address, ahead of the (1
 constexpr int EX_PIPE = EX_STAGES * EX_STAGE;
 static_assert((2 * EX_STAGES + 1) * 8 + 16 <= EX_HEAD, "barrier block");
 
-// fp32 row pitch of one walker's staged columns [2 wl n, 2 (wl + 1) n) widened
-// to 16-column bounds (at most 2n rounded up, plus 16, and at most the tile)
-static int ex_pitch(int n) { return std::min(EX_BN, (2 * n + 15) / 16 * 16 + 16) + 1; }
+// The epilogue stages one walker's accumulator columns [2 wl n, 2 (wl + 1) n),
+// widened to 16-column bounds, transposed: S[c][r] = D[r][c_lo + c] for the
+// tile's 128 rows r.  Row r = (gl, i) of the tile then finds its own f[i][j]
+// down column r (S[c_re + j][r], lanes on consecutive words) and the
+// transposed f[j][i] along row c_re + i (S[c_re + i][gl n + j], 16-byte loads
+// when n % 4 == 0: a pitch of 132 words puts the 8 rows a quarter-warp reads
+// in 8 different 16-byte bank groups; 129 otherwise).
+static int ex_pitch(int n) { return n % 4 == 0 ? 132 : 129; }
+// staged columns per walker: at most 2n rounded up to 16, plus 16, at most the tile
+static int ex_srows(int n) { return std::min(EX_BN, (2 * n + 15) / 16 * 16 + 16); }
+constexpr int EX_PART = 2 * 4 * BM * 4;  // per-row partial sums: 2 slots x 4 sums x 128 rows
+static size_t ex_slot(int n) { return (size_t)ex_srows(n) * ex_pitch(n) * 4; }
+// walkers staged together: two (one per warp half) when both fit in the
+// pipeline's buffers, so that the CTA keeps its half of the SM
+static int ex_wpar(int n) { return 2 * ex_slot(n) + EX_PART <= (size_t)EX_PIPE ? 2 : 1; }
 // dynamic shared memory: the stages, which the staged columns reuse
 static size_t ex_smem(int n) {
-  return 1024 + EX_HEAD + std::max((size_t)EX_PIPE, (size_t)BM * ex_pitch(n) * 4);
+  return 1024 + EX_HEAD + std::max((size_t)EX_PIPE, ex_wpar(n) * ex_slot(n) + EX_PART);
 }
 
 struct ExArgs {
@@ -58,14 +70,18 @@ struct ExArgs {
   int a_bytes, b_bytes;
   int col_off;    // channel column offset in the [nce] axis
   int s;          // channel index
-  int ld;         // fp32 pitch of the staged walker columns (ex_pitch(n))
+  int ld;         // fp32 pitch of the staged columns (ex_pitch(n))
+  int srows;      // staged columns per walker (ex_srows(n))
+  int wpar;       // walkers staged together (ex_wpar(n))
 };
 
 // grid: (walker tiles, g tiles, channels); EX_THREADS threads: warp 0 lane 0
-// loads, warp 1 lane 0 issues the MMAs, and all warps share the epilogue,
-// one walker of the tile at a time: its 2n columns are copied from TMEM to
-// shared memory (warp w reads lane quadrant w % 4, 16-column pieces w / 4,
-// w / 4 + 2, ...) and warp w then reduces the (g, walker) blocks gl = w, w + 8, ...
+// loads, warp 1 lane 0 issues the MMAs, and all warps share the epilogue.
+// Warp w reads TMEM lane quadrant w % 4; its half w / 4 is a walker slot when
+// two walkers are staged together, else a half of the j range of the one
+// walker.  Per staged walker: its columns go from TMEM to S; each thread forms
+// its row's X_r = sum_j f[i][j] f[j][i] and f[i][i]; the n rows of each
+// (g, walker) block are then summed by one thread per (block, sum).
 constexpr int EX_THREADS = 256;
 __global__ void __launch_bounds__(EX_THREADS, 2)
     k_tc_exchange(const __grid_constant__ CUtensorMap tmA0, const __grid_constant__ CUtensorMap tmB0,
@@ -146,59 +162,96 @@ __global__ void __launch_bounds__(EX_THREADS, 2)
   }
   __syncthreads();  // all loads consumed: the pipeline buffers become the staging buffer
   float* tile = (float*)smem;
-  const int n = A.n, ld = A.ld;
+  const int n = A.n, P = A.ld, nslot = A.wpar;
+  float* part = tile + nslot * A.srows * P;  // [2][4][BM] per-row partial sums
   const bool run = have && !s_abort;
-  const int q = warp & 3;
+  const int q = warp & 3, half = warp >> 2;
   const int row = q * 32 + lane;
-  // walk of the n x n block: lane's first (i, j) and the step of 32 entries
-  const int dq = 32 / n, dr = 32 - dq * n;
+  // the j range of this warp half: all of it with two walker slots, else a
+  // half (a multiple of 4 wide, so that the 16-byte loads stay aligned)
+  const int jh = nslot == 2 ? n : ((n + 1) / 2 + 3) & ~3;
+  const int ja = nslot == 2 ? 0 : min(n, half * jh), jb = min(n, ja + jh);
+  const bool vec4 = (n & 3) == 0;
 #pragma unroll 1
-  for (int wl = 0; wl < A.wbox; ++wl) {
-    const int w = w0 + wl;
+  for (int it = 0; it * nslot < A.wbox; ++it) {
+    const int wl = it * nslot + (nslot == 2 ? half : 0);
+    const bool act = run && wl < A.wbox && w0 + wl < W;
+    float* S = tile + (nslot == 2 ? half : 0) * A.srows * P;
     const int c_lo = (2 * wl * n) & ~15, c_hi = (2 * (wl + 1) * n + 15) & ~15;
-    if (run && w < W) {
+    if (act) {
+      // two slots: this half's four warps copy all pieces of its walker;
+      // one slot: the halves take alternate 16-column pieces
+      const int cstep = nslot == 2 ? 16 : 32;
 #pragma unroll 1
-      for (int c = c_lo + (warp >> 2) * 16; c < c_hi; c += 32) {
+      for (int c = c_lo + (nslot == 2 ? 0 : half * 16); c < c_hi; c += cstep) {
         float v[16];
         tc::tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)c, v);
+        float* dst = S + (c - c_lo) * P + row;
 #pragma unroll
-        for (int j = 0; j < 16; ++j) tile[row * ld + (c - c_lo) + j] = v[j];
+        for (int k = 0; k < 16; ++k) dst[k * P] = v[k];
       }
     }
     __syncthreads();
-    if (run && w < W) {
+    float xr = 0.f, xi = 0.f, cr = 0.f, ci = 0.f;
+    if (act && row < A.gbox * n) {
+      const int gl = row / n, i = row - gl * n;
       const int cre = 2 * wl * n - c_lo, cim = cre + n;
-      for (int gl = warp; gl < A.gbox; gl += EX_THREADS / 32) {
-        const int g = g0 + gl;
-        if (g >= Gene) continue;
-        const float* rowbase = tile + (gl * n) * ld;
-        float xr = 0.f, xi = 0.f, cr = 0.f, ci = 0.f;
-        int i = lane / n, j = lane % n;
-        for (int e = lane; e < n * n; e += 32) {
-          const float a_r = rowbase[i * ld + cre + j], a_i = rowbase[i * ld + cim + j];
-          const float b_r = rowbase[j * ld + cre + i], b_i = rowbase[j * ld + cim + i];
-          xr = fmaf(a_r, b_r, fmaf(-a_i, b_i, xr));
-          xi = fmaf(a_r, b_i, fmaf(a_i, b_r, xi));
-          if (i == j) { cr += a_r; ci += a_i; }
-          i += dq;
-          j += dr;
-          if (j >= n) {
-            j -= n;
-            ++i;
-          }
+      const float* are = S + cre * P + row;  // f[i][j] = are[j P] (+ i f_im[i][j] at aim)
+      const float* aim = S + cim * P + row;
+      const float* bre = S + (cre + i) * P + gl * n;  // f[j][i] = bre[j]
+      const float* bim = S + (cim + i) * P + gl * n;
+      if (vec4) {
+#pragma unroll 1
+        for (int j = ja; j < jb; j += 4) {
+          const float4 br = *(const float4*)(bre + j), bi = *(const float4*)(bim + j);
+          const float ar0 = are[j * P], ar1 = are[(j + 1) * P], ar2 = are[(j + 2) * P], ar3 = are[(j + 3) * P];
+          const float ai0 = aim[j * P], ai1 = aim[(j + 1) * P], ai2 = aim[(j + 2) * P], ai3 = aim[(j + 3) * P];
+          xr = fmaf(ar0, br.x, fmaf(-ai0, bi.x, xr));
+          xi = fmaf(ar0, bi.x, fmaf(ai0, br.x, xi));
+          xr = fmaf(ar1, br.y, fmaf(-ai1, bi.y, xr));
+          xi = fmaf(ar1, bi.y, fmaf(ai1, br.y, xi));
+          xr = fmaf(ar2, br.z, fmaf(-ai2, bi.z, xr));
+          xi = fmaf(ar2, bi.z, fmaf(ai2, br.z, xi));
+          xr = fmaf(ar3, br.w, fmaf(-ai3, bi.w, xr));
+          xi = fmaf(ar3, bi.w, fmaf(ai3, br.w, xi));
         }
-        xr = warp_sumf(xr);
-        xi = warp_sumf(xi);
-        cr = warp_sumf(cr);
-        ci = warp_sumf(ci);
-        if (lane == 0) {
-          double2* o = xc + (((size_t)w * 2 + A.s) * Gene + g) * 2;
-          o[0] = make_double2(xr, xi);
-          o[1] = make_double2(cr, ci);
+      } else {
+#pragma unroll 1
+        for (int j = ja; j < jb; ++j) {
+          const float ar = are[j * P], ai = aim[j * P], br = bre[j], bi = bim[j];
+          xr = fmaf(ar, br, fmaf(-ai, bi, xr));
+          xi = fmaf(ar, bi, fmaf(ai, br, xi));
         }
       }
+      if (i >= ja && i < jb) {
+        cr = are[i * P];
+        ci = aim[i * P];
+      }
     }
-    __syncthreads();  // the chunk is consumed before the next one is staged
+    part[(half * 4 + 0) * BM + row] = xr;
+    part[(half * 4 + 1) * BM + row] = xi;
+    part[(half * 4 + 2) * BM + row] = cr;
+    part[(half * 4 + 3) * BM + row] = ci;
+    __syncthreads();
+    // one thread per (slot, g, sum): the n rows of the block, in row order
+    // (one slot: the two j halves of each row added first)
+    const int ntask = nslot * A.gbox * 4;
+    for (int t = threadIdx.x; t < ntask; t += EX_THREADS) {
+      const int qq = t & 3, gl = (t >> 2) % A.gbox, s = (t >> 2) / A.gbox;
+      const int wl2 = it * nslot + s, g = g0 + gl;
+      if (!run || wl2 >= A.wbox || w0 + wl2 >= W || g >= Gene) continue;
+      const float* p0 = part + (s * 4 + qq) * BM + gl * n;
+      float sum = 0.f;
+      if (nslot == 2) {
+        for (int i = 0; i < n; ++i) sum += p0[i];
+      } else {
+        const float* p1 = p0 + 4 * BM;
+        for (int i = 0; i < n; ++i) sum += p0[i] + p1[i];
+      }
+      // xc[w][s][g] = {(X re, X im), (c re, c im)}
+      double* o = (double*)(xc + (((size_t)(w0 + wl2) * 2 + A.s) * Gene + g) * 2);
+      o[qq] = (double)sum;
+    }
   }
   tc::tc_fence_before();
   __syncthreads();
@@ -300,6 +353,8 @@ void launch_local_energy_mixed_subset(afqmc_handle* h, const int* d_idx, int m, 
     a[s].col_off = h->chan[s].col_off;
     a[s].s = s;
     a[s].ld = ex_pitch(n);
+    a[s].srows = ex_srows(n);
+    a[s].wpar = std::min(ex_wpar(n), a[s].wbox);
     smem = std::max(smem, ex_smem(n));
     gt = std::max(gt, (h->nchol_ene + a[s].gbox - 1) / a[s].gbox);
     wt = std::max(wt, (m + a[s].wbox - 1) / a[s].wbox);
