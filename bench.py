@@ -594,11 +594,15 @@ def main():
     # the weights and the step's energy estimate D2H, every step
     rng = np.random.default_rng(1)
     import torch
+    # each step's own fields, drawn beforehand into page-locked host memory
+    # (one buffer per step up to 64, then reused in turn): the walkers take
+    # the random walk that the device-drawn fields give them
+    nbuf = max(1, min(args.steps, 64))
     xis = []
-    for _ in range(2):  # the step's fields in page-locked host memory
+    for _ in range(nbuf):
         t = torch.empty((W, G), dtype=torch.float64, pin_memory=True)
         t.numpy()[:] = rng.standard_normal((W, G))
-        xis.append(t.numpy())
+        xis.append(t)
     from vmc_gb300 import cv as CVM
     ebuf = np.zeros(6)
     wk.sync()
@@ -608,7 +612,7 @@ def main():
     # the handle's copy stream while step k runs) before step k's estimate is
     # taken from the result queue
     for k in range(args.steps):
-        wk.propagate_phaseless(xis[k % 2])
+        wk.propagate_phaseless(xis[k % nbuf].numpy())
         if (k + 1) % ORTHO_EVERY == 0:
             wk.orthogonalize()
         cv.measure(tag=k0 + k, slot=k % 2)
