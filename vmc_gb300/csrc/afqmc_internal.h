@@ -50,6 +50,7 @@ enum {
 };
 constexpr int BLK_MAX = 65536;  // block ring capacity (samples of one run)
 constexpr int WT_MAXPARTS = 1024;  // CTAs of the weight update (partial sums)
+constexpr int CV_EST_THREADS = 256, CV_EST_MAX_CTAS = 64;  // the control-variate estimate's grid
 constexpr int DERR_NAN_ENERGY = 100;  // d_err code: non-finite local energy in a device block
 
 // Stage names for timing.
@@ -194,6 +195,8 @@ struct afqmc_handle {
   double2* cv_esub = nullptr;        // [W]     exact energies of the subsample
   float* cv_ms = nullptr;            // [2][67] feature mean / std
   double* cv_out = nullptr;          // [cv_nslots][4]
+  double* cv_part = nullptr;         // [CV_EST_MAX_CTAS][8] per-CTA sums of the estimate
+  unsigned int* cv_cnt = nullptr;    // CTAs of the estimate finished (the last one resets it to 0)
   int cv_nslots = 4096, cv_den = 8;
   float cv_ymean = 0.f, cv_ystd = 1.f;
   struct afqmc_mlp* cv_mlp = nullptr;

@@ -170,14 +170,22 @@ __global__ void k_split_theta_gather(const float* __restrict__ theta, const int*
 
 // f: the network's outputs in standard units; the prediction is ymean + ystd f
 // (FP32, as the energies were scaled for training)
-__global__ void k_cv_estimate(const double* __restrict__ weights, const float* __restrict__ fraw, float ymean,
-                              float ystd, const int* __restrict__ idx, const double2* __restrict__ esub, int W, int m,
-                              int den, double* __restrict__ out) {
+// Spread over CV_EST_MAX_CTAS CTAs at most (one walker per thread at the
+// bench's 2048): the sums are FP64, whose pipe is narrow on this GPU, so one
+// CTA doing all of them on one SM is the slow form.  Each CTA writes its seven
+// sums to part[cta]; the last CTA to finish (a counter, reset by that CTA)
+// adds the partials in CTA order, so the result does not depend on timing.
+__global__ void __launch_bounds__(CV_EST_THREADS)
+    k_cv_estimate(const double* __restrict__ weights, const float* __restrict__ fraw, float ymean, float ystd,
+                  const int* __restrict__ idx, const double2* __restrict__ esub, int W, int m, int den,
+                  double* __restrict__ part, unsigned int* __restrict__ cnt, double* __restrict__ out) {
   const auto f = [&](int w) { return ymean + ystd * fraw[w]; };
   constexpr int NV = 7;  // sw, swf, corr, ht, nrw, nrwe, nrwf: one reduction for all seven
-  __shared__ double s_part[32][NV];
+  __shared__ double s_part[CV_EST_THREADS / 32][NV];
+  __shared__ bool s_last;
   double v[NV] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
-  for (int w = threadIdx.x; w < W; w += blockDim.x) {
+  const int stride = gridDim.x * blockDim.x;
+  for (int w = blockIdx.x * blockDim.x + threadIdx.x; w < W; w += stride) {
     // dead walkers are skipped, not multiplied by 0: their prediction may be
     // non-finite (a walker that died of a non-finite overlap)
     const double wt = weights[w];
@@ -186,7 +194,7 @@ __global__ void k_cv_estimate(const double* __restrict__ weights, const float* _
       v[1] += wt * (double)f(w);
     }
   }
-  for (int i = threadIdx.x; i < m; i += blockDim.x) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += stride) {
     const int w = idx[i];
     const double inv = (double)min(den, W - i * den);
     const double wt = weights[w];
@@ -207,21 +215,38 @@ __global__ void k_cv_estimate(const double* __restrict__ weights, const float* _
   }
   __syncthreads();
   if (warp == 0) {
-    const int nw = (blockDim.x + 31) >> 5;
+    constexpr int nw = CV_EST_THREADS / 32;
 #pragma unroll
     for (int j = 0; j < NV; ++j) {
       v[j] = lane < nw ? s_part[lane][j] : 0.0;
       for (int o = 16; o > 0; o >>= 1) v[j] += __shfl_down_sync(0xffffffffu, v[j], o);
     }
     if (lane == 0) {
-      const double sw = v[0], swf = v[1], corr = v[2], ht = v[3], nrw = v[4], nrwe = v[5], nrwf = v[6];
-      out[0] = swf / sw + (nrwe - nrwf) / nrw;
-      out[1] = (swf + corr) / sw;
-      out[2] = ht / sw;
-      out[3] = nrwe / nrw;
-      out[4] = sw;
-      out[5] = nrw;
+#pragma unroll
+      for (int j = 0; j < NV; ++j) part[blockIdx.x * 8 + j] = v[j];
+      __threadfence();
+      s_last = atomicAdd(cnt, 1u) == gridDim.x - 1;
     }
+  }
+  __syncthreads();
+  if (!s_last || warp != 0) return;
+  __threadfence();
+  // lane j < 7 adds sum j of every CTA, in CTA order (read from L2: the
+  // other CTAs' stores are not in this SM's L1)
+  double t = 0.0;
+  if (lane < NV)
+    for (int b = 0; b < (int)gridDim.x; ++b) t += __ldcg(part + b * 8 + lane);
+#pragma unroll
+  for (int j = 0; j < NV; ++j) v[j] = __shfl_sync(0xffffffffu, t, j);
+  if (lane == 0) {
+    const double sw = v[0], swf = v[1], corr = v[2], ht = v[3], nrw = v[4], nrwe = v[5], nrwf = v[6];
+    out[0] = swf / sw + (nrwe - nrwf) / nrw;
+    out[1] = (swf + corr) / sw;
+    out[2] = ht / sw;
+    out[3] = nrwe / nrw;
+    out[4] = sw;
+    out[5] = nrw;
+    *cnt = 0u;  // every CTA has counted: the next launch starts from zero
   }
 }
 
@@ -339,8 +364,10 @@ int afqmc_cv_measure(afqmc_handle* h, uint64_t tag, int slot) {
                                             h->cv_ms, h->cv_ms + CV_NF, h->cv_x);
   const int mlp_launches = mlp_forward_on(h->cv_mlp, h->cv_x, W, h->cv_f, h->stream, false);
   cudaStreamWaitEvent(h->stream, h->cv_join, 0);
-  k_cv_estimate<<<1, 256, 0, h->stream>>>(h->weights, h->cv_f, h->cv_ymean, h->cv_ystd, h->cv_idx, h->cv_esub, W, m, den,
-                                           h->cv_out + 6 * (size_t)slot);
+  const int nb = std::max(1, std::min(CV_EST_MAX_CTAS, (W + CV_EST_THREADS - 1) / CV_EST_THREADS));
+  k_cv_estimate<<<nb, CV_EST_THREADS, 0, h->stream>>>(h->weights, h->cv_f, h->cv_ymean, h->cv_ystd, h->cv_idx,
+                                                      h->cv_esub, W, m, den, h->cv_part, h->cv_cnt,
+                                                      h->cv_out + 6 * (size_t)slot);
   h->launches += 3 + mlp_launches;  // features, select, estimate and the MLP (the rest count themselves)
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) {
