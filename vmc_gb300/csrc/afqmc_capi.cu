@@ -180,7 +180,7 @@ void release(afqmc_handle* h) {
                   h->qwork, h->epart, h->eloc, h->scal, h->d_chunks, h->d_err, h->rotA, h->LTA,
                   h->thetaB, h->xB, h->fb32, h->V32, h->expm32, h->d_chunks32, h->rotE, h->thetaE,
                   h->xc, h->cv_x, h->cv_idx, h->cv_esub, h->cv_f, h->cv_ms, h->cv_out, h->cv_part, h->cv_cnt, h->d_step, h->psi32,
-                  h->pt_img, h->comb_cum, h->comb_idx, h->comb_ovl, h->blk, h->blk_zeta, h->wpart,
+                  h->pt_img, h->comb_cum, h->comb_idx, h->comb_ovl, h->blk, h->blk_zeta, h->wpart, h->wt_cnt,
                   h->ovl_tau, h->ovl_bimg, h->ovl_M, h->theta32, h->mf32, h->h1phi32, h->pt_voff,
                   h->rdm_acc, h->rdm_part, h->pb_img, h->pb_scratch, h->phi2, h->xi1};
   for (void* p : ptrs)
@@ -541,6 +541,7 @@ int afqmc_create(const afqmc_ham* ham, const afqmc_trial* trial, const afqmc_opt
   ALLOC(scal, (size_t)afqmc::S_NSLOTS);
   ALLOC(d_chunks, (size_t)h->nchunks);
   ALLOC(wpart, 3 * (size_t)afqmc::WT_MAXPARTS);
+  ALLOC(wt_cnt, 1);
   ALLOC(comb_cum, W);
   ALLOC(comb_idx, W);
   ALLOC(comb_ovl, W);
@@ -607,6 +608,7 @@ int afqmc_create(const afqmc_ham* ham, const afqmc_trial* trial, const afqmc_opt
     ce = cudaMemsetAsync(h->d_err, 0, sizeof(int), h->stream);
     if (ce == cudaSuccess) ce = cudaMemsetAsync(h->d_step, 0, sizeof(unsigned long long), h->stream);
     if (ce == cudaSuccess) ce = cudaMemsetAsync(h->cv_cnt, 0, sizeof(unsigned int), h->stream);
+    if (ce == cudaSuccess) ce = cudaMemsetAsync(h->wt_cnt, 0, sizeof(unsigned int), h->stream);
     if (ce != cudaSuccess) { g_create_err = cudaGetErrorString(ce); release(h); delete h; return AFQMC_ERR_CUDA; }
   }
   std::vector<double> sc(afqmc::S_NSLOTS, 0.0);

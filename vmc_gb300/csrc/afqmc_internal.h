@@ -170,6 +170,7 @@ struct afqmc_handle {
   float2* psi32 = nullptr;               // [W][ncw][N] FP32 copy of psi (mixed form)
   // device-resident blocks: comb scratch, the block ring and host-given zetas
   double* wpart = nullptr;      // [WT_MAXPARTS][2] partial sums of the weight update
+  unsigned int* wt_cnt = nullptr;  // CTAs of the weight update finished (the last one resets it to 0)
   double* comb_cum = nullptr;   // [W]
   int* comb_idx = nullptr;      // [W]
   double2* comb_ovl = nullptr;  // [W]

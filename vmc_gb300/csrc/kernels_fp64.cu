@@ -1118,11 +1118,16 @@ __global__ void k_propagate(double2* __restrict__ psi, const double* __restrict_
 //   val = exp(Re ex) Re(ratio exp(-i sdt Im(shift))).
 // (A non-finite ratio gives a non-finite val, which the window sets to 0.)
 constexpr int WT_THREADS = 32;
+// The last CTA to finish (a counter, reset by that CTA) also forms the totals:
+// one warp, lane summing the partials lane, lane + 32, ... in CTA order, then a
+// butterfly (a fixed order either way), the next eshift and the device step.
 __global__ void __launch_bounds__(WT_THREADS)
     k_weights(double* __restrict__ weights, double2* __restrict__ ovlp, const double2* __restrict__ det,
-              const double2* __restrict__ shift, const double2* __restrict__ fbterm, const double* __restrict__ scal,
+              const double2* __restrict__ shift, const double2* __restrict__ fbterm, double* __restrict__ scal,
               int W, int nchan, int mult, double dt, double c0r, double c0i, double cap,
-              double* __restrict__ part) {
+              double* __restrict__ part, unsigned int* __restrict__ cnt, double target,
+              unsigned long long* __restrict__ stepp) {
+  static_assert(WT_THREADS == 32, "one warp per CTA: the last CTA's totals are one warp's work");
   const double eshift = scal[S_ESHIFT];
   const double sdt = sqrt(dt);
   double sumw = 0.0;
@@ -1152,22 +1157,21 @@ __global__ void __launch_bounds__(WT_THREADS)
   sumw = block_sum(sumw);
   ncap = block_sum(ncap);
   nlive = block_sum(nlive);
+  unsigned int last = 0;
   if (threadIdx.x == 0) {
     part[3 * blockIdx.x] = sumw;
     part[3 * blockIdx.x + 1] = ncap;
     part[3 * blockIdx.x + 2] = nlive;
+    __threadfence();
+    last = atomicAdd(cnt, 1u) == gridDim.x - 1 ? 1u : 0u;
   }
-}
-
-__global__ void k_weights_final(const double* __restrict__ part, int nparts, double* __restrict__ scal, double dt,
-                                double target, unsigned long long* __restrict__ stepp) {
-  // one warp: lane sums the partials lane, lane + 32, ... in order, then a
-  // butterfly (a fixed order either way)
-  double sumw = 0.0, ncap = 0.0, nlive = 0.0;
-  for (int b = threadIdx.x; b < nparts; b += 32) {
-    sumw += part[3 * b];
-    ncap += part[3 * b + 1];
-    nlive += part[3 * b + 2];
+  if (!__shfl_sync(0xffffffffu, last, 0)) return;
+  __threadfence();
+  sumw = ncap = nlive = 0.0;
+  for (int b = threadIdx.x; b < (int)gridDim.x; b += 32) {  // other CTAs' stores: read from L2
+    sumw += __ldcg(part + 3 * b);
+    ncap += __ldcg(part + 3 * b + 1);
+    nlive += __ldcg(part + 3 * b + 2);
   }
   sumw = warp_sum(sumw);
   ncap = warp_sum(ncap);
@@ -1178,6 +1182,7 @@ __global__ void k_weights_final(const double* __restrict__ part, int nparts, dou
     scal[S_NLIVE] += nlive;
     scal[S_ESHIFT] = scal[S_EEST] - 0.1 * log(sumw / target) / dt;
     *stepp += 1;  // the device field stream's step counter (graph replays advance it)
+    *cnt = 0u;    // every CTA has counted: the next launch starts from zero
   }
 }
 
@@ -1187,9 +1192,9 @@ void launch_weights(afqmc_handle* h) {
   const double cr = h->prop_constant.real(), ci = h->prop_constant.imag();
   const int nb = weights_parts(h);
   k_weights<<<nb, WT_THREADS, 0, h->stream>>>(h->weights, h->ovlp, h->det, h->shift, h->fbterm, h->scal, h->nwalk,
-                                               h->nchan, h->mult, h->dt, cr, ci, h->weight_cap, h->wpart);
-  k_weights_final<<<1, 32, 0, h->stream>>>(h->wpart, nb, h->scal, h->dt, h->pop_target, h->d_step);
-  h->launches += 2;
+                                               h->nchan, h->mult, h->dt, cr, ci, h->weight_cap, h->wpart, h->wt_cnt,
+                                               h->pop_target, h->d_step);
+  h->launches += 1;
 }
 
 // ---------------------------------------------------------------------------
