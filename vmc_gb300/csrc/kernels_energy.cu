@@ -43,6 +43,11 @@ constexpr int EX_STAGE = EX_A_BYTES + EX_B_BYTES;
 constexpr int EX_HEAD = 1024;  // barriers and the TMEM address, ahead of the (1024-aligned) stages
 constexpr int EX_PIPE = EX_STAGES * EX_STAGE;
 static_assert((2 * EX_STAGES + 1) * 8 + 16 <= EX_HEAD, "barrier block");
+// 12 warps: warp w reads TMEM lane quadrant w % 4 and belongs to group w / 4
+constexpr int EX_THREADS = 384;
+constexpr int EX_GROUPS = EX_THREADS / 128;
+// staging bytes a CTA may use and still share its SM with a second one
+constexpr int EX_STAGE_CAP = 108 * 1024;
 
 // The epilogue stages one walker's accumulator columns [2 wl n, 2 (wl + 1) n),
 // widened to 16-column bounds, transposed: S[c][r] = D[r][c_lo + c] for the
@@ -54,11 +59,15 @@ static_assert((2 * EX_STAGES + 1) * 8 + 16 <= EX_HEAD, "barrier block");
 static int ex_pitch(int n) { return n % 4 == 0 ? 132 : 129; }
 // staged columns per walker: at most 2n rounded up to 16, plus 16, at most the tile
 static int ex_srows(int n) { return std::min(EX_BN, (2 * n + 15) / 16 * 16 + 16); }
-constexpr int EX_PART = 2 * 4 * BM * 4;  // per-row partial sums: 2 slots x 4 sums x 128 rows
+constexpr int EX_PART = EX_GROUPS * 4 * BM * 4;  // per-row partial sums: groups x 4 sums x 128 rows
 static size_t ex_slot(int n) { return (size_t)ex_srows(n) * ex_pitch(n) * 4; }
-// walkers staged together: two (one per warp half) when both fit in the
-// pipeline's buffers, so that the CTA keeps its half of the SM
-static int ex_wpar(int n) { return 2 * ex_slot(n) + EX_PART <= (size_t)EX_PIPE ? 2 : 1; }
+// walkers staged together (one per group, up to three) while they fit beside
+// a second CTA on the SM
+static int ex_wpar(int n) {
+  for (int s = EX_GROUPS; s > 1; --s)
+    if (s * ex_slot(n) + EX_PART <= (size_t)EX_STAGE_CAP) return s;
+  return 1;
+}
 // dynamic shared memory: the stages, which the staged columns reuse
 static size_t ex_smem(int n) {
   return 1024 + EX_HEAD + std::max((size_t)EX_PIPE, ex_wpar(n) * ex_slot(n) + EX_PART);
@@ -77,12 +86,12 @@ struct ExArgs {
 
 // grid: (walker tiles, g tiles, channels); EX_THREADS threads: warp 0 lane 0
 // loads, warp 1 lane 0 issues the MMAs, and all warps share the epilogue.
-// Warp w reads TMEM lane quadrant w % 4; its half w / 4 is a walker slot when
-// two walkers are staged together, else a half of the j range of the one
-// walker.  Per staged walker: its columns go from TMEM to S; each thread forms
-// its row's X_r = sum_j f[i][j] f[j][i] and f[i][i]; the n rows of each
-// (g, walker) block are then summed by one thread per (block, sum).
-constexpr int EX_THREADS = 256;
+// Warp w reads TMEM lane quadrant w % 4; its group w / 4 stages and reduces
+// one walker when several are staged together (a group without one waits),
+// else a third of the j range of the one walker.  Per staged walker: its
+// columns go from TMEM to S; each thread forms its row's
+// X_r = sum_j f[i][j] f[j][i] and f[i][i]; the n rows of each (g, walker)
+// block are then summed by one thread per (block, sum).
 __global__ void __launch_bounds__(EX_THREADS, 2)
     k_tc_exchange(const __grid_constant__ CUtensorMap tmA0, const __grid_constant__ CUtensorMap tmB0,
                   const __grid_constant__ CUtensorMap tmA1, const __grid_constant__ CUtensorMap tmB1, ExArgs a0,
@@ -163,27 +172,28 @@ __global__ void __launch_bounds__(EX_THREADS, 2)
   __syncthreads();  // all loads consumed: the pipeline buffers become the staging buffer
   float* tile = (float*)smem;
   const int n = A.n, P = A.ld, nslot = A.wpar;
-  float* part = tile + nslot * A.srows * P;  // [2][4][BM] per-row partial sums
+  float* part = tile + nslot * A.srows * P;  // [EX_GROUPS][4][BM] per-row partial sums
   const bool run = have && !s_abort;
-  const int q = warp & 3, half = warp >> 2;
+  const int q = warp & 3, grp = warp >> 2;
   const int row = q * 32 + lane;
-  // the j range of this warp half: all of it with two walker slots, else a
-  // half (a multiple of 4 wide, so that the 16-byte loads stay aligned)
-  const int jh = nslot == 2 ? n : ((n + 1) / 2 + 3) & ~3;
-  const int ja = nslot == 2 ? 0 : min(n, half * jh), jb = min(n, ja + jh);
+  // the j range of this group: all of it when groups take walkers, else a
+  // third (a multiple of 4 wide, so that the 16-byte loads stay aligned)
+  const int jh = nslot > 1 ? n : ((n + EX_GROUPS - 1) / EX_GROUPS + 3) & ~3;
+  const int ja = nslot > 1 ? 0 : min(n, grp * jh), jb = min(n, ja + jh);
   const bool vec4 = (n & 3) == 0;
+  const int gs = nslot > 1 ? grp : 0;  // this group's walker slot
 #pragma unroll 1
   for (int it = 0; it * nslot < A.wbox; ++it) {
-    const int wl = it * nslot + (nslot == 2 ? half : 0);
-    const bool act = run && wl < A.wbox && w0 + wl < W;
-    float* S = tile + (nslot == 2 ? half : 0) * A.srows * P;
+    const int wl = it * nslot + gs;
+    const bool act = run && (nslot == 1 || grp < nslot) && wl < A.wbox && w0 + wl < W;
+    float* S = tile + gs * A.srows * P;
     const int c_lo = (2 * wl * n) & ~15, c_hi = (2 * (wl + 1) * n + 15) & ~15;
     if (act) {
-      // two slots: this half's four warps copy all pieces of its walker;
-      // one slot: the halves take alternate 16-column pieces
-      const int cstep = nslot == 2 ? 16 : 32;
+      // a group with its own walker copies all of its pieces; with one
+      // walker the groups take every third 16-column piece
+      const int cstep = nslot > 1 ? 16 : 16 * EX_GROUPS;
 #pragma unroll 1
-      for (int c = c_lo + (nslot == 2 ? 0 : half * 16); c < c_hi; c += cstep) {
+      for (int c = c_lo + (nslot > 1 ? 0 : grp * 16); c < c_hi; c += cstep) {
         float v[16];
         tc::tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)c, v);
         float* dst = S + (c - c_lo) * P + row;
@@ -228,13 +238,13 @@ __global__ void __launch_bounds__(EX_THREADS, 2)
         ci = aim[i * P];
       }
     }
-    part[(half * 4 + 0) * BM + row] = xr;
-    part[(half * 4 + 1) * BM + row] = xi;
-    part[(half * 4 + 2) * BM + row] = cr;
-    part[(half * 4 + 3) * BM + row] = ci;
+    part[(grp * 4 + 0) * BM + row] = xr;
+    part[(grp * 4 + 1) * BM + row] = xi;
+    part[(grp * 4 + 2) * BM + row] = cr;
+    part[(grp * 4 + 3) * BM + row] = ci;
     __syncthreads();
     // one thread per (slot, g, sum): the n rows of the block, in row order
-    // (one slot: the two j halves of each row added first)
+    // (one slot: the groups' j ranges of each row added first, in group order)
     const int ntask = nslot * A.gbox * 4;
     for (int t = threadIdx.x; t < ntask; t += EX_THREADS) {
       const int qq = t & 3, gl = (t >> 2) % A.gbox, s = (t >> 2) / A.gbox;
@@ -242,11 +252,15 @@ __global__ void __launch_bounds__(EX_THREADS, 2)
       if (!run || wl2 >= A.wbox || w0 + wl2 >= W || g >= Gene) continue;
       const float* p0 = part + (s * 4 + qq) * BM + gl * n;
       float sum = 0.f;
-      if (nslot == 2) {
+      if (nslot > 1) {
         for (int i = 0; i < n; ++i) sum += p0[i];
       } else {
-        const float* p1 = p0 + 4 * BM;
-        for (int i = 0; i < n; ++i) sum += p0[i] + p1[i];
+        for (int i = 0; i < n; ++i) {
+          float r = p0[i];
+#pragma unroll
+          for (int gg = 1; gg < EX_GROUPS; ++gg) r += p0[gg * 4 * BM + i];
+          sum += r;
+        }
       }
       // xc[w][s][g] = {(X re, X im), (c re, c im)}
       double* o = (double*)(xc + (((size_t)(w0 + wl2) * 2 + A.s) * Gene + g) * 2);
