@@ -68,7 +68,8 @@ static int ex_wpar(int n) {
     if (s * ex_slot(n) + EX_PART <= (size_t)EX_STAGE_CAP) return s;
   return 1;
 }
-// dynamic shared memory: the stages, which the staged columns reuse
+// dynamic shared memory: the stages, or the staged columns and partial sums
+// where they need more (they reuse the stages' bytes once the MMAs are done)
 static size_t ex_smem(int n) {
   return 1024 + EX_HEAD + std::max((size_t)EX_PIPE, ex_wpar(n) * ex_slot(n) + EX_PART);
 }
