@@ -140,7 +140,31 @@ __global__ void k_split_theta_gather(const float* __restrict__ theta, const int*
   const int c0 = blockIdx.y * GT_ROWS, rows = min(GT_ROWS, nce - c0);
   const float* s = theta + ((size_t)idx[i] * 2 + plane) * nce * N + (size_t)c0 * N;
   __nv_bfloat16* d = dst + (size_t)ip * nce * kpad + (size_t)c0 * kpad;
-  if (((N | kpad) & 1) == 0) {
+  if (((N | kpad) & 3) == 0) {
+    // one warp per row, four positions per lane step: a 16-byte load and an
+    // 8-byte store, the segment found by comparisons (4 | N, so four
+    // positions never straddle one)
+    const int kq = kpad / 4, lane = threadIdx.x & 31;
+    for (int c = threadIdx.x >> 5; c < rows; c += blockDim.x >> 5) {
+      const float* sr = s + (size_t)c * N;
+      __nv_bfloat16* dr = d + (size_t)c * kpad;
+      for (int k4 = lane; k4 < kq; k4 += 32) {
+        const int k = 4 * k4;
+        uint2 out = make_uint2(0u, 0u);
+        if (k < 3 * N) {
+          const int seg = (k >= N) + (k >= 2 * N), pp = k - seg * N;
+          const float4 x = *(const float4*)(sr + pp);
+          __nv_bfloat162 v0 = __floats2bfloat162_rn(x.x, x.y), v1 = __floats2bfloat162_rn(x.z, x.w);
+          if (seg == 1) {
+            v0 = __floats2bfloat162_rn(x.x - __low2float(v0), x.y - __high2float(v0));
+            v1 = __floats2bfloat162_rn(x.z - __low2float(v1), x.w - __high2float(v1));
+          }
+          out = make_uint2(*reinterpret_cast<const uint32_t*>(&v0), *reinterpret_cast<const uint32_t*>(&v1));
+        }
+        *(uint2*)(dr + k) = out;
+      }
+    }
+  } else if (((N | kpad) & 1) == 0) {
     const int hk = kpad / 2;
     for (int e = threadIdx.x; e < rows * hk; e += blockDim.x) {
       const int c = e / hk, k = 2 * (e - c * hk);
